@@ -1,0 +1,292 @@
+"""Benchmark of the GB300 DEM step engine.
+
+One "step" is one pass of the reference's step loop (advance, force
+evaluation, finish, host MBD) over the whole scene.  Default workload: the
+DEM-MBD scene of 200,000 spheres (r ~ U[1.5, 2.5] mm) in a 0.4 m box with a
+2,216-triangle rotating blade (prescribed, omega_z = 3 rad/s) and a
+192-triangle 1 kg dynamic plate, dt = 5e-6 s, seeded synthetic bed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--config c1|c0|c2] [--precision mixed|fp64]
+
+Prints one JSON line.  ``value`` is particle-steps/s of the headline
+precision with the state resident in HBM (CUDA events on the engine stream);
+``e2e`` is the same metric through the C ABI per step (body states uploaded
+and body loads read back every step, as the reference's host loop does).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def make_scene(config):
+    from dem_mbd_cuda_gb300 import generate as G
+    if config == "c0":
+        return G.pure_dem(n=20000, seed=1000), "pure DEM, 20,000 spheres r~U[1.8,2.2] mm, 5 walls, dt 1e-5"
+    if config == "c2":
+        sc, _ = G.drum(n=2000000, seed=1002)
+        return sc, "rotating drum, 2,000,000 lognormal spheres (median 1 mm), %d-triangle cylinder, dt 2e-6" % sc.n_triangles
+    sc, _ = G.mbd_blade_plate(n=200000, seed=1001)
+    return sc, ("DEM-MBD, 200,000 spheres r~U[1.5,2.5] mm in a 0.4 m box, %d-triangle blade (omega_z 3) + "
+                "%d-triangle 1 kg plate, dt 5e-6" % (int((sc.tri_body == 0).sum()), int((sc.tri_body == 1).sum())))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", "-i", str(self.index),
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"]
+        try:
+            self._proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._thread = threading.Thread(target=self._read, daemon=True)
+            self._thread.start()
+        except Exception:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(n, nc, contacts, wall_contacts, body_manifolds, triangles, h):
+    """Per-step algorithmic bytes (the survey's B_step):
+    N*412 + Nc*24 + (C_pp + C_pw + C_pb)*2*(8 + 9h) + T*288, with C_pp the
+    unordered particle contacts (= contact sides / 2)."""
+    return n * 412 + nc * 24 + (contacts / 2 + wall_contacts + body_manifolds) * 2 * (8 + 9 * h) + triangles * 288
+
+
+def launches_per_step(scene):
+    """Kernels one graph-launched step issues (see dem_engine.cu enqueue)."""
+    k = 2 + 8 + 1 + 2 + 1 + 2   # counters x2, grid build, gather, broadphase+law, owner sum, advance+finish
+    if scene.comp_owner is not None:
+        k += 1
+    if scene.n_bodies:
+        k += 1 + 6 + 5 + 2       # triangle transform, triangle grid, PT compaction + PT, body reduction
+    return k
+
+
+def run_engine(scene, precision, steps, warmup):
+    from dem_mbd_cuda_gb300.engine import CudaDemSolver
+    e = CudaDemSolver().initialize(scene, precision=precision)
+    e.run(max(1, warmup))
+    with ClockSampler() as clk:
+        ms = e.time_steps(steps)
+    stats = e.stepStats()
+    phases = e.compute_forces_timed(diag=True)
+    stats_after = e.stepStats()
+    return e, ms, clk.summary(), stats, phases, stats_after
+
+
+def e2e_run(scene, precision, steps, warmup):
+    """Per-step calls through the C ABI: body states H2D from host memory and
+    body loads D2H every step (dem_run_steps(1) per call)."""
+    from dem_mbd_cuda_gb300.engine import CudaDemSolver
+    e = CudaDemSolver().initialize(scene, precision=precision)
+    e.run(max(1, warmup))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        e.run(1)
+    t1 = time.perf_counter()
+    return (t1 - t0) * 1000.0
+
+
+def cpu_baseline(scene, budget_s=12.0, threads=None):
+    from oracle.oracle import Oracle
+    threads = threads or os.cpu_count() or 1
+    o = Oracle(scene, threads=threads)
+    o.run(1)
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        o.run(1)
+        done += 1
+        if time.perf_counter() - t0 >= budget_s or done >= 200:
+            break
+    dt = time.perf_counter() - t0
+    return scene.n * done / dt, threads, done, dt
+
+
+def load_error(scene):
+    """Body-load and particle-force error of the mixed form against the FP64
+    form from the same state (first evaluation)."""
+    from dem_mbd_cuda_gb300.engine import CudaDemSolver
+    a = CudaDemSolver().initialize(scene, precision="fp64")
+    b = CudaDemSolver().initialize(scene, precision="mixed")
+    bs = scene.body_states() if scene.n_bodies else None
+    la = a.computeForces(0.0, bs, True, True)
+    lb = b.computeForces(0.0, bs, True, True)
+    fa = a.downloadForceOutput(False, False)["total"]
+    fb = b.downloadForceOutput(False, False)["total"]
+    out = {"force_rel_err_max": float(np.abs(fa - fb).max() / max(np.abs(fa).max(), 1e-30))}
+    if la is not None and len(la):
+        out["body_load_rel_err"] = float(np.abs(la - lb).max() / max(np.abs(la).max(), 1e-30))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    scene, desc = make_scene(args.config)
+
+    if args.impl == "reference":
+        # The reference's own hot path is CUDA-only; its CPU implementation of
+        # the path here is the oracle port on the host cores.
+        if rank != 0:
+            return
+        from oracle import oracle as orc
+        orc.build()
+        from oracle.oracle import Oracle
+        threads = os.cpu_count() or 1
+        o = Oracle(scene, threads=threads)
+        o.run(args.warmup)
+        t0 = time.perf_counter()
+        o.run(args.steps)
+        dt = time.perf_counter() - t0
+        v = scene.n * args.steps / dt
+        line = {"impl": "reference", "metric": "particle-steps/s", "value": v, "unit": "particle-steps/s",
+                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": desc, "particles": scene.n, "triangles": scene.n_triangles},
+                "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                                 "sample": f"{args.steps} steps of the workload after {args.warmup} warm-up steps"},
+                "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    from dem_mbd_cuda_gb300 import build
+    build.build()
+    if dist:
+        dist.barrier()
+    e, ms, clocks, stats, phases, _ = run_engine(scene, args.precision, args.steps, args.warmup)
+    other = "fp64" if args.precision == "mixed" else "mixed"
+    e_o, ms_o, _, _, phases_o, _ = run_engine(scene, other, args.steps, args.warmup)
+    del e_o
+    if dist:
+        t = __import__("torch").tensor([ms, ms_o], dtype=__import__("torch").float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, ms_o = float(t[0]), float(t[1])
+    per_step_ms = ms / args.steps
+    value = world * scene.n * args.steps / (ms / 1000.0)
+    value_other = world * scene.n * args.steps / (ms_o / 1000.0)
+    e2e_ms = e2e_run(scene, args.precision, args.steps, args.warmup)
+    e2e_value = world * scene.n * args.steps / (e2e_ms / 1000.0)
+    if rank != 0:
+        return
+    errs = load_error(scene)
+    h = 4 if args.precision == "mixed" else 8
+    contacts = stats["particle_contacts"]
+    bbytes = algorithmic_bytes(scene.n, scene.n_components, contacts, 0, stats["body_contacts"], scene.n_triangles, h)
+    peak, peak_kind = hbm_peak()
+    achieved = bbytes / (per_step_ms / 1000.0) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, cores, done, dt = cpu_baseline(scene)
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{done} steps of the same workload on {cores} threads ({dt:.1f} s)"}
+    nb = scene.n_bodies
+    line = {
+        "metric": "particle-steps/s",
+        "value": value,
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": per_step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-contact/f64-state" if args.precision == "mixed" else "f64",
+        "data": "synthetic",
+        "config": {"workload": desc, "particles": scene.n, "triangles": scene.n_triangles, "precision": args.precision,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "per-step working set (state, records, history, contact list) exceeds the 129 MB L2"},
+        "fp64_value" if args.precision == "mixed" else "mixed_value": value_other,
+        "contacts_per_s": contacts * args.steps / (ms / 1000.0) / 2,
+        "contact_sides_per_step": contacts,
+        "load_error_vs_fp64": errs,
+        "phase_ms": {"grid": phases[0] if len(phases) > 0 else None,
+                     "triangles+gather": phases[1] if len(phases) > 1 else None,
+                     "contacts": phases[2] if len(phases) > 2 else None,
+                     "sum+reduce": phases[3] if len(phases) > 3 else None},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "whole step (algorithmic B_step / step time)", "peak_kind": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 13 * 8 * nb,
+                "d2h_bytes_per_step": 38 * 8 * nb + 16 * 4},
+        "gpu_launches": launches_per_step(scene) * args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,809 @@
+// dem_contact.cu -- contact pipeline of one force evaluation.
+//
+// The reference evaluates everything for one owner in one thread
+// (computeContactsKernel, src/cuda/cuda_contact_backend.cu:1065-1221): walls,
+// a 27-cell sweep with binary searches and the full FP64 particle law inline,
+// then the particle-triangle manifold.  Here the work is split so the
+// expensive law runs without warp divergence:
+//   gather      packed sorted rows of every component (cell order)
+//   broadphase  one thread per component: history expiry, wall law, 27-cell
+//               sweep over the cell start table with an FP32 cell-relative
+//               prefilter and the exact FP64 overlap test, history slot
+//               acquisition in sweep order, append to a flat contact list
+//   pp law      one thread per contact (T = double or float)
+//   pt          one thread per component whose cell holds triangles: the
+//               reference's per-body manifold, then the per-triangle loads
+//   owner sum   per owner, contacts summed in the reference's sweep order,
+//               total force and the acceleration / Euler update fused
+//   body reduce deterministic two-level reduction of the body loads
+#include "dem_kernels.cuh"
+
+#include <climits>
+
+namespace demgb {
+
+namespace {
+
+__device__ __forceinline__ int warp_sum(int v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_maxi(int v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ int block_exclusive_scan_c(int v, int& total)
+{
+    __shared__ int warp_sums[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int s = lane < nw ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    total = warp_sums[nw - 1];
+    const int base = wid > 0 ? warp_sums[wid - 1] : 0;
+    __syncthreads();
+    return base + x - v;
+}
+
+// Block-aggregated counter updates (sum / max).
+__device__ void block_add(int* dst, int v)
+{
+    const int s = warp_sum(v);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst, s);
+}
+__device__ void block_max(int* dst, int v)
+{
+    const int s = warp_maxi(v);
+    if ((threadIdx.x & 31) == 0 && s > 0) atomicMax(dst, s);
+}
+
+template <typename T> __device__ __forceinline__ void zero9(T* v)
+{
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = T(0);
+}
+
+// expireHistory (:217-229) over the occupied prefix [0, hw).
+template <typename T> __device__ void expire(Hist<T> h, int slots, int c, int step)
+{
+    const size_t base = (size_t)c * slots;
+    const int hw = h.hw[c];
+    int nhw = 0;
+    for (int s = 0; s < hw; ++s) {
+        if (h.key[base + s] != 0) {
+            if (h.last[base + s] < step - 1) {
+                h.key[base + s] = 0;
+                h.last[base + s] = -1;
+                zero9(h.val + (base + s) * 9);
+            } else {
+                nhw = s + 1;
+            }
+        }
+    }
+    if (nhw != hw) h.hw[c] = nhw;
+}
+
+// acquireHistorySlot (:190-215): the matching key, else the first empty slot.
+// Returns the slot index within the component, -1 on overflow.
+template <typename T>
+__device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int& hw, int& high)
+{
+    const size_t base = (size_t)c * slots;
+    int empty = -1;
+    for (int s = 0; s < hw; ++s) {
+        const uint64_t k = h.key[base + s];
+        if (k == key) {
+            h.last[base + s] = step;
+            high = max(high, s + 1);
+            return s;
+        }
+        if (k == 0 && empty < 0) empty = s;
+    }
+    if (empty < 0) {
+        if (hw >= slots) return -1;
+        empty = hw;
+    }
+    h.key[base + empty] = key;
+    h.last[base + empty] = step;
+    zero9(h.val + (base + empty) * 9);
+    if (empty + 1 > hw) hw = empty + 1;
+    high = max(high, empty + 1);
+    return empty;
+}
+
+__device__ __forceinline__ V3<double> d3(D4 v) { return {v.x, v.y, v.z}; }
+__device__ __forceinline__ D4 d4(double x, double y, double z, double w) { return D4{x, y, z, w}; }
+
+// ------------------------------------------------------------------ gather
+template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r, double dt_eff)
+{
+    const int nvalid = *g.nvalid;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
+        const int ci = g.sorted_id[t];
+        const int w = c.owner[ci];
+        const double x = c.x[ci], y = c.y[ci], z = c.z[ci], rad = c.radius[ci];
+        r.pos[t] = d4(x, y, z, rad);
+        const double vx = c.vx[ci], vy = c.vy[ci], vz = c.vz[ci];
+        r.v[t] = d4(vx, vy, vz, o.mass[w]);
+        const int st = o.status[w];
+        const bool mid = dt_eff > 0.0 && st != -1;
+        r.vm[t] = mid ? d4(c.vhx[ci], c.vhy[ci], c.vhz[ci], 0.0) : d4(vx, vy, vz, 0.0);
+        const double qw = o.qw[w], qx = o.qx[w], qy = o.qy[w], qz = o.qz[w];
+        const V3<double> ew = rot_iv(qw, qx, qy, qz, mk(o.wx[w], o.wy[w], o.wz[w]));
+        r.w[t] = d4(ew.x, ew.y, ew.z, 0.0);
+        if (mid) {
+            const V3<double> mw = rot_iv(qw, qx, qy, qz, mk(o.whx[w], o.why[w], o.whz[w]));
+            r.wm[t] = d4(mw.x, mw.y, mw.z, 0.0);
+        } else {
+            r.wm[t] = d4(ew.x, ew.y, ew.z, 0.0);
+        }
+        if (r.off) r.off[t] = d4(c.ox[ci], c.oy[ci], c.oz[ci], 0.0);
+        int cx, cy, cz;
+        unpack_cell(g.ckey[ci], cx, cy, cz);
+        r.meta[t] = make_int4(ci, w, c.cid[ci], o.scene[w]);
+        r.cell[t] = make_int4(cx, cy, cz, g.clin[ci]);
+        r.relf[t] = make_float4((float)(x - cx * g.mesh), (float)(y - cy * g.mesh), (float)(z - cz * g.mesh),
+                                (float)rad);
+    }
+}
+
+// ------------------------------------------------------------- broadphase
+constexpr int kMaxContacts = kPSlots;
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_broadphase(Grid g, Recs r, const SceneC* __restrict__ sc, Walls walls,
+                                                    Tris tris, Hist<T> hp, Hist<T> hw, Hist<T> hb, Contacts<T> ct,
+                                                    Counters k, double dt_eff)
+{
+    const int step = *k.step;
+    const int nvalid = *g.nvalid;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int count = 0, pover = 0, bover = 0, phigh = 0, bhigh = 0;
+    int stage_t[kMaxContacts];
+    int stage_s[kMaxContacts];
+    int ci = -1;
+    int pt_flag = 0;
+    if (t < nvalid) {
+        const int4 meta = r.meta[t];
+        ci = meta.x;
+        const int owner = meta.y, s = meta.w;
+        const SceneC S = sc[s];
+        const int4 cell = r.cell[t];
+        const D4 pi = r.pos[t];
+        expire(hp, kPSlots, ci, step);
+        expire(hw, kWSlots, ci, step);
+        expire(hb, kBSlots, ci, step);
+
+        // walls (wallContact, :975-1063)
+        V3<double> wF = mk(0.0, 0.0, 0.0), wT = mk(0.0, 0.0, 0.0);
+        if (S.wall_count > 0) {
+            int whw = hw.hw[ci];
+            const D4 v4 = r.v[t];
+            const D4 w4 = r.w[t];
+            const V3<double> off = r.off ? d3(r.off[t]) : mk(0.0, 0.0, 0.0);
+            for (int wl = 0; wl < S.wall_count; ++wl) {
+                const int wg = S.wall_begin + wl;
+                const V3<double> out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
+                const V3<double> org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
+                const double dist = dot(d3(pi) - org, out);
+                const double depth = pi.w - dist;
+                if (depth <= 0.0) continue;
+                const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
+                if (slot < 0) { ++bover; continue; }
+                T* hv = hw.val + ((size_t)ci * kWSlots + slot) * 9;
+                V3<T> f, cpl;
+                wall_law<T>(S.pw, T(dt_eff), cvt<T>(out), T(depth), T(pi.w), T(v4.w), cvt<T>(d3(v4)), cvt<T>(d3(w4)),
+                            hv, f, cpl);
+                const V3<double> fd = cvt<double>(f);
+                wF = wF + fd;
+                wT = wT + (cvt<double>(cpl) + cross(off, fd));
+            }
+            hw.hw[ci] = whw;
+        }
+        double* wr = ct.wres + 6 * (size_t)ci;
+        wr[0] = wF.x; wr[1] = wF.y; wr[2] = wF.z; wr[3] = wT.x; wr[4] = wT.y; wr[5] = wT.z;
+
+        // particle sweep over the 27 neighbour cells, reference order.
+        const int* lay = g.scene_layout + 8 * s;
+        const float4 fi = r.relf[t];
+        int phw = hp.hw[ci];
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int nx = cell.x + dx;
+            if (nx < lay[0] || nx >= lay[0] + lay[3]) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int ny = cell.y + dy;
+                if (ny < lay[1] || ny >= lay[1] + lay[4]) continue;
+                for (int dz = -1; dz <= 1; ++dz) {
+                    const int nz = cell.z + dz;
+                    if (nz < lay[2] || nz >= lay[2] + lay[5]) continue;
+                    const int lin = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] + (nz - lay[2]);
+                    const int b = g.cell_start[lin], e = g.cell_start[lin + 1];
+                    const float ox = dx * g.mesh_f - fi.x, oy = dy * g.mesh_f - fi.y, oz = dz * g.mesh_f - fi.z;
+                    for (int u = b; u < e; ++u) {
+                        const float4 fj = r.relf[u];
+                        const float ddx = fj.x + ox, ddy = fj.y + oy, ddz = fj.z + oz;
+                        const float rsf = fj.w + fi.w + g.margin_f;
+                        if (ddx * ddx + ddy * ddy + ddz * ddz >= rsf * rsf) continue;
+                        const int4 mj = r.meta[u];
+                        if (mj.y == owner) continue;
+                        const D4 pj = r.pos[u];
+                        const V3<double> delta = mk(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
+                        const double d2 = distance_squared(delta);
+                        const double rs = pi.w + pj.w;
+                        if (d2 >= rs * rs || d2 <= 1.0e-28) continue;
+                        const uint64_t key = (uint64_t)(uint32_t)mj.z + 1ull;
+                        if (count >= kMaxContacts) { ++pover; continue; }
+                        const int slot = acquire(hp, kPSlots, ci, key, step, phw, phigh);
+                        if (slot < 0) { ++pover; continue; }
+                        stage_t[count] = u;
+                        stage_s[count] = slot;
+                        ++count;
+                    }
+                }
+            }
+        }
+        hp.hw[ci] = phw;
+        if (S.body_count > 0 && tris.nt > 0) {
+            const int lin = cell.w;
+            pt_flag = tris.tcell_start[lin + 1] > tris.tcell_start[lin] ? 1 : 0;
+        }
+        ct.pt_flag[t] = pt_flag;
+    }
+    int total;
+    const int ex = block_exclusive_scan_c(count, total);
+    __shared__ int s_base;
+    if (threadIdx.x == 0) s_base = total ? atomicAdd(k.ct_total, total) : 0;
+    __syncthreads();
+    const int base = s_base + ex;
+    if (ci >= 0) {
+        ct.off[ci] = base;
+        ct.cnt[ci] = count;
+        for (int q = 0; q < count; ++q)
+            ct.ent[base + q] = make_int4(t, stage_t[q], ci * kPSlots + stage_s[q], 0);
+    }
+    block_add(k.pcontacts, count);
+    block_add(k.pover, pover);
+    block_add(k.bover, bover);
+    block_max(k.phigh, phigh);
+    block_max(k.bhigh, bhigh);
+}
+
+// ------------------------------------------------------------------ PP law
+template <typename T>
+__global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict__ sc, Hist<T> hp, Contacts<T> ct,
+                                                Counters k, double dt_eff)
+{
+    const int total = *k.ct_total;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+        const int4 e = ct.ent[q];
+        const D4 pi = r.pos[e.x], pj = r.pos[e.y];
+        const V3<double> delta = mk(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
+        const double d2 = distance_squared(delta);
+        const double rs = pi.w + pj.w;
+        T d, depth;
+        V3<T> n;
+        if constexpr (sizeof(T) == sizeof(double)) {
+            const double dd = sqrt(d2);
+            d = dd;
+            depth = rs - dd;
+            n = delta * (1.0 / dd);
+        } else {
+            // Overlap from the FP64 difference of squares, the rest in FP32.
+            const double num = __fma_rn(rs, rs, -d2);
+            const float df = sqrtf((float)d2);
+            d = df;
+            depth = (float)num / ((float)rs + df);
+            n = cvt<float>(delta) * (1.0f / df);
+        }
+        const D4 vi = r.v[e.x], vj = r.v[e.y];
+        const D4 mi = r.vm[e.x], mj = r.vm[e.y];
+        const V3<T> erv = cvt<T>(d3(vj) - d3(vi));
+        const V3<T> mrv = cvt<T>(d3(mj) - d3(mi));
+        const V3<T> ewi = cvt<T>(d3(r.w[e.x])), ewj = cvt<T>(d3(r.w[e.y]));
+        const V3<T> mwi = cvt<T>(d3(r.wm[e.x])), mwj = cvt<T>(d3(r.wm[e.y]));
+        const int s = r.meta[e.x].w;
+        T* hv = hp.val + (size_t)e.z * 9;
+        V3<T> f, cpl;
+        pp_law<T>(sc[s].pp, T(dt_eff), n, d, depth, T(d2), T(pi.w), T(pj.w), T(vi.w), T(vj.w), erv, mrv, ewi, ewj, mwi,
+                  mwj, hv, f, cpl);
+        if (r.off) cpl = cpl + cross(cvt<T>(d3(r.off[e.x])), f);
+        T* out = ct.res + 6 * (size_t)q;
+        out[0] = f.x; out[1] = f.y; out[2] = f.z; out[3] = cpl.x; out[4] = cpl.y; out[5] = cpl.z;
+    }
+}
+
+// PT list in sorted order: item index = exclusive scan of the flags.
+__global__ void k_pt_compact(Grid g, Recs r, int* pt_flag, int* pt_pos, int* pt_list,
+                             int* pt_index, int* pt_total)
+{
+    const int nvalid = *g.nvalid;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *pt_total = pt_pos[nvalid];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
+        const int ci = r.meta[t].x;
+        if (pt_flag[t]) {
+            pt_list[pt_pos[t]] = t;
+            pt_index[ci] = pt_pos[t];
+        } else {
+            pt_index[ci] = -1;
+        }
+    }
+}
+
+// ------------------------------------------------------------------- PT
+constexpr int kTriCache = 24;
+
+// bodyTriangleAreaScale (:380-407); also returns distance along the outward
+// normal.
+template <typename T>
+__device__ double tri_area_scale(const double* W, V3<double> p, double r, double& dist)
+{
+    const V3<double> n = mk(W[12], W[13], W[14]);
+    const V3<double> a = mk(W[3], W[4], W[5]);
+    dist = dot(n, p - a);
+    if (dist <= 0.0) return 0.0;
+    const double c2 = r * r - dist * dist;
+    if (c2 <= 1.0e-30) return 0.0;
+    const V3<double> ce = p - n * dist;
+    const V3<double> ra = a - ce, rb = mk(W[6], W[7], W[8]) - ce, rc = mk(W[9], W[10], W[11]) - ce;
+    double area;
+    if constexpr (sizeof(T) == sizeof(double)) {
+        area = circle_triangle_area<double>(n, ra, rb, rc, sqrt(c2));
+    } else {
+        area = (double)circle_triangle_area<float>(cvt<float>(n), cvt<float>(ra), cvt<float>(rb), cvt<float>(rc),
+                                                   sqrtf((float)c2));
+    }
+    if (area <= 0.0) return 0.0;
+    const double sc = fmin(1.0, area / (kPi * c2));
+    return sc > 1.0e-12 ? sc : 0.0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_pt(Recs r, const SceneC* __restrict__ sc, Tris tris, Bodies bodies,
+                                            Hist<T> hb, Contacts<T> ct, Counters k, double dt_eff)
+{
+    const int step = *k.step;
+    const int total = *ct.pt_total_ptr;
+    int bover = 0, bhigh = 0;
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
+        const int t = ct.pt_list[item];
+        const int4 meta = r.meta[t];
+        const int ci = meta.x, s = meta.w;
+        const SceneC S = sc[s];
+        const D4 p4 = r.pos[t];
+        const V3<double> p = d3(p4);
+        const double rad = p4.w;
+        const D4 v4 = r.v[t];
+        const double mass = v4.w;
+        const V3<double> ev = d3(v4), mv = d3(r.vm[t]);
+        const V3<double> ew = d3(r.w[t]), mw = d3(r.wm[t]);
+        const V3<double> off = r.off ? d3(r.off[t]) : mk(0.0, 0.0, 0.0);
+        const int lin = r.cell[t].w;
+        const int tb = tris.tcell_start[lin];
+        const int te = min(tris.tcell_start[lin + 1], tris.capacity);
+        V3<double> bF = mk(0.0, 0.0, 0.0), bT = mk(0.0, 0.0, 0.0);
+        int bhw = hb.hw[ci];
+        for (int j = 0; j < S.body_count; ++j) {
+            const int b = S.body_begin + j;
+            double* rec = ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord;
+            for (int f = 0; f < kPtRecord; ++f) rec[f] = 0.0;
+            double* outd = ct.pt_out ? ct.pt_out + ((size_t)item * ct.nbs + j) * 25 : nullptr;
+            if (outd) for (int f = 0; f < 25; ++f) outd[f] = 0.0;
+            // manifold sums over the component's own cell (:1154-1183)
+            int ctri[kTriCache];
+            double cas[kTriCache];
+            int ncache = 0;
+            bool spill = false;
+            double tot = 0.0, wd = 0.0;
+            V3<double> wn = mk(0.0, 0.0, 0.0), wc = mk(0.0, 0.0, 0.0);
+            for (int e = tb; e < te; ++e) {
+                const int tri = tris.ttri[e];
+                if (tris.body[tri] != b) continue;
+                const double* W = tris.world + 16 * (size_t)tri;
+                double dist;
+                const double as = tri_area_scale<T>(W, p, rad, dist);
+                if (as <= 0.0) continue;
+                const V3<double> out = mk(W[12], W[13], W[14]);
+                const V3<double> ce = p - out * dist;
+                tot += as;
+                wn = wn + out * (-as);
+                wc = wc + ce * as;
+                wd += dist * as;
+                if (ncache < kTriCache) { ctri[ncache] = tri; cas[ncache] = as; ++ncache; }
+                else spill = true;
+            }
+            if (tot <= 0.0) continue;
+            const V3<double> mn = normalized(wn);
+            const V3<double> mc = wc * (1.0 / tot);
+            const double md = wd / tot;
+            const int slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh);
+            if (slot < 0) { ++bover; continue; }
+            T* hv = hb.val + ((size_t)ci * kBSlots + slot) * 9;
+            const V3<double> center = mk(bodies.c[3 * b], bodies.c[3 * b + 1], bodies.c[3 * b + 2]);
+            const double* bq = bodies.q + 4 * b;
+            const V3<double> wb = rot_iv(bq[0], bq[1], bq[2], bq[3], mk(bodies.w[3 * b], bodies.w[3 * b + 1], bodies.w[3 * b + 2]));
+            const V3<double> bv = mk(bodies.v[3 * b], bodies.v[3 * b + 1], bodies.v[3 * b + 2]);
+            const MatC& m = S.pt;
+            // advanceBodyManifoldHistory (:855-949)
+            bool slide = false, twist = false;
+            {
+                const V3<double> arm = mc - center;
+                const V3<double> bvel = bv + cross(wb, arm);
+                const V3<T> erv = cvt<T>(bvel - ev), mrv = cvt<T>(bvel - mv);
+                const V3<T> n = cvt<T>(mn);
+                const LawC<T> c = law_constants<T>(m, T(mass), T(rad));
+                const T depth = T(rad - md);
+                V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(erv, n));
+                fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
+                V3<T> tv = mrv - n * dot(mrv, n);
+                tv = tv + cross(n, cvt<T>(mw)) * T(md);
+                V3<T> st;
+                limited_rates<T>(tv, tv, c.kS, c.cS, T(dt_eff), transport_tangent(hload(hv, 1), n), T(m.mu) * norm(fn),
+                                 st, slide);
+                hstore(hv, 1, st);
+                const V3<T> rw = cvt<T>(wb - mw);
+                const V3<T> twr = n * dot(rw, n);
+                const V3<T> rlr = (rw - twr) + cross(n, tv) * (T(0.5) / fmax(T(md), T(1.0e-14)));
+                const T ms = T(m.beta) * T(rad) * norm(fn);
+                limited_rates<T>(twr, twr, c.kT, c.cT, T(dt_eff), transport_axial(hload(hv, 2), n),
+                                 T(m.mu) * T(m.muT) * ms, st, twist);
+                hstore(hv, 2, st);
+                bool dummy;
+                limited_rates<T>(rlr, rlr, c.kR, c.cR, T(dt_eff), transport_tangent(hload(hv, 0), n), T(m.muR) * ms, st,
+                                 dummy);
+                hstore(hv, 0, st);
+            }
+            rec[9] = (double)(1 | (slide ? 2 : 0) | (twist ? 4 : 0));
+            // per-triangle loads with read-only history (bodyContact, :708-853)
+            double maxdepth = 0.0;
+            int tcount = 0;
+            const LawC<T> c = law_constants<T>(m, T(mass), T(rad));
+            const V3<T> hroll = hload(hv, 0), htan = hload(hv, 1), htw = hload(hv, 2);
+            const int nloop = spill ? (te - tb) : ncache;
+            for (int qi = 0; qi < nloop; ++qi) {
+                int tri;
+                double as, dist;
+                const double* W;
+                if (!spill) {
+                    tri = ctri[qi];
+                    as = cas[qi];
+                    W = tris.world + 16 * (size_t)tri;
+                    dist = dot(mk(W[12], W[13], W[14]), p - mk(W[3], W[4], W[5]));
+                } else {
+                    tri = tris.ttri[tb + qi];
+                    if (tris.body[tri] != b) continue;
+                    W = tris.world + 16 * (size_t)tri;
+                    as = tri_area_scale<T>(W, p, rad, dist);
+                    if (as <= 0.0) continue;
+                }
+                const double depthd = rad - dist;
+                if (dist <= 0.0 || depthd <= 0.0) continue;
+                const V3<double> nout = mk(W[12], W[13], W[14]);
+                const V3<double> ce = p - nout * dist;
+                const V3<double> arm = ce - center;
+                const V3<double> bvel = bv + cross(wb, arm);
+                const V3<T> n = cvt<T>(nout * -1.0);
+                const V3<T> rv = cvt<T>(bvel - ev);
+                const V3<T> wp = cvt<T>(ew);
+                const T depth = T(depthd), distT = T(dist);
+                V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(rv, n));
+                fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
+                V3<T> tv = rv - n * dot(rv, n);
+                tv = tv + cross(n, wp) * distT;
+                V3<T> st;
+                bool y;
+                const V3<T> fr = limited_rates<T>(tv, tv, c.kS, c.cS, T(0), transport_tangent(htan, n), T(m.mu) * norm(fn),
+                                                  st, y);
+                const V3<T> rw = cvt<T>(wb) - wp;
+                const V3<T> twr = n * dot(rw, n);
+                const V3<T> rlr = (rw - twr) + cross(n, tv) * (T(0.5) / fmax(distT, T(1.0e-14)));
+                const T ms = T(m.beta) * T(rad) * norm(fn);
+                const V3<T> tw = limited_rates<T>(twr, twr, c.kT, c.cT, T(0), transport_axial(htw, n),
+                                                  T(m.mu) * T(m.muT) * ms, st, y);
+                const V3<T> rl = limited_rates<T>(rlr, rlr, c.kR, c.cR, T(0), transport_tangent(hroll, n), T(m.muR) * ms,
+                                                  st, y);
+                const V3<double> fnd = cvt<double>(fn), frd = cvt<double>(fr);
+                const V3<double> pf = (fnd + frd) * as;
+                const V3<double> nd = cvt<double>(n);
+                const V3<double> cm = cvt<double>(tw) + cvt<double>(rl);
+                const V3<double> cpl = (cm + cross(nd, frd) * dist) * as;
+                const V3<double> ptq = cpl + cross(off, pf);
+                const V3<double> bnf = fnd * (-as), bfr = frd * (-as);
+                const V3<double> bnt = cross(arm, fnd) * (-as), bft = cross(arm, frd) * (-as);
+                const V3<double> btw = cvt<double>(tw) * (-as), brl = cvt<double>(rl) * (-as);
+                const V3<double> bt = (bnt + bft) + (btw + brl);
+                bF = bF + pf;
+                bT = bT + ptq;
+                rec[0] += bnf.x + bfr.x; rec[1] += bnf.y + bfr.y; rec[2] += bnf.z + bfr.z;
+                rec[3] += bt.x; rec[4] += bt.y; rec[5] += bt.z;
+                rec[8] += bnf.z + bfr.z;
+                ++tcount;
+                maxdepth = fmax(maxdepth, depthd);
+                if (outd) {
+                    outd[0] += pf.x; outd[1] += pf.y; outd[2] += pf.z; outd[3] += ptq.x; outd[4] += ptq.y; outd[5] += ptq.z;
+                    const V3<double> vals[6] = {bnf, bfr, bnt, bft, btw, brl};
+                    for (int gq = 0; gq < 6; ++gq) {
+                        outd[6 + 3 * gq] += vals[gq].x; outd[7 + 3 * gq] += vals[gq].y; outd[8 + 3 * gq] += vals[gq].z;
+                    }
+                    outd[24] = fmax(outd[24], depthd);
+                }
+            }
+            rec[6] = (double)tcount;
+            rec[7] = maxdepth;
+            // observeBodyMicrostateKernel (:1226-1356), fused
+            {
+                const V3<double> arm = mc - center;
+                const V3<double> bvel = bv + cross(wb, arm);
+                const V3<double> rv = bvel - ev;
+                const double logN = m.logN;
+                const double cN = -2.0 * logN * sqrt(m.kN * mass / m.denN);
+                const double brs = m.beta * rad * m.beta * rad;
+                const double depth = rad - md;
+                V3<double> fn = mn * (-m.kN * depth) + mn * (cN * dot(rv, mn));
+                fn = fn + mn * (m.coh * 4.0 * brs);
+                const double fnn = norm(fn);
+                const double ms = m.beta * rad * fnn;
+                const double tl = m.mu * fnn;
+                const double twl = m.mu * m.muT * ms;
+                const V3<double> th = cvt<double>(hload(hv, 1)), twh = cvt<double>(hload(hv, 2));
+                const V3<double> az = rot_iv(bq[0], bq[1], bq[2], bq[3], mk(0.0, 0.0, 1.0));
+                const V3<double> radial = arm - az * dot(arm, az);
+                const double tu = tl > 1.0e-30 ? fmin(1.0, norm(th) / tl) : 0.0;
+                const double twu = twl > 1.0e-30 ? fmin(1.0, norm(twh) / twl) : 0.0;
+                const V3<double> btw = twh * (-tot), bnl = fn * (-tot), bth = th * (-tot);
+                const V3<double> btt = cross(arm, bth);
+                double* mcr = rec + 10;
+                mcr[0] = fnn * tot; mcr[1] = fnn * rad * tot; mcr[2] = fnn * norm(radial) * tot;
+                mcr[3] = btw.x; mcr[4] = btw.y; mcr[5] = btw.z;
+                mcr[6] = norm(twh) * tot; mcr[7] = twl * tot; mcr[8] = norm(th) * tot; mcr[9] = tl * tot;
+                mcr[10] = twu * tot; mcr[11] = tu * tot; mcr[12] = tot;
+                mcr[13] = bnl.x; mcr[14] = bnl.y; mcr[15] = bnl.z;
+                mcr[16] = bth.x; mcr[17] = bth.y; mcr[18] = bth.z;
+                mcr[19] = btt.x; mcr[20] = btt.y; mcr[21] = btt.z;
+            }
+        }
+        hb.hw[ci] = bhw;
+        double* pr = ct.pt_res + 6 * (size_t)item;
+        pr[0] = bF.x; pr[1] = bF.y; pr[2] = bF.z; pr[3] = bT.x; pr[4] = bT.y; pr[5] = bT.z;
+    }
+    block_add(k.bover, bover);
+    block_max(k.bhigh, bhigh);
+}
+
+// --------------------------------------------------------------- owner sum
+// Per owner: the reference's accumulators (:1082-1094, 1211-1220) and the
+// acceleration / Euler equations (src/cuda/cuda_particle_backend.cu:71-101).
+template <typename T>
+__global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Contacts<T> ct, int outputs, double* fc,
+                            double* ff, double* fw, double* ft)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= o.n) return;
+    const int s = o.scene[i];
+    const double m = o.mass[i];
+    V3<double> fF = mk(0.0, 0.0, 0.0);
+    if (sc[s].grav) fF = mk(m * sc[s].g[0], m * sc[s].g[1], m * sc[s].g[2]);
+    if (o.ugx) fF = fF + mk(o.ugx[i], o.ugy[i], o.ugz[i]);
+    V3<double> cF = mk(0.0, 0.0, 0.0), cT = cF, wF = cF, wT = cF, bF = cF, bT = cF;
+    const int c0 = c.sphere ? i : c.ostart[i], c1 = c.sphere ? i + 1 : c.ostart[i + 1];
+    for (int ci = c0; ci < c1; ++ci) {
+        const int off = ct.off[ci], cnt = ct.cnt[ci];
+        for (int q = 0; q < cnt; ++q) {
+            const T* rr = ct.res + 6 * (size_t)(off + q);
+            cF = cF + mk((double)rr[0], (double)rr[1], (double)rr[2]);
+            cT = cT + mk((double)rr[3], (double)rr[4], (double)rr[5]);
+        }
+        const double* wr = ct.wres + 6 * (size_t)ci;
+        wF = wF + mk(wr[0], wr[1], wr[2]);
+        wT = wT + mk(wr[3], wr[4], wr[5]);
+        const int pk = ct.pt_index[ci];
+        if (pk >= 0) {
+            const double* pr = ct.pt_res + 6 * (size_t)pk;
+            bF = bF + mk(pr[0], pr[1], pr[2]);
+            bT = bT + mk(pr[3], pr[4], pr[5]);
+        }
+    }
+    const V3<double> TF = (cF + fF) + (wF + bF);
+    const V3<double> TT = cT + (wT + bT);
+    if (outputs) {
+        double* a = fc + 6 * (size_t)i; a[0] = cF.x; a[1] = cF.y; a[2] = cF.z; a[3] = cT.x; a[4] = cT.y; a[5] = cT.z;
+        a = ff + 6 * (size_t)i; a[0] = fF.x; a[1] = fF.y; a[2] = fF.z; a[3] = 0.0; a[4] = 0.0; a[5] = 0.0;
+        a = fw + 6 * (size_t)i; a[0] = wF.x; a[1] = wF.y; a[2] = wF.z; a[3] = wT.x; a[4] = wT.y; a[5] = wT.z;
+        a = ft + 6 * (size_t)i; a[0] = TF.x; a[1] = TF.y; a[2] = TF.z; a[3] = TT.x; a[4] = TT.y; a[5] = TT.z;
+        return;
+    }
+    o.ax[i] = TF.x / m; o.ay[i] = TF.y / m; o.az[i] = TF.z / m;
+    const double qw = o.qw[i], qx = o.qx[i], qy = o.qy[i], qz = o.qz[i];
+    const double tx = (1.0 - 2.0 * (qy * qy + qz * qz)) * TT.x + 2.0 * (qx * qy + qw * qz) * TT.y + 2.0 * (qx * qz - qw * qy) * TT.z;
+    const double ty = 2.0 * (qx * qy - qw * qz) * TT.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * TT.y + 2.0 * (qy * qz + qw * qx) * TT.z;
+    const double tz = 2.0 * (qx * qz + qw * qy) * TT.x + 2.0 * (qy * qz - qw * qx) * TT.y + (1.0 - 2.0 * (qx * qx + qy * qy)) * TT.z;
+    const double wx = o.wx[i], wy = o.wy[i], wz = o.wz[i];
+    const double Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
+    o.awx[i] = (tx - (Iz - Iy) * wz * wy) / Ix;
+    o.awy[i] = (ty - (Ix - Iz) * wx * wz) / Iy;
+    o.awz[i] = (tz - (Iy - Ix) * wy * wx) / Iz;
+}
+
+// ------------------------------------------------------------ body reduce
+// Level 1: blocks (group g, body b) reduce a contiguous item range in a
+// fixed order; level 2 reduces the groups in order.  Fields: [0..5] load,
+// [6] triangle contacts, [7] max depth, [8] Fz, [9..15] regime counters,
+// [16..37] microstate -> stored as kPtRecord + 6 doubles.
+constexpr int kBodyFields = kBodyFieldCount;
+
+__device__ void accumulate_record(double* acc, const double* rec)
+{
+    for (int f = 0; f < 6; ++f) acc[f] += rec[f];
+    acc[6] += rec[6];
+    acc[7] = fmax(acc[7], rec[7]);
+    acc[8] += rec[8];
+    const int st = (int)rec[9];
+    if (st & 1) {
+        const bool sl = (st & 2) != 0, tw = (st & 4) != 0;
+        acc[9] += 1.0;
+        acc[9 + (tw ? 3 : (sl ? 2 : 1))] += 1.0;
+        if (sl) acc[13] += 1.0;
+        if (tw) acc[14] += 1.0;
+        if (sl && tw) acc[15] += 1.0;
+        for (int f = 0; f < kMicro; ++f) acc[16 + f] += rec[10 + f];
+    }
+}
+__device__ void combine(double* a, const double* b)
+{
+    for (int f = 0; f < kBodyFields; ++f) a[f] = (f == 7) ? fmax(a[f], b[f]) : a[f] + b[f];
+}
+
+template <typename T>
+__global__ void k_body_partial(Recs r, const SceneC* __restrict__ sc, Bodies bodies, Contacts<T> ct, BodyOut bo)
+{
+    const int b = blockIdx.y;
+    const int total = *ct.pt_total_ptr;
+    const int chunk = (total + bo.groups - 1) / bo.groups;
+    const int beg = blockIdx.x * chunk, end = min(total, beg + chunk);
+    const int bs = bodies.scene[b];
+    const int j = b - sc[bs].body_begin;
+    double acc[kBodyFields];
+    for (int f = 0; f < kBodyFields; ++f) acc[f] = 0.0;
+    for (int item = beg + threadIdx.x; item < end; item += blockDim.x) {
+        const int t = ct.pt_list[item];
+        if (r.meta[t].w != bs) continue;
+        accumulate_record(acc, ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord);
+    }
+    __shared__ double sh[128][kBodyFields + 1];
+    for (int f = 0; f < kBodyFields; ++f) sh[threadIdx.x][f] = acc[f];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) combine(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double* out = bo.partial + ((size_t)b * bo.groups + blockIdx.x) * kBodyFields;
+        for (int f = 0; f < kBodyFields; ++f) out[f] = sh[0][f];
+    }
+}
+
+__global__ void k_body_final(BodyOut bo, int nb, int interval)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    double acc[kBodyFields];
+    for (int f = 0; f < kBodyFields; ++f) acc[f] = 0.0;
+    for (int g = 0; g < bo.groups; ++g) combine(acc, bo.partial + ((size_t)b * bo.groups + g) * kBodyFields);
+    double* res = bo.result + (size_t)b * kBodyFields;
+    for (int f = 0; f < kBodyFields; ++f) res[f] = acc[f];
+    if (interval) {
+        for (int f = 0; f < kRegime; ++f) bo.reg_int[b * kRegime + f] += (unsigned long long)acc[9 + f];
+        for (int f = 0; f < kMicro; ++f) bo.micro_int[b * kMicro + f] += acc[16 + f];
+        if (b == 0) *bo.native_steps += 1ull;
+    }
+}
+
+// ------------------------------------------------ body output assembly
+template <typename T>
+__global__ void k_body_outputs(Comps c, Owners o, Bodies bodies, const SceneC* __restrict__ sc, Contacts<T> ct,
+                               double* bp, double* bd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (i >= o.n) return;
+    double acc[25];
+    for (int f = 0; f < 25; ++f) acc[f] = 0.0;
+    const int s = o.scene[i];
+    if (bodies.scene[b] == s && ct.pt_out) {
+        const int j = b - sc[s].body_begin;
+        const int c0 = c.sphere ? i : c.ostart[i], c1 = c.sphere ? i + 1 : c.ostart[i + 1];
+        for (int ci = c0; ci < c1; ++ci) {
+            const int pk = ct.pt_index[ci];
+            if (pk < 0) continue;
+            const double* src = ct.pt_out + ((size_t)pk * ct.nbs + j) * 25;
+            for (int f = 0; f < 24; ++f) acc[f] += src[f];
+            acc[24] = fmax(acc[24], src[24]);
+        }
+    }
+    if (bp) for (int f = 0; f < 6; ++f) bp[((size_t)b * o.n + i) * 6 + f] = acc[f];
+    if (bd) for (int f = 0; f < 19; ++f) bd[((size_t)b * o.n + i) * 19 + f] = acc[6 + f];
+}
+
+inline int blocks(int n, int b) { return (n + b - 1) / b; }
+
+}  // namespace
+
+template <typename T>
+void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
+                   cudaStream_t s)
+{
+    k_gather<T><<<sm_count * 8, 256, 0, s>>>(c, o, g, r, dt_eff);
+}
+
+template <typename T>
+void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs& r, const SceneC* sc, const Walls& w,
+                     const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<T> hb, Contacts<T> ct,
+                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s)
+{
+    (void)o;
+    (void)block;
+    k_broadphase<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, w, t, hp, hw, hb, ct, k, dt_eff);
+    k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff);
+    if (t.nt > 0 && b.nb > 0) {
+        launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);
+        k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list,
+                                                  ct.pt_index, ct.pt_total_ptr);
+        k_pt<T><<<sm_count * 4, 128, 0, s>>>(r, sc, t, b, hb, ct, k, dt_eff);
+    }
+}
+
+template <typename T>
+void launch_owner_sum(const Comps& c, const Owners& o, const SceneC* sc, Contacts<T> ct, bool outputs, double* fc,
+                      double* ff, double* fw, double* ft, cudaStream_t s)
+{
+    k_owner_sum<T><<<blocks(o.n, 256), 256, 0, s>>>(c, o, sc, ct, outputs ? 1 : 0, fc, ff, fw, ft);
+}
+
+template <typename T>
+void launch_body_reduce(const Recs& r, const SceneC* sc, const Bodies& b, Contacts<T> ct, BodyOut bo, bool interval,
+                        cudaStream_t s)
+{
+    if (b.nb <= 0) return;
+    k_body_partial<T><<<dim3(bo.groups, b.nb), 128, 0, s>>>(r, sc, b, ct, bo);
+    k_body_final<<<blocks(b.nb, 32), 32, 0, s>>>(bo, b.nb, interval ? 1 : 0);
+}
+
+template <typename T>
+void launch_body_outputs(const Comps& c, const Owners& o, const Bodies& b, const SceneC* sc, Contacts<T> ct,
+                         double* bp, double* bd, cudaStream_t s)
+{
+    if (b.nb <= 0) return;
+    k_body_outputs<T><<<dim3(blocks(o.n, 128), b.nb), 128, 0, s>>>(c, o, b, sc, ct, bp, bd);
+}
+
+#define DEM_INSTANTIATE(T)                                                                                            \
+    template void launch_gather<T>(const Comps&, const Owners&, const Grid&, const Recs&, double, int, cudaStream_t); \
+    template void launch_contacts<T>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,           \
+                                     const Walls&, const Tris&, const Bodies&, Hist<T>, Hist<T>, Hist<T>,            \
+                                     Contacts<T>, const Counters&, double, int, int, cudaStream_t);                 \
+    template void launch_owner_sum<T>(const Comps&, const Owners&, const SceneC*, Contacts<T>, bool, double*,       \
+                                      double*, double*, double*, cudaStream_t);                                       \
+    template void launch_body_reduce<T>(const Recs&, const SceneC*, const Bodies&, Contacts<T>, BodyOut, bool,       \
+                                        cudaStream_t);                                                                \
+    template void launch_body_outputs<T>(const Comps&, const Owners&, const Bodies&, const SceneC*, Contacts<T>,     \
+                                         double*, double*, cudaStream_t);
+
+DEM_INSTANTIATE(double)
+DEM_INSTANTIATE(float)
+
+}  // namespace demgb

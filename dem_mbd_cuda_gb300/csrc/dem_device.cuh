@@ -1,0 +1,301 @@
+// dem_device.cuh -- device math and contact laws of the GB300 DEM engine.
+//
+// The laws restate the reference's constitutive model
+// (src/cuda/cuda_contact_backend.cu:245-311 history response, :319-407 disk /
+// triangle overlap area, :579-706 particle-particle, :708-949 particle-triangle
+// manifold, :951-1063 particle-wall).  They are templated on the arithmetic
+// type T: T = double is the reference's all-FP64 method, T = float is the
+// mixed-precision form in which positions, overlaps and reductions stay FP64
+// and the per-contact force arithmetic and the history run in FP32.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define DEM_DEV __device__ __forceinline__
+
+namespace demgb {
+
+constexpr double kPi = 3.1415926535897932384626433832795;
+constexpr double kGravityConstant = 6.67430e-11;
+constexpr int kPSlots = 64;   // particle history slots per component
+constexpr int kWSlots = 16;   // wall history slots per component
+constexpr int kBSlots = 64;   // body history slots per component
+constexpr int kRegime = 7;
+constexpr int kMicro = 22;
+constexpr int kPtRecord = 32;  // doubles per (PT component, body) record
+
+template <typename T> struct V3 { T x, y, z; };
+
+template <typename T> DEM_DEV V3<T> mk(T x, T y, T z) { return {x, y, z}; }
+template <typename T> DEM_DEV V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename T> DEM_DEV V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename T> DEM_DEV V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
+template <typename T> DEM_DEV T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename T> DEM_DEV V3<T> cross(V3<T> a, V3<T> b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <typename T> DEM_DEV T norm(V3<T> a) { return sqrt(dot(a, a)); }
+template <typename T> DEM_DEV V3<T> normalized(V3<T> a)
+{
+    const T l = norm(a);
+    return l > T(1.0e-14) ? a * (T(1) / l) : mk<T>(0, 0, 0);
+}
+template <typename T, typename S> DEM_DEV V3<T> cvt(V3<S> a) { return {T(a.x), T(a.y), T(a.z)}; }
+
+// Overlap predicate operand with a fixed contraction pattern so the contact
+// set is decided by the same bits as the oracle and the reference build:
+// fma(dz, dz, fma(dy, dy, dx * dx)).
+DEM_DEV double distance_squared(V3<double> d)
+{
+    return __fma_rn(d.z, d.z, __fma_rn(d.y, d.y, __dmul_rn(d.x, d.x)));
+}
+
+// Quat2IvDCM rotation (src/cuda/cuda_contact_backend.cu:109-116).
+DEM_DEV V3<double> rot_iv(double qw, double qx, double qy, double qz, V3<double> v)
+{
+    return {(1.0 - 2.0 * (qy * qy + qz * qz)) * v.x + 2.0 * (qx * qy - qw * qz) * v.y + 2.0 * (qx * qz + qw * qy) * v.z,
+            2.0 * (qx * qy + qw * qz) * v.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * v.y + 2.0 * (qy * qz - qw * qx) * v.z,
+            2.0 * (qx * qz - qw * qy) * v.x + 2.0 * (qy * qz + qw * qx) * v.y + (1.0 - 2.0 * (qx * qx + qy * qy)) * v.z};
+}
+
+// packCell (src/cuda/cuda_grid_backend.cu:19-26).
+__host__ __device__ inline uint64_t pack_cell(int x, int y, int z)
+{
+    constexpr int bias = 1 << 20;
+    constexpr uint64_t mask = (1ull << 21) - 1ull;
+    return ((static_cast<uint64_t>(x + bias) & mask) << 42) | ((static_cast<uint64_t>(y + bias) & mask) << 21) |
+           (static_cast<uint64_t>(z + bias) & mask);
+}
+__host__ __device__ inline void unpack_cell(uint64_t k, int& x, int& y, int& z)
+{
+    constexpr int bias = 1 << 20;
+    constexpr uint64_t mask = (1ull << 21) - 1ull;
+    x = static_cast<int>((k >> 42) & mask) - bias;
+    y = static_cast<int>((k >> 21) & mask) - bias;
+    z = static_cast<int>(k & mask) - bias;
+}
+
+// Material constants of one contact class, hoisted once per scene.  The
+// logarithms and the denominators pi^2 + log^2 are the exact values the
+// reference recomputes per contact (:619-626).
+struct MatC {
+    double kN, kS, logN, logS, denN, denS, mu, muT, muR, beta, coh, dt;
+};
+
+// ---------------------------------------------------------------- history
+// transportTangentHistory (:245-256)
+template <typename T> DEM_DEV V3<T> transport_tangent(V3<T> prev, V3<T> n)
+{
+    const T pn = norm(prev);
+    const V3<T> proj = prev - n * dot(prev, n);
+    const T qn = norm(proj);
+    if (pn <= T(1.0e-30) || qn <= T(1.0e-30)) return mk<T>(0, 0, 0);
+    return proj * (pn / qn);
+}
+// transportAxialHistory (:258-265)
+template <typename T> DEM_DEV V3<T> transport_axial(V3<T> prev, V3<T> n)
+{
+    const T pn = norm(prev);
+    if (pn <= T(1.0e-30)) return mk<T>(0, 0, 0);
+    const T al = dot(prev, n);
+    if (fabs(al) <= T(1.0e-30)) return mk<T>(0, 0, 0);
+    return n * (al < T(0) ? -pn : pn);
+}
+// limitedHistoryResponseRates (:267-299).  `stored` receives the new history
+// value (only meaningful when the caller stores it).
+template <typename T>
+DEM_DEV V3<T> limited_rates(V3<T> hrate, V3<T> rrate, T k, T c, T dt, V3<T> prev, T limit, V3<T>& stored, bool& yielded)
+{
+    const V3<T> delta = hrate * dt;
+    const V3<T> inc = delta * k;
+    const V3<T> et = inc + prev;
+    const V3<T> trial = rrate * c + et;
+    const T tn = norm(et);
+    yielded = tn > limit;
+    if (yielded) {
+        V3<T> resp;
+        const T dn = norm(delta);
+        if (dn > T(1.0e-14)) {
+            resp = et * (limit / tn);
+        } else {
+            const T pn = norm(prev);
+            resp = pn > T(1.0e-14) ? prev * (limit / pn) : mk<T>(0, 0, 0);
+        }
+        stored = resp;
+        return resp;
+    }
+    stored = prev + inc;
+    return trial;
+}
+// wallHistoryResponse (:951-973)
+template <typename T>
+DEM_DEV V3<T> wall_response(V3<T> rate, T k, T c, T dt, V3<T> prev, T limit, bool check_damped, bool zero_at_zero,
+                            V3<T>& stored)
+{
+    const V3<T> delta = rate * dt;
+    const V3<T> et = prev + delta * k;
+    const V3<T> st = et + rate * c;
+    const T tn = norm(check_damped ? st : et);
+    if (tn > limit) {
+        const T dn = norm(delta);
+        const V3<T> lt = check_damped ? st : et;
+        const V3<T> resp = (dn > T(1.0e-14) && tn > T(1.0e-14)) ? lt * (limit / tn)
+                                                                  : (zero_at_zero ? mk<T>(0, 0, 0) : prev);
+        stored = resp;
+        return resp;
+    }
+    stored = et;
+    return st;
+}
+
+template <typename T> DEM_DEV V3<T> hload(const T* v, int cat) { return {v[3 * cat], v[3 * cat + 1], v[3 * cat + 2]}; }
+template <typename T> DEM_DEV void hstore(T* v, int cat, V3<T> x)
+{
+    v[3 * cat] = x.x; v[3 * cat + 1] = x.y; v[3 * cat + 2] = x.z;
+}
+
+// Damping coefficients of the reference's restitution model (:619-632).
+template <typename T> struct LawC { T kN, kS, cN, cS, kT, cT, kR, cR, brs; };
+template <typename T> DEM_DEV LawC<T> law_constants(const MatC& m, T mred, T radius_term)
+{
+    LawC<T> c;
+    c.kN = T(m.kN);
+    c.kS = T(m.kS);
+    c.cN = T(-2.0) * T(m.logN) * sqrt(c.kN * mred / T(m.denN));
+    c.cS = T(-2.0) * T(m.logS) * sqrt(c.kS * mred / T(m.denS));
+    c.brs = T(m.beta) * radius_term * T(m.beta) * radius_term;
+    c.kT = T(2.0) * c.kS * c.brs;
+    c.cT = T(2.0) * c.cS * c.brs;
+    c.kR = c.kN * c.brs;
+    c.cR = c.cN * c.brs;
+    return c;
+}
+
+// ------------------------------------------------------------ PP contact
+// particleContact (:579-706) after the overlap test and slot acquisition.
+// n: unit direction i->j; erv/mrv: endpoint/midpoint velocity of j minus i;
+// h: history slot values [roll, tangent, twist] updated in place.
+template <typename T>
+DEM_DEV void pp_law(const MatC& m, T dt, V3<T> n, T d, T depth, T d2, T ri, T rj, T mi, T mj, V3<T> erv, V3<T> mrv,
+                    V3<T> ewi, V3<T> ewj, V3<T> mwi, V3<T> mwj, T* h, V3<T>& force, V3<T>& couple)
+{
+    const T mred = mi * mj / (mi + mj);
+    const T rs = ri + rj;
+    const T reff = ri * rj / rs;
+    const LawC<T> c = law_constants<T>(m, mred, reff);
+    V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(erv, n));
+    fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
+    const T li = (ri * ri - rj * rj + d2) / (T(2.0) * d);
+    const T lj = d - li;
+    V3<T> etv = erv - n * dot(erv, n);
+    etv = etv + cross(n, ewi) * li;
+    etv = etv + cross(n, ewj) * lj;
+    V3<T> mtv = mrv - n * dot(mrv, n);
+    mtv = mtv + cross(n, mwi) * li;
+    mtv = mtv + cross(n, mwj) * lj;
+    bool y;
+    V3<T> st;
+    const V3<T> fr = limited_rates<T>(mtv, etv, c.kS, c.cS, dt, transport_tangent(hload(h, 1), n), T(m.mu) * norm(fn),
+                                      st, y);
+    hstore(h, 1, st);
+    const V3<T> erw = ewj - ewi, mrw = mwj - mwi;
+    const V3<T> etw = n * dot(erw, n), mtw = n * dot(mrw, n);
+    const V3<T> erl = erw - etw, mrl = mrw - mtw;
+    const T ms = T(m.beta) * reff * norm(fn);
+    const V3<T> tw = limited_rates<T>(mtw, etw, c.kT, c.cT, dt, transport_axial(hload(h, 2), n),
+                                      T(m.mu) * T(m.muT) * ms, st, y);
+    hstore(h, 2, st);
+    const V3<T> rl = limited_rates<T>(mrl, erl, c.kR, c.cR, dt, transport_tangent(hload(h, 0), n), T(m.muR) * ms, st, y);
+    hstore(h, 0, st);
+    force = fn + fr;
+    couple = (tw + rl) + cross(n, fr) * li;
+}
+
+// ---------------------------------------------------------- wall contact
+// wallContact (:975-1063) after the slot acquisition; out = outward normal.
+template <typename T>
+DEM_DEV void wall_law(const MatC& m, T dt, V3<T> out, T depth, T r, T mass, V3<T> vel, V3<T> om, T* h, V3<T>& force,
+                      V3<T>& couple)
+{
+    const V3<T> n = out * T(-1.0);
+    const T lever = r - depth;
+    const V3<T> rv = vel * T(-1.0);
+    V3<T> tv = rv - n * dot(rv, n);
+    tv = tv + cross(n, om) * lever;
+    const V3<T> rw = om * T(-1.0);
+    const V3<T> twr = n * dot(rw, n);
+    V3<T> rlr = rw - twr;
+    if (fabs(lever) > T(1.0e-30)) rlr = rlr + cross(n, tv) * (T(0.5) / lever);
+    const LawC<T> c = law_constants<T>(m, mass, r);
+    const V3<T> en = n * (-c.kN * depth);
+    const V3<T> dn = n * (c.cN * dot(rv, n));
+    const V3<T> fn = en + dn;
+    const T flim = T(m.mu) * norm(fn);
+    const T ms = T(m.beta) * r * norm(fn);
+    V3<T> st;
+    const V3<T> fr = wall_response<T>(tv, c.kS, c.cS, dt, transport_tangent(hload(h, 1), n), flim, false, false, st);
+    hstore(h, 1, st);
+    const V3<T> tw = wall_response<T>(twr, c.kT, c.cT, dt, transport_axial(hload(h, 2), n), T(m.mu) * T(m.muT) * ms,
+                                      false, true, st);
+    hstore(h, 2, st);
+    const V3<T> rl = wall_response<T>(rlr, c.kR, c.cR, dt, transport_tangent(hload(h, 0), n), T(m.muR) * ms, true, true,
+                                      st);
+    hstore(h, 0, st);
+    force = fn + fr;
+    couple = (tw + rl) + cross(n, fr) * lever;
+}
+
+// ----------------------------------------------------------- disk area
+// circleEdgeArea (:319-358), 2-D coordinates relative to the disk centre.
+template <typename T> DEM_DEV T circle_edge_area(T ax, T ay, T bx, T by, T r)
+{
+    const T dx = bx - ax, dy = by - ay;
+    const T aa = dx * dx + dy * dy;
+    T cuts[4] = {T(0), T(1), T(0), T(0)};
+    int n = 2;
+    if (aa > T(1.0e-30)) {
+        const T bb = T(2.0) * (ax * dx + ay * dy);
+        const T cc = (ax * ax + ay * ay) - r * r;
+        const T disc = bb * bb - T(4.0) * aa * cc;
+        if (disc > T(0)) {
+            const T root = sqrt(disc);
+            const T t0 = (-bb - root) / (T(2.0) * aa);
+            const T t1 = (-bb + root) / (T(2.0) * aa);
+            if (t0 > T(0) && t0 < T(1)) cuts[n++] = t0;
+            if (t1 > T(0) && t1 < T(1)) cuts[n++] = t1;
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j)
+            if (cuts[j] < cuts[i]) { const T tmp = cuts[i]; cuts[i] = cuts[j]; cuts[j] = tmp; }
+    T area = T(0);
+    for (int i = 0; i + 1 < n; ++i) {
+        const T ta = cuts[i], tb = cuts[i + 1];
+        const T ux = ax + dx * ta, uy = ay + dy * ta;
+        const T vx = ax + dx * tb, vy = ay + dy * tb;
+        const T tm = T(0.5) * (ta + tb);
+        const T mx = ax + dx * tm, my = ay + dy * tm;
+        const T cr = ux * vy - uy * vx;
+        if (mx * mx + my * my <= r * r) area += T(0.5) * cr;
+        else area += T(0.5) * r * r * atan2(cr, ux * vx + uy * vy);
+    }
+    return area;
+}
+
+// circleTriangleArea (:360-378).  ra, rb, rc: triangle vertices minus the
+// disk centre.
+template <typename T> DEM_DEV T circle_triangle_area(V3<T> normal, V3<T> ra, V3<T> rb, V3<T> rc, T r)
+{
+    const V3<T> axis = fabs(normal.x) < T(0.8) ? mk<T>(1, 0, 0) : mk<T>(0, 1, 0);
+    const V3<T> u = normalized(cross(normal, axis));
+    const V3<T> v = cross(normal, u);
+    const T ax = dot(ra, u), ay = dot(ra, v), bx = dot(rb, u), by = dot(rb, v), cx = dot(rc, u), cy = dot(rc, v);
+    T area = circle_edge_area<T>(ax, ay, bx, by, r) + circle_edge_area<T>(bx, by, cx, cy, r) +
+             circle_edge_area<T>(cx, cy, ax, ay, r);
+    area = fabs(area);
+    return fmin(area, T(kPi) * r * r);
+}
+
+}  // namespace demgb

@@ -1,0 +1,1319 @@
+// dem_engine.cu -- host side of the GB300 DEM engine and its C ABI.
+//
+// Engine::init restates CudaDemSolver::initialize (src/cuda_backend_cuda.cu:
+// 302-381, component ordering of uploadComponents :121-190); forces() the
+// pipeline of computeForces (:383-524); the leapfrog entry points :526-543;
+// the checkpoint the DMHIST2 format of :545-822.  runSteps() drives the
+// integration loop of src/cuda_simulation_integrator.cpp:245-446 with the
+// host MBD step of src/dyneq.cpp:97-130.
+#include "../../include/dem_gb300.h"
+#include "dem_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+namespace demgb {
+
+static thread_local std::string g_last_error;
+
+struct DemError : std::runtime_error {
+    int code;
+    DemError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+static void check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw DemError(DEM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+class DeviceArena {
+public:
+    ~DeviceArena() { release(); }
+    template <typename T> T* alloc(size_t count, const char* what)
+    {
+        if (count == 0) count = 1;
+        void* p = nullptr;
+        check(cudaMalloc(&p, count * sizeof(T)), what);
+        ptrs_.push_back(p);
+        bytes_ += count * sizeof(T);
+        return static_cast<T*>(p);
+    }
+    template <typename T> T* upload(const T* src, size_t count, const char* what, cudaStream_t s)
+    {
+        T* d = alloc<T>(count, what);
+        if (count && src) check(cudaMemcpyAsync(d, src, count * sizeof(T), cudaMemcpyHostToDevice, s), what);
+        return d;
+    }
+    void release()
+    {
+        for (void* p : ptrs_) cudaFree(p);
+        ptrs_.clear();
+        bytes_ = 0;
+    }
+    size_t bytes() const { return bytes_; }
+
+private:
+    std::vector<void*> ptrs_;
+    size_t bytes_ = 0;
+};
+
+static MatC make_mat(const dem_mech& m, double dt)
+{
+    MatC c;
+    c.kN = m.kN;
+    c.kS = 2.0 * m.kN / 7.0;
+    c.logN = std::log(m.epsN);
+    c.logS = std::log(m.epsS);
+    c.denN = kPi * kPi + c.logN * c.logN;
+    c.denS = kPi * kPi + c.logS * c.logS;
+    c.mu = m.mu; c.muT = m.muT; c.muR = m.muR; c.beta = m.beta; c.coh = m.cohesion;
+    c.dt = dt;
+    return c;
+}
+
+class Engine {
+public:
+    ~Engine()
+    {
+        if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+        if (graph_exec_mbd_) cudaGraphExecDestroy(graph_exec_mbd_);
+        for (auto* e : ev_) if (e) cudaEventDestroy(e);
+        arena_.release();
+        if (pinned_) cudaFreeHost(pinned_);
+        if (stream_) cudaStreamDestroy(stream_);
+    }
+
+    // ---------------------------------------------------------------- init
+    void init(const dem_scene* scenes, int nscenes, const dem_options* opt)
+    {
+        if (initialized_) throw DemError(DEM_ERR_STATE, "CUDA DEM solver already initialized");
+        if (!scenes || nscenes <= 0) throw DemError(DEM_ERR_INVALID, "no scenes");
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0)
+            throw DemError(DEM_ERR_NO_DEVICE, "no CUDA device is available");
+        dem_options o;
+        dem_default_options(&o);
+        if (opt) o = *opt;
+        if (o.cell_factor < 2.0) throw DemError(DEM_ERR_INVALID, "cell_factor must be >= 2");
+        precision_ = o.precision;
+        cell_factor_ = o.cell_factor;
+        block_ = o.block_size > 0 ? o.block_size : 128;
+        check(cudaFree(nullptr), "initialize CUDA context");
+        int dev = 0;
+        check(cudaGetDevice(&dev), "cudaGetDevice");
+        check(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        size_t total_mem = 0;
+        check(cudaMemGetInfo(&free_before_, &total_mem), "cudaMemGetInfo");
+        check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto*& e : ev_) check(cudaEventCreate(&e), "cudaEventCreate");
+
+        S_ = nscenes;
+        dt_ = scenes[0].dt;
+        // ---- concatenate scenes on the host
+        std::vector<int> oid, ost, oscene;
+        std::vector<double> om, orad, oin, opos, ovel, oomg, oq;
+        std::vector<int> cown, cid;
+        std::vector<double> crad, cbody;
+        std::vector<double> wo, wn;
+        std::vector<double> bmass, bc, bq, bv, bw, bin;
+        std::vector<int> bstate, bscene;
+        std::vector<int> tbody, tscene;
+        std::vector<double> tloc;
+        std::vector<SceneC> sc(nscenes);
+        bool any_clump = false, any_ug = false;
+        nbs_ = 0;
+        for (int s = 0; s < nscenes; ++s) {
+            const dem_scene& x = scenes[s];
+            if (x.n_owners <= 0) throw DemError(DEM_ERR_INVALID, "CUDA DEM solver requires particles");
+            if (x.dt != dt_) throw DemError(DEM_ERR_INVALID, "all scenes of a batch must share dt");
+            if (!x.owner_id || !x.owner_status || !x.owner_mass || !x.owner_radius || !x.owner_inertia ||
+                !x.owner_pos || !x.owner_vel || !x.owner_omega || !x.owner_quat)
+                throw DemError(DEM_ERR_INVALID, "scene owner arrays must not be NULL");
+            std::unordered_set<int> ids;
+            ids.reserve((size_t)x.n_owners);
+            for (int i = 0; i < x.n_owners; ++i)
+                if (!ids.insert(x.owner_id[i]).second)
+                    throw DemError(DEM_ERR_INVALID, "duplicate particle ID " + std::to_string(x.owner_id[i]) +
+                                                        "; contact history requires stable unique particle IDs");
+            const int obase = (int)oid.size();
+            for (int i = 0; i < x.n_owners; ++i) {
+                oid.push_back(x.owner_id[i]); ost.push_back(x.owner_status[i]); oscene.push_back(s);
+                om.push_back(x.owner_mass[i]); orad.push_back(x.owner_radius[i]);
+                for (int a = 0; a < 3; ++a) {
+                    oin.push_back(x.owner_inertia[3 * i + a]); opos.push_back(x.owner_pos[3 * i + a]);
+                    ovel.push_back(x.owner_vel[3 * i + a]); oomg.push_back(x.owner_omega[3 * i + a]);
+                }
+                for (int a = 0; a < 4; ++a) oq.push_back(x.owner_quat[4 * i + a]);
+            }
+            // components: uploadComponents ordering (owner, component id)
+            const int nc = x.n_components > 0 ? x.n_components : x.n_owners;
+            std::vector<int> order(nc);
+            std::iota(order.begin(), order.end(), 0);
+            auto own = [&](int c) { return x.n_components > 0 ? x.comp_owner[c] : c; };
+            auto idf = [&](int c) { return x.n_components > 0 ? x.comp_id[c] : x.owner_id[c]; };
+            if (x.n_components > 0) {
+                any_clump = true;
+                std::sort(order.begin(), order.end(), [&](int a, int b) {
+                    if (own(a) != own(b)) return own(a) < own(b);
+                    return idf(a) < idf(b);
+                });
+            }
+            std::vector<int> per_owner(x.n_owners, 0);
+            for (int k = 0; k < nc; ++k) {
+                const int c = order[k];
+                const int ow = own(c);
+                const double r = x.n_components > 0 ? x.comp_radius[c] : x.owner_radius[c];
+                if (ow < 0 || ow >= x.n_owners || idf(c) < 0 || !std::isfinite(r) || r <= 0.0)
+                    throw DemError(DEM_ERR_INVALID, "invalid native clump component topology");
+                per_owner[ow]++;
+                cown.push_back(obase + ow);
+                cid.push_back(idf(c));
+                crad.push_back(r);
+                for (int a = 0; a < 3; ++a) cbody.push_back(x.n_components > 0 ? x.comp_offset[3 * c + a] : 0.0);
+                max_radius_ = std::max(max_radius_, r);
+                comp_owner_ids_.push_back(x.owner_id[ow]);
+            }
+            for (int i = 0; i < x.n_owners; ++i)
+                if (per_owner[i] < 1 || per_owner[i] > 8)
+                    throw DemError(DEM_ERR_INVALID, "each CUDA owner requires 1 to 8 components");
+            SceneC& S = sc[s];
+            S.pp = make_mat(x.pp, x.dt); S.pt = make_mat(x.pt, x.dt); S.pw = make_mat(x.pw, x.dt);
+            for (int a = 0; a < 3; ++a) S.g[a] = x.gravity[a];
+            S.grav = x.gravity_enabled ? 1 : 0;
+            S.wall_begin = (int)wo.size() / 3;
+            S.wall_count = x.n_walls > 0 ? x.n_walls : 0;
+            for (int w = 0; w < S.wall_count; ++w)
+                for (int a = 0; a < 3; ++a) { wo.push_back(x.wall_origin[3 * w + a]); wn.push_back(x.wall_normal[3 * w + a]); }
+            S.body_begin = (int)bmass.size();
+            S.body_count = x.n_bodies > 0 ? x.n_bodies : 0;
+            nbs_ = std::max(nbs_, S.body_count);
+            for (int b = 0; b < S.body_count; ++b) {
+                bmass.push_back(x.body_mass[b]);
+                for (int a = 0; a < 3; ++a) { bc.push_back(x.body_center[3 * b + a]); bv.push_back(x.body_vel[3 * b + a]); bw.push_back(x.body_omega[3 * b + a]); }
+                for (int a = 0; a < 4; ++a) bq.push_back(x.body_quat[4 * b + a]);
+                for (int a = 0; a < 9; ++a) bin.push_back(x.body_inertia[9 * b + a]);
+                bstate.push_back(x.body_state ? x.body_state[b] : 0);
+                bscene.push_back(s);
+            }
+            if (S.body_count > 0 && x.n_triangles > 0) {
+                for (int t = 0; t < x.n_triangles; ++t) {
+                    const int b = x.tri_body[t];
+                    if (b < 0 || b >= S.body_count) throw DemError(DEM_ERR_INVALID, "triangle body index out of range");
+                    tbody.push_back(S.body_begin + b);
+                    tscene.push_back(s);
+                    for (int a = 0; a < 15; ++a) tloc.push_back(x.tri_local[15 * t + a]);
+                }
+            }
+            if (x.universal_gravity_enabled) any_ug = true;
+            keep_bp_ = keep_bp_ || x.keep_body_particle;
+            keep_bd_ = keep_bd_ || x.keep_body_detail;
+            grav_.push_back(x.gravity_enabled ? 1 : 0);
+            gvec_.push_back({x.gravity[0], x.gravity[1], x.gravity[2]});
+        }
+        n_ = (int)oid.size();
+        nc_ = (int)cown.size();
+        nw_ = (int)wo.size() / 3;
+        nb_ = (int)bmass.size();
+        nt_ = (int)tbody.size();
+        sphere_ = !any_clump;
+        owner_ids_ = oid;
+        comp_ids_ = cid;
+        comp_radius_ = crad;
+        comp_body_ = cbody;
+        body_mass_ = bmass; body_inertia_ = bin; body_state_ = bstate; body_scene_ = bscene;
+        hbc_ = bc; hbq_ = bq; hbv_ = bv; hbw_ = bw;
+        mesh_ = cell_factor_ * max_radius_;
+        if (!(mesh_ > 0.0)) throw DemError(DEM_ERR_INVALID, "invalid mesh size");
+        cudaStream_t s = stream_;
+
+        // ---- owners
+        O_.n = n_;
+        auto col = [&](const std::vector<double>& v, int stride, int a) {
+            std::vector<double> out(n_);
+            for (int i = 0; i < n_; ++i) out[i] = v[(size_t)stride * i + a];
+            return out;
+        };
+        auto upd = [&](const std::vector<double>& v, const char* w) { return arena_.upload(v.data(), v.size(), w, s); };
+        std::vector<std::vector<double>> cols;
+        for (int a = 0; a < 3; ++a) cols.push_back(col(opos, 3, a));
+        for (int a = 0; a < 3; ++a) cols.push_back(col(ovel, 3, a));
+        for (int a = 0; a < 3; ++a) cols.push_back(col(oomg, 3, a));
+        for (int a = 0; a < 4; ++a) cols.push_back(col(oq, 4, a));
+        for (int a = 0; a < 3; ++a) cols.push_back(col(oin, 3, a));
+        O_.px = upd(cols[0], "px"); O_.py = upd(cols[1], "py"); O_.pz = upd(cols[2], "pz");
+        O_.vx = upd(cols[3], "vx"); O_.vy = upd(cols[4], "vy"); O_.vz = upd(cols[5], "vz");
+        O_.wx = upd(cols[6], "wx"); O_.wy = upd(cols[7], "wy"); O_.wz = upd(cols[8], "wz");
+        O_.qw = upd(cols[9], "qw"); O_.qx = upd(cols[10], "qx"); O_.qy = upd(cols[11], "qy"); O_.qz = upd(cols[12], "qz");
+        O_.ix = upd(cols[13], "ix"); O_.iy = upd(cols[14], "iy"); O_.iz = upd(cols[15], "iz");
+        O_.mass = upd(om, "mass"); O_.radius = upd(orad, "radius");
+        double** zeros[] = {&O_.ax, &O_.ay, &O_.az, &O_.awx, &O_.awy, &O_.awz, &O_.vhx, &O_.vhy, &O_.vhz,
+                            &O_.whx, &O_.why, &O_.whz, &O_.hqw, &O_.hqx, &O_.hqy, &O_.hqz};
+        for (double** z : zeros) {
+            *z = arena_.alloc<double>(n_, "owner state");
+            check(cudaMemsetAsync(*z, 0, sizeof(double) * n_, s), "clear owner state");
+        }
+        O_.id = arena_.upload(oid.data(), oid.size(), "id", s);
+        O_.status = arena_.upload(ost.data(), ost.size(), "status", s);
+        O_.scene = arena_.upload(oscene.data(), oscene.size(), "scene", s);
+        if (any_ug) {
+            O_.ugx = arena_.alloc<double>(n_, "ug"); O_.ugy = arena_.alloc<double>(n_, "ug"); O_.ugz = arena_.alloc<double>(n_, "ug");
+        }
+
+        // ---- components
+        C_.n = nc_;
+        C_.sphere = sphere_ ? 1 : 0;
+        C_.owner = arena_.upload(cown.data(), cown.size(), "comp owner", s);
+        C_.cid = arena_.upload(cid.data(), cid.size(), "comp id", s);
+        C_.radius = arena_.upload(crad.data(), crad.size(), "comp radius", s);
+        if (sphere_) {
+            C_.x = O_.px; C_.y = O_.py; C_.z = O_.pz; C_.vx = O_.vx; C_.vy = O_.vy; C_.vz = O_.vz;
+            C_.vhx = O_.vhx; C_.vhy = O_.vhy; C_.vhz = O_.vhz;
+        } else {
+            std::vector<int> ostart(n_ + 1, 0);
+            for (int c = 0; c < nc_; ++c) ostart[cown[c] + 1]++;
+            for (int i = 0; i < n_; ++i) ostart[i + 1] += ostart[i];
+            C_.ostart = arena_.upload(ostart.data(), ostart.size(), "ostart", s);
+            std::vector<double> bx(nc_), by(nc_), bz(nc_);
+            for (int c = 0; c < nc_; ++c) { bx[c] = cbody[3 * c]; by[c] = cbody[3 * c + 1]; bz[c] = cbody[3 * c + 2]; }
+            C_.bx = upd(bx, "bx"); C_.by = upd(by, "by"); C_.bz = upd(bz, "bz");
+            double** cw[] = {&C_.x, &C_.y, &C_.z, &C_.vx, &C_.vy, &C_.vz, &C_.vhx, &C_.vhy, &C_.vhz, &C_.ox, &C_.oy, &C_.oz};
+            for (double** z : cw) *z = arena_.alloc<double>(nc_, "component world state");
+        }
+
+        // ---- grid
+        long long cap = o.max_cells > 0 ? o.max_cells : std::max<long long>(16LL * nc_, 1LL << 22);
+        cap = std::min<long long>(cap, (1LL << 31) - 64);
+        G_.capacity = (int)cap;
+        G_.nscenes = S_;
+        G_.mesh = mesh_;
+        G_.inv_mesh = 1.0 / mesh_;
+        G_.mesh_f = (float)mesh_;
+        G_.margin_f = (float)(1.0e-5 * mesh_);
+        G_.ckey = arena_.alloc<uint64_t>(nc_, "ckey");
+        G_.clin = arena_.alloc<int>(nc_, "clin");
+        G_.crank = arena_.alloc<int>(nc_, "crank");
+        G_.cell_count = arena_.alloc<int>(cap + 1, "cell count");
+        check(cudaMemsetAsync(G_.cell_count, 0, sizeof(int) * (cap + 1), s), "clear cell count");
+        G_.cell_start = arena_.alloc<int>(cap + 2, "cell start");
+        G_.sorted_id = arena_.alloc<int>(nc_, "sorted id");
+        G_.pos_of = arena_.alloc<int>(nc_, "pos of");
+        G_.sorted_key = arena_.alloc<uint64_t>(nc_, "sorted key");
+        std::vector<int> box(6 * S_);
+        for (int q = 0; q < S_; ++q) { box[6 * q] = box[6 * q + 1] = box[6 * q + 2] = INT_MAX; box[6 * q + 3] = box[6 * q + 4] = box[6 * q + 5] = INT_MIN; }
+        G_.scene_box = arena_.upload(box.data(), box.size(), "scene box", s);
+        G_.scene_layout = arena_.alloc<int>(8 * S_, "scene layout");
+        G_.total_cells = arena_.alloc<int>(1, "total cells");
+        G_.nvalid = arena_.alloc<int>(1, "nvalid");
+        G_.tile_sums = arena_.alloc<int>(cap / 4096 + 64, "tile sums");
+        G_.err = arena_.alloc<unsigned>(1, "err");
+        check(cudaMemsetAsync(G_.err, 0, sizeof(unsigned), s), "clear err");
+
+        // ---- records
+        R_.pos = arena_.alloc<D4>(nc_, "rec pos"); R_.v = arena_.alloc<D4>(nc_, "rec v");
+        R_.vm = arena_.alloc<D4>(nc_, "rec vm"); R_.w = arena_.alloc<D4>(nc_, "rec w");
+        R_.wm = arena_.alloc<D4>(nc_, "rec wm");
+        R_.off = sphere_ ? nullptr : arena_.alloc<D4>(nc_, "rec off");
+        R_.meta = arena_.alloc<int4>(nc_, "rec meta"); R_.cell = arena_.alloc<int4>(nc_, "rec cell");
+        R_.relf = arena_.alloc<float4>(nc_, "rec relf");
+
+        // ---- walls, bodies, triangles
+        W_.o = upd(wo, "wall origin"); W_.n = upd(wn, "wall normal");
+        B_.nb = nb_;
+        B_.c = arena_.upload(bc.data(), bc.size(), "body c", s); B_.q = arena_.upload(bq.data(), bq.size(), "body q", s);
+        B_.v = arena_.upload(bv.data(), bv.size(), "body v", s); B_.w = arena_.upload(bw.data(), bw.size(), "body w", s);
+        B_.scene = arena_.upload(bscene.data(), bscene.size(), "body scene", s);
+        T_.nt = nt_;
+        if (nt_ > 0) {
+            T_.body = arena_.upload(tbody.data(), tbody.size(), "tri body", s);
+            T_.scene = arena_.upload(tscene.data(), tscene.size(), "tri scene", s);
+            T_.local = upd(tloc, "tri local");
+            T_.world = arena_.alloc<double>(16 * (size_t)nt_, "tri world");
+            T_.aabb = arena_.alloc<double>(6 * (size_t)nt_, "tri aabb");
+            // rotation-invariant bound of the cells a padded triangle box covers
+            long long tcap = 0;
+            for (int t = 0; t < nt_; ++t) {
+                const double* L = &tloc[15 * (size_t)t];
+                double cx = 0, cy = 0, cz = 0;
+                for (int k = 0; k < 4; ++k) { cx += L[3 * k]; cy += L[3 * k + 1]; cz += L[3 * k + 2]; }
+                cx /= 4; cy /= 4; cz /= 4;
+                double rho = 0;
+                for (int k = 0; k < 4; ++k)
+                    rho = std::max(rho, std::sqrt((L[3 * k] - cx) * (L[3 * k] - cx) + (L[3 * k + 1] - cy) * (L[3 * k + 1] - cy) +
+                                                  (L[3 * k + 2] - cz) * (L[3 * k + 2] - cz)));
+                const long long per = (long long)std::floor((2 * rho + 2 * max_radius_) / mesh_) + 2;
+                tcap += per * per * per;
+            }
+            tcap = std::min<long long>(tcap + 1024, (1LL << 31) - 64);
+            T_.capacity = (int)tcap;
+            T_.ttri = arena_.alloc<int>(tcap, "tri grid ids");
+            T_.tcell_count = arena_.alloc<int>(cap + 1, "tri cell count");
+            T_.tcell_cursor = arena_.alloc<int>(cap + 1, "tri cell cursor");
+            T_.tcell_start = arena_.alloc<int>(cap + 2, "tri cell start");
+            check(cudaMemsetAsync(T_.tcell_count, 0, sizeof(int) * (cap + 1), s), "clear");
+            check(cudaMemsetAsync(T_.tcell_cursor, 0, sizeof(int) * (cap + 1), s), "clear");
+        }
+
+        // ---- counters
+        int* cnt = arena_.alloc<int>(16, "counters");
+        check(cudaMemsetAsync(cnt, 0, sizeof(int) * 16, s), "clear counters");
+        K_.pcontacts = cnt; K_.pover = cnt + 1; K_.bover = cnt + 2; K_.phigh = cnt + 3; K_.bhigh = cnt + 4;
+        K_.tgover = cnt + 5; K_.ct_total = cnt + 6; K_.pt_total = cnt + 7; K_.step = cnt + 8;
+
+        // ---- scene constants
+        d_sc_ = arena_.upload(sc.data(), sc.size(), "scene constants", s);
+        scenes_h_ = sc;
+
+        // ---- history and contacts
+        if (precision_ == DEM_PRECISION_MIXED) alloc_state<float>(hp32_, hw32_, hb32_, ct32_);
+        else alloc_state<double>(hp64_, hw64_, hb64_, ct64_);
+
+        // ---- body reduction
+        if (nb_ > 0) {
+            BO_.groups = std::max(1, std::min(sm_count_ * 2, (nc_ + 4095) / 4096));
+            BO_.partial = arena_.alloc<double>((size_t)nb_ * BO_.groups * kBodyFieldCount, "body partial");
+            BO_.result = arena_.alloc<double>((size_t)nb_ * kBodyFieldCount, "body result");
+            check(cudaMemsetAsync(BO_.result, 0, sizeof(double) * nb_ * kBodyFieldCount, s), "clear");
+            BO_.reg_int = arena_.alloc<unsigned long long>((size_t)nb_ * kRegime, "regime interval");
+            BO_.micro_int = arena_.alloc<double>((size_t)nb_ * kMicro, "micro interval");
+            BO_.native_steps = arena_.alloc<unsigned long long>(1, "native steps");
+            check(cudaMemsetAsync(BO_.reg_int, 0, sizeof(unsigned long long) * nb_ * kRegime, s), "clear");
+            check(cudaMemsetAsync(BO_.micro_int, 0, sizeof(double) * nb_ * kMicro, s), "clear");
+            check(cudaMemsetAsync(BO_.native_steps, 0, sizeof(unsigned long long), s), "clear");
+        }
+        // pinned staging: body state (13 doubles/body) + body results
+        pinned_bytes_ = sizeof(double) * ((size_t)13 * std::max(nb_, 1) + (size_t)kBodyFieldCount * std::max(nb_, 1) + 64);
+        check(cudaMallocHost(&pinned_, pinned_bytes_), "cudaMallocHost");
+        // host MBD state
+        hbhv_.assign(3 * nb_, 0.0); hbhw_.assign(3 * nb_, 0.0); hbhq_.assign(4 * nb_, 0.0); hbhdq_.assign(4 * nb_, 0.0);
+        hbacc_.assign(3 * nb_, 0.0); hbdom_.assign(3 * nb_, 0.0); hbloads_.assign(6 * nb_, 0.0);
+        if (nb_ > 0) launch_tri_transform(T_, B_, s);
+        if (!sphere_) launch_update_components(C_, O_, s);
+        check(cudaStreamSynchronize(s), "initialize");
+        initialized_ = true;
+    }
+
+    template <typename T> void alloc_state(Hist<T>& hp, Hist<T>& hw, Hist<T>& hb, Contacts<T>& ct)
+    {
+        cudaStream_t s = stream_;
+        auto mk_hist = [&](Hist<T>& h, int slots) {
+            const size_t n = (size_t)nc_ * slots;
+            h.key = arena_.alloc<uint64_t>(n, "history keys");
+            h.last = arena_.alloc<int>(n, "history last seen");
+            h.val = arena_.alloc<T>(n * 9, "history values");
+            h.hw = arena_.alloc<int>(nc_, "history hw");
+            check(cudaMemsetAsync(h.key, 0, n * sizeof(uint64_t), s), "clear history keys");
+            check(cudaMemsetAsync(h.last, 0xff, n * sizeof(int), s), "clear history age");
+            check(cudaMemsetAsync(h.val, 0, n * 9 * sizeof(T), s), "clear history values");
+            check(cudaMemsetAsync(h.hw, 0, nc_ * sizeof(int), s), "clear history hw");
+        };
+        mk_hist(hp, kPSlots);
+        mk_hist(hw, kWSlots);
+        mk_hist(hb, kBSlots);
+        ct.capacity = nc_ * kPSlots;
+        ct.ent = arena_.alloc<int4>((size_t)ct.capacity, "contact entries");
+        ct.res = arena_.alloc<T>((size_t)ct.capacity * 6, "contact results");
+        ct.off = arena_.alloc<int>(nc_, "contact offsets");
+        ct.cnt = arena_.alloc<int>(nc_, "contact counts");
+        check(cudaMemsetAsync(ct.cnt, 0, nc_ * sizeof(int), s), "clear");
+        check(cudaMemsetAsync(ct.off, 0, nc_ * sizeof(int), s), "clear");
+        ct.wres = arena_.alloc<double>((size_t)nc_ * 6, "wall results");
+        check(cudaMemsetAsync(ct.wres, 0, (size_t)nc_ * 6 * sizeof(double), s), "clear");
+        ct.pt_index = arena_.alloc<int>(nc_, "pt index");
+        check(cudaMemsetAsync(ct.pt_index, 0xff, nc_ * sizeof(int), s), "clear");
+        ct.pt_flag = arena_.alloc<int>(nc_ + 1, "pt flag");
+        check(cudaMemsetAsync(ct.pt_flag, 0, (nc_ + 1) * sizeof(int), s), "clear");
+        ct.pt_total_ptr = K_.pt_total;
+        ct.nbs = std::max(nbs_, 1);
+        if (nb_ > 0 && nt_ > 0) {
+            ct.pt_pos = arena_.alloc<int>(nc_ + 2, "pt pos");
+            ct.pt_list = arena_.alloc<int>(nc_, "pt list");
+            ct.pt_res = arena_.alloc<double>((size_t)nc_ * 6, "pt results");
+            ct.pt_body = arena_.alloc<double>((size_t)nc_ * ct.nbs * kPtRecord, "pt body records");
+            if (keep_bp_ || keep_bd_) ct.pt_out = arena_.alloc<double>((size_t)nc_ * ct.nbs * 25, "pt outputs");
+        }
+    }
+
+    // ----------------------------------------------------------- pipeline
+    template <typename T>
+    void enqueue_forces(double dt_eff, Hist<T>& hp, Hist<T>& hw, Hist<T>& hb, Contacts<T>& ct, bool timed)
+    {
+        cudaStream_t s = stream_;
+        int e = 0;
+        auto mark = [&]() { if (timed && e < (int)ev_.size()) check(cudaEventRecord(ev_[e++], s), "event"); };
+        mark();
+        launch_step_counter(K_, 1, s);
+        if (!sphere_) launch_update_components(C_, O_, s);
+        launch_grid_build(C_, O_, G_, sm_count_, s);
+        mark();
+        if (nb_ > 0 && nt_ > 0) launch_tri_build(T_, B_, G_, max_radius_, K_.tgover, sm_count_, s);
+        if (O_.ugx) launch_universal_gravity(O_, s);
+        launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
+        mark();
+        launch_contacts<T>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, s);
+        mark();
+        launch_owner_sum<T>(C_, O_, d_sc_, ct, false, nullptr, nullptr, nullptr, nullptr, s);
+        if (nb_ > 0) launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
+        launch_step_counter(K_, 0, s);
+        mark();
+        n_marks_ = e;
+    }
+
+    void forces(double dt_eff, bool timed = false)
+    {
+        if (precision_ == DEM_PRECISION_MIXED) enqueue_forces<float>(dt_eff, hp32_, hw32_, hb32_, ct32_, timed);
+        else enqueue_forces<double>(dt_eff, hp64_, hw64_, hb64_, ct64_, timed);
+        check(cudaGetLastError(), "force pipeline launch");
+    }
+
+    double* pin_body_state() { return static_cast<double*>(pinned_); }
+    double* pin_body_result() { return static_cast<double*>(pinned_) + 13 * std::max(nb_, 1); }
+
+    void upload_body_state_async()
+    {
+        if (nb_ <= 0) return;
+        double* p = pin_body_state();
+        std::memcpy(p, hbc_.data(), sizeof(double) * 3 * nb_);
+        std::memcpy(p + 3 * nb_, hbq_.data(), sizeof(double) * 4 * nb_);
+        std::memcpy(p + 7 * nb_, hbv_.data(), sizeof(double) * 3 * nb_);
+        std::memcpy(p + 10 * nb_, hbw_.data(), sizeof(double) * 3 * nb_);
+        enqueue_body_h2d();
+    }
+    void enqueue_body_h2d()
+    {
+        double* p = pin_body_state();
+        check(cudaMemcpyAsync(B_.c, p, sizeof(double) * 3 * nb_, cudaMemcpyHostToDevice, stream_), "upload body c");
+        check(cudaMemcpyAsync(B_.q, p + 3 * nb_, sizeof(double) * 4 * nb_, cudaMemcpyHostToDevice, stream_), "upload body q");
+        check(cudaMemcpyAsync(B_.v, p + 7 * nb_, sizeof(double) * 3 * nb_, cudaMemcpyHostToDevice, stream_), "upload body v");
+        check(cudaMemcpyAsync(B_.w, p + 10 * nb_, sizeof(double) * 3 * nb_, cudaMemcpyHostToDevice, stream_), "upload body w");
+    }
+    void enqueue_body_d2h()
+    {
+        check(cudaMemcpyAsync(pin_body_result(), BO_.result, sizeof(double) * nb_ * kBodyFieldCount,
+                              cudaMemcpyDeviceToHost, stream_), "download body result");
+    }
+    void body_forces_from_pinned(double* out)
+    {
+        const double* r = pin_body_result();
+        for (int b = 0; b < nb_; ++b) {
+            for (int k = 0; k < 6; ++k) out[6 * b + k] = r[(size_t)b * kBodyFieldCount + k];
+            const int s = body_scene_[b];
+            if (grav_[s]) for (int a = 0; a < 3; ++a) out[6 * b + a] += gvec_[s][a] * body_mass_[b];
+        }
+    }
+
+    // computeForces (src/cuda_backend_cuda.cu:383-524)
+    int compute_forces(const dem_body_states* bodies, double* body_forces, int diag, bool timed = false)
+    {
+        need_init();
+        cudaStream_t s = stream_;
+        if (bodies && nb_ > 0) {
+            std::memcpy(hbc_.data(), bodies->center, sizeof(double) * 3 * nb_);
+            std::memcpy(hbq_.data(), bodies->quat, sizeof(double) * 4 * nb_);
+            std::memcpy(hbv_.data(), bodies->vel, sizeof(double) * 3 * nb_);
+            std::memcpy(hbw_.data(), bodies->omega, sizeof(double) * 3 * nb_);
+            upload_body_state_async();
+        }
+        if (nb_ > 0) launch_tri_transform(T_, B_, s);
+        const double dt_eff = step_index_ == 0 ? 0.0 : dt_;
+        forces(dt_eff, timed);
+        ++step_index_;
+        if (nb_ > 0 && (body_forces || diag)) enqueue_body_d2h();
+        if (diag) return collect_diagnostics(body_forces);
+        if (body_forces && nb_ > 0) {
+            check(cudaStreamSynchronize(s), "compute forces");
+            body_forces_from_pinned(body_forces);
+        }
+        return DEM_OK;
+    }
+
+    int collect_diagnostics(double* body_forces)
+    {
+        cudaStream_t s = stream_;
+        int cnt[16];
+        unsigned err = 0;
+        check(cudaMemcpyAsync(cnt, K_.pcontacts, sizeof(int) * 16, cudaMemcpyDeviceToHost, s), "download counters");
+        check(cudaMemcpyAsync(&err, G_.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "download err");
+        std::vector<unsigned long long> rint(kRegime * std::max(nb_, 1));
+        std::vector<double> mint(kMicro * std::max(nb_, 1));
+        unsigned long long native = 0;
+        if (nb_ > 0) {
+            check(cudaMemcpyAsync(rint.data(), BO_.reg_int, sizeof(unsigned long long) * nb_ * kRegime,
+                                  cudaMemcpyDeviceToHost, s), "download regime interval");
+            check(cudaMemcpyAsync(mint.data(), BO_.micro_int, sizeof(double) * nb_ * kMicro, cudaMemcpyDeviceToHost, s),
+                  "download micro interval");
+            check(cudaMemcpyAsync(&native, BO_.native_steps, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
+                  "download native steps");
+            check(cudaMemsetAsync(BO_.reg_int, 0, sizeof(unsigned long long) * nb_ * kRegime, s), "reset regime interval");
+            check(cudaMemsetAsync(BO_.micro_int, 0, sizeof(double) * nb_ * kMicro, s), "reset micro interval");
+            check(cudaMemsetAsync(BO_.native_steps, 0, sizeof(unsigned long long), s), "reset native steps");
+        }
+        check(cudaStreamSynchronize(s), "collect diagnostics");
+        dem_step_stats st{};
+        st.particle_contacts = cnt[0];
+        st.particle_history_overflows = cnt[1];
+        st.body_history_overflows = cnt[2];
+        st.particle_history_high_water = cnt[3];
+        st.body_history_high_water = cnt[4];
+        st.triangle_grid_overflows = cnt[5];
+        st.cell_table_overflows = (err & kErrCellCapacity) ? 1 : 0;
+        st.body_regime_interval_native_steps = native;
+        reg_inst_.assign((size_t)kRegime * nb_, 0ull);
+        reg_int_.assign(rint.begin(), rint.begin() + (size_t)kRegime * nb_);
+        micro_inst_.assign((size_t)kMicro * nb_, 0.0);
+        micro_int_.assign(mint.begin(), mint.begin() + (size_t)kMicro * nb_);
+        if (nb_ > 0) {
+            const double* r = pin_body_result();
+            double fz = 0.0, md = 0.0;
+            int bc = 0;
+            for (int b = 0; b < nb_; ++b) {
+                const double* x = r + (size_t)b * kBodyFieldCount;
+                bc += (int)x[6];
+                md = std::max(md, x[7]);
+                fz += x[8];
+                for (int f = 0; f < kRegime; ++f) reg_inst_[b * kRegime + f] = (unsigned long long)x[9 + f];
+                for (int f = 0; f < kMicro; ++f) micro_inst_[b * kMicro + f] = x[16 + f];
+            }
+            st.body_contacts = bc;
+            st.body_max_depth = md;
+            st.body_contact_fz = fz;
+            if (body_forces) body_forces_from_pinned(body_forces);
+        }
+        stats_ = st;
+        if (err & kErrKeyRange) throw DemError(DEM_ERR_CAPACITY, "component grid coordinate exceeds signed 21-bit hash range");
+        if (err & kErrCellCapacity)
+            throw DemError(DEM_ERR_CAPACITY, "particle cell box exceeds the dense cell-table capacity; raise dem_options.max_cells");
+        if (st.particle_history_overflows)
+            throw DemError(DEM_ERR_CAPACITY, "CUDA particle contact-history capacity exceeded; increase kGpuParticleHistorySlots");
+        if (st.body_history_overflows)
+            throw DemError(DEM_ERR_CAPACITY, "CUDA wall/body contact-history capacity exceeded; increase the configured history slots");
+        if (st.triangle_grid_overflows || (err & (kErrTriCapacity | kErrTriRange)))
+            throw DemError(DEM_ERR_CAPACITY, "CUDA triangle-grid coordinate/count overflow");
+        return DEM_OK;
+    }
+
+    void leapfrog_init(double h) { need_init(); launch_leapfrog_init(O_, h, stream_); check(cudaGetLastError(), "leapfrog init"); }
+    void advance(double dt) { need_init(); launch_advance(O_, dt, stream_); check(cudaGetLastError(), "advance"); }
+    void finish(double dt) { need_init(); launch_finish(O_, dt, stream_); check(cudaGetLastError(), "finish"); }
+
+    // ------------------------------------------------------- host MBD step
+    // DynEqnBodySet (src/dyneq.cpp:97-130) with Quat2DCM (src/matrixtrans.cpp:36-63).
+    void dyn_eqn(const double* F, double* ddu)
+    {
+        for (int b = 0; b < nb_; ++b) {
+            double* d = ddu + 6 * b;
+            if (body_state_[b] != 0) { for (int k = 0; k < 6; ++k) d[k] = 0.0; continue; }
+            for (int k = 0; k < 3; ++k) d[k] = F[6 * b + k] / body_mass_[b];
+            const double* q = &hbq_[4 * b];
+            const double qq[10] = {q[0] * q[0], q[1] * q[1], q[2] * q[2], q[3] * q[3], 2.0 * q[0] * q[1], 2.0 * q[0] * q[2],
+                                   2.0 * q[0] * q[3], 2.0 * q[1] * q[2], 2.0 * q[1] * q[3], 2.0 * q[2] * q[3]};
+            const double M[9] = {qq[0] + qq[1] - qq[2] - qq[3], qq[7] + qq[6], qq[8] - qq[5],
+                                 qq[7] - qq[6], qq[0] - qq[1] + qq[2] - qq[3], qq[9] + qq[4],
+                                 qq[8] + qq[5], qq[9] - qq[4], qq[0] - qq[1] - qq[2] + qq[3]};
+            const double T[3] = {F[6 * b + 3], F[6 * b + 4], F[6 * b + 5]};
+            double t[3];
+            for (int r = 0; r < 3; ++r) t[r] = M[3 * r] * T[0] + M[3 * r + 1] * T[1] + M[3 * r + 2] * T[2];
+            const double* I = &body_inertia_[9 * b];
+            const double* w = &hbw_[3 * b];
+            d[3] = (t[0] - (I[8] - I[4]) * w[2] * w[1]) / I[0];
+            d[4] = (t[1] - (I[0] - I[8]) * w[0] * w[2]) / I[4];
+            d[5] = (t[2] - (I[4] - I[0]) * w[1] * w[0]) / I[8];
+        }
+    }
+    static void gama(const double* q, const double* w, double* d)
+    {
+        d[0] = 0.5 * (-q[1] * w[0] - q[2] * w[1] - q[3] * w[2]);
+        d[1] = 0.5 * (q[0] * w[0] + q[2] * w[2] - q[3] * w[1]);
+        d[2] = 0.5 * (q[0] * w[1] - q[1] * w[2] + q[3] * w[0]);
+        d[3] = 0.5 * (q[0] * w[2] + q[1] * w[1] - q[2] * w[0]);
+    }
+    static void normalize4(double* q)
+    {
+        const double len = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+        if (len > 1e-10) { const double s = 1.0 / len; for (int k = 0; k < 4; ++k) q[k] *= s; }
+        else for (int k = 0; k < 4; ++k) q[k] = 0.0;
+    }
+    // Body half-step update after the loads (src/cuda_simulation_integrator.cpp:348-374, 401-425).
+    void body_half_update(bool first, double dt)
+    {
+        const double half = 0.5 * dt;
+        std::vector<double> ddu(6 * nb_);
+        dyn_eqn(hbloads_.data(), ddu.data());
+        for (int b = 0; b < nb_; ++b) {
+            double *hv = &hbhv_[3 * b], *hw = &hbhw_[3 * b], *acc = &hbacc_[3 * b], *dom = &hbdom_[3 * b];
+            double *V = &hbv_[3 * b], *W = &hbw_[3 * b];
+            for (int a = 0; a < 3; ++a) { acc[a] = ddu[6 * b + a]; dom[a] = ddu[6 * b + 3 + a]; }
+            const int st = body_state_[b];
+            if (st == 0) {
+                for (int a = 0; a < 3; ++a) {
+                    if (first) { hv[a] = V[a] + acc[a] * half; hw[a] = W[a] + dom[a] * half; }
+                    else { hv[a] += acc[a] * dt; hw[a] += dom[a] * dt; }
+                }
+            } else if (st == 1) {
+                for (int a = 0; a < 3; ++a) {
+                    acc[a] = dom[a] = hv[a] = hw[a] = 0.0;
+                    if (!first) V[a] = W[a] = 0.0;
+                }
+            } else {
+                for (int a = 0; a < 3; ++a) { hv[a] = V[a]; hw[a] = W[a]; }
+            }
+            double d[4], q[4];
+            gama(&hbq_[4 * b], W, d);
+            for (int k = 0; k < 4; ++k) q[k] = hbq_[4 * b + k] + d[k] * half;
+            normalize4(q);
+            std::memcpy(&hbhq_[4 * b], q, sizeof q);
+            gama(q, hw, &hbhdq_[4 * b]);
+        }
+    }
+    void body_position_update(double dt)
+    {
+        const double half = 0.5 * dt;
+        for (int b = 0; b < nb_; ++b) {
+            if (body_state_[b] == 1) continue;
+            for (int a = 0; a < 3; ++a) hbc_[3 * b + a] += hbhv_[3 * b + a] * dt;
+            double q[4];
+            for (int k = 0; k < 4; ++k) q[k] = hbq_[4 * b + k] + hbhdq_[4 * b + k] * dt;
+            normalize4(q);
+            std::memcpy(&hbq_[4 * b], q, sizeof q);
+            for (int a = 0; a < 3; ++a) {
+                hbv_[3 * b + a] = hbhv_[3 * b + a] + hbacc_[3 * b + a] * half;
+                hbw_[3 * b + a] = hbhw_[3 * b + a] + hbdom_[3 * b + a] * half;
+            }
+        }
+    }
+
+    // IntegrateDem / IntegrateDemMultiBody without output frames.
+    void run_steps(int steps)
+    {
+        need_init();
+        const double dt = dt_;
+        if (!started_) {
+            dem_body_states bs{hbc_.data(), hbq_.data(), hbv_.data(), hbw_.data()};
+            compute_forces(nb_ > 0 ? &bs : nullptr, nb_ > 0 ? hbloads_.data() : nullptr, 1);
+            if (!restored_) leapfrog_init(0.5 * dt);
+            if (nb_ > 0) body_half_update(true, dt);
+            started_ = true;
+        }
+        if (steps <= 0) return;
+        if (nb_ == 0) {
+            ensure_graph(false);
+            for (int s = 0; s < steps; ++s) check(cudaGraphLaunch(graph_exec_, stream_), "cudaGraphLaunch");
+            step_index_ += steps;
+            collect_diagnostics(nullptr);
+            return;
+        }
+        ensure_graph(true);
+        for (int s = 0; s < steps; ++s) {
+            body_position_update(dt);
+            double* p = pin_body_state();
+            std::memcpy(p, hbc_.data(), sizeof(double) * 3 * nb_);
+            std::memcpy(p + 3 * nb_, hbq_.data(), sizeof(double) * 4 * nb_);
+            std::memcpy(p + 7 * nb_, hbv_.data(), sizeof(double) * 3 * nb_);
+            std::memcpy(p + 10 * nb_, hbw_.data(), sizeof(double) * 3 * nb_);
+            check(cudaGraphLaunch(graph_exec_mbd_, stream_), "cudaGraphLaunch");
+            check(cudaStreamSynchronize(stream_), "mbd step");
+            ++step_index_;
+            body_forces_from_pinned(hbloads_.data());
+            body_half_update(false, dt);
+        }
+        collect_diagnostics(nullptr);
+    }
+
+    // One step on the stream (advance, optional body upload, forces with dt,
+    // optional body download, finish) captured as a CUDA graph.
+    void ensure_graph(bool mbd)
+    {
+        cudaGraphExec_t& ex = mbd ? graph_exec_mbd_ : graph_exec_;
+        if (ex) return;
+        cudaGraph_t g = nullptr;
+        check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
+        try {
+            launch_advance(O_, dt_, stream_);
+            if (mbd) {
+                enqueue_body_h2d();
+                launch_tri_transform(T_, B_, stream_);
+            }
+            forces(dt_, false);
+            if (mbd) enqueue_body_d2h();
+            launch_finish(O_, dt_, stream_);
+        } catch (...) {
+            cudaStreamEndCapture(stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        check(cudaStreamEndCapture(stream_, &g), "end capture");
+        check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
+        cudaGraphDestroy(g);
+    }
+
+    // Time `steps` graph-launched steps (pure DEM) on the device; the state is
+    // resident.  Returns milliseconds.
+    float time_steps(int steps)
+    {
+        need_init();
+        if (!started_) run_steps(1);
+        ensure_graph(nb_ > 0);
+        cudaEvent_t a, b;
+        check(cudaEventCreate(&a), "event"); check(cudaEventCreate(&b), "event");
+        check(cudaEventRecord(a, stream_), "event");
+        if (nb_ == 0) {
+            for (int s = 0; s < steps; ++s) check(cudaGraphLaunch(graph_exec_, stream_), "launch");
+            step_index_ += steps;
+        } else {
+            for (int s = 0; s < steps; ++s) {
+                body_position_update(dt_);
+                double* p = pin_body_state();
+                std::memcpy(p, hbc_.data(), sizeof(double) * 3 * nb_);
+                std::memcpy(p + 3 * nb_, hbq_.data(), sizeof(double) * 4 * nb_);
+                std::memcpy(p + 7 * nb_, hbv_.data(), sizeof(double) * 3 * nb_);
+                std::memcpy(p + 10 * nb_, hbw_.data(), sizeof(double) * 3 * nb_);
+                check(cudaGraphLaunch(graph_exec_mbd_, stream_), "launch");
+                check(cudaStreamSynchronize(stream_), "mbd step");
+                ++step_index_;
+                body_forces_from_pinned(hbloads_.data());
+                body_half_update(false, dt_);
+            }
+        }
+        check(cudaEventRecord(b, stream_), "event");
+        check(cudaEventSynchronize(b), "event sync");
+        float ms = 0;
+        check(cudaEventElapsedTime(&ms, a, b), "elapsed");
+        cudaEventDestroy(a); cudaEventDestroy(b);
+        return ms;
+    }
+
+    // -------------------------------------------------------------- outputs
+    void download_state(double* pos, double* vel, double* omg, double* quat)
+    {
+        need_init();
+        check(cudaStreamSynchronize(stream_), "sync");
+        auto get3 = [&](double* out, double* x, double* y, double* z) {
+            if (!out) return;
+            std::vector<double> a(n_), b(n_), c(n_);
+            check(cudaMemcpy(a.data(), x, sizeof(double) * n_, cudaMemcpyDeviceToHost), "download");
+            check(cudaMemcpy(b.data(), y, sizeof(double) * n_, cudaMemcpyDeviceToHost), "download");
+            check(cudaMemcpy(c.data(), z, sizeof(double) * n_, cudaMemcpyDeviceToHost), "download");
+            for (int i = 0; i < n_; ++i) { out[3 * i] = a[i]; out[3 * i + 1] = b[i]; out[3 * i + 2] = c[i]; }
+        };
+        get3(pos, O_.px, O_.py, O_.pz);
+        get3(vel, O_.vx, O_.vy, O_.vz);
+        get3(omg, O_.wx, O_.wy, O_.wz);
+        if (quat) {
+            std::vector<double> a(n_);
+            double* src[4] = {O_.qw, O_.qx, O_.qy, O_.qz};
+            for (int k = 0; k < 4; ++k) {
+                check(cudaMemcpy(a.data(), src[k], sizeof(double) * n_, cudaMemcpyDeviceToHost), "download");
+                for (int i = 0; i < n_; ++i) quat[4 * i + k] = a[i];
+            }
+        }
+    }
+
+    void download_owner_fields(double* const* dst, double* const* src, int count, int stride)
+    {
+        std::vector<double> a(n_);
+        for (int k = 0; k < count; ++k) {
+            check(cudaMemcpy(a.data(), src[k], sizeof(double) * n_, cudaMemcpyDeviceToHost), "download");
+            for (int i = 0; i < n_; ++i) (*dst)[(size_t)stride * i + k] = a[i];
+        }
+    }
+
+    void download_half(double* vh, double* wh, double* hdq, double* acc, double* aacc)
+    {
+        need_init();
+        check(cudaStreamSynchronize(stream_), "sync");
+        if (vh) { double* s[3] = {O_.vhx, O_.vhy, O_.vhz}; download_owner_fields(&vh, s, 3, 3); }
+        if (wh) { double* s[3] = {O_.whx, O_.why, O_.whz}; download_owner_fields(&wh, s, 3, 3); }
+        if (hdq) { double* s[4] = {O_.hqw, O_.hqx, O_.hqy, O_.hqz}; download_owner_fields(&hdq, s, 4, 4); }
+        if (acc) { double* s[3] = {O_.ax, O_.ay, O_.az}; download_owner_fields(&acc, s, 3, 3); }
+        if (aacc) { double* s[3] = {O_.awx, O_.awy, O_.awz}; download_owner_fields(&aacc, s, 3, 3); }
+    }
+
+    template <typename T> void assemble_forces(Contacts<T>& ct, double* c, double* f, double* w, double* t, double* bp, double* bd)
+    {
+        const size_t n6 = (size_t)n_ * 6;
+        double* buf = arena_tmp_.alloc<double>(n6 * 4, "force output");
+        launch_owner_sum<T>(C_, O_, d_sc_, ct, true, buf, buf + n6, buf + 2 * n6, buf + 3 * n6, stream_);
+        double* bpd = nullptr;
+        double* bdd = nullptr;
+        if (nb_ > 0 && (bp || bd)) {
+            bpd = arena_tmp_.alloc<double>((size_t)nb_ * n6, "body particle output");
+            bdd = arena_tmp_.alloc<double>((size_t)nb_ * n_ * 19, "body detail output");
+            launch_body_outputs<T>(C_, O_, B_, d_sc_, ct, bpd, bdd, stream_);
+        }
+        check(cudaStreamSynchronize(stream_), "assemble forces");
+        double* dst[4] = {c, f, w, t};
+        for (int k = 0; k < 4; ++k)
+            if (dst[k]) check(cudaMemcpy(dst[k], buf + k * n6, n6 * sizeof(double), cudaMemcpyDeviceToHost), "download forces");
+        if (bp && bpd) check(cudaMemcpy(bp, bpd, (size_t)nb_ * n6 * sizeof(double), cudaMemcpyDeviceToHost), "download");
+        if (bd && bdd) check(cudaMemcpy(bd, bdd, (size_t)nb_ * n_ * 19 * sizeof(double), cudaMemcpyDeviceToHost), "download");
+        arena_tmp_.release();
+    }
+    void download_forces(double* c, double* f, double* w, double* t, double* bp, double* bd)
+    {
+        need_init();
+        if (precision_ == DEM_PRECISION_MIXED) assemble_forces<float>(ct32_, c, f, w, t, bp, bd);
+        else assemble_forces<double>(ct64_, c, f, w, t, bp, bd);
+    }
+
+    void download_grid(uint64_t* keys, int* ids)
+    {
+        need_init();
+        check(cudaStreamSynchronize(stream_), "sync");
+        if (keys) check(cudaMemcpy(keys, G_.sorted_key, sizeof(uint64_t) * nc_, cudaMemcpyDeviceToHost), "download keys");
+        if (ids) check(cudaMemcpy(ids, G_.sorted_id, sizeof(int) * nc_, cudaMemcpyDeviceToHost), "download ids");
+    }
+
+    template <typename T> void download_hist(const Hist<T>& h, int slots, uint64_t* keys, int* last, double* val)
+    {
+        const size_t n = (size_t)nc_ * slots;
+        if (keys) check(cudaMemcpy(keys, h.key, n * sizeof(uint64_t), cudaMemcpyDeviceToHost), "download keys");
+        if (last) check(cudaMemcpy(last, h.last, n * sizeof(int), cudaMemcpyDeviceToHost), "download last");
+        if (val) {
+            std::vector<T> v(n * 9);
+            check(cudaMemcpy(v.data(), h.val, n * 9 * sizeof(T), cudaMemcpyDeviceToHost), "download values");
+            for (size_t k = 0; k < n * 9; ++k) val[k] = (double)v[k];
+        }
+    }
+    void download_history(int kind, uint64_t* keys, int* last, double* val)
+    {
+        need_init();
+        check(cudaStreamSynchronize(stream_), "sync");
+        const int slots = kind == 0 ? kPSlots : (kind == 1 ? kWSlots : kBSlots);
+        if (kind < 0 || kind > 2) throw DemError(DEM_ERR_INVALID, "history kind must be 0, 1 or 2");
+        if (precision_ == DEM_PRECISION_MIXED) download_hist(kind == 0 ? hp32_ : (kind == 1 ? hw32_ : hb32_), slots, keys, last, val);
+        else download_hist(kind == 0 ? hp64_ : (kind == 1 ? hw64_ : hb64_), slots, keys, last, val);
+    }
+
+    template <typename T> void upload_hist(Hist<T>& h, int slots, const uint64_t* keys, const double* val)
+    {
+        const size_t n = (size_t)nc_ * slots;
+        check(cudaMemcpy(h.key, keys, n * sizeof(uint64_t), cudaMemcpyHostToDevice), "upload keys");
+        std::vector<T> v(n * 9);
+        for (size_t k = 0; k < n * 9; ++k) v[k] = (T)val[k];
+        check(cudaMemcpy(h.val, v.data(), n * 9 * sizeof(T), cudaMemcpyHostToDevice), "upload values");
+        check(cudaMemset(h.last, 0xff, n * sizeof(int)), "reset history age");
+        std::vector<int> hw(nc_, 0);
+        for (int c = 0; c < nc_; ++c)
+            for (int s = slots - 1; s >= 0; --s)
+                if (keys[(size_t)c * slots + s] != 0) { hw[c] = s + 1; break; }
+        check(cudaMemcpy(h.hw, hw.data(), nc_ * sizeof(int), cudaMemcpyHostToDevice), "upload hw");
+    }
+
+    // ------------------------------------------------- DMHIST2 checkpoint
+    // saveContactHistory (src/cuda_backend_cuda.cu:545-656)
+    void save_history(const char* path)
+    {
+        need_init();
+        if (!path) throw DemError(DEM_ERR_INVALID, "NULL path");
+        check(cudaStreamSynchronize(stream_), "sync");
+        const size_t ps = (size_t)nc_ * kPSlots, ws = (size_t)nc_ * kWSlots, bs = (size_t)nc_ * kBSlots;
+        std::vector<uint64_t> pk(ps), wk(ws), bk(bs);
+        std::vector<double> pv(ps * 9), wv(ws * 9), bv(bs * 9);
+        download_history(0, pk.data(), nullptr, pv.data());
+        download_history(1, wk.data(), nullptr, wv.data());
+        download_history(2, bk.data(), nullptr, bv.data());
+        std::vector<double> st(23 * (size_t)n_);
+        {
+            std::vector<double> a(n_);
+            double* src[23] = {O_.px, O_.py, O_.pz, O_.vx, O_.vy, O_.vz, O_.qw, O_.qx, O_.qy, O_.qz, O_.wx, O_.wy,
+                               O_.wz, O_.vhx, O_.vhy, O_.vhz, O_.whx, O_.why, O_.whz, O_.hqw, O_.hqx, O_.hqy, O_.hqz};
+            for (int k = 0; k < 23; ++k) {
+                check(cudaMemcpy(a.data(), src[k], sizeof(double) * n_, cudaMemcpyDeviceToHost), "checkpoint state");
+                for (int i = 0; i < n_; ++i) st[23 * (size_t)i + k] = a[i];
+            }
+        }
+        std::ofstream out(path, std::ios::binary | std::ios::trunc);
+        if (!out) throw DemError(DEM_ERR_IO, std::string("cannot create CUDA contact-history checkpoint: ") + path);
+        auto wr = [&](const void* p, size_t bytes) { out.write(static_cast<const char*>(p), (std::streamsize)bytes); };
+        const char magic[8] = {'D', 'M', 'H', 'I', 'S', 'T', '2', '\0'};
+        const uint32_t version = 2, endian = 0x01020304u, owners = (uint32_t)n_, comps = (uint32_t)nc_;
+        const uint32_t slots[3] = {kPSlots, kWSlots, kBSlots};
+        const uint32_t topo = 2u * sizeof(int32_t) + 4u * sizeof(double), ownrec = sizeof(int32_t) + 23u * sizeof(double);
+        wr(magic, 8); wr(&version, 4); wr(&endian, 4); wr(&owners, 4); wr(&comps, 4); wr(slots, 12); wr(&topo, 4); wr(&ownrec, 4);
+        for (int c = 0; c < nc_; ++c) {
+            const int32_t cid = comp_ids_[c], oid = comp_owner_ids_[c];
+            const double geo[4] = {comp_radius_[c], comp_body_[3 * c], comp_body_[3 * c + 1], comp_body_[3 * c + 2]};
+            wr(&cid, 4); wr(&oid, 4); wr(geo, 32);
+        }
+        for (int i = 0; i < n_; ++i) {
+            const int32_t oid = owner_ids_[i];
+            wr(&oid, 4);
+            wr(&st[23 * (size_t)i], 23 * sizeof(double));
+        }
+        wr(pk.data(), ps * 8); wr(wk.data(), ws * 8); wr(bk.data(), bs * 8);
+        wr(pv.data(), ps * 72); wr(wv.data(), ws * 72); wr(bv.data(), bs * 72);
+        if (!out) throw DemError(DEM_ERR_IO, std::string("failed to write CUDA contact-history checkpoint: ") + path);
+    }
+
+    // loadContactHistory (src/cuda_backend_cuda.cu:658-822)
+    void load_history(const char* path)
+    {
+        need_init();
+        if (!path) throw DemError(DEM_ERR_INVALID, "NULL path");
+        std::ifstream in(path, std::ios::binary);
+        const std::string name(path);
+        if (!in) throw DemError(DEM_ERR_IO, "cannot open CUDA contact-history checkpoint: " + name);
+        auto rd = [&](void* p, size_t bytes) {
+            in.read(static_cast<char*>(p), (std::streamsize)bytes);
+            if (!in) throw DemError(DEM_ERR_IO, "truncated CUDA contact-history checkpoint: " + name);
+        };
+        char magic[8];
+        uint32_t version = 0, comps = 0, slots[3] = {0, 0, 0};
+        rd(magic, 8); rd(&version, 4);
+        const char v1[8] = {'D', 'M', 'H', 'I', 'S', 'T', '1', '\0'}, v2[8] = {'D', 'M', 'H', 'I', 'S', 'T', '2', '\0'};
+        restored_ = false;
+        std::vector<double> st;
+        if (std::memcmp(magic, v1, 8) == 0 && version == 1) {
+            rd(&comps, 4); rd(slots, 12);
+            bool legacy = sphere_;
+            for (int i = 0; i < nc_ && legacy; ++i) legacy = comp_ids_[i] == owner_ids_[i];
+            if (!legacy) throw DemError(DEM_ERR_IO, "legacy DMHIST1 checkpoint is forbidden for clump topology: " + name);
+        } else if (std::memcmp(magic, v2, 8) == 0 && version == 2) {
+            uint32_t endian = 0, owners = 0, topo = 0, ownrec = 0;
+            rd(&endian, 4); rd(&owners, 4); rd(&comps, 4); rd(slots, 12); rd(&topo, 4); rd(&ownrec, 4);
+            if (endian != 0x01020304u || owners != (uint32_t)n_ || topo != 2u * sizeof(int32_t) + 4u * sizeof(double) ||
+                ownrec != sizeof(int32_t) + 23u * sizeof(double))
+                throw DemError(DEM_ERR_IO, "incompatible DMHIST2 header: " + name);
+            if (comps != (uint32_t)nc_) throw DemError(DEM_ERR_IO, "DMHIST2 component count mismatch: " + name);
+            for (uint32_t c = 0; c < comps; ++c) {
+                int32_t cid = 0, oid = 0;
+                double geo[4];
+                rd(&cid, 4); rd(&oid, 4); rd(geo, 32);
+                if (cid != comp_ids_[c] || oid != comp_owner_ids_[c] || geo[0] != comp_radius_[c] ||
+                    geo[1] != comp_body_[3 * c] || geo[2] != comp_body_[3 * c + 1] || geo[3] != comp_body_[3 * c + 2])
+                    throw DemError(DEM_ERR_IO, "DMHIST2 component topology mismatch: " + name);
+            }
+            st.resize(23 * (size_t)n_);
+            for (int i = 0; i < n_; ++i) {
+                int32_t oid = 0;
+                rd(&oid, 4);
+                rd(&st[23 * (size_t)i], 23 * sizeof(double));
+                if (oid != owner_ids_[i]) throw DemError(DEM_ERR_IO, "DMHIST2 owner identity mismatch: " + name);
+            }
+        } else {
+            throw DemError(DEM_ERR_IO, "unsupported contact-history checkpoint: " + name);
+        }
+        if (comps != (uint32_t)nc_ || slots[0] != kPSlots || slots[1] != kWSlots || slots[2] != kBSlots)
+            throw DemError(DEM_ERR_IO, "incompatible CUDA contact-history checkpoint: " + name);
+        const size_t ps = (size_t)nc_ * kPSlots, ws = (size_t)nc_ * kWSlots, bs = (size_t)nc_ * kBSlots;
+        std::vector<uint64_t> pk(ps), wk(ws), bk(bs);
+        std::vector<double> pv(ps * 9), wv(ws * 9), bv(bs * 9);
+        rd(pk.data(), ps * 8); rd(wk.data(), ws * 8); rd(bk.data(), bs * 8);
+        rd(pv.data(), ps * 72); rd(wv.data(), ws * 72); rd(bv.data(), bs * 72);
+        char trailing;
+        if (in.read(&trailing, 1)) throw DemError(DEM_ERR_IO, "oversized CUDA contact-history checkpoint: " + name);
+        check(cudaStreamSynchronize(stream_), "sync");
+        if (!st.empty()) {
+            std::vector<double> a(n_);
+            double* dst[23] = {O_.px, O_.py, O_.pz, O_.vx, O_.vy, O_.vz, O_.qw, O_.qx, O_.qy, O_.qz, O_.wx, O_.wy,
+                               O_.wz, O_.vhx, O_.vhy, O_.vhz, O_.whx, O_.why, O_.whz, O_.hqw, O_.hqx, O_.hqy, O_.hqz};
+            for (int k = 0; k < 23; ++k) {
+                for (int i = 0; i < n_; ++i) a[i] = st[23 * (size_t)i + k];
+                check(cudaMemcpy(dst[k], a.data(), sizeof(double) * n_, cudaMemcpyHostToDevice), "restore state");
+            }
+            restored_ = true;
+        }
+        if (precision_ == DEM_PRECISION_MIXED) {
+            upload_hist(hp32_, kPSlots, pk.data(), pv.data()); upload_hist(hw32_, kWSlots, wk.data(), wv.data());
+            upload_hist(hb32_, kBSlots, bk.data(), bv.data());
+        } else {
+            upload_hist(hp64_, kPSlots, pk.data(), pv.data()); upload_hist(hw64_, kWSlots, wk.data(), wv.data());
+            upload_hist(hb64_, kBSlots, bk.data(), bv.data());
+        }
+        check(cudaMemset(K_.step, 0, sizeof(int)), "reset step");
+        step_index_ = 0;
+        started_ = false;
+        if (!sphere_) { launch_update_components(C_, O_, stream_); check(cudaStreamSynchronize(stream_), "sync"); }
+    }
+
+    // -------------------------------------------------------------- misc
+    void need_init() const
+    {
+        if (!initialized_) throw DemError(DEM_ERR_STATE, "CUDA DEM solver is not initialized");
+    }
+
+    int n_ = 0, nc_ = 0, nw_ = 0, nb_ = 0, nt_ = 0, S_ = 0, nbs_ = 0;
+    bool sphere_ = true, initialized_ = false, started_ = false, restored_ = false;
+    bool keep_bp_ = false, keep_bd_ = false;
+    int precision_ = 0, block_ = 128, sm_count_ = 0;
+    double cell_factor_ = 2.5, mesh_ = 0.0, max_radius_ = 0.0, dt_ = 0.0;
+    int step_index_ = 0;
+    size_t free_before_ = 0;
+    cudaStream_t stream_ = nullptr;
+    std::array<cudaEvent_t, 8> ev_{};
+    int n_marks_ = 0;
+    DeviceArena arena_, arena_tmp_;
+    void* pinned_ = nullptr;
+    size_t pinned_bytes_ = 0;
+    cudaGraphExec_t graph_exec_ = nullptr, graph_exec_mbd_ = nullptr;
+
+    Owners O_{};
+    Comps C_{};
+    Grid G_{};
+    Recs R_{};
+    Walls W_{};
+    Tris T_{};
+    Bodies B_{};
+    Counters K_{};
+    SceneC* d_sc_ = nullptr;
+    std::vector<SceneC> scenes_h_;
+    Hist<double> hp64_{}, hw64_{}, hb64_{};
+    Hist<float> hp32_{}, hw32_{}, hb32_{};
+    Contacts<double> ct64_{};
+    Contacts<float> ct32_{};
+    BodyOut BO_{};
+
+    std::vector<int> owner_ids_, comp_ids_, comp_owner_ids_, body_state_, body_scene_, grav_;
+    std::vector<std::array<double, 3>> gvec_;
+    std::vector<double> comp_radius_, comp_body_, body_mass_, body_inertia_;
+    std::vector<double> hbc_, hbq_, hbv_, hbw_, hbhv_, hbhw_, hbhq_, hbhdq_, hbacc_, hbdom_, hbloads_;
+    dem_step_stats stats_{};
+    std::vector<unsigned long long> reg_inst_, reg_int_;
+    std::vector<double> micro_inst_, micro_int_;
+};
+
+}  // namespace demgb
+
+// ====================================================================== ABI
+using demgb::DemError;
+using demgb::Engine;
+
+struct dem_engine {
+    Engine e;
+};
+
+template <typename F> static int guarded(F&& f)
+{
+    try {
+        f();
+        demgb::g_last_error.clear();
+        return DEM_OK;
+    } catch (const DemError& e) {
+        demgb::g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        demgb::g_last_error = "host allocation failed";
+        return DEM_ERR_INVALID;
+    } catch (const std::exception& e) {
+        demgb::g_last_error = e.what();
+        return DEM_ERR_INVALID;
+    }
+}
+
+#define NEED(x) do { if (!(x)) throw DemError(DEM_ERR_INVALID, "NULL argument: " #x); } while (0)
+
+extern "C" {
+
+int dem_abi_version(void) { return DEM_GB300_ABI_VERSION; }
+const char* dem_last_error(void) { return demgb::g_last_error.c_str(); }
+
+int dem_device_available(void)
+{
+    int count = 0;
+    return cudaGetDeviceCount(&count) == cudaSuccess && count > 0;
+}
+
+const char* dem_device_description(void)
+{
+    static char description[256] = {0};
+    if (description[0] == '\0') {
+        cudaDeviceProp p{};
+        if (cudaGetDeviceProperties(&p, 0) == cudaSuccess)
+            std::snprintf(description, sizeof description, "%s, compute capability %d.%d, %.1f GiB", p.name, p.major,
+                          p.minor, (double)p.totalGlobalMem / (1024.0 * 1024.0 * 1024.0));
+        else
+            std::snprintf(description, sizeof description, "unavailable");
+    }
+    return description;
+}
+
+void dem_default_options(dem_options* o)
+{
+    if (!o) return;
+    o->precision = DEM_PRECISION_FP64;
+    o->cell_factor = 2.5;
+    o->max_cells = 0;
+    o->block_size = 0;
+}
+
+int dem_create(dem_engine** out)
+{
+    return guarded([&] { NEED(out); *out = new dem_engine(); });
+}
+
+int dem_destroy(dem_engine* e)
+{
+    return guarded([&] { delete e; });
+}
+
+int dem_initialize(dem_engine* e, const dem_scene* scene, const dem_options* options)
+{
+    return guarded([&] { NEED(e); NEED(scene); e->e.init(scene, 1, options); });
+}
+
+int dem_initialize_batch(dem_engine* e, const dem_scene* scenes, int n, const dem_options* options)
+{
+    return guarded([&] { NEED(e); NEED(scenes); e->e.init(scenes, n, options); });
+}
+
+int dem_compute_forces(dem_engine* e, double, const dem_body_states* bodies, double* body_forces, int diag)
+{
+    return guarded([&] {
+        NEED(e);
+        if (bodies) { NEED(bodies->center); NEED(bodies->quat); NEED(bodies->vel); NEED(bodies->omega); }
+        e->e.compute_forces(bodies, body_forces, diag);
+    });
+}
+
+int dem_leapfrog_init(dem_engine* e, double h) { return guarded([&] { NEED(e); e->e.leapfrog_init(h); }); }
+int dem_leapfrog_advance(dem_engine* e, double dt) { return guarded([&] { NEED(e); e->e.advance(dt); }); }
+int dem_leapfrog_finish(dem_engine* e, double dt, double) { return guarded([&] { NEED(e); e->e.finish(dt); }); }
+int dem_run_steps(dem_engine* e, int steps) { return guarded([&] { NEED(e); e->e.run_steps(steps); }); }
+
+int dem_get_bodies(dem_engine* e, double* c, double* q, double* v, double* w, double* loads)
+{
+    return guarded([&] {
+        NEED(e);
+        Engine& x = e->e;
+        const size_t nb = (size_t)x.nb_;
+        if (c) std::memcpy(c, x.hbc_.data(), 3 * nb * sizeof(double));
+        if (q) std::memcpy(q, x.hbq_.data(), 4 * nb * sizeof(double));
+        if (v) std::memcpy(v, x.hbv_.data(), 3 * nb * sizeof(double));
+        if (w) std::memcpy(w, x.hbw_.data(), 3 * nb * sizeof(double));
+        if (loads) std::memcpy(loads, x.hbloads_.data(), 6 * nb * sizeof(double));
+    });
+}
+
+int dem_save_history(dem_engine* e, const char* path) { return guarded([&] { NEED(e); e->e.save_history(path); }); }
+int dem_load_history(dem_engine* e, const char* path) { return guarded([&] { NEED(e); e->e.load_history(path); }); }
+int dem_has_restored_leapfrog_state(dem_engine* e, int* r)
+{
+    return guarded([&] { NEED(e); NEED(r); *r = e->e.restored_ ? 1 : 0; });
+}
+
+int dem_download_state(dem_engine* e, double* pos, double* vel, double* omg, double* quat)
+{
+    return guarded([&] { NEED(e); e->e.download_state(pos, vel, omg, quat); });
+}
+
+int dem_download_forces(dem_engine* e, double* c, double* f, double* w, double* t, double* bp, double* bd)
+{
+    return guarded([&] { NEED(e); e->e.download_forces(c, f, w, t, bp, bd); });
+}
+
+int dem_stats(dem_engine* e, dem_step_stats* s) { return guarded([&] { NEED(e); NEED(s); *s = e->e.stats_; }); }
+
+int dem_body_diagnostics(dem_engine* e, uint64_t* ri, uint64_t* rv, double* mi, double* mv)
+{
+    return guarded([&] {
+        NEED(e);
+        Engine& x = e->e;
+        if (ri && !x.reg_inst_.empty()) std::memcpy(ri, x.reg_inst_.data(), x.reg_inst_.size() * 8);
+        if (rv && !x.reg_int_.empty()) std::memcpy(rv, x.reg_int_.data(), x.reg_int_.size() * 8);
+        if (mi && !x.micro_inst_.empty()) std::memcpy(mi, x.micro_inst_.data(), x.micro_inst_.size() * 8);
+        if (mv && !x.micro_int_.empty()) std::memcpy(mv, x.micro_int_.data(), x.micro_int_.size() * 8);
+    });
+}
+
+int dem_grid_entry_counts(dem_engine* e, size_t* pe, size_t* te)
+{
+    return guarded([&] {
+        NEED(e);
+        Engine& x = e->e;
+        if (pe) *pe = (size_t)x.nc_;
+        if (te) {
+            int tot = 0, total_cells = 0;
+            if (x.nt_ > 0) {
+                demgb::check(cudaStreamSynchronize(x.stream_), "sync");
+                demgb::check(cudaMemcpy(&total_cells, x.G_.total_cells, sizeof(int), cudaMemcpyDeviceToHost), "download");
+                demgb::check(cudaMemcpy(&tot, x.T_.tcell_start + total_cells, sizeof(int), cudaMemcpyDeviceToHost), "download");
+            }
+            *te = (size_t)tot;
+        }
+    });
+}
+
+int dem_device_memory_bytes(dem_engine* e, size_t* bytes)
+{
+    return guarded([&] {
+        NEED(e); NEED(bytes);
+        size_t fr = 0, tot = 0;
+        demgb::check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+        *bytes = e->e.free_before_ > fr ? e->e.free_before_ - fr : 0;
+    });
+}
+
+int dem_counts(dem_engine* e, int* n, int* nc, int* nb, int* nt, int* nw)
+{
+    return guarded([&] {
+        NEED(e);
+        Engine& x = e->e;
+        if (n) *n = x.n_;
+        if (nc) *nc = x.nc_;
+        if (nb) *nb = x.nb_;
+        if (nt) *nt = x.nt_;
+        if (nw) *nw = x.nw_;
+    });
+}
+
+int dem_download_grid(dem_engine* e, uint64_t* k, int* i) { return guarded([&] { NEED(e); e->e.download_grid(k, i); }); }
+
+int dem_download_history(dem_engine* e, int kind, uint64_t* keys, int* last, double* val)
+{
+    return guarded([&] { NEED(e); e->e.download_history(kind, keys, last, val); });
+}
+
+int dem_last_phase_times(dem_engine* e, float* ms, int capacity, int* count)
+{
+    return guarded([&] {
+        NEED(e);
+        Engine& x = e->e;
+        const int n = std::max(0, x.n_marks_ - 1);
+        if (count) *count = n;
+        if (ms) {
+            demgb::check(cudaStreamSynchronize(x.stream_), "sync");
+            for (int k = 0; k < n && k < capacity; ++k)
+                demgb::check(cudaEventElapsedTime(ms + k, x.ev_[k], x.ev_[k + 1]), "elapsed");
+        }
+    });
+}
+
+}  // extern "C"
+
+// Engine-internal entry points used by the Python binding for timing and
+// parity introspection (not part of the reference-facing ABI).
+extern "C" {
+
+int dem_x_compute_forces_timed(dem_engine* e, int diag)
+{
+    return guarded([&] { NEED(e); e->e.compute_forces(nullptr, nullptr, diag, true); });
+}
+
+int dem_x_time_steps(dem_engine* e, int steps, float* ms)
+{
+    return guarded([&] { NEED(e); NEED(ms); *ms = e->e.time_steps(steps); });
+}
+
+int dem_x_download_half(dem_engine* e, double* vh, double* wh, double* hdq, double* acc, double* aacc)
+{
+    return guarded([&] { NEED(e); e->e.download_half(vh, wh, hdq, acc, aacc); });
+}
+
+int dem_x_synchronize(dem_engine* e)
+{
+    return guarded([&] { NEED(e); demgb::check(cudaStreamSynchronize(e->e.stream_), "sync"); });
+}
+
+}  // extern "C"

@@ -1,0 +1,570 @@
+// dem_grid.cu -- cell hash, counting sort with cell start tables, triangle
+// grid, leapfrog and quaternion integration.
+//
+// The particle grid replaces the reference's thrust::sequence +
+// thrust::sort_by_key over 63-bit packed cell keys followed by per-lookup
+// binary searches (src/cuda/cuda_grid_backend.cu:121-145,
+// src/cuda/cuda_contact_backend.cu:144-176,1131-1135).  Each step:
+//   1. cell key of every component (same floor(x * 1/mesh), same range check)
+//      and the per-scene cell box (warp-reduced atomics);
+//   2. a dense per-scene cell layout over that box (one block);
+//   3. counting sort: per-cell atomic count + rank, device-wide exclusive
+//      scan (the start table), scatter;
+//   4. per cell, its entries are put in ascending component order.
+// Step 4 makes the result equal to a stable sort of the keys over component
+// indices, i.e. the reference's sortedCellKey / sortedEntityId, and the scan
+// is the cell start/end table the contact kernels index directly.
+#include "dem_kernels.cuh"
+
+#include <climits>
+
+namespace demgb {
+
+namespace {
+
+constexpr int kScanBlock = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanBlock * kScanItems;
+
+__device__ __forceinline__ int warp_min(int v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max(int v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide exclusive scan of one int per thread (blockDim multiple of 32).
+__device__ int block_exclusive_scan(int v, int& total)
+{
+    __shared__ int warp_sums[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int s = lane < nw ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    total = warp_sums[nw - 1];
+    const int base = wid > 0 ? warp_sums[wid - 1] : 0;
+    __syncthreads();
+    return base + x - v;
+}
+
+// ------------------------------------------------------------------ keys
+// updateComponentsKernel (src/cuda/cuda_particle_backend.cu:116-147).
+__global__ void k_update_components(Comps c, Owners o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const int w = c.owner[i];
+    const double qw = o.qw[w], qx = o.qx[w], qy = o.qy[w], qz = o.qz[w];
+    const V3<double> off = rot_iv(qw, qx, qy, qz, mk(c.bx[i], c.by[i], c.bz[i]));
+    c.ox[i] = off.x; c.oy[i] = off.y; c.oz[i] = off.z;
+    c.x[i] = o.px[w] + off.x; c.y[i] = o.py[w] + off.y; c.z[i] = o.pz[w] + off.z;
+    const V3<double> ow = rot_iv(qw, qx, qy, qz, mk(o.wx[w], o.wy[w], o.wz[w]));
+    c.vx[i] = o.vx[w] + ow.y * off.z - ow.z * off.y;
+    c.vy[i] = o.vy[w] + ow.z * off.x - ow.x * off.z;
+    c.vz[i] = o.vz[w] + ow.x * off.y - ow.y * off.x;
+    const V3<double> hw = rot_iv(qw, qx, qy, qz, mk(o.whx[w], o.why[w], o.whz[w]));
+    c.vhx[i] = o.vhx[w] + hw.y * off.z - hw.z * off.y;
+    c.vhy[i] = o.vhy[w] + hw.z * off.x - hw.x * off.z;
+    c.vhz[i] = o.vhz[w] + hw.x * off.y - hw.y * off.x;
+}
+
+// computeComponentKeysKernel (src/cuda/cuda_grid_backend.cu:51-71) plus the
+// per-scene cell box.
+__global__ void k_cell_keys(Comps c, Owners o, Grid g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = false;
+    int cx = 0, cy = 0, cz = 0, s = INT_MAX;
+    if (i < c.n) {
+        const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
+        const double fx = floor(c.x[i] * g.inv_mesh);
+        const double fy = floor(c.y[i] * g.inv_mesh);
+        const double fz = floor(c.z[i] * g.inv_mesh);
+        ok = isfinite(fx) && isfinite(fy) && isfinite(fz) && fx >= minCell && fx <= maxCell && fy >= minCell &&
+             fy <= maxCell && fz >= minCell && fz <= maxCell;
+        if (ok) {
+            cx = (int)fx; cy = (int)fy; cz = (int)fz;
+            s = o.scene[c.owner[i]];
+            g.ckey[i] = pack_cell(cx, cy, cz);
+            g.clin[i] = 0;
+        } else {
+            g.ckey[i] = 0;
+            g.clin[i] = -1;
+            atomicOr(g.err, kErrKeyRange);
+        }
+    }
+    const int smin = warp_min(ok ? s : INT_MAX);
+    const bool uniform = __all_sync(0xffffffffu, !ok || s == smin);
+    if (uniform) {
+        if (smin == INT_MAX) return;
+        const int a0 = warp_min(ok ? cx : INT_MAX), a1 = warp_min(ok ? cy : INT_MAX), a2 = warp_min(ok ? cz : INT_MAX);
+        const int b0 = warp_max(ok ? cx : INT_MIN), b1 = warp_max(ok ? cy : INT_MIN), b2 = warp_max(ok ? cz : INT_MIN);
+        if ((threadIdx.x & 31) == 0) {
+            int* box = g.scene_box + 6 * smin;
+            atomicMin(box + 0, a0); atomicMin(box + 1, a1); atomicMin(box + 2, a2);
+            atomicMax(box + 3, b0); atomicMax(box + 4, b1); atomicMax(box + 5, b2);
+        }
+    } else if (ok) {
+        int* box = g.scene_box + 6 * s;
+        atomicMin(box + 0, cx); atomicMin(box + 1, cy); atomicMin(box + 2, cz);
+        atomicMax(box + 3, cx); atomicMax(box + 4, cy); atomicMax(box + 5, cz);
+    }
+}
+
+// Dense segmented cell layout: scene s owns cells [offset, offset + cells).
+__global__ void k_layout(Grid g)
+{
+    if (threadIdx.x == 0) {
+        long long off = 0;
+        for (int s = 0; s < g.nscenes; ++s) {
+            const int* box = g.scene_box + 6 * s;
+            int* lay = g.scene_layout + 8 * s;
+            long long cells = 0;
+            long long nx = 0, ny = 0, nz = 0;
+            if (box[0] <= box[3]) {
+                nx = (long long)box[3] - box[0] + 1;
+                ny = (long long)box[4] - box[1] + 1;
+                nz = (long long)box[5] - box[2] + 1;
+                cells = nx * ny * nz;
+                if (off + cells > (long long)g.capacity) {
+                    atomicOr(g.err, kErrCellCapacity);
+                    cells = 0;
+                }
+            }
+            lay[0] = box[0]; lay[1] = box[1]; lay[2] = box[2];
+            lay[3] = cells ? (int)nx : 0; lay[4] = cells ? (int)ny : 0; lay[5] = cells ? (int)nz : 0;
+            lay[6] = (int)off; lay[7] = (int)cells;
+            off += cells;
+        }
+        *g.total_cells = (int)off;
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < g.nscenes; s += blockDim.x) {
+        int* box = g.scene_box + 6 * s;
+        box[0] = box[1] = box[2] = INT_MAX;
+        box[3] = box[4] = box[5] = INT_MIN;
+    }
+}
+
+__device__ __forceinline__ int cell_lin(const int* lay, int cx, int cy, int cz)
+{
+    return lay[6] + ((cx - lay[0]) * lay[4] + (cy - lay[1])) * lay[5] + (cz - lay[2]);
+}
+
+__global__ void k_cell_count(Comps c, Owners o, Grid g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n || g.clin[i] < 0) return;
+    const int s = o.scene[c.owner[i]];
+    const int* lay = g.scene_layout + 8 * s;
+    if (lay[7] == 0) { g.clin[i] = -1; return; }
+    int cx, cy, cz;
+    unpack_cell(g.ckey[i], cx, cy, cz);
+    const int lin = cell_lin(lay, cx, cy, cz);
+    g.clin[i] = lin;
+    g.crank[i] = atomicAdd(g.cell_count + lin, 1);
+}
+
+__global__ void k_scatter(Comps c, Grid g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const int lin = g.clin[i];
+    if (lin < 0) return;
+    g.sorted_id[g.cell_start[lin] + g.crank[i]] = i;
+}
+
+// Per cell: ascending component order (stable-sort equivalence), inverse
+// permutation, sorted keys; restores the zero count invariant.
+__global__ void k_cell_finalize(Grid g)
+{
+    const int total = *g.total_cells;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *g.nvalid = g.cell_start[total];
+    for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < total; cell += gridDim.x * blockDim.x) {
+        const int b = g.cell_start[cell], e = g.cell_start[cell + 1];
+        g.cell_count[cell] = 0;
+        for (int p = b + 1; p < e; ++p) {
+            const int v = g.sorted_id[p];
+            int q = p - 1;
+            while (q >= b && g.sorted_id[q] > v) { g.sorted_id[q + 1] = g.sorted_id[q]; --q; }
+            g.sorted_id[q + 1] = v;
+        }
+        for (int p = b; p < e; ++p) {
+            const int id = g.sorted_id[p];
+            g.pos_of[id] = p;
+            g.sorted_key[p] = g.ckey[id];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ scan
+__global__ void k_scan_reduce(const int* in, const int* n_dev, int* tile_sums)
+{
+    const int n = *n_dev;
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    __shared__ int red[32];
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int base = tile * kScanTile + threadIdx.x * kScanItems;
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) s += (base + k < n) ? in[base + k] : 0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int v = red[threadIdx.x];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (threadIdx.x == 0) tile_sums[tile] = v;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_scan_tile_sums(int* tile_sums, const int* n_dev)
+{
+    const int n = *n_dev;
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    int running = 0;
+    for (int base = 0; base < ntiles; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int v = i < ntiles ? tile_sums[i] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, total);
+        if (i < ntiles) tile_sums[i] = running + ex;
+        running += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tile_sums[ntiles] = running;
+}
+
+__global__ void k_scan_apply(const int* in, int* out, const int* n_dev, const int* tile_sums)
+{
+    const int n = *n_dev;
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = tile_sums[ntiles];
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int base = tile * kScanTile + threadIdx.x * kScanItems;
+        int v[kScanItems];
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) { v[k] = (base + k < n) ? in[base + k] : 0; s += v[k]; }
+        int total;
+        int ex = block_exclusive_scan(s, total) + tile_sums[tile];
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            if (base + k < n) out[base + k] = ex;
+            ex += v[k];
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------- triangles
+// transformTrianglesKernel (src/cuda/cuda_body_backend.cu:71-112).
+__global__ void k_tri_transform(Tris t, Bodies b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= t.nt) return;
+    const int ib = t.body[i];
+    const double qw = b.q[4 * ib], qx = b.q[4 * ib + 1], qy = b.q[4 * ib + 2], qz = b.q[4 * ib + 3];
+    const double* L = t.local + 15 * (size_t)i;
+    double* W = t.world + 16 * (size_t)i;
+    const double cx = b.c[3 * ib], cy = b.c[3 * ib + 1], cz = b.c[3 * ib + 2];
+    for (int k = 0; k < 4; ++k) {
+        const V3<double> p = rot_iv(qw, qx, qy, qz, mk(L[3 * k], L[3 * k + 1], L[3 * k + 2]));
+        W[3 * k] = p.x + cx; W[3 * k + 1] = p.y + cy; W[3 * k + 2] = p.z + cz;
+    }
+    const V3<double> nn = rot_iv(qw, qx, qy, qz, mk(L[12], L[13], L[14]));
+    W[12] = nn.x; W[13] = nn.y; W[14] = nn.z; W[15] = 0.0;
+    double* A = t.aabb + 6 * (size_t)i;
+    double mnx = W[0], mny = W[1], mnz = W[2], mxx = W[0], mxy = W[1], mxz = W[2];
+    for (int k = 1; k < 4; ++k) {
+        mnx = fmin(mnx, W[3 * k]); mny = fmin(mny, W[3 * k + 1]); mnz = fmin(mnz, W[3 * k + 2]);
+        mxx = fmax(mxx, W[3 * k]); mxy = fmax(mxy, W[3 * k + 1]); mxz = fmax(mxz, W[3 * k + 2]);
+    }
+    A[0] = mnx; A[1] = mny; A[2] = mnz; A[3] = mxx; A[4] = mxy; A[5] = mxz;
+}
+
+// Padded-AABB cell range of a triangle (countTriangleCellsKernel,
+// src/cuda/cuda_contact_backend.cu:409-452), clipped to the particle cell box
+// of its scene: only those cells are ever looked up.
+__device__ bool tri_cell_range(const Tris& t, const Grid& g, int i, double pad, int lo[3], int hi[3], const int*& lay)
+{
+    const double* A = t.aabb + 6 * (size_t)i;
+    const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
+    for (int a = 0; a < 3; ++a) {
+        const double mn = floor((A[a] - pad) * g.inv_mesh);
+        const double mx = floor((A[3 + a] + pad) * g.inv_mesh);
+        if (!isfinite(mn) || !isfinite(mx) || mn < minCell || mx > maxCell) return false;
+        lo[a] = (int)mn;
+        hi[a] = (int)mx;
+    }
+    lay = g.scene_layout + 8 * t.scene[i];
+    if (lay[7] == 0) return false;
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = max(lo[a], lay[a]);
+        hi[a] = min(hi[a], lay[a] + lay[3 + a] - 1);
+        if (lo[a] > hi[a]) return false;
+    }
+    return true;
+}
+
+__device__ bool tri_range_valid(const Tris& t, const Grid& g, int i, double pad)
+{
+    const double* A = t.aabb + 6 * (size_t)i;
+    const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
+    for (int a = 0; a < 3; ++a) {
+        const double mn = floor((A[a] - pad) * g.inv_mesh);
+        const double mx = floor((A[3 + a] + pad) * g.inv_mesh);
+        if (!isfinite(mn) || !isfinite(mx) || mn < minCell || mx > maxCell) return false;
+    }
+    return true;
+}
+
+__global__ void k_tri_count(Tris t, Grid g, double pad, int* tgover)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= t.nt) return;
+    if (!tri_range_valid(t, g, i, pad)) {
+        atomicAdd(tgover, 1);
+        atomicOr(g.err, kErrTriRange);
+        return;
+    }
+    int lo[3], hi[3];
+    const int* lay;
+    if (!tri_cell_range(t, g, i, pad, lo, hi, lay)) return;
+    for (int x = lo[0]; x <= hi[0]; ++x)
+        for (int y = lo[1]; y <= hi[1]; ++y)
+            for (int z = lo[2]; z <= hi[2]; ++z) atomicAdd(t.tcell_count + cell_lin(lay, x, y, z), 1);
+}
+
+__global__ void k_tri_fill(Tris t, Grid g, double pad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= t.nt) return;
+    if (!tri_range_valid(t, g, i, pad)) return;
+    int lo[3], hi[3];
+    const int* lay;
+    if (!tri_cell_range(t, g, i, pad, lo, hi, lay)) return;
+    for (int x = lo[0]; x <= hi[0]; ++x)
+        for (int y = lo[1]; y <= hi[1]; ++y)
+            for (int z = lo[2]; z <= hi[2]; ++z) {
+                const int lin = cell_lin(lay, x, y, z);
+                const int pos = t.tcell_start[lin] + atomicAdd(t.tcell_cursor + lin, 1);
+                if (pos < t.capacity) t.ttri[pos] = i;
+                else atomicOr(g.err, kErrTriCapacity);
+            }
+}
+
+__global__ void k_tri_finalize(Tris t, Grid g)
+{
+    const int total = *g.total_cells;
+    for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < total; cell += gridDim.x * blockDim.x) {
+        const int b = t.tcell_start[cell];
+        const int e = min(t.tcell_start[cell + 1], t.capacity);
+        t.tcell_count[cell] = 0;
+        t.tcell_cursor[cell] = 0;
+        for (int p = b + 1; p < e; ++p) {
+            const int v = t.ttri[p];
+            int q = p - 1;
+            while (q >= b && t.ttri[q] > v) { t.ttri[q + 1] = t.ttri[q]; --q; }
+            t.ttri[q + 1] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------ integrator
+// quatDerivative / normalizeQuat (src/cuda/cuda_particle_backend.cu:149-183)
+__device__ __forceinline__ void quat_derivative(double qw, double qx, double qy, double qz, double wx, double wy,
+                                                double wz, double& dw, double& dx, double& dy, double& dz)
+{
+    dw = 0.5 * (-qx * wx - qy * wy - qz * wz);
+    dx = 0.5 * (qw * wx + qy * wz - qz * wy);
+    dy = 0.5 * (qw * wy - qx * wz + qz * wx);
+    dz = 0.5 * (qw * wz + qx * wy - qy * wx);
+}
+__device__ __forceinline__ void normalize_quat(double& qw, double& qx, double& qy, double& qz)
+{
+    const double n2 = qw * qw + qx * qx + qy * qy + qz * qz;
+    if (n2 <= 1.0e-24) { qw = 1.0; qx = qy = qz = 0.0; return; }
+    const double inv = 1.0 / sqrt(n2);
+    qw *= inv; qx *= inv; qy *= inv; qz *= inv;
+}
+
+// initializeLeapfrogKernel (:185-210)
+__global__ void k_leapfrog_init(Owners d, double h)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    d.vhx[i] = d.vx[i] + d.ax[i] * h;
+    d.vhy[i] = d.vy[i] + d.ay[i] * h;
+    d.vhz[i] = d.vz[i] + d.az[i] * h;
+    d.whx[i] = d.wx[i] + d.awx[i] * h;
+    d.why[i] = d.wy[i] + d.awy[i] * h;
+    d.whz[i] = d.wz[i] + d.awz[i] * h;
+    double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i], dw, dx, dy, dz;
+    quat_derivative(qw, qx, qy, qz, d.wx[i], d.wy[i], d.wz[i], dw, dx, dy, dz);
+    qw += dw * h; qx += dx * h; qy += dy * h; qz += dz * h;
+    normalize_quat(qw, qx, qy, qz);
+    quat_derivative(qw, qx, qy, qz, d.whx[i], d.why[i], d.whz[i], d.hqw[i], d.hqx[i], d.hqy[i], d.hqz[i]);
+}
+
+// advancePositionKernel (:212-237)
+__global__ void k_advance(Owners d, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n || d.status[i] == -1) return;
+    d.px[i] += d.vhx[i] * dt;
+    d.py[i] += d.vhy[i] * dt;
+    d.pz[i] += d.vhz[i] * dt;
+    double qw = d.qw[i] + d.hqw[i] * dt, qx = d.qx[i] + d.hqx[i] * dt;
+    double qy = d.qy[i] + d.hqy[i] * dt, qz = d.qz[i] + d.hqz[i] * dt;
+    normalize_quat(qw, qx, qy, qz);
+    d.qw[i] = qw; d.qx[i] = qx; d.qy[i] = qy; d.qz[i] = qz;
+    d.vx[i] = d.vhx[i] + d.ax[i] * (0.5 * dt);
+    d.vy[i] = d.vhy[i] + d.ay[i] * (0.5 * dt);
+    d.vz[i] = d.vhz[i] + d.az[i] * (0.5 * dt);
+    d.wx[i] = d.whx[i] + d.awx[i] * (0.5 * dt);
+    d.wy[i] = d.why[i] + d.awy[i] * (0.5 * dt);
+    d.wz[i] = d.whz[i] + d.awz[i] * (0.5 * dt);
+}
+
+// advanceHalfVelocityKernel (:239-265)
+__global__ void k_finish(Owners d, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    d.vhx[i] += d.ax[i] * dt;
+    d.vhy[i] += d.ay[i] * dt;
+    d.vhz[i] += d.az[i] * dt;
+    d.whx[i] += d.awx[i] * dt;
+    d.why[i] += d.awy[i] * dt;
+    d.whz[i] += d.awz[i] * dt;
+    const double h = 0.5 * dt;
+    double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i], dw, dx, dy, dz;
+    quat_derivative(qw, qx, qy, qz, d.wx[i], d.wy[i], d.wz[i], dw, dx, dy, dz);
+    qw += dw * h; qx += dx * h; qy += dy * h; qz += dz * h;
+    normalize_quat(qw, qx, qy, qz);
+    quat_derivative(qw, qx, qy, qz, d.whx[i], d.why[i], d.whz[i], d.hqw[i], d.hqx[i], d.hqy[i], d.hqz[i]);
+}
+
+// Universal gravitation (src/cuda/cuda_contact_backend.cu:1095-1106): the
+// reference adds delta * G m_i m_j / d^3 with delta = p_i - p_j, summed in
+// owner order.  Tiled through shared memory, same summation order.
+__global__ void k_universal_gravity(Owners o)
+{
+    __shared__ double sx[256], sy[256], sz[256], sm[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < o.n;
+    const double px = act ? o.px[i] : 0.0, py = act ? o.py[i] : 0.0, pz = act ? o.pz[i] : 0.0;
+    const double mi = act ? o.mass[i] : 0.0;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int base = 0; base < o.n; base += blockDim.x) {
+        const int j = base + threadIdx.x;
+        if (j < o.n) { sx[threadIdx.x] = o.px[j]; sy[threadIdx.x] = o.py[j]; sz[threadIdx.x] = o.pz[j]; sm[threadIdx.x] = o.mass[j]; }
+        __syncthreads();
+        const int lim = min((int)blockDim.x, o.n - base);
+        for (int k = 0; k < lim; ++k) {
+            if (base + k == i) continue;
+            const double dx = px - sx[k], dy = py - sy[k], dz = pz - sz[k];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 > 1.0e-28) {
+                const double s = kGravityConstant * mi * sm[k] / (d2 * sqrt(d2));
+                fx += dx * s; fy += dy * s; fz += dz * s;
+            }
+        }
+        __syncthreads();
+    }
+    if (act) { o.ugx[i] = fx; o.ugy[i] = fy; o.ugz[i] = fz; }
+}
+
+__global__ void k_step_counter(Counters k, int reset)
+{
+    if (threadIdx.x != 0) return;
+    if (reset) {
+        *k.pcontacts = 0; *k.phigh = 0; *k.bhigh = 0; *k.ct_total = 0; *k.tgover = 0;
+    } else {
+        *k.step += 1;
+    }
+}
+
+inline int blocks(int n, int b) { return (n + b - 1) / b; }
+
+}  // namespace
+
+void launch_update_components(const Comps& c, const Owners& o, cudaStream_t s)
+{
+    if (c.n > 0) k_update_components<<<blocks(c.n, 256), 256, 0, s>>>(c, o);
+}
+
+void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int sm_count, cudaStream_t s)
+{
+    const int g = sm_count * 2;
+    k_scan_reduce<<<g, kScanBlock, 0, s>>>(in, n_dev, tile_sums);
+    k_scan_tile_sums<<<1, kScanBlock, 0, s>>>(tile_sums, n_dev);
+    k_scan_apply<<<g, kScanBlock, 0, s>>>(in, out, n_dev, tile_sums);
+}
+
+void launch_grid_build(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s)
+{
+    if (c.n <= 0) return;
+    k_cell_keys<<<blocks(c.n, 256), 256, 0, s>>>(c, o, g);
+    k_layout<<<1, 256, 0, s>>>(g);
+    k_cell_count<<<blocks(c.n, 256), 256, 0, s>>>(c, o, g);
+    launch_scan(g.cell_count, g.cell_start, g.total_cells, g.tile_sums, sm_count, s);
+    k_scatter<<<blocks(c.n, 256), 256, 0, s>>>(c, g);
+    k_cell_finalize<<<sm_count * 8, 256, 0, s>>>(g);
+}
+
+void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s)
+{
+    if (t.nt > 0) k_tri_transform<<<blocks(t.nt, 128), 128, 0, s>>>(t, b);
+}
+
+void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, double pad, int* tgover, int sm_count,
+                      cudaStream_t s)
+{
+    if (t.nt <= 0) return;
+    k_tri_count<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, pad, tgover);
+    launch_scan(t.tcell_count, t.tcell_start, g.total_cells, g.tile_sums, sm_count, s);
+    k_tri_fill<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, pad);
+    k_tri_finalize<<<sm_count * 8, 256, 0, s>>>(t, g);
+}
+
+void launch_universal_gravity(const Owners& o, cudaStream_t s)
+{
+    if (o.n > 0) k_universal_gravity<<<blocks(o.n, 256), 256, 0, s>>>(o);
+}
+
+void launch_leapfrog_init(const Owners& o, double h, cudaStream_t s)
+{
+    if (o.n > 0) k_leapfrog_init<<<blocks(o.n, 256), 256, 0, s>>>(o, h);
+}
+void launch_advance(const Owners& o, double dt, cudaStream_t s)
+{
+    if (o.n > 0) k_advance<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_finish(const Owners& o, double dt, cudaStream_t s)
+{
+    if (o.n > 0) k_finish<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_step_counter(const Counters& k, int reset, cudaStream_t s) { k_step_counter<<<1, 32, 0, s>>>(k, reset); }
+
+}  // namespace demgb

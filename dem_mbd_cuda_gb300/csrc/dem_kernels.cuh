@@ -1,0 +1,189 @@
+// dem_kernels.cuh -- device data layout and kernel launchers of the engine.
+//
+// HBM layout (one engine, all scenes concatenated):
+//   owners      input-order SoA, FP64 (positions, velocities, quaternions,
+//               half-step state, accelerations, constants)
+//   components  input-order SoA; for plain spheres the position and velocity
+//               pointers alias the owner arrays (no copy kernel runs)
+//   cell table  dense int32 start table over the per-step cell box of every
+//               scene (segmented: scene s owns [offset_s, offset_s + cells_s))
+//   records     per sorted position t (cell order), packed double4/float4
+//               rows of the component the contact kernels read
+//   history     reference slot layout [component][slot] (keys u64, last-seen
+//               i32, 9 values of T per slot) updated in place
+//   contacts    flat list of (i sorted pos, j sorted pos, history slot) with
+//               per-contact force/torque rows of T
+#pragma once
+
+#include "dem_device.cuh"
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace demgb {
+
+// Error word bits (reported at diagnostic points).
+enum : unsigned {
+    kErrKeyRange = 1u,        // cell coordinate outside the signed 21-bit range
+    kErrCellCapacity = 2u,    // dense cell table too small for the cell box
+    kErrTriCapacity = 4u,     // triangle grid entries beyond capacity
+    kErrTriRange = 8u,        // triangle cell range overflow (reference :422-450)
+};
+
+struct Owners {
+    int n;
+    double *px, *py, *pz, *vx, *vy, *vz, *wx, *wy, *wz, *qw, *qx, *qy, *qz;
+    double *ax, *ay, *az, *awx, *awy, *awz;
+    double *vhx, *vhy, *vhz, *whx, *why, *whz, *hqw, *hqx, *hqy, *hqz;
+    double *mass, *ix, *iy, *iz, *radius;
+    int *id, *status, *scene;
+    double *ugx, *ugy, *ugz;  // universal-gravitation field force (optional)
+};
+
+struct Comps {
+    int n;
+    int sphere;  // 1: component c is owner c with zero offset
+    int *owner, *cid, *ostart;
+    double *radius, *bx, *by, *bz;                                      // body-frame offset
+    double *x, *y, *z, *vx, *vy, *vz, *vhx, *vhy, *vhz, *ox, *oy, *oz;  // world (aliases for spheres)
+};
+
+// Per-scene constants.
+struct SceneC {
+    MatC pp, pt, pw;
+    double g[3];
+    int grav;
+    int wall_begin, wall_count;
+    int body_begin, body_count;
+};
+
+struct Grid {
+    double inv_mesh, mesh;
+    float mesh_f, margin_f;
+    int capacity;  // cells in the dense table
+    int nscenes;
+    uint64_t* ckey;
+    int *clin, *crank;
+    int *cell_count, *cell_start;
+    int *sorted_id, *pos_of;
+    uint64_t* sorted_key;
+    int* scene_box;     // [S][6]
+    int* scene_layout;  // [S][8]: min xyz, n xyz, offset, cells
+    int* total_cells;   // [1]
+    int* nvalid;        // [1] = cell_start[total_cells]
+    int* tile_sums;
+    unsigned* err;
+};
+
+// 32-byte aligned row of four doubles (one full sector per row).
+struct __align__(32) D4 {
+    double x, y, z, w;
+};
+
+struct Recs {
+    D4 *pos, *v, *vm, *w, *wm, *off;  // off: clumps only
+    int4* meta;                             // c, owner, component id, scene
+    int4* cell;                             // cx, cy, cz, lin
+    float4* relf;                           // position relative to the cell origin, radius
+};
+
+template <typename T> struct Hist {
+    uint64_t* key;
+    int* last;
+    T* val;
+    int* hw;  // per component: 1 + highest occupied slot
+};
+
+struct Walls {
+    double *o, *n;  // [nw][3]
+};
+
+struct Tris {
+    int nt;
+    int* body;
+    double* local;  // [t][15]
+    double* world;  // [t][16] v1..v4, normal, pad
+    double* aabb;   // [t][6]
+    int* scene;     // per triangle
+    int capacity;   // triangle grid entry capacity
+    int *tcell_count, *tcell_cursor, *tcell_start, *ttri;
+};
+
+struct Bodies {
+    int nb;
+    double *c, *q, *v, *w;  // [nb][3/4/3/3] device copies uploaded per step
+    int* scene;
+};
+
+struct Counters {
+    int* pcontacts;     // per step
+    int* pover;         // cumulative
+    int* bover;         // cumulative (wall + body, as the reference)
+    int* phigh;         // per step
+    int* bhigh;         // per step
+    int* tgover;        // per build
+    int* ct_total;      // contacts this step
+    int* pt_total;      // PT components this step
+    int* step;          // contact step index
+};
+
+template <typename T> struct Contacts {
+    int4* ent;      // ti, tj, slot, -
+    T* res;         // [k][6]
+    int *off, *cnt; // per component
+    int capacity;
+    double* wres;   // [c][6] wall force/torque per component
+    int* pt_index;  // per component: PT item or -1
+    int* pt_flag;   // per sorted position
+    int* pt_pos;    // scan of pt_flag
+    int* pt_list;   // item -> sorted position
+    int* pt_total_ptr;  // [1] PT items this step
+    double* pt_res; // [k][6]
+    double* pt_body;    // [k][nbs][kPtRecord]
+    double* pt_out;     // [k][nbs][25] optional output detail
+    int nbs;            // max bodies per scene
+};
+
+struct BodyOut {
+    double* partial;   // [nb][G][kPtRecord]
+    double* result;    // [nb][kPtRecord]: load 6, count, maxdepth, fz, regime 7, micro 22 (see kernels)
+    unsigned long long* reg_int;  // [nb][7]
+    double* micro_int;            // [nb][22]
+    unsigned long long* native_steps;
+    int groups;
+};
+
+// ------------------------------------------------------------- launchers
+void launch_update_components(const Comps& c, const Owners& o, cudaStream_t s);
+void launch_grid_build(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s);
+void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int sm_count, cudaStream_t s);
+void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s);
+void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, double pad, int* tgover, int sm_count,
+                      cudaStream_t s);
+void launch_universal_gravity(const Owners& o, cudaStream_t s);
+void launch_leapfrog_init(const Owners& o, double half_dt, cudaStream_t s);
+void launch_advance(const Owners& o, double dt, cudaStream_t s);
+void launch_finish(const Owners& o, double dt, cudaStream_t s);
+// reset != 0: clear the per-step counters; 0: advance the contact step index.
+void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
+
+template <typename T>
+void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
+                   cudaStream_t s);
+template <typename T>
+void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs& r, const SceneC* sc, const Walls& w,
+                     const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<T> hb, Contacts<T> ct,
+                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s);
+template <typename T>
+void launch_owner_sum(const Comps& c, const Owners& o, const SceneC* sc, Contacts<T> ct, bool outputs, double* fc,
+                      double* ff, double* fw, double* ft, cudaStream_t s);
+template <typename T>
+void launch_body_reduce(const Recs& r, const SceneC* sc, const Bodies& b, Contacts<T> ct, BodyOut bo, bool interval,
+                        cudaStream_t s);
+template <typename T>
+void launch_body_outputs(const Comps& c, const Owners& o, const Bodies& b, const SceneC* sc, Contacts<T> ct,
+                         double* bp, double* bd, cudaStream_t s);
+
+constexpr int kBodyFieldCount = 38;  // body reduction record, see dem_contact.cu
+
+}  // namespace demgb

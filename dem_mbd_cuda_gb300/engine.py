@@ -1,0 +1,273 @@
+"""Python mirror of the reference's ``CudaDemSolver`` over the C ABI.
+
+``CudaDemSolver`` keeps the reference's member names and call order
+(include/cuda_backend.h:40-72): ``initialize``, ``computeForces``,
+``initializeParticleHalfStep``, ``advanceParticles``, ``finishParticleStep``,
+``saveContactHistory`` / ``loadContactHistory``, ``downloadParticleState``,
+``downloadForceOutput``, ``stepStats``.  Errors raise ``RuntimeError`` with the
+library's message, as the reference throws ``std::runtime_error``.  There is
+no CPU fallback: without the CUDA library or a device every call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import CBodyStates, COptions, CStepStats, DEM_PRECISION_FP64, DEM_PRECISION_MIXED  # noqa: F401
+from .scene import Scene
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdemgb300.so")
+
+_lib = None
+
+_SIGS = {
+    "dem_abi_version": ([], C.c_int),
+    "dem_last_error": ([], C.c_char_p),
+    "dem_device_available": ([], C.c_int),
+    "dem_device_description": ([], C.c_char_p),
+    "dem_create": ([C.c_void_p], C.c_int),
+    "dem_destroy": ([C.c_void_p], C.c_int),
+    "dem_default_options": ([C.c_void_p], None),
+    "dem_initialize": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "dem_initialize_batch": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "dem_compute_forces": ([C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int], C.c_int),
+    "dem_leapfrog_init": ([C.c_void_p, C.c_double], C.c_int),
+    "dem_leapfrog_advance": ([C.c_void_p, C.c_double], C.c_int),
+    "dem_leapfrog_finish": ([C.c_void_p, C.c_double, C.c_double], C.c_int),
+    "dem_run_steps": ([C.c_void_p, C.c_int], C.c_int),
+    "dem_get_bodies": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),
+    "dem_save_history": ([C.c_void_p, C.c_char_p], C.c_int),
+    "dem_load_history": ([C.c_void_p, C.c_char_p], C.c_int),
+    "dem_has_restored_leapfrog_state": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dem_download_state": ([C.c_void_p] + [C.c_void_p] * 4, C.c_int),
+    "dem_download_forces": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
+    "dem_stats": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dem_body_diagnostics": ([C.c_void_p] + [C.c_void_p] * 4, C.c_int),
+    "dem_grid_entry_counts": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "dem_device_memory_bytes": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dem_counts": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),
+    "dem_download_grid": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "dem_download_history": ([C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "dem_last_phase_times": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "dem_x_compute_forces_timed": ([C.c_void_p, C.c_int], C.c_int),
+    "dem_x_time_steps": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "dem_x_download_half": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),
+    "dem_x_synchronize": ([C.c_void_p], C.c_int),
+}
+
+
+def load_library(path=LIB_PATH):
+    """Load libdemgb300.so (built by ``dem_mbd_cuda_gb300.build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"CUDA engine library missing: {path}; run dem_mbd_cuda_gb300.build.build()")
+        lib = C.CDLL(path)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def options(precision="fp64", cell_factor=2.5, max_cells=0, block_size=0):
+    o = COptions()
+    o.precision = DEM_PRECISION_MIXED if precision in ("mixed", "fp32", DEM_PRECISION_MIXED) else DEM_PRECISION_FP64
+    o.cell_factor = float(cell_factor)
+    o.max_cells = int(max_cells)
+    o.block_size = int(block_size)
+    return o
+
+
+class CudaDemSolver:
+    """GB300 engine with the reference's CudaDemSolver call surface."""
+
+    def __init__(self):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self._check(self.lib.dem_create(C.byref(h)))
+        self.h = h
+        self._keep = []
+        self.n = self.nc = self.nb = self.nt = self.nw = 0
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(self.lib.dem_last_error().decode() or f"dem error {rc}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ lifecycle
+    def initialize(self, scene, opts=None, **kw):
+        """CudaDemSolver::initialize; ``scene`` is a Scene or a list (batch)."""
+        o = opts if opts is not None else options(**kw)
+        if isinstance(scene, (list, tuple)):
+            cs = (self._scene_struct() * len(scene))()
+            for k, s in enumerate(scene):
+                c, keep = s.to_c()
+                cs[k] = c
+                self._keep.append(keep)
+            self._keep.append(cs)
+            self._check(self.lib.dem_initialize_batch(self.h, C.cast(cs, C.c_void_p), len(scene), C.byref(o)))
+        else:
+            c, keep = scene.to_c()
+            self._keep += [c, keep]
+            self._check(self.lib.dem_initialize(self.h, C.byref(c), C.byref(o)))
+        vals = [C.c_int() for _ in range(5)]
+        self._check(self.lib.dem_counts(self.h, *[C.byref(v) for v in vals]))
+        self.n, self.nc, self.nb, self.nt, self.nw = (v.value for v in vals)
+        return self
+
+    @staticmethod
+    def _scene_struct():
+        from .scene import CScene
+        return CScene
+
+    def computeForces(self, time=0.0, bodies=None, body_forces=True, collect_diagnostics=False):
+        """Returns the [nb, 6] body loads (contact + m g) when requested."""
+        bs = None
+        if bodies is not None and self.nb > 0:
+            arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in bodies]
+            self._keep_bs = arrs
+            bs = CBodyStates(*[a.ctypes.data for a in arrs])
+        out = np.zeros((max(self.nb, 1), 6)) if (body_forces and self.nb > 0) else None
+        self._check(self.lib.dem_compute_forces(self.h, float(time), C.byref(bs) if bs is not None else None, _p(out),
+                                                int(bool(collect_diagnostics))))
+        return None if out is None else out[:self.nb]
+
+    def initializeParticleHalfStep(self, half_dt):
+        self._check(self.lib.dem_leapfrog_init(self.h, float(half_dt)))
+
+    def advanceParticles(self, dt):
+        self._check(self.lib.dem_leapfrog_advance(self.h, float(dt)))
+        return 0.0
+
+    def finishParticleStep(self, dt, half_dt=None):
+        self._check(self.lib.dem_leapfrog_finish(self.h, float(dt), float(0.5 * dt if half_dt is None else half_dt)))
+
+    def run(self, steps):
+        """Reference integration loop (pure DEM or DEM-MBD) for ``steps`` steps."""
+        self._check(self.lib.dem_run_steps(self.h, int(steps)))
+
+    def saveContactHistory(self, path):
+        self._check(self.lib.dem_save_history(self.h, os.fsencode(path)))
+
+    def loadContactHistory(self, path):
+        self._check(self.lib.dem_load_history(self.h, os.fsencode(path)))
+
+    def hasRestoredParticleLeapfrogState(self):
+        r = C.c_int()
+        self._check(self.lib.dem_has_restored_leapfrog_state(self.h, C.byref(r)))
+        return bool(r.value)
+
+    # -------------------------------------------------------------- outputs
+    def downloadParticleState(self):
+        n = self.n
+        pos, vel, omg, q = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 4))
+        self._check(self.lib.dem_download_state(self.h, _p(pos), _p(vel), _p(omg), _p(q)))
+        return dict(pos=pos, vel=vel, omega=omg, quat=q)
+
+    def downloadHalfState(self):
+        n = self.n
+        vh, wh, hdq, acc, aacc = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 4)), np.zeros((n, 3)), np.zeros((n, 3))
+        self._check(self.lib.dem_x_download_half(self.h, _p(vh), _p(wh), _p(hdq), _p(acc), _p(aacc)))
+        return dict(vh=vh, wh=wh, hdq=hdq, acc=acc, aacc=aacc)
+
+    def downloadForceOutput(self, particle_forces=True, body_forces=True):
+        n, nb = self.n, self.nb
+        c, f, w, t = (np.zeros((n, 6)) for _ in range(4))
+        bp = np.zeros((nb, n, 6)) if (nb and particle_forces) else None
+        bd = np.zeros((nb, n, 19)) if (nb and body_forces) else None
+        self._check(self.lib.dem_download_forces(self.h, _p(c), _p(f), _p(w), _p(t), _p(bp), _p(bd)))
+        return dict(contact=c, field=f, wall=w, total=t, body_particle=bp, body_detail=bd)
+
+    def stepStats(self):
+        s = CStepStats()
+        self._check(self.lib.dem_stats(self.h, C.byref(s)))
+        return s.to_dict()
+
+    def bodyDiagnostics(self):
+        nb = max(self.nb, 1)
+        ri = np.zeros((nb, 7), dtype=np.uint64)
+        rv = np.zeros((nb, 7), dtype=np.uint64)
+        mi = np.zeros((nb, 22))
+        mv = np.zeros((nb, 22))
+        self._check(self.lib.dem_body_diagnostics(self.h, _p(ri), _p(rv), _p(mi), _p(mv)))
+        k = self.nb
+        return dict(regime_instant=ri[:k], regime_interval=rv[:k], micro_instant=mi[:k], micro_interval=mv[:k])
+
+    def bodies(self):
+        nb = max(self.nb, 1)
+        c, q, v, w, l = np.zeros((nb, 3)), np.zeros((nb, 4)), np.zeros((nb, 3)), np.zeros((nb, 3)), np.zeros((nb, 6))
+        self._check(self.lib.dem_get_bodies(self.h, _p(c), _p(q), _p(v), _p(w), _p(l)))
+        k = self.nb
+        return dict(center=c[:k], quat=q[:k], vel=v[:k], omega=w[:k], loads=l[:k])
+
+    def particleGridEntryCount(self):
+        a, b = C.c_size_t(), C.c_size_t()
+        self._check(self.lib.dem_grid_entry_counts(self.h, C.byref(a), C.byref(b)))
+        return a.value
+
+    def triangleGridEntryCount(self):
+        a, b = C.c_size_t(), C.c_size_t()
+        self._check(self.lib.dem_grid_entry_counts(self.h, C.byref(a), C.byref(b)))
+        return b.value
+
+    def deviceMemoryBytes(self):
+        b = C.c_size_t()
+        self._check(self.lib.dem_device_memory_bytes(self.h, C.byref(b)))
+        return b.value
+
+    # ------------------------------------------------- parity introspection
+    def grid(self):
+        k = np.zeros(self.nc, dtype=np.uint64)
+        i = np.zeros(self.nc, dtype=np.int32)
+        self._check(self.lib.dem_download_grid(self.h, _p(k), _p(i)))
+        return k, i
+
+    def history(self, kind):
+        slots = (64, 16, 64)[kind]
+        s = self.nc * slots
+        keys = np.zeros(s, dtype=np.uint64)
+        last = np.zeros(s, dtype=np.int32)
+        val = np.zeros((s, 9))
+        self._check(self.lib.dem_download_history(self.h, int(kind), _p(keys), _p(last), _p(val)))
+        return keys.reshape(self.nc, slots), last.reshape(self.nc, slots), val.reshape(self.nc, slots, 9)
+
+    def compute_forces_timed(self, diag=False):
+        self._check(self.lib.dem_x_compute_forces_timed(self.h, int(diag)))
+        ms = (C.c_float * 16)()
+        cnt = C.c_int()
+        self._check(self.lib.dem_last_phase_times(self.h, ms, 16, C.byref(cnt)))
+        return [ms[k] for k in range(cnt.value)]
+
+    def time_steps(self, steps):
+        ms = C.c_float()
+        self._check(self.lib.dem_x_time_steps(self.h, int(steps), C.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        self._check(self.lib.dem_x_synchronize(self.h))
+
+
+def device_available():
+    try:
+        return bool(load_library().dem_device_available())
+    except Exception:
+        return False

@@ -1,0 +1,380 @@
+"""Seeded synthetic scenes in the reference's units and conventions.
+
+The reference ships no benchmark inputs beyond its 1704-particle validation
+cases, so every workload is generated here from a fixed seed.  Beds are built
+on a jittered simple-cubic lattice; radii are drawn from the stated
+distribution and then clipped, in lattice-wavefront order, so that no pair
+overlaps by more than ``overlap`` metres.  That gives a resting bed with
+gentle initial contacts (a settled-bed contact count without a settling run).
+All MECH fields are set explicitly (the reference's defaults enable cohesion).
+
+Meshes follow the reference's convention: faces are 1-based vertex triples
+whose normal (v3 - v2) x (v4 - v2) points toward the particles
+(src/multibody.cpp:123-135), with vertices in the body frame.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .scene import Mech, Scene, make_spheres, mesh_to_triangles
+
+DENSITY = 2500.0
+
+
+def mech(kN=1e5, epsN=0.5, epsS=0.5, mu=0.3, muT=0.0, muR=0.0, beta=0.5, cohesion=0.0):
+    return Mech(epsS=epsS, mu=mu, epsN=epsN, cohesion=cohesion, beta=beta, muT=muT, muR=muR, kN=kN)
+
+
+def box_walls(lo, hi, top=False):
+    """Floor and four side walls of an axis-aligned box, normals inward
+    (Wall.bt convention, src/wall.cpp:13-35)."""
+    lo = np.asarray(lo, float)
+    hi = np.asarray(hi, float)
+    o, n = [], []
+    o.append([0, 0, lo[2]]); n.append([0, 0, 1])
+    if top:
+        o.append([0, 0, hi[2]]); n.append([0, 0, -1])
+    o.append([lo[0], 0, 0]); n.append([1, 0, 0])
+    o.append([hi[0], 0, 0]); n.append([-1, 0, 0])
+    o.append([0, lo[1], 0]); n.append([0, 1, 0])
+    o.append([0, hi[1], 0]); n.append([0, -1, 0])
+    return np.array(o, float), np.array(n, float)
+
+
+def lattice_sites(counts, pitch, origin, jitter, rng):
+    nx, ny, nz = counts
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    idx = np.stack([ix.ravel(), iy.ravel(), iz.ravel()], axis=1)
+    pos = np.asarray(origin, float) + idx * pitch
+    pos = pos + rng.uniform(-jitter, jitter, size=pos.shape)
+    return idx, pos
+
+
+def clip_radii(idx, pos, radius, counts, overlap, keep=None):
+    """Clip radii in wavefront order (ix+iy+iz) against the six face
+    neighbours assigned before, so every pair overlaps by at most
+    ``overlap``; pairs that would have overlapped more end up in contact."""
+    nx, ny, nz = counts
+    r = radius.copy()
+    lin = (idx[:, 0] * ny + idx[:, 1]) * nz + idx[:, 2]
+    grid = -np.ones(nx * ny * nz, dtype=np.int64)
+    grid[lin] = np.arange(len(lin))
+    if keep is not None:
+        grid[lin[~keep]] = -1
+    wave = idx.sum(axis=1)
+    order = np.argsort(wave, kind="stable")
+    bounds = np.searchsorted(wave[order], np.arange(wave.max() + 2))
+    for k in range(len(bounds) - 1):
+        sel = order[bounds[k]:bounds[k + 1]]
+        if keep is not None:
+            sel = sel[keep[sel]]
+        if len(sel) == 0:
+            continue
+        for d in ((1, 0, 0), (0, 1, 0), (0, 0, 1)):
+            nb = idx[sel] - np.array(d)
+            ok = (nb >= 0).all(axis=1)
+            nl = (nb[:, 0] * ny + nb[:, 1]) * nz + nb[:, 2]
+            j = np.where(ok, grid[np.where(ok, nl, 0)], -1)
+            has = j >= 0
+            if not has.any():
+                continue
+            s, jj = sel[has], j[has]
+            dist = np.linalg.norm(pos[s] - pos[jj], axis=1)
+            r[s] = np.minimum(r[s], dist - r[jj] + overlap)
+    return r
+
+
+def bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=0, jitter=0.2e-3, overlap=1e-7, radius_fn=None,
+        inside=None, center_xy=True):
+    """Lattice bed of about ``n`` spheres; ``inside(pos) -> bool mask`` removes
+    sites (e.g. the volume of a body).  With ``center_xy`` the lattice is
+    centred on x = y = 0 and ``origin`` only sets its lowest z."""
+    rng = np.random.default_rng(seed)
+    ax, ay = aspect[0], aspect[1]
+    base = (n / (ax * ay)) ** (1.0 / 3.0)
+    nx = max(1, int(round(base * ax)))
+    ny = max(1, int(round(base * ay)))
+    nz = max(1, int(np.ceil(n / (nx * ny))))
+    counts = (nx, ny, nz)
+    origin = np.array(origin, float)
+    if center_xy:
+        origin[0] = -(nx - 1) * pitch / 2
+        origin[1] = -(ny - 1) * pitch / 2
+    while True:
+        counts = (nx, ny, nz)
+        idx, pos = lattice_sites(counts, pitch, origin, jitter, np.random.default_rng(seed))
+        keep = np.ones(len(pos), bool)
+        if inside is not None:
+            keep &= ~inside(pos)
+        if keep.sum() >= n:
+            break
+        nz += max(1, int(np.ceil((n - keep.sum()) / (nx * ny))))
+    # trim to exactly n kept sites, lowest layers first
+    order = np.lexsort((idx[:, 1], idx[:, 0], idx[:, 2]))
+    kept = order[keep[order]][:n]
+    keep = np.zeros(len(pos), bool)
+    keep[kept] = True
+    if radius_fn is None:
+        radius = rng.uniform(rmin, rmax, size=len(pos))
+    else:
+        radius = radius_fn(rng, len(pos))
+    radius = clip_radii(idx, pos, radius, counts, overlap, keep=keep)
+    radius = np.maximum(radius, 0.25 * rmin)
+    sel = np.nonzero(keep)[0]
+    return pos[sel], radius[sel], rng
+
+
+def box_mesh(half, subdiv):
+    """Closed box centred at the origin, faces subdivided (na, nb, nc) along
+    x, y, z; outward normals."""
+    hx, hy, hz = half
+    na, nb, nc = subdiv
+    verts, faces = [], []
+
+    def face(origin, u, v, nu, nv, normal):
+        o = np.asarray(origin, float)
+        u = np.asarray(u, float)
+        v = np.asarray(v, float)
+        base = len(verts)
+        for a in range(nu + 1):
+            for b in range(nv + 1):
+                verts.append(o + u * (a / nu) + v * (b / nv))
+        for a in range(nu):
+            for b in range(nv):
+                p00 = base + a * (nv + 1) + b
+                p10 = p00 + (nv + 1)
+                p01 = p00 + 1
+                p11 = p10 + 1
+                tri = [(p00, p10, p11), (p00, p11, p01)]
+                for t in tri:
+                    vv = [verts[k] for k in t]
+                    nrm = np.cross(vv[1] - vv[0], vv[2] - vv[0])
+                    if np.dot(nrm, normal) < 0:
+                        t = (t[0], t[2], t[1])
+                    faces.append([k + 1 for k in t])
+
+    face([hx, -hy, -hz], [0, 2 * hy, 0], [0, 0, 2 * hz], nb, nc, [1, 0, 0])
+    face([-hx, -hy, -hz], [0, 2 * hy, 0], [0, 0, 2 * hz], nb, nc, [-1, 0, 0])
+    face([-hx, hy, -hz], [2 * hx, 0, 0], [0, 0, 2 * hz], na, nc, [0, 1, 0])
+    face([-hx, -hy, -hz], [2 * hx, 0, 0], [0, 0, 2 * hz], na, nc, [0, -1, 0])
+    face([-hx, -hy, hz], [2 * hx, 0, 0], [0, 2 * hy, 0], na, nb, [0, 0, 1])
+    face([-hx, -hy, -hz], [2 * hx, 0, 0], [0, 2 * hy, 0], na, nb, [0, 0, -1])
+    return np.array(verts), np.array(faces, dtype=np.int64)
+
+
+def cylinder_mesh(radius, length, ntheta, nx, nrings):
+    """Closed cylinder along x centred at the origin with INWARD normals (a
+    drum: particles are inside)."""
+    verts, faces = [], []
+    th = np.linspace(0, 2 * np.pi, ntheta, endpoint=False)
+    xs = np.linspace(-length / 2, length / 2, nx + 1)
+
+    def tri(a, b, c, want):
+        va, vb, vc = verts[a], verts[b], verts[c]
+        nrm = np.cross(vb - va, vc - va)
+        if np.dot(nrm, want) < 0:
+            b, c = c, b
+        faces.append([a + 1, b + 1, c + 1])
+
+    base = len(verts)
+    for x in xs:
+        for t in th:
+            verts.append(np.array([x, radius * np.cos(t), radius * np.sin(t)]))
+    for i in range(nx):
+        for j in range(ntheta):
+            a = base + i * ntheta + j
+            b = base + i * ntheta + (j + 1) % ntheta
+            c = base + (i + 1) * ntheta + j
+            d = base + (i + 1) * ntheta + (j + 1) % ntheta
+            mid = (verts[a] + verts[d]) / 2
+            want = -np.array([0, mid[1], mid[2]])
+            tri(a, b, d, want)
+            tri(a, d, c, want)
+    for side, x in ((-1, -length / 2), (1, length / 2)):
+        want = np.array([-side, 0, 0], float)
+        center = len(verts)
+        verts.append(np.array([x, 0.0, 0.0]))
+        rings = [center]
+        for k in range(1, nrings + 1):
+            rk = radius * k / nrings
+            start = len(verts)
+            for t in th:
+                verts.append(np.array([x, rk * np.cos(t), rk * np.sin(t)]))
+            rings.append(start)
+        for j in range(ntheta):
+            tri(center, rings[1] + j, rings[1] + (j + 1) % ntheta, want)
+        for k in range(1, nrings):
+            for j in range(ntheta):
+                a = rings[k] + j
+                b = rings[k] + (j + 1) % ntheta
+                c = rings[k + 1] + j
+                d = rings[k + 1] + (j + 1) % ntheta
+                tri(a, b, d, want)
+                tri(a, d, c, want)
+    return np.array(verts), np.array(faces, dtype=np.int64)
+
+
+def _attach(kw, bodies):
+    nb = len(bodies)
+    tris, tb = [], []
+    for i, b in enumerate(bodies):
+        t = mesh_to_triangles(b["vertices"], b["faces"])
+        tris.append(t)
+        tb.append(np.full(len(t), i, dtype=np.int32))
+    kw.update(body_mass=np.array([b["mass"] for b in bodies], float),
+              body_center=np.array([b["center"] for b in bodies], float).reshape(nb, 3),
+              body_quat=np.array([b.get("quat", [1, 0, 0, 0]) for b in bodies], float).reshape(nb, 4),
+              body_vel=np.array([b.get("vel", [0, 0, 0]) for b in bodies], float).reshape(nb, 3),
+              body_omega=np.array([b.get("omega", [0, 0, 0]) for b in bodies], float).reshape(nb, 3),
+              body_inertia=np.array([b["inertia"] for b in bodies], float).reshape(nb, 9),
+              body_state=np.array([b["state"] for b in bodies], np.int32),
+              tri_body=np.concatenate(tb), tri_local=np.concatenate(tris))
+    return kw
+
+
+def pure_dem(n=20000, seed=1000, rmin=1.8e-3, rmax=2.2e-3, box=(0.2, 0.2, 0.4), dt=1e-5, kN=1e5, epsN=0.5, mu=0.3,
+             pitch=None, name="c0_pure_dem"):
+    """Config 0: spheres r ~ U[rmin, rmax] on a jittered lattice in a box of 5
+    walls (floor + 4 sides), kN 1e5, restitution 0.5, friction 0.3."""
+    pitch = pitch if pitch is not None else 2.0 * rmin + 0.1e-3
+    lo = np.array([-box[0] / 2, -box[1] / 2, 0.0])
+    hi = np.array([box[0] / 2, box[1] / 2, box[2]])
+    width = box[0] - 2 * rmax
+    per = int(width // pitch)
+    origin = lo + np.array([rmax, rmax, rmax]) + (width - (per - 1) * pitch) / 2 * np.array([1, 1, 0])
+    origin[2] = rmax + 0.3e-3
+    pos, rad, _ = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed)
+    assert pos[:, 0].max() + rad.max() < hi[0] and pos[:, 1].max() + rad.max() < hi[1], "bed exceeds the box"
+    kw = make_spheres(pos, rad, DENSITY)
+    wo, wn = box_walls(lo, hi)
+    m = mech(kN=kN, epsN=epsN, epsS=epsN, mu=mu)
+    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
+                 wall_normal=wn, name=name)
+
+
+def mbd_blade_plate(n=200000, seed=1001, rmin=1.5e-3, rmax=2.5e-3, box=0.4, dt=5e-6, name="c1_dem_mbd"):
+    """Config 1: spheres r ~ U[1.5, 2.5] mm in a 0.4 m box with a rotating
+    blade (prescribed, omega_z = 3) and a 1 kg dynamic plate
+    (inertia 1e-3 I) resting on the bed; wall/triangle friction 0.4."""
+    pitch = 2.0 * rmin + 0.3e-3
+    lo = np.array([-box / 2, -box / 2, 0.0])
+    hi = np.array([box / 2, box / 2, box])
+    per = int((box - 2 * rmax) // pitch)
+    span = (per - 1) * pitch
+    origin = np.array([-span / 2, -span / 2, rmax + 0.3e-3])
+    blade_half = (0.12, 0.006, 0.05)
+    blade_center = np.array([0.0, 0.0, 0.06])
+    blade_v, blade_f = box_mesh(blade_half, (32, 2, 13))
+
+    def in_blade(p):
+        d = np.abs(p - blade_center)
+        return (d[:, 0] < blade_half[0] + rmax + 0.5e-3) & (d[:, 1] < blade_half[1] + rmax + 0.5e-3) & \
+               (d[:, 2] < blade_half[2] + rmax + 0.5e-3)
+
+    pos, rad, _ = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed, inside=in_blade)
+    plate_half = (0.05, 0.05, 0.002)
+    plate_xy = np.array([0.08, 0.08])
+    under = (np.abs(pos[:, 0] - plate_xy[0]) < plate_half[0]) & (np.abs(pos[:, 1] - plate_xy[1]) < plate_half[1])
+    top = float((pos[under, 2] + rad[under]).max())
+    plate_v, plate_f = box_mesh(plate_half, (6, 6, 1))
+    plate_center = np.array([plate_xy[0], plate_xy[1], top + plate_half[2] - 2e-7])
+    kw = make_spheres(pos, rad, DENSITY)
+    wo, wn = box_walls(lo, hi)
+    pp = mech(kN=1e5, epsN=0.5, epsS=0.5, mu=0.3)
+    pt = mech(kN=1e5, epsN=0.5, epsS=0.5, mu=0.4)
+    bodies = [dict(vertices=blade_v, faces=blade_f, mass=5.0, center=blade_center, omega=[0, 0, 3.0],
+                   inertia=[1, 0, 0, 0, 1, 0, 0, 0, 1], state=2),
+              dict(vertices=plate_v, faces=plate_f, mass=1.0, center=plate_center,
+                   inertia=[1e-3, 0, 0, 0, 1e-3, 0, 0, 0, 1e-3], state=0)]
+    _attach(kw, bodies)
+    return Scene(**kw, pp=pp, pt=pt, pw=pt, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
+                 wall_normal=wn, name=name), [(blade_v, blade_f), (plate_v, plate_f)]
+
+
+def drum(n=2000000, seed=1002, radius=0.3, length=0.5, omega=2.0, dt=2e-6, name="c2_drum", ntheta=160, nx=50,
+         nrings=6):
+    """Config 2: lognormal radii (median 1 mm, sigma 0.25, clipped to
+    [0.5, 2] mm) in a rotating closed cylinder (axis x, inward normals,
+    prescribed omega_x), friction 0.5, restitution 0.3, kN 1e5."""
+
+    def radius_fn(rng, k):
+        return np.clip(np.exp(np.log(1e-3) + 0.25 * rng.standard_normal(k)), 0.5e-3, 2.0e-3)
+
+    rmax = 2.0e-3
+    pitch = 2.15e-3
+    inner = radius - rmax - 1e-3
+    ny = int(2 * inner / pitch)
+    nxl = int((length - 2 * rmax - 2e-3) / pitch)
+
+    def outside(p):
+        return (p[:, 1] ** 2 + p[:, 2] ** 2) > inner ** 2
+
+    origin = np.array([-(nxl - 1) * pitch / 2, -(ny - 1) * pitch / 2, -inner + 0.2e-3])
+    aspect = (nxl / ny, 1.0, None)
+    pos, rad, _ = bed(n, 0.5e-3, rmax, pitch, origin, aspect=aspect, seed=seed, jitter=0.1e-3, radius_fn=radius_fn,
+                      inside=outside)
+    kw = make_spheres(pos, rad, DENSITY)
+    v, f = cylinder_mesh(radius, length, ntheta, nx, nrings)
+    m = mech(kN=1e5, epsN=0.3, epsS=0.3, mu=0.5)
+    bodies = [dict(vertices=v, faces=f, mass=100.0, center=[0, 0, 0], omega=[omega, 0, 0],
+                   inertia=[10, 0, 0, 0, 10, 0, 0, 0, 10], state=2)]
+    _attach(kw, bodies)
+    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, name=name), [(v, f)]
+
+
+def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5):
+    """Config 4: independent box scenes with N_s ~ U[2k, 40k], per-scene
+    friction ~ U[0.1, 0.7] and restitution ~ U[0.2, 0.8]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(nscenes):
+        ns = int(rng.integers(nmin, nmax + 1))
+        mu = float(rng.uniform(0.1, 0.7))
+        e = float(rng.uniform(0.2, 0.8))
+        sc = pure_dem(n=ns, seed=seed * 1000 + s, box=(0.1, 0.1, 0.4), dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}")
+        out.append(sc)
+    return out
+
+
+def small_mbd(n=400, seed=7, dt=2e-5, name="small_mbd"):
+    """A few hundred spheres on a tilted plate body plus walls, for tests."""
+    rmin, rmax = 1.8e-3, 2.2e-3
+    pitch = 3.9e-3
+    k = int(np.ceil(np.sqrt(n / 4)))
+    origin = np.array([-(k - 1) * pitch / 2, -(k - 1) * pitch / 2, 0.004])
+    pos, rad, rng = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed, overlap=5e-6)
+    kw = make_spheres(pos, rad, DENSITY, vel=rng.normal(0, 0.01, size=(len(pos), 3)))
+    kw["omega"] = rng.normal(0, 5.0, size=(len(pos), 3))
+    half = k * pitch / 2 + 0.01
+    plate_v, plate_f = box_mesh((half, half, 0.001), (8, 8, 1))
+    th = 0.05
+    qp = [np.cos(th / 2), np.sin(th / 2), 0.0, 0.0]
+    wo, wn = box_walls([-half, -half, -0.05], [half, half, 0.2])
+    m = mech(kN=1e5, epsN=0.5, epsS=0.6, mu=0.4, muT=0.1, muR=0.05, beta=0.5, cohesion=0.0)
+    bodies = [dict(vertices=plate_v, faces=plate_f, mass=0.5, center=[0.0, 0.0, 0.0011], quat=qp,
+                   omega=[0.0, 0.0, 0.5], inertia=[1e-3, 0, 0, 0, 1e-3, 0, 0, 0, 2e-3], state=0)]
+    _attach(kw, bodies)
+    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
+                 wall_normal=wn, keep_body_particle=1, keep_body_detail=1, name=name)
+
+
+def small_dem(n=500, seed=3, dt=1e-5, rmin=1.8e-3, rmax=2.2e-3, vel_std=0.01, omega_std=5.0, muT=0.1, muR=0.05,
+              overlap=5e-6, name="small_dem"):
+    """A few hundred spheres in a small box with random velocities and spins,
+    all history channels active (tests)."""
+    box = (0.04, 0.04, 0.1)
+    pitch = 3.9e-3
+    lo = np.array([-box[0] / 2, -box[1] / 2, 0.0])
+    hi = np.array([box[0] / 2, box[1] / 2, box[2]])
+    per = int((box[0] - 2 * rmax) // pitch)
+    span = (per - 1) * pitch
+    origin = np.array([-span / 2, -span / 2, rmax + 0.1e-3])
+    pos, rad, rng = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed, overlap=overlap)
+    kw = make_spheres(pos, rad, DENSITY, vel=rng.normal(0, vel_std, size=(len(pos), 3)))
+    kw["omega"] = rng.normal(0, omega_std, size=(len(pos), 3))
+    q = rng.normal(size=(len(pos), 4))
+    kw["quat"] = q / np.linalg.norm(q, axis=1, keepdims=True)
+    wo, wn = box_walls(lo, hi)
+    m = mech(kN=1e5, epsN=0.5, epsS=0.6, mu=0.4, muT=muT, muR=muR, beta=0.5)
+    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
+                 wall_normal=wn, name=name)
