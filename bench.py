@@ -158,20 +158,40 @@ def cpu_baseline(scene, budget_s=12.0, threads=None):
     return scene.n * done / dt, threads, done, dt
 
 
-def load_error(scene):
-    """Body-load and particle-force error of the mixed form against the FP64
-    form from the same state (first evaluation)."""
+def load_error(scene, evaluations=3):
+    """Error of the mixed form against the FP64 form, body loads and particle
+    forces, over the first evaluations of the reference's step sequence
+    (evaluation 0 has dt = 0; later ones start from states that differ only by
+    the previous step's force difference times dt^2).  Reported for the
+    default mixed form (particle-triangle law in FP64) and with the
+    particle-triangle law in FP32 as well."""
     from dem_mbd_cuda_gb300.engine import CudaDemSolver
-    a = CudaDemSolver().initialize(scene, precision="fp64")
-    b = CudaDemSolver().initialize(scene, precision="mixed")
-    bs = scene.body_states() if scene.n_bodies else None
-    la = a.computeForces(0.0, bs, True, True)
-    lb = b.computeForces(0.0, bs, True, True)
-    fa = a.downloadForceOutput(False, False)["total"]
-    fb = b.downloadForceOutput(False, False)["total"]
-    out = {"force_rel_err_max": float(np.abs(fa - fb).max() / max(np.abs(fa).max(), 1e-30))}
-    if la is not None and len(la):
-        out["body_load_rel_err"] = float(np.abs(la - lb).max() / max(np.abs(la).max(), 1e-30))
+    out = {}
+    for label, kw in (("mixed", {}), ("mixed_pt_fp32", {"pt_fp32": True})):
+        a = CudaDemSolver().initialize(scene, precision="fp64")
+        b = CudaDemSolver().initialize(scene, precision="mixed", **kw)
+        bs = scene.body_states() if scene.n_bodies else None
+        dt = scene.dt
+        load_err, force_err = [], []
+        for k in range(evaluations):
+            if k == 1:
+                a.initializeParticleHalfStep(0.5 * dt)
+                b.initializeParticleHalfStep(0.5 * dt)
+            if k >= 1:
+                a.advanceParticles(dt)
+                b.advanceParticles(dt)
+            la = a.computeForces(k * dt, bs, True, True)
+            lb = b.computeForces(k * dt, bs, True, True)
+            fa = a.downloadForceOutput(False, False)["total"]
+            fb = b.downloadForceOutput(False, False)["total"]
+            force_err.append(float(np.abs(fa - fb).max() / max(np.abs(fa).max(), 1e-30)))
+            if la is not None and len(la):
+                load_err.append(float(np.abs(la - lb).max() / max(np.abs(la).max(), 1e-30)))
+            a.finishParticleStep(dt)
+            b.finishParticleStep(dt)
+        out[label] = {"force_rel_err_max": force_err, "body_load_rel_err": load_err}
+        if scene.n_bodies == 0:
+            break
     return out
 
 
@@ -184,6 +204,8 @@ def main():
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--single", action="store_true",
+                    help="headline precision only: no second precision, e2e, error or CPU legs (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -227,6 +249,11 @@ def main():
     if dist:
         dist.barrier()
     e, ms, clocks, stats, phases, _ = run_engine(scene, args.precision, args.steps, args.warmup)
+    if args.single:
+        print(json.dumps({"metric": "particle-steps/s", "value": scene.n * args.steps / (ms / 1000.0),
+                          "ms_per_step": ms / args.steps, "precision": args.precision, "phase_ms": phases,
+                          "contact_sides_per_step": stats["particle_contacts"], "clocks": clocks}))
+        return
     other = "fp64" if args.precision == "mixed" else "mixed"
     e_o, ms_o, _, _, phases_o, _ = run_engine(scene, other, args.steps, args.warmup)
     del e_o

@@ -11,7 +11,8 @@ DEM_PRECISION_MIXED = 1
 
 
 class COptions(C.Structure):
-    _fields_ = [("precision", C.c_int), ("cell_factor", C.c_double), ("max_cells", C.c_int), ("block_size", C.c_int)]
+    _fields_ = [("precision", C.c_int), ("cell_factor", C.c_double), ("max_cells", C.c_int), ("block_size", C.c_int),
+                ("pt_fp32", C.c_int)]
 
 
 class CBodyStates(C.Structure):

@@ -163,53 +163,44 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
     }
 }
 
-// ------------------------------------------------------------- broadphase
-constexpr int kMaxContacts = kPSlots;
-
-template <typename T>
-__global__ void __launch_bounds__(128) k_broadphase(Grid g, Recs r, const SceneC* __restrict__ sc, Walls walls,
-                                                    Tris tris, Hist<T> hp, Hist<T> hw, Hist<T> hb, Contacts<T> ct,
-                                                    Counters k, double dt_eff)
+// ------------------------------------------------------ expiry and walls
+// Per component in input order: expireHistory for the three slot arrays
+// (:1109-1117), then the planar walls of its scene (wallContact, :975-1063).
+template <typename T, typename TB>
+__global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
+                                                      Hist<T> hp, Hist<T> hw, Hist<TB> hb, Contacts<T> ct, Counters k,
+                                                      double dt_eff)
 {
     const int step = *k.step;
-    const int nvalid = *g.nvalid;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int count = 0, pover = 0, bover = 0, phigh = 0, bhigh = 0;
-    int stage_t[kMaxContacts];
-    int stage_s[kMaxContacts];
-    int ci = -1;
-    int pt_flag = 0;
-    if (t < nvalid) {
-        const int4 meta = r.meta[t];
-        ci = meta.x;
-        const int owner = meta.y, s = meta.w;
-        const SceneC S = sc[s];
-        const int4 cell = r.cell[t];
-        const D4 pi = r.pos[t];
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    int bover = 0, bhigh = 0;
+    if (ci < c.n) {
         expire(hp, kPSlots, ci, step);
         expire(hw, kWSlots, ci, step);
         expire(hb, kBSlots, ci, step);
-
-        // walls (wallContact, :975-1063)
+        const int w = c.owner[ci];
+        const SceneC& S = sc[o.scene[w]];
         V3<double> wF = mk(0.0, 0.0, 0.0), wT = mk(0.0, 0.0, 0.0);
         if (S.wall_count > 0) {
+            const V3<double> p = mk(c.x[ci], c.y[ci], c.z[ci]);
+            const double rad = c.radius[ci];
             int whw = hw.hw[ci];
-            const D4 v4 = r.v[t];
-            const D4 w4 = r.w[t];
-            const V3<double> off = r.off ? d3(r.off[t]) : mk(0.0, 0.0, 0.0);
             for (int wl = 0; wl < S.wall_count; ++wl) {
                 const int wg = S.wall_begin + wl;
                 const V3<double> out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
                 const V3<double> org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
-                const double dist = dot(d3(pi) - org, out);
-                const double depth = pi.w - dist;
+                const double depth = rad - dot(p - org, out);
                 if (depth <= 0.0) continue;
                 const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
                 if (slot < 0) { ++bover; continue; }
                 T* hv = hw.val + ((size_t)ci * kWSlots + slot) * 9;
+                const V3<double> vel = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
+                const V3<double> om =
+                    rot_iv(o.qw[w], o.qx[w], o.qy[w], o.qz[w], mk(o.wx[w], o.wy[w], o.wz[w]));
+                const V3<double> off = c.ox ? mk(c.ox[ci], c.oy[ci], c.oz[ci]) : mk(0.0, 0.0, 0.0);
                 V3<T> f, cpl;
-                wall_law<T>(S.pw, T(dt_eff), cvt<T>(out), T(depth), T(pi.w), T(v4.w), cvt<T>(d3(v4)), cvt<T>(d3(w4)),
-                            hv, f, cpl);
+                wall_law<T>(S.pw, T(dt_eff), cvt<T>(out), T(depth), T(rad), T(o.mass[w]), cvt<T>(vel), cvt<T>(om), hv, f,
+                            cpl);
                 const V3<double> fd = cvt<double>(f);
                 wF = wF + fd;
                 wT = wT + (cvt<double>(cpl) + cross(off, fd));
@@ -218,8 +209,38 @@ __global__ void __launch_bounds__(128) k_broadphase(Grid g, Recs r, const SceneC
         }
         double* wr = ct.wres + 6 * (size_t)ci;
         wr[0] = wF.x; wr[1] = wF.y; wr[2] = wF.z; wr[3] = wT.x; wr[4] = wT.y; wr[5] = wT.z;
+    }
+    block_add(k.bover, bover);
+    block_max(k.bhigh, bhigh);
+}
 
-        // particle sweep over the 27 neighbour cells, reference order.
+// ------------------------------------------------------------- particle sweep
+constexpr int kMaxContacts = kPSlots;
+
+// One thread per component in cell order: the reference's 27-cell sweep
+// (:1124-1146) over the cell start table.  An FP32 test on cell-relative
+// coordinates with a margin of 1e-5 cell edges discards far candidates; the
+// survivors get the reference's exact FP64 overlap test, then the history
+// slot in sweep order (acquireHistorySlot, :190-215).  Contacts go to a flat
+// list; results are stored per (slot rank, component) so the owner sum reads
+// them coalesced.
+template <typename T>
+__global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __restrict__ sc, Tris tris, Hist<T> hp,
+                                               Contacts<T> ct, Counters k, int nc)
+{
+    const int step = *k.step;
+    const int nvalid = *g.nvalid;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int count = 0, pover = 0, phigh = 0;
+    int stage_t[kMaxContacts];
+    int stage_s[kMaxContacts];
+    int ci = -1;
+    if (t < nvalid) {
+        const int4 meta = r.meta[t];
+        ci = meta.x;
+        const int owner = meta.y, s = meta.w;
+        const int4 cell = r.cell[t];
+        const D4 pi = r.pos[t];
         const int* lay = g.scene_layout + 8 * s;
         const float4 fi = r.relf[t];
         int phw = hp.hw[ci];
@@ -229,10 +250,11 @@ __global__ void __launch_bounds__(128) k_broadphase(Grid g, Recs r, const SceneC
             for (int dy = -1; dy <= 1; ++dy) {
                 const int ny = cell.y + dy;
                 if (ny < lay[1] || ny >= lay[1] + lay[4]) continue;
+                const int row = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] - lay[2];
                 for (int dz = -1; dz <= 1; ++dz) {
                     const int nz = cell.z + dz;
                     if (nz < lay[2] || nz >= lay[2] + lay[5]) continue;
-                    const int lin = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] + (nz - lay[2]);
+                    const int lin = row + nz;
                     const int b = g.cell_start[lin], e = g.cell_start[lin + 1];
                     const float ox = dx * g.mesh_f - fi.x, oy = dy * g.mesh_f - fi.y, oz = dz * g.mesh_f - fi.z;
                     for (int u = b; u < e; ++u) {
@@ -259,7 +281,9 @@ __global__ void __launch_bounds__(128) k_broadphase(Grid g, Recs r, const SceneC
             }
         }
         hp.hw[ci] = phw;
-        if (S.body_count > 0 && tris.nt > 0) {
+        ct.cnt[ci] = count;
+        int pt_flag = 0;
+        if (tris.nt > 0 && sc[s].body_count > 0) {
             const int lin = cell.w;
             pt_flag = tris.tcell_start[lin + 1] > tris.tcell_start[lin] ? 1 : 0;
         }
@@ -271,17 +295,11 @@ __global__ void __launch_bounds__(128) k_broadphase(Grid g, Recs r, const SceneC
     if (threadIdx.x == 0) s_base = total ? atomicAdd(k.ct_total, total) : 0;
     __syncthreads();
     const int base = s_base + ex;
-    if (ci >= 0) {
-        ct.off[ci] = base;
-        ct.cnt[ci] = count;
-        for (int q = 0; q < count; ++q)
-            ct.ent[base + q] = make_int4(t, stage_t[q], ci * kPSlots + stage_s[q], 0);
-    }
+    for (int q = 0; q < count; ++q)
+        ct.ent[base + q] = make_int4(t, stage_t[q], ci * kPSlots + stage_s[q], q * nc + ci);
     block_add(k.pcontacts, count);
     block_add(k.pover, pover);
-    block_add(k.bover, bover);
     block_max(k.phigh, phigh);
-    block_max(k.bhigh, bhigh);
 }
 
 // ------------------------------------------------------------------ PP law
@@ -323,7 +341,7 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
         pp_law<T>(sc[s].pp, T(dt_eff), n, d, depth, T(d2), T(pi.w), T(pj.w), T(vi.w), T(vj.w), erv, mrv, ewi, ewj, mwi,
                   mwj, hv, f, cpl);
         if (r.off) cpl = cpl + cross(cvt<T>(d3(r.off[e.x])), f);
-        T* out = ct.res + 6 * (size_t)q;
+        T* out = ct.res + 6 * (size_t)e.w;
         out[0] = f.x; out[1] = f.y; out[2] = f.z; out[3] = cpl.x; out[4] = cpl.y; out[5] = cpl.z;
     }
 }
@@ -373,9 +391,9 @@ __device__ double tri_area_scale(const double* W, V3<double> p, double r, double
     return sc > 1.0e-12 ? sc : 0.0;
 }
 
-template <typename T>
+template <typename TC, typename T>
 __global__ void __launch_bounds__(128) k_pt(Recs r, const SceneC* __restrict__ sc, Tris tris, Bodies bodies,
-                                            Hist<T> hb, Contacts<T> ct, Counters k, double dt_eff)
+                                            Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff)
 {
     const int step = *k.step;
     const int total = *ct.pt_total_ptr;
@@ -578,7 +596,7 @@ __global__ void __launch_bounds__(128) k_pt(Recs r, const SceneC* __restrict__ s
             }
         }
         hb.hw[ci] = bhw;
-        double* pr = ct.pt_res + 6 * (size_t)item;
+        double* pr = ct.pt_res + 6 * (size_t)ci;
         pr[0] = bF.x; pr[1] = bF.y; pr[2] = bF.z; pr[3] = bT.x; pr[4] = bT.y; pr[5] = bT.z;
     }
     block_add(k.bover, bover);
@@ -602,9 +620,9 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
     V3<double> cF = mk(0.0, 0.0, 0.0), cT = cF, wF = cF, wT = cF, bF = cF, bT = cF;
     const int c0 = c.sphere ? i : c.ostart[i], c1 = c.sphere ? i + 1 : c.ostart[i + 1];
     for (int ci = c0; ci < c1; ++ci) {
-        const int off = ct.off[ci], cnt = ct.cnt[ci];
+        const int cnt = ct.cnt[ci];
         for (int q = 0; q < cnt; ++q) {
-            const T* rr = ct.res + 6 * (size_t)(off + q);
+            const T* rr = ct.res + 6 * ((size_t)q * c.n + ci);
             cF = cF + mk((double)rr[0], (double)rr[1], (double)rr[2]);
             cT = cT + mk((double)rr[3], (double)rr[4], (double)rr[5]);
         }
@@ -613,7 +631,7 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
         wT = wT + mk(wr[3], wr[4], wr[5]);
         const int pk = ct.pt_index[ci];
         if (pk >= 0) {
-            const double* pr = ct.pt_res + 6 * (size_t)pk;
+            const double* pr = ct.pt_res + 6 * (size_t)ci;
             bF = bF + mk(pr[0], pr[1], pr[2]);
             bT = bT + mk(pr[3], pr[4], pr[5]);
         }
@@ -697,19 +715,21 @@ __global__ void k_body_partial(Recs r, const SceneC* __restrict__ sc, Bodies bod
     }
 }
 
-__global__ void k_body_final(BodyOut bo, int nb, int interval)
+// One block per body, one thread per field, groups summed in a fixed order.
+__global__ void k_body_final(BodyOut bo, int interval)
 {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
-    double acc[kBodyFields];
-    for (int f = 0; f < kBodyFields; ++f) acc[f] = 0.0;
-    for (int g = 0; g < bo.groups; ++g) combine(acc, bo.partial + ((size_t)b * bo.groups + g) * kBodyFields);
-    double* res = bo.result + (size_t)b * kBodyFields;
-    for (int f = 0; f < kBodyFields; ++f) res[f] = acc[f];
+    const int b = blockIdx.x, f = threadIdx.x;
+    if (f >= kBodyFields) return;
+    double acc = 0.0;
+    for (int g = 0; g < bo.groups; ++g) {
+        const double v = bo.partial[((size_t)b * bo.groups + g) * kBodyFields + f];
+        acc = (f == 7) ? fmax(acc, v) : acc + v;
+    }
+    bo.result[(size_t)b * kBodyFields + f] = acc;
     if (interval) {
-        for (int f = 0; f < kRegime; ++f) bo.reg_int[b * kRegime + f] += (unsigned long long)acc[9 + f];
-        for (int f = 0; f < kMicro; ++f) bo.micro_int[b * kMicro + f] += acc[16 + f];
-        if (b == 0) *bo.native_steps += 1ull;
+        if (f >= 9 && f < 9 + kRegime) bo.reg_int[b * kRegime + (f - 9)] += (unsigned long long)acc;
+        if (f >= 16) bo.micro_int[b * kMicro + (f - 16)] += acc;
+        if (b == 0 && f == 0) *bo.native_steps += 1ull;
     }
 }
 
@@ -750,20 +770,20 @@ void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r
     k_gather<T><<<sm_count * 8, 256, 0, s>>>(c, o, g, r, dt_eff);
 }
 
-template <typename T>
+template <typename T, typename TB>
 void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs& r, const SceneC* sc, const Walls& w,
-                     const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<T> hb, Contacts<T> ct,
+                     const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<TB> hb, Contacts<T> ct,
                      const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s)
 {
-    (void)o;
     (void)block;
-    k_broadphase<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, w, t, hp, hw, hb, ct, k, dt_eff);
+    k_expire_walls<T, TB><<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, hp, hw, hb, ct, k, dt_eff);
+    k_sweep<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, ct, k, c.n);
     k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff);
     if (t.nt > 0 && b.nb > 0) {
         launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);
         k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list,
                                                   ct.pt_index, ct.pt_total_ptr);
-        k_pt<T><<<sm_count * 4, 128, 0, s>>>(r, sc, t, b, hb, ct, k, dt_eff);
+        k_pt<T, TB><<<sm_count * 4, 128, 0, s>>>(r, sc, t, b, hb, ct, k, dt_eff);
     }
 }
 
@@ -780,7 +800,7 @@ void launch_body_reduce(const Recs& r, const SceneC* sc, const Bodies& b, Contac
 {
     if (b.nb <= 0) return;
     k_body_partial<T><<<dim3(bo.groups, b.nb), 128, 0, s>>>(r, sc, b, ct, bo);
-    k_body_final<<<blocks(b.nb, 32), 32, 0, s>>>(bo, b.nb, interval ? 1 : 0);
+    k_body_final<<<b.nb, 64, 0, s>>>(bo, interval ? 1 : 0);
 }
 
 template <typename T>
@@ -793,9 +813,10 @@ void launch_body_outputs(const Comps& c, const Owners& o, const Bodies& b, const
 
 #define DEM_INSTANTIATE(T)                                                                                            \
     template void launch_gather<T>(const Comps&, const Owners&, const Grid&, const Recs&, double, int, cudaStream_t); \
-    template void launch_contacts<T>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,           \
-                                     const Walls&, const Tris&, const Bodies&, Hist<T>, Hist<T>, Hist<T>,            \
-                                     Contacts<T>, const Counters&, double, int, int, cudaStream_t);                 \
+    template void launch_contacts<T, double>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,   \
+                                             const Walls&, const Tris&, const Bodies&, Hist<T>, Hist<T>,             \
+                                             Hist<double>, Contacts<T>, const Counters&, double, int, int,            \
+                                             cudaStream_t);                                                          \
     template void launch_owner_sum<T>(const Comps&, const Owners&, const SceneC*, Contacts<T>, bool, double*,       \
                                       double*, double*, double*, cudaStream_t);                                       \
     template void launch_body_reduce<T>(const Recs&, const SceneC*, const Bodies&, Contacts<T>, BodyOut, bool,       \
@@ -805,5 +826,9 @@ void launch_body_outputs(const Comps& c, const Owners& o, const Bodies& b, const
 
 DEM_INSTANTIATE(double)
 DEM_INSTANTIATE(float)
+template void launch_contacts<float, float>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,
+                                            const Walls&, const Tris&, const Bodies&, Hist<float>, Hist<float>,
+                                            Hist<float>, Contacts<float>, const Counters&, double, int, int,
+                                            cudaStream_t);
 
 }  // namespace demgb

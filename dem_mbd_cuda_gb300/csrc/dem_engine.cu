@@ -109,6 +109,7 @@ public:
         if (opt) o = *opt;
         if (o.cell_factor < 2.0) throw DemError(DEM_ERR_INVALID, "cell_factor must be >= 2");
         precision_ = o.precision;
+        pt_fp32_ = (o.precision == DEM_PRECISION_MIXED) && o.pt_fp32;
         cell_factor_ = o.cell_factor;
         block_ = o.block_size > 0 ? o.block_size : 128;
         check(cudaFree(nullptr), "initialize CUDA context");
@@ -310,6 +311,7 @@ public:
         G_.cell_start = arena_.alloc<int>(cap + 2, "cell start");
         G_.sorted_id = arena_.alloc<int>(nc_, "sorted id");
         G_.pos_of = arena_.alloc<int>(nc_, "pos of");
+        G_.sorted_tmp = arena_.alloc<int>(nc_, "sorted scratch");
         G_.sorted_key = arena_.alloc<uint64_t>(nc_, "sorted key");
         std::vector<int> box(6 * S_);
         for (int q = 0; q < S_; ++q) { box[6 * q] = box[6 * q + 1] = box[6 * q + 2] = INT_MAX; box[6 * q + 3] = box[6 * q + 4] = box[6 * q + 5] = INT_MIN; }
@@ -359,6 +361,8 @@ public:
             tcap = std::min<long long>(tcap + 1024, (1LL << 31) - 64);
             T_.capacity = (int)tcap;
             T_.ttri = arena_.alloc<int>(tcap, "tri grid ids");
+            T_.ttri_tmp = arena_.alloc<int>(tcap, "tri grid scratch ids");
+            T_.tlin_tmp = arena_.alloc<int>(tcap, "tri grid scratch cells");
             T_.tcell_count = arena_.alloc<int>(cap + 1, "tri cell count");
             T_.tcell_cursor = arena_.alloc<int>(cap + 1, "tri cell cursor");
             T_.tcell_start = arena_.alloc<int>(cap + 2, "tri cell start");
@@ -377,8 +381,12 @@ public:
         scenes_h_ = sc;
 
         // ---- history and contacts
-        if (precision_ == DEM_PRECISION_MIXED) alloc_state<float>(hp32_, hw32_, hb32_, ct32_);
-        else alloc_state<double>(hp64_, hw64_, hb64_, ct64_);
+        if (precision_ == DEM_PRECISION_MIXED) {
+            if (pt_fp32_) alloc_state<float, float>(hp32_, hw32_, hb32_, ct32_);
+            else alloc_state<float, double>(hp32_, hw32_, hb64_, ct32_);
+        } else {
+            alloc_state<double, double>(hp64_, hw64_, hb64_, ct64_);
+        }
 
         // ---- body reduction
         if (nb_ > 0) {
@@ -405,20 +413,23 @@ public:
         initialized_ = true;
     }
 
-    template <typename T> void alloc_state(Hist<T>& hp, Hist<T>& hw, Hist<T>& hb, Contacts<T>& ct)
+    template <typename H> void mk_hist(Hist<H>& h, int slots)
     {
         cudaStream_t s = stream_;
-        auto mk_hist = [&](Hist<T>& h, int slots) {
-            const size_t n = (size_t)nc_ * slots;
-            h.key = arena_.alloc<uint64_t>(n, "history keys");
-            h.last = arena_.alloc<int>(n, "history last seen");
-            h.val = arena_.alloc<T>(n * 9, "history values");
-            h.hw = arena_.alloc<int>(nc_, "history hw");
-            check(cudaMemsetAsync(h.key, 0, n * sizeof(uint64_t), s), "clear history keys");
-            check(cudaMemsetAsync(h.last, 0xff, n * sizeof(int), s), "clear history age");
-            check(cudaMemsetAsync(h.val, 0, n * 9 * sizeof(T), s), "clear history values");
-            check(cudaMemsetAsync(h.hw, 0, nc_ * sizeof(int), s), "clear history hw");
-        };
+        const size_t n = (size_t)nc_ * slots;
+        h.key = arena_.alloc<uint64_t>(n, "history keys");
+        h.last = arena_.alloc<int>(n, "history last seen");
+        h.val = arena_.alloc<H>(n * 9, "history values");
+        h.hw = arena_.alloc<int>(nc_, "history hw");
+        check(cudaMemsetAsync(h.key, 0, n * sizeof(uint64_t), s), "clear history keys");
+        check(cudaMemsetAsync(h.last, 0xff, n * sizeof(int), s), "clear history age");
+        check(cudaMemsetAsync(h.val, 0, n * 9 * sizeof(H), s), "clear history values");
+        check(cudaMemsetAsync(h.hw, 0, nc_ * sizeof(int), s), "clear history hw");
+    }
+
+    template <typename T, typename TB> void alloc_state(Hist<T>& hp, Hist<T>& hw, Hist<TB>& hb, Contacts<T>& ct)
+    {
+        cudaStream_t s = stream_;
         mk_hist(hp, kPSlots);
         mk_hist(hw, kWSlots);
         mk_hist(hb, kBSlots);
@@ -447,8 +458,8 @@ public:
     }
 
     // ----------------------------------------------------------- pipeline
-    template <typename T>
-    void enqueue_forces(double dt_eff, Hist<T>& hp, Hist<T>& hw, Hist<T>& hb, Contacts<T>& ct, bool timed)
+    template <typename T, typename TB>
+    void enqueue_forces(double dt_eff, Hist<T>& hp, Hist<T>& hw, Hist<TB>& hb, Contacts<T>& ct, bool timed)
     {
         cudaStream_t s = stream_;
         int e = 0;
@@ -462,7 +473,7 @@ public:
         if (O_.ugx) launch_universal_gravity(O_, s);
         launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
         mark();
-        launch_contacts<T>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, s);
+        launch_contacts<T, TB>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, s);
         mark();
         launch_owner_sum<T>(C_, O_, d_sc_, ct, false, nullptr, nullptr, nullptr, nullptr, s);
         if (nb_ > 0) launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
@@ -473,8 +484,12 @@ public:
 
     void forces(double dt_eff, bool timed = false)
     {
-        if (precision_ == DEM_PRECISION_MIXED) enqueue_forces<float>(dt_eff, hp32_, hw32_, hb32_, ct32_, timed);
-        else enqueue_forces<double>(dt_eff, hp64_, hw64_, hb64_, ct64_, timed);
+        if (precision_ == DEM_PRECISION_MIXED) {
+            if (pt_fp32_) enqueue_forces<float, float>(dt_eff, hp32_, hw32_, hb32_, ct32_, timed);
+            else enqueue_forces<float, double>(dt_eff, hp32_, hw32_, hb64_, ct32_, timed);
+        } else {
+            enqueue_forces<double, double>(dt_eff, hp64_, hw64_, hb64_, ct64_, timed);
+        }
         check(cudaGetLastError(), "force pipeline launch");
     }
 
@@ -892,8 +907,14 @@ public:
         check(cudaStreamSynchronize(stream_), "sync");
         const int slots = kind == 0 ? kPSlots : (kind == 1 ? kWSlots : kBSlots);
         if (kind < 0 || kind > 2) throw DemError(DEM_ERR_INVALID, "history kind must be 0, 1 or 2");
-        if (precision_ == DEM_PRECISION_MIXED) download_hist(kind == 0 ? hp32_ : (kind == 1 ? hw32_ : hb32_), slots, keys, last, val);
-        else download_hist(kind == 0 ? hp64_ : (kind == 1 ? hw64_ : hb64_), slots, keys, last, val);
+        if (kind == 2) {
+            if (pt_fp32_) download_hist(hb32_, slots, keys, last, val);
+            else download_hist(hb64_, slots, keys, last, val);
+        } else if (precision_ == DEM_PRECISION_MIXED) {
+            download_hist(kind == 0 ? hp32_ : hw32_, slots, keys, last, val);
+        } else {
+            download_hist(kind == 0 ? hp64_ : hw64_, slots, keys, last, val);
+        }
     }
 
     template <typename T> void upload_hist(Hist<T>& h, int slots, const uint64_t* keys, const double* val)
@@ -1027,11 +1048,11 @@ public:
         }
         if (precision_ == DEM_PRECISION_MIXED) {
             upload_hist(hp32_, kPSlots, pk.data(), pv.data()); upload_hist(hw32_, kWSlots, wk.data(), wv.data());
-            upload_hist(hb32_, kBSlots, bk.data(), bv.data());
         } else {
             upload_hist(hp64_, kPSlots, pk.data(), pv.data()); upload_hist(hw64_, kWSlots, wk.data(), wv.data());
-            upload_hist(hb64_, kBSlots, bk.data(), bv.data());
         }
+        if (pt_fp32_) upload_hist(hb32_, kBSlots, bk.data(), bv.data());
+        else upload_hist(hb64_, kBSlots, bk.data(), bv.data());
         check(cudaMemset(K_.step, 0, sizeof(int)), "reset step");
         step_index_ = 0;
         started_ = false;
@@ -1048,6 +1069,7 @@ public:
     bool sphere_ = true, initialized_ = false, started_ = false, restored_ = false;
     bool keep_bp_ = false, keep_bd_ = false;
     int precision_ = 0, block_ = 128, sm_count_ = 0;
+    bool pt_fp32_ = false;
     double cell_factor_ = 2.5, mesh_ = 0.0, max_radius_ = 0.0, dt_ = 0.0;
     int step_index_ = 0;
     size_t free_before_ = 0;
@@ -1146,6 +1168,7 @@ void dem_default_options(dem_options* o)
     o->cell_factor = 2.5;
     o->max_cells = 0;
     o->block_size = 0;
+    o->pt_fp32 = 0;
 }
 
 int dem_create(dem_engine** out)

@@ -110,21 +110,42 @@ __global__ void k_cell_keys(Comps c, Owners o, Grid g)
             atomicOr(g.err, kErrKeyRange);
         }
     }
+    // Cell box: warp min/max, then one set of atomics per scene and block.
+    __shared__ int sh_box[8][7];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int smin = warp_min(ok ? s : INT_MAX);
     const bool uniform = __all_sync(0xffffffffu, !ok || s == smin);
     if (uniform) {
-        if (smin == INT_MAX) return;
         const int a0 = warp_min(ok ? cx : INT_MAX), a1 = warp_min(ok ? cy : INT_MAX), a2 = warp_min(ok ? cz : INT_MAX);
         const int b0 = warp_max(ok ? cx : INT_MIN), b1 = warp_max(ok ? cy : INT_MIN), b2 = warp_max(ok ? cz : INT_MIN);
-        if ((threadIdx.x & 31) == 0) {
-            int* box = g.scene_box + 6 * smin;
-            atomicMin(box + 0, a0); atomicMin(box + 1, a1); atomicMin(box + 2, a2);
-            atomicMax(box + 3, b0); atomicMax(box + 4, b1); atomicMax(box + 5, b2);
+        if (lane == 0) {
+            sh_box[wid][0] = smin; sh_box[wid][1] = a0; sh_box[wid][2] = a1; sh_box[wid][3] = a2;
+            sh_box[wid][4] = b0; sh_box[wid][5] = b1; sh_box[wid][6] = b2;
         }
-    } else if (ok) {
-        int* box = g.scene_box + 6 * s;
-        atomicMin(box + 0, cx); atomicMin(box + 1, cy); atomicMin(box + 2, cz);
-        atomicMax(box + 3, cx); atomicMax(box + 4, cy); atomicMax(box + 5, cz);
+    } else {
+        if (lane == 0) sh_box[wid][0] = INT_MAX;
+        if (ok) {
+            int* box = g.scene_box + 6 * s;
+            atomicMin(box + 0, cx); atomicMin(box + 1, cy); atomicMin(box + 2, cz);
+            atomicMax(box + 3, cx); atomicMax(box + 4, cy); atomicMax(box + 5, cz);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int w = 0; w < nw; ++w) {
+            const int sc = sh_box[w][0];
+            if (sc == INT_MAX) continue;
+            int a[3] = {sh_box[w][1], sh_box[w][2], sh_box[w][3]}, b[3] = {sh_box[w][4], sh_box[w][5], sh_box[w][6]};
+            for (int v = w + 1; v < nw; ++v) {
+                if (sh_box[v][0] != sc) continue;
+                for (int k = 0; k < 3; ++k) { a[k] = min(a[k], sh_box[v][1 + k]); b[k] = max(b[k], sh_box[v][4 + k]); }
+                sh_box[v][0] = INT_MAX;
+            }
+            int* box = g.scene_box + 6 * sc;
+            atomicMin(box + 0, a[0]); atomicMin(box + 1, a[1]); atomicMin(box + 2, a[2]);
+            atomicMax(box + 3, b[0]); atomicMax(box + 4, b[1]); atomicMax(box + 5, b[2]);
+        }
     }
 }
 
@@ -188,30 +209,29 @@ __global__ void k_scatter(Comps c, Grid g)
     if (i >= c.n) return;
     const int lin = g.clin[i];
     if (lin < 0) return;
-    g.sorted_id[g.cell_start[lin] + g.crank[i]] = i;
+    g.sorted_tmp[g.cell_start[lin] + g.crank[i]] = i;
 }
 
-// Per cell: ascending component order (stable-sort equivalence), inverse
-// permutation, sorted keys; restores the zero count invariant.
-__global__ void k_cell_finalize(Grid g)
+// Final position of a component inside its cell = number of cell members
+// with a smaller index, so every cell lists its members in ascending
+// component order: the result equals a stable sort of the cell keys.  Also
+// writes the inverse permutation and sorted keys, and restores the zero
+// count invariant of the cell table.
+__global__ void k_place(Comps c, Grid g)
 {
-    const int total = *g.total_cells;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *g.nvalid = g.cell_start[total];
-    for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < total; cell += gridDim.x * blockDim.x) {
-        const int b = g.cell_start[cell], e = g.cell_start[cell + 1];
-        g.cell_count[cell] = 0;
-        for (int p = b + 1; p < e; ++p) {
-            const int v = g.sorted_id[p];
-            int q = p - 1;
-            while (q >= b && g.sorted_id[q] > v) { g.sorted_id[q + 1] = g.sorted_id[q]; --q; }
-            g.sorted_id[q + 1] = v;
-        }
-        for (int p = b; p < e; ++p) {
-            const int id = g.sorted_id[p];
-            g.pos_of[id] = p;
-            g.sorted_key[p] = g.ckey[id];
-        }
-    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *g.nvalid = g.cell_start[*g.total_cells];
+    if (i >= c.n) return;
+    const int lin = g.clin[i];
+    if (lin < 0) return;
+    const int b = g.cell_start[lin], e = g.cell_start[lin + 1];
+    int rank = 0;
+    for (int p = b; p < e; ++p) rank += g.sorted_tmp[p] < i;
+    const int pos = b + rank;
+    g.sorted_id[pos] = i;
+    g.pos_of[i] = pos;
+    g.sorted_key[pos] = g.ckey[i];
+    g.cell_count[lin] = 0;
 }
 
 // ------------------------------------------------------------------ scan
@@ -368,25 +388,25 @@ __global__ void k_tri_fill(Tris t, Grid g, double pad)
             for (int z = lo[2]; z <= hi[2]; ++z) {
                 const int lin = cell_lin(lay, x, y, z);
                 const int pos = t.tcell_start[lin] + atomicAdd(t.tcell_cursor + lin, 1);
-                if (pos < t.capacity) t.ttri[pos] = i;
+                if (pos < t.capacity) { t.ttri_tmp[pos] = i; t.tlin_tmp[pos] = lin; }
                 else atomicOr(g.err, kErrTriCapacity);
             }
 }
 
-__global__ void k_tri_finalize(Tris t, Grid g)
+// Triangle-cell entries in ascending triangle order per cell (the order of
+// the reference's stable sort of its fill list), placed by rank.
+__global__ void k_tri_place(Tris t, Grid g)
 {
-    const int total = *g.total_cells;
-    for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < total; cell += gridDim.x * blockDim.x) {
-        const int b = t.tcell_start[cell];
-        const int e = min(t.tcell_start[cell + 1], t.capacity);
-        t.tcell_count[cell] = 0;
-        t.tcell_cursor[cell] = 0;
-        for (int p = b + 1; p < e; ++p) {
-            const int v = t.ttri[p];
-            int q = p - 1;
-            while (q >= b && t.ttri[q] > v) { t.ttri[q + 1] = t.ttri[q]; --q; }
-            t.ttri[q + 1] = v;
-        }
+    const int entries = min(t.tcell_start[*g.total_cells], t.capacity);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < entries; p += gridDim.x * blockDim.x) {
+        const int lin = t.tlin_tmp[p];
+        const int id = t.ttri_tmp[p];
+        const int b = t.tcell_start[lin], e = min(t.tcell_start[lin + 1], t.capacity);
+        int rank = 0;
+        for (int q = b; q < e; ++q) rank += t.ttri_tmp[q] < id;
+        t.ttri[b + rank] = id;
+        t.tcell_count[lin] = 0;
+        t.tcell_cursor[lin] = 0;
     }
 }
 
@@ -530,7 +550,7 @@ void launch_grid_build(const Comps& c, const Owners& o, const Grid& g, int sm_co
     k_cell_count<<<blocks(c.n, 256), 256, 0, s>>>(c, o, g);
     launch_scan(g.cell_count, g.cell_start, g.total_cells, g.tile_sums, sm_count, s);
     k_scatter<<<blocks(c.n, 256), 256, 0, s>>>(c, g);
-    k_cell_finalize<<<sm_count * 8, 256, 0, s>>>(g);
+    k_place<<<blocks(c.n, 256), 256, 0, s>>>(c, g);
 }
 
 void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s)
@@ -545,7 +565,7 @@ void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, double pad,
     k_tri_count<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, pad, tgover);
     launch_scan(t.tcell_count, t.tcell_start, g.total_cells, g.tile_sums, sm_count, s);
     k_tri_fill<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, pad);
-    k_tri_finalize<<<sm_count * 8, 256, 0, s>>>(t, g);
+    k_tri_place<<<sm_count * 8, 256, 0, s>>>(t, g);
 }
 
 void launch_universal_gravity(const Owners& o, cudaStream_t s)

@@ -65,7 +65,7 @@ struct Grid {
     uint64_t* ckey;
     int *clin, *crank;
     int *cell_count, *cell_start;
-    int *sorted_id, *pos_of;
+    int *sorted_id, *pos_of, *sorted_tmp;
     uint64_t* sorted_key;
     int* scene_box;     // [S][6]
     int* scene_layout;  // [S][8]: min xyz, n xyz, offset, cells
@@ -106,7 +106,7 @@ struct Tris {
     double* aabb;   // [t][6]
     int* scene;     // per triangle
     int capacity;   // triangle grid entry capacity
-    int *tcell_count, *tcell_cursor, *tcell_start, *ttri;
+    int *tcell_count, *tcell_cursor, *tcell_start, *ttri, *ttri_tmp, *tlin_tmp;
 };
 
 struct Bodies {
@@ -170,9 +170,11 @@ void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
 template <typename T>
 void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
                    cudaStream_t s);
-template <typename T>
+// T: particle-particle and wall law / history type; TB: particle-triangle
+// law, area and body history type.
+template <typename T, typename TB>
 void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs& r, const SceneC* sc, const Walls& w,
-                     const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<T> hb, Contacts<T> ct,
+                     const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<TB> hb, Contacts<T> ct,
                      const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s);
 template <typename T>
 void launch_owner_sum(const Comps& c, const Owners& o, const SceneC* sc, Contacts<T> ct, bool outputs, double* fc,

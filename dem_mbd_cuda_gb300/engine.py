@@ -78,8 +78,9 @@ def _p(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 
 
-def options(precision="fp64", cell_factor=2.5, max_cells=0, block_size=0):
+def options(precision="fp64", cell_factor=2.5, max_cells=0, block_size=0, pt_fp32=False):
     o = COptions()
+    o.pt_fp32 = int(bool(pt_fp32))
     o.precision = DEM_PRECISION_MIXED if precision in ("mixed", "fp32", DEM_PRECISION_MIXED) else DEM_PRECISION_FP64
     o.cell_factor = float(cell_factor)
     o.max_cells = int(max_cells)

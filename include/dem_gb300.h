@@ -108,6 +108,9 @@ typedef struct dem_options {
     double cell_factor;      /* cell edge / r_max; >= 2.0; 2.5 = reference */
     int max_cells;           /* dense cell-table capacity, 0 = automatic */
     int block_size;          /* threads per block of the contact kernels, 0 = 128 */
+    int pt_fp32;             /* mixed form only: particle-triangle law, area and
+                                history in FP32 too (default 0: FP64, since
+                                they alone make the body loads) */
 } dem_options;
 
 /* Per-step body state uploaded by compute_forces (the 13 doubles per body

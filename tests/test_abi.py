@@ -42,7 +42,7 @@ def test_struct_layouts_match_header():
     from dem_mbd_cuda_gb300.abi import COptions, CStepStats
     from dem_mbd_cuda_gb300.scene import CMech, CScene
     assert C.sizeof(CMech) == 8 * 8
-    assert C.sizeof(COptions) == 24
+    assert C.sizeof(COptions) == 32
     assert C.sizeof(CStepStats) == 56
     assert C.sizeof(CScene) % 8 == 0
 

@@ -84,9 +84,21 @@ def test_single_evaluation_parity(maker):
         assert np.abs(le - lo).max() <= 1e-9 * scale + 1e-12
 
 
-@pytest.mark.parametrize("maker", ["small_dem", "small_mbd", "data1_mbd"])
+def _multi_scene(maker):
+    if maker == "data1_pure_dem":
+        return load_golden(maker)[0]
+    if maker == "small_mbd_nocap":
+        return G.small_mbd(caps=False)
+    return getattr(G, maker)()
+
+
+# Trajectory parity needs scenes whose particle-triangle caps are not reached:
+# the reference re-tests a capped manifold history per triangle at dt = 0
+# against a limit equal to it up to rounding (cuda_contact_backend.cu:783-807
+# after :922-947), a branch no two builds decide alike.
+@pytest.mark.parametrize("maker", ["small_dem", "small_mbd_nocap", "data1_pure_dem"])
 def test_multi_step_parity(maker):
-    sc = load_golden(maker)[0] if maker.startswith("data1") else getattr(G, maker)()
+    sc = _multi_scene(maker)
     steps = 25
     e = engine_for(sc)
     o = Oracle(sc)
