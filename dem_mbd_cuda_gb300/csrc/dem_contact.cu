@@ -129,6 +129,15 @@ __device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int&
 
 __device__ __forceinline__ V3<double> d3(D4 v) { return {v.x, v.y, v.z}; }
 __device__ __forceinline__ D4 d4(double x, double y, double z, double w) { return D4{x, y, z, w}; }
+__device__ __forceinline__ V3<float> f3(float4 v) { return {v.x, v.y, v.z}; }
+
+// Quat2IvDCM rotation in FP32 (mixed form only).
+__device__ __forceinline__ V3<float> rot_ivf(float qw, float qx, float qy, float qz, V3<float> v)
+{
+    return {(1.f - 2.f * (qy * qy + qz * qz)) * v.x + 2.f * (qx * qy - qw * qz) * v.y + 2.f * (qx * qz + qw * qy) * v.z,
+            2.f * (qx * qy + qw * qz) * v.x + (1.f - 2.f * (qx * qx + qz * qz)) * v.y + 2.f * (qy * qz - qw * qx) * v.z,
+            2.f * (qx * qz - qw * qy) * v.x + 2.f * (qy * qz + qw * qx) * v.y + (1.f - 2.f * (qx * qx + qy * qy)) * v.z};
+}
 
 // ------------------------------------------------------------------ gather
 template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r, double dt_eff)
@@ -140,18 +149,26 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
         const double x = c.x[ci], y = c.y[ci], z = c.z[ci], rad = c.radius[ci];
         r.pos[t] = d4(x, y, z, rad);
         const double vx = c.vx[ci], vy = c.vy[ci], vz = c.vz[ci];
-        r.v[t] = d4(vx, vy, vz, o.mass[w]);
-        const int st = o.status[w];
-        const bool mid = dt_eff > 0.0 && st != -1;
-        r.vm[t] = mid ? d4(c.vhx[ci], c.vhy[ci], c.vhz[ci], 0.0) : d4(vx, vy, vz, 0.0);
-        const double qw = o.qw[w], qx = o.qx[w], qy = o.qy[w], qz = o.qz[w];
-        const V3<double> ew = rot_iv(qw, qx, qy, qz, mk(o.wx[w], o.wy[w], o.wz[w]));
-        r.w[t] = d4(ew.x, ew.y, ew.z, 0.0);
-        if (mid) {
-            const V3<double> mw = rot_iv(qw, qx, qy, qz, mk(o.whx[w], o.why[w], o.whz[w]));
+        const bool mid = dt_eff > 0.0 && o.status[w] != -1;
+        if constexpr (sizeof(T) == sizeof(double)) {
+            r.v[t] = d4(vx, vy, vz, o.mass[w]);
+            r.vm[t] = mid ? d4(c.vhx[ci], c.vhy[ci], c.vhz[ci], 0.0) : d4(vx, vy, vz, 0.0);
+            const double qw = o.qw[w], qx = o.qx[w], qy = o.qy[w], qz = o.qz[w];
+            const V3<double> ew = rot_iv(qw, qx, qy, qz, mk(o.wx[w], o.wy[w], o.wz[w]));
+            r.w[t] = d4(ew.x, ew.y, ew.z, 0.0);
+            const V3<double> mw = mid ? rot_iv(qw, qx, qy, qz, mk(o.whx[w], o.why[w], o.whz[w])) : ew;
             r.wm[t] = d4(mw.x, mw.y, mw.z, 0.0);
         } else {
-            r.wm[t] = d4(ew.x, ew.y, ew.z, 0.0);
+            // mixed form: FP32 rows; the world-frame rotation of omega is part
+            // of the per-contact FP32 arithmetic.
+            r.vf[t] = make_float4((float)vx, (float)vy, (float)vz, (float)o.mass[w]);
+            r.vmf[t] = mid ? make_float4((float)c.vhx[ci], (float)c.vhy[ci], (float)c.vhz[ci], 0.f)
+                           : make_float4((float)vx, (float)vy, (float)vz, 0.f);
+            const float qw = (float)o.qw[w], qx = (float)o.qx[w], qy = (float)o.qy[w], qz = (float)o.qz[w];
+            const V3<float> ew = rot_ivf(qw, qx, qy, qz, mk((float)o.wx[w], (float)o.wy[w], (float)o.wz[w]));
+            r.wf[t] = make_float4(ew.x, ew.y, ew.z, 0.f);
+            const V3<float> mw = mid ? rot_ivf(qw, qx, qy, qz, mk((float)o.whx[w], (float)o.why[w], (float)o.whz[w])) : ew;
+            r.wmf[t] = make_float4(mw.x, mw.y, mw.z, 0.f);
         }
         if (r.off) r.off[t] = d4(c.ox[ci], c.oy[ci], c.oz[ci], 0.0);
         int cx, cy, cz;
@@ -189,6 +206,11 @@ __global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const S
                 const int wg = S.wall_begin + wl;
                 const V3<double> out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
                 const V3<double> org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
+                // FP32 prefilter, conservative by 1e-4 of the wall distance
+                // scale plus a micrometre
+                const V3<float> dpf = cvt<float>(p - org);
+                const float distf = dot(dpf, cvt<float>(out));
+                if (distf - (float)rad > 1e-4f * fabsf(distf) + 1e-6f) continue;
                 const double depth = rad - dot(p - org, out);
                 if (depth <= 0.0) continue;
                 const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
@@ -329,17 +351,30 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
             depth = (float)num / ((float)rs + df);
             n = cvt<float>(delta) * (1.0f / df);
         }
-        const D4 vi = r.v[e.x], vj = r.v[e.y];
-        const D4 mi = r.vm[e.x], mj = r.vm[e.y];
-        const V3<T> erv = cvt<T>(d3(vj) - d3(vi));
-        const V3<T> mrv = cvt<T>(d3(mj) - d3(mi));
-        const V3<T> ewi = cvt<T>(d3(r.w[e.x])), ewj = cvt<T>(d3(r.w[e.y]));
-        const V3<T> mwi = cvt<T>(d3(r.wm[e.x])), mwj = cvt<T>(d3(r.wm[e.y]));
+        V3<T> erv, mrv, ewi, ewj, mwi, mwj;
+        T mi_, mj_;
+        if constexpr (sizeof(T) == sizeof(double)) {
+            const D4 vi = r.v[e.x], vj = r.v[e.y];
+            const D4 ui = r.vm[e.x], uj = r.vm[e.y];
+            erv = d3(vj) - d3(vi);
+            mrv = d3(uj) - d3(ui);
+            ewi = d3(r.w[e.x]); ewj = d3(r.w[e.y]);
+            mwi = d3(r.wm[e.x]); mwj = d3(r.wm[e.y]);
+            mi_ = vi.w; mj_ = vj.w;
+        } else {
+            const float4 vi = r.vf[e.x], vj = r.vf[e.y];
+            const float4 ui = r.vmf[e.x], uj = r.vmf[e.y];
+            erv = f3(vj) - f3(vi);
+            mrv = f3(uj) - f3(ui);
+            ewi = f3(r.wf[e.x]); ewj = f3(r.wf[e.y]);
+            mwi = f3(r.wmf[e.x]); mwj = f3(r.wmf[e.y]);
+            mi_ = vi.w; mj_ = vj.w;
+        }
         const int s = r.meta[e.x].w;
         T* hv = hp.val + (size_t)e.z * 9;
         V3<T> f, cpl;
-        pp_law<T>(sc[s].pp, T(dt_eff), n, d, depth, T(d2), T(pi.w), T(pj.w), T(vi.w), T(vj.w), erv, mrv, ewi, ewj, mwi,
-                  mwj, hv, f, cpl);
+        pp_law<T>(sc[s].pp, T(dt_eff), n, d, depth, T(d2), T(pi.w), T(pj.w), mi_, mj_, erv, mrv, ewi, ewj, mwi, mwj, hv,
+                  f, cpl);
         if (r.off) cpl = cpl + cross(cvt<T>(d3(r.off[e.x])), f);
         T* out = ct.res + 6 * (size_t)e.w;
         out[0] = f.x; out[1] = f.y; out[2] = f.z; out[3] = cpl.x; out[4] = cpl.y; out[5] = cpl.z;
@@ -379,6 +414,15 @@ __device__ double tri_area_scale(const double* W, V3<double> p, double r, double
     if (c2 <= 1.0e-30) return 0.0;
     const V3<double> ce = p - n * dist;
     const V3<double> ra = a - ce, rb = mk(W[6], W[7], W[8]) - ce, rc = mk(W[9], W[10], W[11]) - ce;
+    // Disk and triangle disjoint (disk centre farther from the triangle's
+    // centroid than the disk radius plus the triangle's circumradius about
+    // it, W[15]): the reference's edge sum then cancels to rounding noise,
+    // far below its 1e-12 threshold, so the scale is 0 either way.
+    {
+        const V3<double> cen = (ra + rb + rc) * (1.0 / 3.0);
+        const double reach = (sqrt(c2) + W[15]) * (1.0 + 1e-9);
+        if (dot(cen, cen) > reach * reach) return 0.0;
+    }
     double area;
     if constexpr (sizeof(T) == sizeof(double)) {
         area = circle_triangle_area<double>(n, ra, rb, rc, sqrt(c2));
@@ -392,8 +436,8 @@ __device__ double tri_area_scale(const double* W, V3<double> p, double r, double
 }
 
 template <typename TC, typename T>
-__global__ void __launch_bounds__(128) k_pt(Recs r, const SceneC* __restrict__ sc, Tris tris, Bodies bodies,
-                                            Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff)
+__global__ void __launch_bounds__(128) k_pt(Comps c, Owners o, Recs r, const SceneC* __restrict__ sc, Tris tris,
+                                            Bodies bodies, Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff)
 {
     const int step = *k.step;
     const int total = *ct.pt_total_ptr;
@@ -406,10 +450,16 @@ __global__ void __launch_bounds__(128) k_pt(Recs r, const SceneC* __restrict__ s
         const D4 p4 = r.pos[t];
         const V3<double> p = d3(p4);
         const double rad = p4.w;
-        const D4 v4 = r.v[t];
-        const double mass = v4.w;
-        const V3<double> ev = d3(v4), mv = d3(r.vm[t]);
-        const V3<double> ew = d3(r.w[t]), mw = d3(r.wm[t]);
+        // FP64 velocities straight from the state (the mixed form keeps FP32
+        // rows only for the particle-particle law).
+        const int w = meta.y;
+        const double mass = o.mass[w];
+        const bool mid = dt_eff > 0.0 && o.status[w] != -1;
+        const V3<double> ev = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
+        const V3<double> mv = mid ? mk(c.vhx[ci], c.vhy[ci], c.vhz[ci]) : ev;
+        const double oqw = o.qw[w], oqx = o.qx[w], oqy = o.qy[w], oqz = o.qz[w];
+        const V3<double> ew = rot_iv(oqw, oqx, oqy, oqz, mk(o.wx[w], o.wy[w], o.wz[w]));
+        const V3<double> mw = mid ? rot_iv(oqw, oqx, oqy, oqz, mk(o.whx[w], o.why[w], o.whz[w])) : ew;
         const V3<double> off = r.off ? d3(r.off[t]) : mk(0.0, 0.0, 0.0);
         const int lin = r.cell[t].w;
         const int tb = tris.tcell_start[lin];
@@ -645,16 +695,17 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
         a = ft + 6 * (size_t)i; a[0] = TF.x; a[1] = TF.y; a[2] = TF.z; a[3] = TT.x; a[4] = TT.y; a[5] = TT.z;
         return;
     }
-    o.ax[i] = TF.x / m; o.ay[i] = TF.y / m; o.az[i] = TF.z / m;
+    const double im = o.inv_mass[i];
+    o.ax[i] = TF.x * im; o.ay[i] = TF.y * im; o.az[i] = TF.z * im;
     const double qw = o.qw[i], qx = o.qx[i], qy = o.qy[i], qz = o.qz[i];
     const double tx = (1.0 - 2.0 * (qy * qy + qz * qz)) * TT.x + 2.0 * (qx * qy + qw * qz) * TT.y + 2.0 * (qx * qz - qw * qy) * TT.z;
     const double ty = 2.0 * (qx * qy - qw * qz) * TT.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * TT.y + 2.0 * (qy * qz + qw * qx) * TT.z;
     const double tz = 2.0 * (qx * qz + qw * qy) * TT.x + 2.0 * (qy * qz - qw * qx) * TT.y + (1.0 - 2.0 * (qx * qx + qy * qy)) * TT.z;
     const double wx = o.wx[i], wy = o.wy[i], wz = o.wz[i];
     const double Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
-    o.awx[i] = (tx - (Iz - Iy) * wz * wy) / Ix;
-    o.awy[i] = (ty - (Ix - Iz) * wx * wz) / Iy;
-    o.awz[i] = (tz - (Iy - Ix) * wy * wx) / Iz;
+    o.awx[i] = (tx - (Iz - Iy) * wz * wy) * o.inv_ix[i];
+    o.awy[i] = (ty - (Ix - Iz) * wx * wz) * o.inv_iy[i];
+    o.awz[i] = (tz - (Iy - Ix) * wy * wx) * o.inv_iz[i];
 }
 
 // ------------------------------------------------------------ body reduce
@@ -783,7 +834,7 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
         launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);
         k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list,
                                                   ct.pt_index, ct.pt_total_ptr);
-        k_pt<T, TB><<<sm_count * 4, 128, 0, s>>>(r, sc, t, b, hb, ct, k, dt_eff);
+        k_pt<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
     }
 }
 

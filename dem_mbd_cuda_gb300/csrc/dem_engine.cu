@@ -88,8 +88,8 @@ class Engine {
 public:
     ~Engine()
     {
-        if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
-        if (graph_exec_mbd_) cudaGraphExecDestroy(graph_exec_mbd_);
+        for (cudaGraphExec_t g : {graph_fa_, graph_f_, graph_mbd_fa_, graph_mbd_f_})
+            if (g) cudaGraphExecDestroy(g);
         for (auto* e : ev_) if (e) cudaEventDestroy(e);
         arena_.release();
         if (pinned_) cudaFreeHost(pinned_);
@@ -260,6 +260,15 @@ public:
         O_.qw = upd(cols[9], "qw"); O_.qx = upd(cols[10], "qx"); O_.qy = upd(cols[11], "qy"); O_.qz = upd(cols[12], "qz");
         O_.ix = upd(cols[13], "ix"); O_.iy = upd(cols[14], "iy"); O_.iz = upd(cols[15], "iz");
         O_.mass = upd(om, "mass"); O_.radius = upd(orad, "radius");
+        {
+            std::vector<double> inv(n_);
+            for (int i = 0; i < n_; ++i) inv[i] = 1.0 / om[i];
+            O_.inv_mass = upd(inv, "inverse mass");
+            for (int a = 0; a < 3; ++a) {
+                for (int i = 0; i < n_; ++i) inv[i] = 1.0 / oin[3 * (size_t)i + a];
+                (a == 0 ? O_.inv_ix : (a == 1 ? O_.inv_iy : O_.inv_iz)) = upd(inv, "inverse inertia");
+            }
+        }
         double** zeros[] = {&O_.ax, &O_.ay, &O_.az, &O_.awx, &O_.awy, &O_.awz, &O_.vhx, &O_.vhy, &O_.vhz,
                             &O_.whx, &O_.why, &O_.whz, &O_.hqw, &O_.hqx, &O_.hqy, &O_.hqz};
         for (double** z : zeros) {
@@ -324,9 +333,14 @@ public:
         check(cudaMemsetAsync(G_.err, 0, sizeof(unsigned), s), "clear err");
 
         // ---- records
-        R_.pos = arena_.alloc<D4>(nc_, "rec pos"); R_.v = arena_.alloc<D4>(nc_, "rec v");
-        R_.vm = arena_.alloc<D4>(nc_, "rec vm"); R_.w = arena_.alloc<D4>(nc_, "rec w");
-        R_.wm = arena_.alloc<D4>(nc_, "rec wm");
+        R_.pos = arena_.alloc<D4>(nc_, "rec pos");
+        if (precision_ == DEM_PRECISION_MIXED) {
+            R_.vf = arena_.alloc<float4>(nc_, "rec v"); R_.vmf = arena_.alloc<float4>(nc_, "rec vm");
+            R_.wf = arena_.alloc<float4>(nc_, "rec w"); R_.wmf = arena_.alloc<float4>(nc_, "rec wm");
+        } else {
+            R_.v = arena_.alloc<D4>(nc_, "rec v"); R_.vm = arena_.alloc<D4>(nc_, "rec vm");
+            R_.w = arena_.alloc<D4>(nc_, "rec w"); R_.wm = arena_.alloc<D4>(nc_, "rec wm");
+        }
         R_.off = sphere_ ? nullptr : arena_.alloc<D4>(nc_, "rec off");
         R_.meta = arena_.alloc<int4>(nc_, "rec meta"); R_.cell = arena_.alloc<int4>(nc_, "rec cell");
         R_.relf = arena_.alloc<float4>(nc_, "rec relf");
@@ -722,47 +736,57 @@ public:
             started_ = true;
         }
         if (steps <= 0) return;
-        if (nb_ == 0) {
-            ensure_graph(false);
-            for (int s = 0; s < steps; ++s) check(cudaGraphLaunch(graph_exec_, stream_), "cudaGraphLaunch");
-            step_index_ += steps;
-            collect_diagnostics(nullptr);
-            return;
-        }
-        ensure_graph(true);
-        for (int s = 0; s < steps; ++s) {
-            body_position_update(dt);
-            double* p = pin_body_state();
-            std::memcpy(p, hbc_.data(), sizeof(double) * 3 * nb_);
-            std::memcpy(p + 3 * nb_, hbq_.data(), sizeof(double) * 4 * nb_);
-            std::memcpy(p + 7 * nb_, hbv_.data(), sizeof(double) * 3 * nb_);
-            std::memcpy(p + 10 * nb_, hbw_.data(), sizeof(double) * 3 * nb_);
-            check(cudaGraphLaunch(graph_exec_mbd_, stream_), "cudaGraphLaunch");
-            check(cudaStreamSynchronize(stream_), "mbd step");
-            ++step_index_;
-            body_forces_from_pinned(hbloads_.data());
-            body_half_update(false, dt);
-        }
+        step_loop(steps);
         collect_diagnostics(nullptr);
     }
 
-    // One step on the stream (advance, optional body upload, forces with dt,
-    // optional body download, finish) captured as a CUDA graph.
-    void ensure_graph(bool mbd)
+    // `steps` reference steps after the start: advance, then for every step
+    // the captured force evaluation; all but the last step end with the
+    // fused finish + next advance, the last with finish alone.  With bodies
+    // the host MBD step runs between graph launches.
+    void step_loop(int steps)
     {
-        cudaGraphExec_t& ex = mbd ? graph_exec_mbd_ : graph_exec_;
+        const bool mbd = nb_ > 0;
+        ensure_graphs(mbd);
+        launch_advance(O_, dt_, stream_);
+        for (int s = 0; s < steps; ++s) {
+            const bool last = s == steps - 1;
+            cudaGraphExec_t g = mbd ? (last ? graph_mbd_f_ : graph_mbd_fa_) : (last ? graph_f_ : graph_fa_);
+            if (mbd) {
+                body_position_update(dt_);
+                double* p = pin_body_state();
+                std::memcpy(p, hbc_.data(), sizeof(double) * 3 * nb_);
+                std::memcpy(p + 3 * nb_, hbq_.data(), sizeof(double) * 4 * nb_);
+                std::memcpy(p + 7 * nb_, hbv_.data(), sizeof(double) * 3 * nb_);
+                std::memcpy(p + 10 * nb_, hbw_.data(), sizeof(double) * 3 * nb_);
+            }
+            check(cudaGraphLaunch(g, stream_), "cudaGraphLaunch");
+            ++step_index_;
+            if (mbd) {
+                check(cudaStreamSynchronize(stream_), "mbd step");
+                body_forces_from_pinned(hbloads_.data());
+                body_half_update(false, dt_);
+            }
+        }
+        if (!mbd) check(cudaStreamSynchronize(stream_), "run steps");
+    }
+
+    // Captured force evaluation with dt, optionally with the body upload /
+    // load download around it, followed by finish (+ next advance).
+    void capture(cudaGraphExec_t& ex, bool mbd, bool fused)
+    {
         if (ex) return;
         cudaGraph_t g = nullptr;
         check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
         try {
-            launch_advance(O_, dt_, stream_);
             if (mbd) {
                 enqueue_body_h2d();
                 launch_tri_transform(T_, B_, stream_);
             }
             forces(dt_, false);
             if (mbd) enqueue_body_d2h();
-            launch_finish(O_, dt_, stream_);
+            if (fused) launch_finish_advance(O_, dt_, stream_);
+            else launch_finish(O_, dt_, stream_);
         } catch (...) {
             cudaStreamEndCapture(stream_, &g);
             if (g) cudaGraphDestroy(g);
@@ -772,6 +796,11 @@ public:
         check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
         cudaGraphDestroy(g);
     }
+    void ensure_graphs(bool mbd)
+    {
+        if (mbd) { capture(graph_mbd_fa_, true, true); capture(graph_mbd_f_, true, false); }
+        else { capture(graph_fa_, false, true); capture(graph_f_, false, false); }
+    }
 
     // Time `steps` graph-launched steps (pure DEM) on the device; the state is
     // resident.  Returns milliseconds.
@@ -779,28 +808,12 @@ public:
     {
         need_init();
         if (!started_) run_steps(1);
-        ensure_graph(nb_ > 0);
+        ensure_graphs(nb_ > 0);
         cudaEvent_t a, b;
         check(cudaEventCreate(&a), "event"); check(cudaEventCreate(&b), "event");
+        check(cudaStreamSynchronize(stream_), "sync");
         check(cudaEventRecord(a, stream_), "event");
-        if (nb_ == 0) {
-            for (int s = 0; s < steps; ++s) check(cudaGraphLaunch(graph_exec_, stream_), "launch");
-            step_index_ += steps;
-        } else {
-            for (int s = 0; s < steps; ++s) {
-                body_position_update(dt_);
-                double* p = pin_body_state();
-                std::memcpy(p, hbc_.data(), sizeof(double) * 3 * nb_);
-                std::memcpy(p + 3 * nb_, hbq_.data(), sizeof(double) * 4 * nb_);
-                std::memcpy(p + 7 * nb_, hbv_.data(), sizeof(double) * 3 * nb_);
-                std::memcpy(p + 10 * nb_, hbw_.data(), sizeof(double) * 3 * nb_);
-                check(cudaGraphLaunch(graph_exec_mbd_, stream_), "launch");
-                check(cudaStreamSynchronize(stream_), "mbd step");
-                ++step_index_;
-                body_forces_from_pinned(hbloads_.data());
-                body_half_update(false, dt_);
-            }
-        }
+        step_loop(steps);
         check(cudaEventRecord(b, stream_), "event");
         check(cudaEventSynchronize(b), "event sync");
         float ms = 0;
@@ -1079,7 +1092,7 @@ public:
     DeviceArena arena_, arena_tmp_;
     void* pinned_ = nullptr;
     size_t pinned_bytes_ = 0;
-    cudaGraphExec_t graph_exec_ = nullptr, graph_exec_mbd_ = nullptr;
+    cudaGraphExec_t graph_fa_ = nullptr, graph_f_ = nullptr, graph_mbd_fa_ = nullptr, graph_mbd_f_ = nullptr;
 
     Owners O_{};
     Comps C_{};

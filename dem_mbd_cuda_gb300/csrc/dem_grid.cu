@@ -312,7 +312,18 @@ __global__ void k_tri_transform(Tris t, Bodies b)
         W[3 * k] = p.x + cx; W[3 * k + 1] = p.y + cy; W[3 * k + 2] = p.z + cz;
     }
     const V3<double> nn = rot_iv(qw, qx, qy, qz, mk(L[12], L[13], L[14]));
-    W[12] = nn.x; W[13] = nn.y; W[14] = nn.z; W[15] = 0.0;
+    W[12] = nn.x; W[13] = nn.y; W[14] = nn.z;
+    // circumradius of v2, v3, v4 about their centroid (disjointness test)
+    {
+        const double gx = (W[3] + W[6] + W[9]) * (1.0 / 3.0), gy = (W[4] + W[7] + W[10]) * (1.0 / 3.0),
+                     gz = (W[5] + W[8] + W[11]) * (1.0 / 3.0);
+        double r2 = 0.0;
+        for (int k = 1; k < 4; ++k) {
+            const double dx = W[3 * k] - gx, dy = W[3 * k + 1] - gy, dz = W[3 * k + 2] - gz;
+            r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
+        }
+        W[15] = sqrt(r2) * (1.0 + 1e-12) + 1e-15;
+    }
     double* A = t.aabb + 6 * (size_t)i;
     double mnx = W[0], mny = W[1], mnz = W[2], mxx = W[0], mxy = W[1], mxz = W[2];
     for (int k = 1; k < 4; ++k) {
@@ -424,7 +435,7 @@ __device__ __forceinline__ void normalize_quat(double& qw, double& qx, double& q
 {
     const double n2 = qw * qw + qx * qx + qy * qy + qz * qz;
     if (n2 <= 1.0e-24) { qw = 1.0; qx = qy = qz = 0.0; return; }
-    const double inv = 1.0 / sqrt(n2);
+    const double inv = rsqrt(n2);
     qw *= inv; qx *= inv; qy *= inv; qz *= inv;
 }
 
@@ -483,6 +494,42 @@ __global__ void k_finish(Owners d, double dt)
     qw += dw * h; qx += dx * h; qy += dy * h; qz += dz * h;
     normalize_quat(qw, qx, qy, qz);
     quat_derivative(qw, qx, qy, qz, d.whx[i], d.why[i], d.whz[i], d.hqw[i], d.hqx[i], d.hqy[i], d.hqz[i]);
+}
+
+// advanceHalfVelocityKernel of step s followed by advancePositionKernel of
+// step s+1 for one owner, in registers (the two run back to back when no
+// output is taken between steps).
+__global__ void k_finish_advance(Owners d, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double ax = d.ax[i], ay = d.ay[i], az = d.az[i], awx = d.awx[i], awy = d.awy[i], awz = d.awz[i];
+    const double vhx = d.vhx[i] + ax * dt, vhy = d.vhy[i] + ay * dt, vhz = d.vhz[i] + az * dt;
+    const double whx = d.whx[i] + awx * dt, why = d.why[i] + awy * dt, whz = d.whz[i] + awz * dt;
+    d.vhx[i] = vhx; d.vhy[i] = vhy; d.vhz[i] = vhz;
+    d.whx[i] = whx; d.why[i] = why; d.whz[i] = whz;
+    const double h = 0.5 * dt;
+    double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
+    double pw = qw, px = qx, py = qy, pz = qz, dw, dx, dy, dz;
+    quat_derivative(pw, px, py, pz, d.wx[i], d.wy[i], d.wz[i], dw, dx, dy, dz);
+    pw += dw * h; px += dx * h; py += dy * h; pz += dz * h;
+    normalize_quat(pw, px, py, pz);
+    double hqw, hqx, hqy, hqz;
+    quat_derivative(pw, px, py, pz, whx, why, whz, hqw, hqx, hqy, hqz);
+    d.hqw[i] = hqw; d.hqx[i] = hqx; d.hqy[i] = hqy; d.hqz[i] = hqz;
+    if (d.status[i] == -1) return;
+    d.px[i] += vhx * dt;
+    d.py[i] += vhy * dt;
+    d.pz[i] += vhz * dt;
+    qw += hqw * dt; qx += hqx * dt; qy += hqy * dt; qz += hqz * dt;
+    normalize_quat(qw, qx, qy, qz);
+    d.qw[i] = qw; d.qx[i] = qx; d.qy[i] = qy; d.qz[i] = qz;
+    d.vx[i] = vhx + ax * (0.5 * dt);
+    d.vy[i] = vhy + ay * (0.5 * dt);
+    d.vz[i] = vhz + az * (0.5 * dt);
+    d.wx[i] = whx + awx * (0.5 * dt);
+    d.wy[i] = why + awy * (0.5 * dt);
+    d.wz[i] = whz + awz * (0.5 * dt);
 }
 
 // Universal gravitation (src/cuda/cuda_contact_backend.cu:1095-1106): the
@@ -584,6 +631,10 @@ void launch_advance(const Owners& o, double dt, cudaStream_t s)
 void launch_finish(const Owners& o, double dt, cudaStream_t s)
 {
     if (o.n > 0) k_finish<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_finish_advance(const Owners& o, double dt, cudaStream_t s)
+{
+    if (o.n > 0) k_finish_advance<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
 }
 void launch_step_counter(const Counters& k, int reset, cudaStream_t s) { k_step_counter<<<1, 32, 0, s>>>(k, reset); }
 

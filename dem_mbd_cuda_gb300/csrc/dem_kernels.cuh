@@ -36,6 +36,7 @@ struct Owners {
     double *ax, *ay, *az, *awx, *awy, *awz;
     double *vhx, *vhy, *vhz, *whx, *why, *whz, *hqw, *hqx, *hqy, *hqz;
     double *mass, *ix, *iy, *iz, *radius;
+    double *inv_mass, *inv_ix, *inv_iy, *inv_iz;
     int *id, *status, *scene;
     double *ugx, *ugy, *ugz;  // universal-gravitation field force (optional)
 };
@@ -80,8 +81,12 @@ struct __align__(32) D4 {
     double x, y, z, w;
 };
 
+// Velocity rows are D4 in the FP64 form and float4 in the mixed form (the
+// law reads them as FP32 there; the particle-triangle law reads FP64 state
+// from the owner and component arrays instead).
 struct Recs {
     D4 *pos, *v, *vm, *w, *wm, *off;  // off: clumps only
+    float4 *vf, *vmf, *wf, *wmf;      // mixed form
     int4* meta;                             // c, owner, component id, scene
     int4* cell;                             // cx, cy, cz, lin
     float4* relf;                           // position relative to the cell origin, radius
@@ -164,6 +169,8 @@ void launch_universal_gravity(const Owners& o, cudaStream_t s);
 void launch_leapfrog_init(const Owners& o, double half_dt, cudaStream_t s);
 void launch_advance(const Owners& o, double dt, cudaStream_t s);
 void launch_finish(const Owners& o, double dt, cudaStream_t s);
+// finishParticleStep of one step fused with advanceParticles of the next.
+void launch_finish_advance(const Owners& o, double dt, cudaStream_t s);
 // reset != 0: clear the per-step counters; 0: advance the contact step index.
 void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
 
