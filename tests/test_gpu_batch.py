@@ -21,7 +21,7 @@ def scenes():
     b.pp.mu = b.pw.mu = 0.7
     b.pp.epsN = b.pw.epsN = 0.3
     b.pos = b.pos + np.array([0.001, -0.002, 0.0])   # overlapping coordinates on purpose
-    c = G.small_mbd(n=250, seed=3, caps=False)
+    c = G.small_mbd(n=250, seed=3, caps=False, dt=a.dt)
     return [a, b, c]
 
 
