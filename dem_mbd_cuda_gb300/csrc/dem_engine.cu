@@ -29,6 +29,8 @@ namespace demgb {
 
 static thread_local std::string g_last_error;
 
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
 struct DemError : std::runtime_error {
     int code;
     DemError(int c, const std::string& m) : std::runtime_error(m), code(c) {}

@@ -52,6 +52,7 @@ _SIGS = {
     "dem_download_grid": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "dem_download_history": ([C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "dem_last_phase_times": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "dem_cell_sort_static": ([C.c_void_p] * 3 + [C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "dem_x_compute_forces_timed": ([C.c_void_p, C.c_int], C.c_int),
     "dem_x_time_steps": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "dem_x_download_half": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),

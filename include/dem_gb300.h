@@ -254,6 +254,30 @@ int dem_download_history(dem_engine* engine, int kind, uint64_t* keys,
 int dem_last_phase_times(dem_engine* engine, float* ms, int capacity,
                          int* count);
 
+/* Limits of dem_cell_sort_static's built-in working memory. */
+#define DEM_STATIC_SORT_MAX_COMPONENTS 262144
+#define DEM_STATIC_SORT_MAX_CELLS 1048576
+
+/* The cell sort without any device allocation.  No counterpart in the
+ * reference: it serves callers that may not call cudaMalloc where they need
+ * the sort (device memory owned by another pool or arena, allocation-free
+ * real-time loops, an exhausted memory quota).  Same result as the engine's
+ * grid build and the reference's sortedCellKey / sortedEntityId: cell keys
+ * packCell(floor(p / mesh_size)) of the n positions, sorted stably over the
+ * input order.  x, y, z, sorted_key[n] and sorted_id[n] are DEVICE buffers
+ * owned by the caller; stream is a cudaStream_t (NULL = default stream) and
+ * the call returns after that stream has finished the work.
+ * Working memory is one built-in device array of about 14 MB that every GPU
+ * loading this library keeps until the process exits; n is limited to
+ * DEM_STATIC_SORT_MAX_COMPONENTS and the occupied cell box to
+ * DEM_STATIC_SORT_MAX_CELLS cells (DEM_ERR_CAPACITY beyond).  The first call
+ * on a device looks up that array's device address and should come before
+ * any stream capture on that device.  All calls share the array, so calls
+ * that overlap on the GPU race: order them on one stream or synchronize. */
+int dem_cell_sort_static(const double* x, const double* y, const double* z,
+                         int n, double mesh_size, uint64_t* sorted_key,
+                         int* sorted_id, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
