@@ -175,7 +175,8 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
         unpack_cell(g.ckey[ci], cx, cy, cz);
         r.meta[t] = make_int4(ci, w, c.cid[ci], o.scene[w]);
         r.cell[t] = make_int4(cx, cy, cz, g.clin[ci]);
-        r.relf[t] = make_float4((float)(x - cx * g.mesh), (float)(y - cy * g.mesh), (float)(z - cz * g.mesh),
+        const double mesh = g.sc[o.scene[w]].mesh;
+        r.relf[t] = make_float4((float)(x - cx * mesh), (float)(y - cy * mesh), (float)(z - cz * mesh),
                                 (float)rad);
     }
 }
@@ -265,6 +266,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         const D4 pi = r.pos[t];
         const int* lay = g.scene_layout + 8 * s;
         const float4 fi = r.relf[t];
+        const float mesh_f = sc[s].mesh_f, margin_f = sc[s].margin_f;
         int phw = hp.hw[ci];
         for (int dx = -1; dx <= 1; ++dx) {
             const int nx = cell.x + dx;
@@ -278,11 +280,11 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
                     if (nz < lay[2] || nz >= lay[2] + lay[5]) continue;
                     const int lin = row + nz;
                     const int b = g.cell_start[lin], e = g.cell_start[lin + 1];
-                    const float ox = dx * g.mesh_f - fi.x, oy = dy * g.mesh_f - fi.y, oz = dz * g.mesh_f - fi.z;
+                    const float ox = dx * mesh_f - fi.x, oy = dy * mesh_f - fi.y, oz = dz * mesh_f - fi.z;
                     for (int u = b; u < e; ++u) {
                         const float4 fj = r.relf[u];
                         const float ddx = fj.x + ox, ddy = fj.y + oy, ddz = fj.z + oz;
-                        const float rsf = fj.w + fi.w + g.margin_f;
+                        const float rsf = fj.w + fi.w + margin_f;
                         if (ddx * ddx + ddy * ddy + ddz * ddz >= rsf * rsf) continue;
                         const int4 mj = r.meta[u];
                         if (mj.y == owner) continue;

@@ -137,6 +137,7 @@ public:
         std::vector<double> tloc;
         std::vector<SceneC> sc(nscenes);
         bool any_clump = false, any_ug = false;
+        std::vector<double> scene_rmax(nscenes, 0.0);
         nbs_ = 0;
         for (int s = 0; s < nscenes; ++s) {
             const dem_scene& x = scenes[s];
@@ -187,6 +188,7 @@ public:
                 crad.push_back(r);
                 for (int a = 0; a < 3; ++a) cbody.push_back(x.n_components > 0 ? x.comp_offset[3 * c + a] : 0.0);
                 max_radius_ = std::max(max_radius_, r);
+                scene_rmax[s] = std::max(scene_rmax[s], r);
                 comp_owner_ids_.push_back(x.owner_id[ow]);
             }
             for (int i = 0; i < x.n_owners; ++i)
@@ -194,6 +196,12 @@ public:
                     throw DemError(DEM_ERR_INVALID, "each CUDA owner requires 1 to 8 components");
             SceneC& S = sc[s];
             S.pp = make_mat(x.pp, x.dt); S.pt = make_mat(x.pt, x.dt); S.pw = make_mat(x.pw, x.dt);
+            S.mesh = cell_factor_ * scene_rmax[s];
+            if (!(S.mesh > 0.0)) throw DemError(DEM_ERR_INVALID, "invalid mesh size");
+            S.inv_mesh = 1.0 / S.mesh;
+            S.pad = scene_rmax[s];
+            S.mesh_f = (float)S.mesh;
+            S.margin_f = (float)(1.0e-5 * S.mesh);
             for (int a = 0; a < 3; ++a) S.g[a] = x.gravity[a];
             S.grav = x.gravity_enabled ? 1 : 0;
             S.wall_begin = (int)wo.size() / 3;
@@ -305,15 +313,14 @@ public:
             for (double** z : cw) *z = arena_.alloc<double>(nc_, "component world state");
         }
 
+        d_sc_ = arena_.upload(sc.data(), sc.size(), "scene constants", s);
+        G_.sc = d_sc_;
+
         // ---- grid
         long long cap = o.max_cells > 0 ? o.max_cells : std::max<long long>(16LL * nc_, 1LL << 22);
         cap = std::min<long long>(cap, (1LL << 31) - 64);
         G_.capacity = (int)cap;
         G_.nscenes = S_;
-        G_.mesh = mesh_;
-        G_.inv_mesh = 1.0 / mesh_;
-        G_.mesh_f = (float)mesh_;
-        G_.margin_f = (float)(1.0e-5 * mesh_);
         G_.ckey = arena_.alloc<uint64_t>(nc_, "ckey");
         G_.clin = arena_.alloc<int>(nc_, "clin");
         G_.crank = arena_.alloc<int>(nc_, "crank");
@@ -371,7 +378,8 @@ public:
                 for (int k = 0; k < 4; ++k)
                     rho = std::max(rho, std::sqrt((L[3 * k] - cx) * (L[3 * k] - cx) + (L[3 * k + 1] - cy) * (L[3 * k + 1] - cy) +
                                                   (L[3 * k + 2] - cz) * (L[3 * k + 2] - cz)));
-                const long long per = (long long)std::floor((2 * rho + 2 * max_radius_) / mesh_) + 2;
+                const SceneC& St = sc[tscene[t]];
+                const long long per = (long long)std::floor((2 * rho + 2 * St.pad) / St.mesh) + 2;
                 tcap += per * per * per;
             }
             tcap = std::min<long long>(tcap + 1024, (1LL << 31) - 64);
@@ -393,7 +401,6 @@ public:
         K_.tgover = cnt + 5; K_.ct_total = cnt + 6; K_.pt_total = cnt + 7; K_.step = cnt + 8;
 
         // ---- scene constants
-        d_sc_ = arena_.upload(sc.data(), sc.size(), "scene constants", s);
         scenes_h_ = sc;
 
         // ---- history and contacts
@@ -485,7 +492,7 @@ public:
         if (!sphere_) launch_update_components(C_, O_, s);
         launch_grid_build(C_, O_, G_, sm_count_, s);
         mark();
-        if (nb_ > 0 && nt_ > 0) launch_tri_build(T_, B_, G_, max_radius_, K_.tgover, sm_count_, s);
+        if (nb_ > 0 && nt_ > 0) launch_tri_build(T_, B_, G_, K_.tgover, sm_count_, s);
         if (O_.ugx) launch_universal_gravity(O_, s);
         launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
         mark();

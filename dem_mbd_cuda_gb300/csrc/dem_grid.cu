@@ -94,9 +94,10 @@ __global__ void k_cell_keys(Comps c, Owners o, Grid g)
     int cx = 0, cy = 0, cz = 0, s = INT_MAX;
     if (i < c.n) {
         const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
-        const double fx = floor(c.x[i] * g.inv_mesh);
-        const double fy = floor(c.y[i] * g.inv_mesh);
-        const double fz = floor(c.z[i] * g.inv_mesh);
+        const double inv_mesh = g.sc[o.scene[c.owner[i]]].inv_mesh;
+        const double fx = floor(c.x[i] * inv_mesh);
+        const double fy = floor(c.y[i] * inv_mesh);
+        const double fz = floor(c.z[i] * inv_mesh);
         ok = isfinite(fx) && isfinite(fy) && isfinite(fz) && fx >= minCell && fx <= maxCell && fy >= minCell &&
              fy <= maxCell && fz >= minCell && fz <= maxCell;
         if (ok) {
@@ -336,13 +337,15 @@ __global__ void k_tri_transform(Tris t, Bodies b)
 // Padded-AABB cell range of a triangle (countTriangleCellsKernel,
 // src/cuda/cuda_contact_backend.cu:409-452), clipped to the particle cell box
 // of its scene: only those cells are ever looked up.
-__device__ bool tri_cell_range(const Tris& t, const Grid& g, int i, double pad, int lo[3], int hi[3], const int*& lay)
+__device__ bool tri_cell_range(const Tris& t, const Grid& g, int i, int lo[3], int hi[3], const int*& lay)
 {
     const double* A = t.aabb + 6 * (size_t)i;
     const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
+    const SceneC& S = g.sc[t.scene[i]];
+    const double pad = S.pad, inv_mesh = S.inv_mesh;
     for (int a = 0; a < 3; ++a) {
-        const double mn = floor((A[a] - pad) * g.inv_mesh);
-        const double mx = floor((A[3 + a] + pad) * g.inv_mesh);
+        const double mn = floor((A[a] - pad) * inv_mesh);
+        const double mx = floor((A[3 + a] + pad) * inv_mesh);
         if (!isfinite(mn) || !isfinite(mx) || mn < minCell || mx > maxCell) return false;
         lo[a] = (int)mn;
         hi[a] = (int)mx;
@@ -357,43 +360,44 @@ __device__ bool tri_cell_range(const Tris& t, const Grid& g, int i, double pad, 
     return true;
 }
 
-__device__ bool tri_range_valid(const Tris& t, const Grid& g, int i, double pad)
+__device__ bool tri_range_valid(const Tris& t, const Grid& g, int i)
 {
     const double* A = t.aabb + 6 * (size_t)i;
     const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
+    const SceneC& S = g.sc[t.scene[i]];
     for (int a = 0; a < 3; ++a) {
-        const double mn = floor((A[a] - pad) * g.inv_mesh);
-        const double mx = floor((A[3 + a] + pad) * g.inv_mesh);
+        const double mn = floor((A[a] - S.pad) * S.inv_mesh);
+        const double mx = floor((A[3 + a] + S.pad) * S.inv_mesh);
         if (!isfinite(mn) || !isfinite(mx) || mn < minCell || mx > maxCell) return false;
     }
     return true;
 }
 
-__global__ void k_tri_count(Tris t, Grid g, double pad, int* tgover)
+__global__ void k_tri_count(Tris t, Grid g, int* tgover)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= t.nt) return;
-    if (!tri_range_valid(t, g, i, pad)) {
+    if (!tri_range_valid(t, g, i)) {
         atomicAdd(tgover, 1);
         atomicOr(g.err, kErrTriRange);
         return;
     }
     int lo[3], hi[3];
     const int* lay;
-    if (!tri_cell_range(t, g, i, pad, lo, hi, lay)) return;
+    if (!tri_cell_range(t, g, i, lo, hi, lay)) return;
     for (int x = lo[0]; x <= hi[0]; ++x)
         for (int y = lo[1]; y <= hi[1]; ++y)
             for (int z = lo[2]; z <= hi[2]; ++z) atomicAdd(t.tcell_count + cell_lin(lay, x, y, z), 1);
 }
 
-__global__ void k_tri_fill(Tris t, Grid g, double pad)
+__global__ void k_tri_fill(Tris t, Grid g)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= t.nt) return;
-    if (!tri_range_valid(t, g, i, pad)) return;
+    if (!tri_range_valid(t, g, i)) return;
     int lo[3], hi[3];
     const int* lay;
-    if (!tri_cell_range(t, g, i, pad, lo, hi, lay)) return;
+    if (!tri_cell_range(t, g, i, lo, hi, lay)) return;
     for (int x = lo[0]; x <= hi[0]; ++x)
         for (int y = lo[1]; y <= hi[1]; ++y)
             for (int z = lo[2]; z <= hi[2]; ++z) {
@@ -605,13 +609,12 @@ void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s)
     if (t.nt > 0) k_tri_transform<<<blocks(t.nt, 128), 128, 0, s>>>(t, b);
 }
 
-void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, double pad, int* tgover, int sm_count,
-                      cudaStream_t s)
+void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover, int sm_count, cudaStream_t s)
 {
     if (t.nt <= 0) return;
-    k_tri_count<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, pad, tgover);
+    k_tri_count<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, tgover);
     launch_scan(t.tcell_count, t.tcell_start, g.total_cells, g.tile_sums, sm_count, s);
-    k_tri_fill<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, pad);
+    k_tri_fill<<<blocks(t.nt, 128), 128, 0, s>>>(t, g);
     k_tri_place<<<sm_count * 8, 256, 0, s>>>(t, g);
 }
 

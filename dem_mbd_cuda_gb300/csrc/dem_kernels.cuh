@@ -53,15 +53,19 @@ struct Comps {
 struct SceneC {
     MatC pp, pt, pw;
     double g[3];
+    // Cell edge (cell factor x the scene's largest component radius), its
+    // inverse and the triangle-grid padding (the largest radius): each scene
+    // of a batch is gridded exactly as it would be alone.
+    double mesh, inv_mesh, pad;
+    float mesh_f, margin_f;
     int grav;
     int wall_begin, wall_count;
     int body_begin, body_count;
 };
 
 struct Grid {
-    double inv_mesh, mesh;
-    float mesh_f, margin_f;
-    int capacity;  // cells in the dense table
+    const SceneC* sc;  // per-scene cell edge
+    int capacity;      // cells in the dense table
     int nscenes;
     uint64_t* ckey;
     int *clin, *crank;
@@ -163,8 +167,7 @@ void launch_update_components(const Comps& c, const Owners& o, cudaStream_t s);
 void launch_grid_build(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s);
 void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int sm_count, cudaStream_t s);
 void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s);
-void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, double pad, int* tgover, int sm_count,
-                      cudaStream_t s);
+void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover, int sm_count, cudaStream_t s);
 void launch_universal_gravity(const Owners& o, cudaStream_t s);
 void launch_leapfrog_init(const Owners& o, double half_dt, cudaStream_t s);
 void launch_advance(const Owners& o, double dt, cudaStream_t s);
