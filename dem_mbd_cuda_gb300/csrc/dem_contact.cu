@@ -230,8 +230,12 @@ __global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const S
             }
             hw.hw[ci] = whw;
         }
-        double* wr = ct.wres + 6 * (size_t)ci;
-        wr[0] = wF.x; wr[1] = wF.y; wr[2] = wF.z; wr[3] = wT.x; wr[4] = wT.y; wr[5] = wT.z;
+        const bool hit = wF.x != 0.0 || wF.y != 0.0 || wF.z != 0.0 || wT.x != 0.0 || wT.y != 0.0 || wT.z != 0.0;
+        ct.wflag[ci] = hit ? 1 : 0;
+        if (hit) {
+            double* wr = ct.wres + 6 * (size_t)ci;
+            wr[0] = wF.x; wr[1] = wF.y; wr[2] = wF.z; wr[3] = wT.x; wr[4] = wT.y; wr[5] = wT.z;
+        }
     }
     block_add(k.bover, bover);
     block_max(k.bhigh, bhigh);
@@ -239,14 +243,35 @@ __global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const S
 
 // ------------------------------------------------------------- particle sweep
 constexpr int kMaxContacts = kPSlots;
+constexpr int kCandidates = 96;  // FP32-prefilter survivors held before the exact pass
+
+// Exact part of the reference's overlap test for one candidate (:587-597):
+// same owner skipped, FP64 d^2 with the reference's contraction, strict
+// inequality against (ri + rj)^2, coincident centres skipped.  Kept out of
+// line so the FP64 work runs for prefilter survivors only.
+__device__ __noinline__ bool exact_contact(const D4* __restrict__ pos, const int4* __restrict__ meta, int u, int owner,
+                                           double px, double py, double pz, double pr, int& cid)
+{
+    const int4 mj = meta[u];
+    if (mj.y == owner) return false;
+    const D4 pj = pos[u];
+    const V3<double> delta = mk(pj.x - px, pj.y - py, pj.z - pz);
+    const double d2 = distance_squared(delta);
+    const double rs = pr + pj.w;
+    if (d2 >= rs * rs || d2 <= 1.0e-28) return false;
+    cid = mj.z;
+    return true;
+}
 
 // One thread per component in cell order: the reference's 27-cell sweep
-// (:1124-1146) over the cell start table.  An FP32 test on cell-relative
-// coordinates with a margin of 1e-5 cell edges discards far candidates; the
-// survivors get the reference's exact FP64 overlap test, then the history
-// slot in sweep order (acquireHistorySlot, :190-215).  Contacts go to a flat
-// list; results are stored per (slot rank, component) so the owner sum reads
-// them coalesced.
+// (:1124-1146) over the cell start table, in the reference's order (dx, dy,
+// dz ascending; members of a cell in ascending component order).  For each
+// (dx, dy) column the up to three z-cells are one contiguous range of the
+// sorted order.  Phase 1 keeps candidates that pass an FP32 test on
+// cell-relative coordinates (margin 1e-5 cell edges); phase 2 runs the exact
+// FP64 test and the history slot acquisition (acquireHistorySlot, :190-215)
+// on them in order.  Contacts go to a flat list; results are stored per
+// (slot rank, component) so the owner sum reads them coalesced.
 template <typename T>
 __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __restrict__ sc, Tris tris, Hist<T> hp,
                                                Contacts<T> ct, Counters k, int nc)
@@ -255,7 +280,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     const int nvalid = *g.nvalid;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int count = 0, pover = 0, phigh = 0;
-    int stage_t[kMaxContacts];
+    int stage_t[kCandidates];
     int stage_s[kMaxContacts];
     int ci = -1;
     if (t < nvalid) {
@@ -267,43 +292,63 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         const int* lay = g.scene_layout + 8 * s;
         const float4 fi = r.relf[t];
         const float mesh_f = sc[s].mesh_f, margin_f = sc[s].margin_f;
+        const float offx[3] = {-mesh_f - fi.x, -fi.x, mesh_f - fi.x};
+        const float offy[3] = {-mesh_f - fi.y, -fi.y, mesh_f - fi.y};
+        const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
+        const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
         int phw = hp.hw[ci];
+        int pending = 0;  // candidates in stage_t[count .. count + pending)
+        auto exact_pass = [&]() {
+            const int first = count, last = count + pending;
+            for (int q = first; q < last; ++q) {
+                const int u = stage_t[q];
+                int cid;
+                if (!exact_contact(r.pos, r.meta, u, owner, pi.x, pi.y, pi.z, pi.w, cid)) continue;
+                if (count >= kMaxContacts) { ++pover; continue; }
+                const int slot = acquire(hp, kPSlots, ci, (uint64_t)(uint32_t)cid + 1ull, step, phw, phigh);
+                if (slot < 0) { ++pover; continue; }
+                stage_t[count] = u;
+                stage_s[count] = slot;
+                ++count;
+            }
+            pending = 0;
+        };
         for (int dx = -1; dx <= 1; ++dx) {
             const int nx = cell.x + dx;
             if (nx < lay[0] || nx >= lay[0] + lay[3]) continue;
+            const float ox = offx[dx + 1];
             for (int dy = -1; dy <= 1; ++dy) {
                 const int ny = cell.y + dy;
                 if (ny < lay[1] || ny >= lay[1] + lay[4]) continue;
+                const float oy = offy[dy + 1];
                 const int row = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] - lay[2];
-                for (int dz = -1; dz <= 1; ++dz) {
-                    const int nz = cell.z + dz;
-                    if (nz < lay[2] || nz >= lay[2] + lay[5]) continue;
-                    const int lin = row + nz;
-                    const int b = g.cell_start[lin], e = g.cell_start[lin + 1];
-                    const float ox = dx * mesh_f - fi.x, oy = dy * mesh_f - fi.y, oz = dz * mesh_f - fi.z;
-                    for (int u = b; u < e; ++u) {
-                        const float4 fj = r.relf[u];
-                        const float ddx = fj.x + ox, ddy = fj.y + oy, ddz = fj.z + oz;
-                        const float rsf = fj.w + fi.w + margin_f;
-                        if (ddx * ddx + ddy * ddy + ddz * ddz >= rsf * rsf) continue;
-                        const int4 mj = r.meta[u];
-                        if (mj.y == owner) continue;
-                        const D4 pj = r.pos[u];
-                        const V3<double> delta = mk(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
-                        const double d2 = distance_squared(delta);
-                        const double rs = pi.w + pj.w;
-                        if (d2 >= rs * rs || d2 <= 1.0e-28) continue;
-                        const uint64_t key = (uint64_t)(uint32_t)mj.z + 1ull;
-                        if (count >= kMaxContacts) { ++pover; continue; }
-                        const int slot = acquire(hp, kPSlots, ci, key, step, phw, phigh);
-                        if (slot < 0) { ++pover; continue; }
-                        stage_t[count] = u;
-                        stage_s[count] = slot;
-                        ++count;
+                // boundaries of the z-cells z0..z1 of this column
+                int bnd[4];
+                for (int z = z0; z <= z1 + 1; ++z) bnd[z - z0] = g.cell_start[row + z];
+                for (int zc = z0; zc <= z1; ++zc) {
+                    const float oz = offz[zc - cell.z + 1];
+                    const int e = bnd[zc - z0 + 1];
+                    // four candidates per iteration: their loads are issued
+                    // together, the survivors are appended in order
+                    for (int u0 = bnd[zc - z0]; u0 < e; u0 += 4) {
+                        float4 fj[4];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            fj[q] = (u0 + q < e) ? r.relf[u0 + q] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const float ddx = fj[q].x + ox, ddy = fj[q].y + oy, ddz = fj[q].z + oz;
+                            const float rsf = fj[q].w + fi.w + margin_f;
+                            if (ddx * ddx + ddy * ddy + ddz * ddz >= rsf * rsf) continue;
+                            if (count + pending == kCandidates) exact_pass();
+                            stage_t[count + pending] = u0 + q;
+                            ++pending;
+                        }
                     }
                 }
             }
         }
+        exact_pass();
         hp.hw[ci] = phw;
         ct.cnt[ci] = count;
         int pt_flag = 0;
@@ -664,32 +709,54 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= o.n) return;
-    const int s = o.scene[i];
-    const double m = o.mass[i];
-    V3<double> fF = mk(0.0, 0.0, 0.0);
-    if (sc[s].grav) fF = mk(m * sc[s].g[0], m * sc[s].g[1], m * sc[s].g[2]);
+    // field force m*g (precomputed per owner, the same products as
+    // :1090-1094) plus universal gravitation when enabled
+    V3<double> fF = mk(o.mg[3 * (size_t)i], o.mg[3 * (size_t)i + 1], o.mg[3 * (size_t)i + 2]);
     if (o.ugx) fF = fF + mk(o.ugx[i], o.ugy[i], o.ugz[i]);
     V3<double> cF = mk(0.0, 0.0, 0.0), cT = cF, wF = cF, wT = cF, bF = cF, bT = cF;
+    bool any_wall = false, any_body = false;
     const int c0 = c.sphere ? i : c.ostart[i], c1 = c.sphere ? i + 1 : c.ostart[i + 1];
     for (int ci = c0; ci < c1; ++ci) {
         const int cnt = ct.cnt[ci];
-        for (int q = 0; q < cnt; ++q) {
-            const T* rr = ct.res + 6 * ((size_t)q * c.n + ci);
-            cF = cF + mk((double)rr[0], (double)rr[1], (double)rr[2]);
-            cT = cT + mk((double)rr[3], (double)rr[4], (double)rr[5]);
+        if constexpr (sizeof(T) == sizeof(double)) {
+            for (int q = 0; q < cnt; ++q) {
+                const T* rr = ct.res + 6 * ((size_t)q * c.n + ci);
+                cF = cF + mk((double)rr[0], (double)rr[1], (double)rr[2]);
+                cT = cT + mk((double)rr[3], (double)rr[4], (double)rr[5]);
+            }
+        } else {
+            // mixed form: the per-contact rows are FP32; their sum stays FP32
+            // and enters the FP64 totals once per component.
+            V3<float> sf = mk(0.f, 0.f, 0.f), st = mk(0.f, 0.f, 0.f);
+            for (int q = 0; q < cnt; ++q) {
+                const float* rr = reinterpret_cast<const float*>(ct.res) + 6 * ((size_t)q * c.n + ci);
+                sf = sf + mk(rr[0], rr[1], rr[2]);
+                st = st + mk(rr[3], rr[4], rr[5]);
+            }
+            if (cnt) {
+                cF = cF + cvt<double>(sf);
+                cT = cT + cvt<double>(st);
+            }
         }
-        const double* wr = ct.wres + 6 * (size_t)ci;
-        wF = wF + mk(wr[0], wr[1], wr[2]);
-        wT = wT + mk(wr[3], wr[4], wr[5]);
+        if (ct.wflag[ci]) {
+            const double* wr = ct.wres + 6 * (size_t)ci;
+            wF = wF + mk(wr[0], wr[1], wr[2]);
+            wT = wT + mk(wr[3], wr[4], wr[5]);
+            any_wall = true;
+        }
         const int pk = ct.pt_index[ci];
         if (pk >= 0) {
             const double* pr = ct.pt_res + 6 * (size_t)ci;
             bF = bF + mk(pr[0], pr[1], pr[2]);
             bT = bT + mk(pr[3], pr[4], pr[5]);
+            any_body = true;
         }
     }
-    const V3<double> TF = (cF + fF) + (wF + bF);
-    const V3<double> TT = cT + (wT + bT);
+    // total = (contact + field) + (wall + body) (:1215-1217); zero terms are
+    // skipped, which leaves every sum unchanged
+    const V3<double> wb = any_wall ? (any_body ? wF + bF : wF) : bF;
+    const V3<double> TF = (any_wall || any_body) ? (cF + fF) + wb : cF + fF;
+    const V3<double> TT = any_wall ? (any_body ? cT + (wT + bT) : cT + wT) : (any_body ? cT + bT : cT);
     if (outputs) {
         double* a = fc + 6 * (size_t)i; a[0] = cF.x; a[1] = cF.y; a[2] = cF.z; a[3] = cT.x; a[4] = cT.y; a[5] = cT.z;
         a = ff + 6 * (size_t)i; a[0] = fF.x; a[1] = fF.y; a[2] = fF.z; a[3] = 0.0; a[4] = 0.0; a[5] = 0.0;
@@ -703,8 +770,15 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
     const double tx = (1.0 - 2.0 * (qy * qy + qz * qz)) * TT.x + 2.0 * (qx * qy + qw * qz) * TT.y + 2.0 * (qx * qz - qw * qy) * TT.z;
     const double ty = 2.0 * (qx * qy - qw * qz) * TT.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * TT.y + 2.0 * (qy * qz + qw * qx) * TT.z;
     const double tz = 2.0 * (qx * qz + qw * qy) * TT.x + 2.0 * (qy * qz - qw * qx) * TT.y + (1.0 - 2.0 * (qx * qx + qy * qy)) * TT.z;
-    const double wx = o.wx[i], wy = o.wy[i], wz = o.wz[i];
     const double Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
+    if (Ix == Iy && Iy == Iz) {
+        // isotropic inertia: the gyroscopic terms are exactly zero
+        o.awx[i] = tx * o.inv_ix[i];
+        o.awy[i] = ty * o.inv_iy[i];
+        o.awz[i] = tz * o.inv_iz[i];
+        return;
+    }
+    const double wx = o.wx[i], wy = o.wy[i], wz = o.wz[i];
     o.awx[i] = (tx - (Iz - Iy) * wz * wy) * o.inv_ix[i];
     o.awy[i] = (ty - (Ix - Iz) * wx * wz) * o.inv_iy[i];
     o.awz[i] = (tz - (Iy - Ix) * wy * wx) * o.inv_iz[i];
@@ -826,16 +900,16 @@ void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r
 template <typename T, typename TB>
 void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs& r, const SceneC* sc, const Walls& w,
                      const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<TB> hb, Contacts<T> ct,
-                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s)
+                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s, int stage)
 {
     (void)block;
-    k_expire_walls<T, TB><<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, hp, hw, hb, ct, k, dt_eff);
-    k_sweep<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, ct, k, c.n);
-    k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff);
-    if (t.nt > 0 && b.nb > 0) {
+    if (stage & 1) k_expire_walls<T, TB><<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, hp, hw, hb, ct, k, dt_eff);
+    if (stage & 2) k_sweep<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, ct, k, c.n);
+    if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff);
+    if ((stage & 8) && t.nt > 0 && b.nb > 0) {
         launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);
-        k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list,
-                                                  ct.pt_index, ct.pt_total_ptr);
+        k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list, ct.pt_index,
+                                                  ct.pt_total_ptr);
         k_pt<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
     }
 }
@@ -869,7 +943,7 @@ void launch_body_outputs(const Comps& c, const Owners& o, const Bodies& b, const
     template void launch_contacts<T, double>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,   \
                                              const Walls&, const Tris&, const Bodies&, Hist<T>, Hist<T>,             \
                                              Hist<double>, Contacts<T>, const Counters&, double, int, int,            \
-                                             cudaStream_t);                                                          \
+                                             cudaStream_t, int);                                                     \
     template void launch_owner_sum<T>(const Comps&, const Owners&, const SceneC*, Contacts<T>, bool, double*,       \
                                       double*, double*, double*, cudaStream_t);                                       \
     template void launch_body_reduce<T>(const Recs&, const SceneC*, const Bodies&, Contacts<T>, BodyOut, bool,       \
@@ -882,6 +956,6 @@ DEM_INSTANTIATE(float)
 template void launch_contacts<float, float>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,
                                             const Walls&, const Tris&, const Bodies&, Hist<float>, Hist<float>,
                                             Hist<float>, Contacts<float>, const Counters&, double, int, int,
-                                            cudaStream_t);
+                                            cudaStream_t, int);
 
 }  // namespace demgb

@@ -274,6 +274,13 @@ public:
             std::vector<double> inv(n_);
             for (int i = 0; i < n_; ++i) inv[i] = 1.0 / om[i];
             O_.inv_mass = upd(inv, "inverse mass");
+            std::vector<double> mg(3 * (size_t)n_, 0.0);
+            for (int i = 0; i < n_; ++i) {
+                const SceneC& S = sc[oscene[i]];
+                if (S.grav)
+                    for (int a = 0; a < 3; ++a) mg[3 * (size_t)i + a] = om[i] * S.g[a];
+            }
+            O_.mg = upd(mg, "field force");
             for (int a = 0; a < 3; ++a) {
                 for (int i = 0; i < n_; ++i) inv[i] = 1.0 / oin[3 * (size_t)i + a];
                 (a == 0 ? O_.inv_ix : (a == 1 ? O_.inv_iy : O_.inv_iz)) = upd(inv, "inverse inertia");
@@ -464,6 +471,8 @@ public:
         check(cudaMemsetAsync(ct.cnt, 0, nc_ * sizeof(int), s), "clear");
         check(cudaMemsetAsync(ct.off, 0, nc_ * sizeof(int), s), "clear");
         ct.wres = arena_.alloc<double>((size_t)nc_ * 6, "wall results");
+        ct.wflag = arena_.alloc<unsigned char>(nc_, "wall flags");
+        check(cudaMemsetAsync(ct.wflag, 0, nc_, s), "clear");
         check(cudaMemsetAsync(ct.wres, 0, (size_t)nc_ * 6 * sizeof(double), s), "clear");
         ct.pt_index = arena_.alloc<int>(nc_, "pt index");
         check(cudaMemsetAsync(ct.pt_index, 0xff, nc_ * sizeof(int), s), "clear");
@@ -496,9 +505,13 @@ public:
         if (O_.ugx) launch_universal_gravity(O_, s);
         launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
         mark();
-        launch_contacts<T, TB>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, s);
-        mark();
+        for (int stage : {1, 2, 4, 8}) {
+            launch_contacts<T, TB>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, s,
+                                   stage);
+            mark();
+        }
         launch_owner_sum<T>(C_, O_, d_sc_, ct, false, nullptr, nullptr, nullptr, nullptr, s);
+        mark();
         if (nb_ > 0) launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
         launch_step_counter(K_, 0, s);
         mark();
@@ -1096,7 +1109,7 @@ public:
     int step_index_ = 0;
     size_t free_before_ = 0;
     cudaStream_t stream_ = nullptr;
-    std::array<cudaEvent_t, 8> ev_{};
+    std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;
     DeviceArena arena_, arena_tmp_;
     void* pinned_ = nullptr;

@@ -37,6 +37,7 @@ struct Owners {
     double *vhx, *vhy, *vhz, *whx, *why, *whz, *hqw, *hqx, *hqy, *hqz;
     double *mass, *ix, *iy, *iz, *radius;
     double *inv_mass, *inv_ix, *inv_iy, *inv_iz;
+    double* mg;  // [n][3] field force m*g of the owner's scene (0 without gravity)
     int *id, *status, *scene;
     double *ugx, *ugy, *ugz;  // universal-gravitation field force (optional)
 };
@@ -141,7 +142,8 @@ template <typename T> struct Contacts {
     T* res;         // [k][6]
     int *off, *cnt; // per component
     int capacity;
-    double* wres;   // [c][6] wall force/torque per component
+    double* wres;   // [c][6] wall force/torque per component (valid where wflag)
+    unsigned char* wflag;  // per component: nonzero wall force/torque this step
     int* pt_index;  // per component: PT item or -1
     int* pt_flag;   // per sorted position
     int* pt_pos;    // scan of pt_flag
@@ -181,11 +183,13 @@ template <typename T>
 void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
                    cudaStream_t s);
 // T: particle-particle and wall law / history type; TB: particle-triangle
-// law, area and body history type.
+// law, area and body history type.  `stage` selects kernels (1 expiry and
+// walls, 2 sweep, 4 particle law, 8 particle-triangle) so callers can time
+// them separately; 15 runs all in order.
 template <typename T, typename TB>
 void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs& r, const SceneC* sc, const Walls& w,
                      const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<TB> hb, Contacts<T> ct,
-                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s);
+                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s, int stage = 15);
 template <typename T>
 void launch_owner_sum(const Comps& c, const Owners& o, const SceneC* sc, Contacts<T> ct, bool outputs, double* fc,
                       double* ff, double* fw, double* ft, cudaStream_t s);
