@@ -35,16 +35,21 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PHASES = ["grid", "triangles+gather", "expire+walls", "sweep", "pp_law", "pt", "owner_sum", "body_reduce"]
 
 
-def make_scene(config):
+def make_scene(config, particles=None):
     from dem_mbd_cuda_gb300 import generate as G
     if config == "c0":
-        return G.pure_dem(n=20000, seed=1000), "pure DEM, 20,000 spheres r~U[1.8,2.2] mm, 5 walls, dt 1e-5"
+        n = particles or 20000
+        return G.pure_dem(n=n, seed=1000), "pure DEM, %d spheres r~U[1.8,2.2] mm on a lattice, 5 walls, dt 1e-5" % n
     if config == "c2":
-        sc, _ = G.drum(n=2000000, seed=1002)
-        return sc, "rotating drum, 2,000,000 lognormal spheres (median 1 mm), %d-triangle cylinder, dt 2e-6" % sc.n_triangles
-    sc, _ = G.mbd_blade_plate(n=200000, seed=1001)
-    return sc, ("DEM-MBD, 200,000 spheres r~U[1.5,2.5] mm in a 0.4 m box, %d-triangle blade (omega_z 3) + "
-                "%d-triangle 1 kg plate, dt 5e-6" % (int((sc.tri_body == 0).sum()), int((sc.tri_body == 1).sum())))
+        n = particles or 2000000
+        sc, _ = G.drum(n=n, seed=1002)
+        return sc, ("rotating drum, %d lognormal spheres (median 1 mm) settled in columns and co-rotating, "
+                    "%d-triangle cylinder, dt 2e-6" % (n, sc.n_triangles))
+    n = particles or 200000
+    sc, _ = G.mbd_blade_plate(n=n, seed=1001)
+    return sc, ("DEM-MBD, %d spheres r~U[1.5,2.5] mm settled in columns in a 0.4 m box, %d-triangle blade "
+                "(omega_z 3) + %d-triangle 1 kg plate, dt 5e-6"
+                % (n, int((sc.tri_body == 0).sum()), int((sc.tri_body == 1).sum())))
 
 
 class ClockSampler:
@@ -206,6 +211,8 @@ def main():
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--particles", type=int, default=None,
+                    help="particle count of the generated scene (profiling captures of a smaller case)")
     ap.add_argument("--single", action="store_true",
                     help="headline precision only: no second precision, e2e, error or CPU legs (profiling runs)")
     args = ap.parse_args()
@@ -218,7 +225,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    scene, desc = make_scene(args.config)
+    scene, desc = make_scene(args.config, args.particles)
 
     if args.impl == "reference":
         # The reference's own hot path is CUDA-only; its CPU implementation of

@@ -73,10 +73,60 @@ __device__ void block_max(int* dst, int v)
     if ((threadIdx.x & 31) == 0 && s > 0) atomicMax(dst, s);
 }
 
-template <typename T> __device__ __forceinline__ void zero9(T* v)
+// One history slot <-> registers (h[0..8]; the padding is written as 0).
+__device__ __forceinline__ void hv_load(const float* p, float* h)
 {
+    const float4* q = reinterpret_cast<const float4*>(p);
+    const float4 a = q[0], b = q[1], c = q[2];
+    h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
+    h[4] = b.x; h[5] = b.y; h[6] = b.z; h[7] = b.w;
+    h[8] = c.x;
+}
+__device__ __forceinline__ void hv_store(float* p, const float* h)
+{
+    float4* q = reinterpret_cast<float4*>(p);
+    q[0] = make_float4(h[0], h[1], h[2], h[3]);
+    q[1] = make_float4(h[4], h[5], h[6], h[7]);
+    q[2] = make_float4(h[8], 0.f, 0.f, 0.f);
+}
+__device__ __forceinline__ void hv_load(const double* p, double* h)
+{
+    const double2* q = reinterpret_cast<const double2*>(p);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) v[k] = T(0);
+    for (int k = 0; k < 4; ++k) {
+        const double2 v = q[k];
+        h[2 * k] = v.x; h[2 * k + 1] = v.y;
+    }
+    h[8] = q[4].x;
+}
+__device__ __forceinline__ void hv_store(double* p, const double* h)
+{
+    double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q[k] = make_double2(h[2 * k], h[2 * k + 1]);
+    q[4] = make_double2(h[8], 0.0);
+}
+template <typename T> __device__ __forceinline__ void zero_hv(T* v)
+{
+    T z[9] = {};
+    hv_store(v, z);
+}
+
+// The material constants a law of precision T reads.
+template <typename T> __device__ __forceinline__ const auto& mat(const MatC& d, const MatF& f)
+{
+    if constexpr (sizeof(T) == sizeof(double)) return d;
+    else return f;
+}
+
+// Read-only load of a 32-byte record.
+__device__ __forceinline__ D4 ldg_d4(const D4* p)
+{
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    D4 v;
+    v.x = a.x; v.y = a.y; v.z = b.x; v.w = b.y;
+    return v;
 }
 
 // expireHistory (:217-229) over the occupied prefix [0, hw).
@@ -90,7 +140,7 @@ template <typename T> __device__ void expire(Hist<T> h, int slots, int c, int st
             if (h.last[base + s] < step - 1) {
                 h.key[base + s] = 0;
                 h.last[base + s] = -1;
-                zero9(h.val + (base + s) * 9);
+                zero_hv(h.val + (base + s) * kHV);
             } else {
                 nhw = s + 1;
             }
@@ -121,7 +171,7 @@ __device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int&
     }
     h.key[base + empty] = key;
     h.last[base + empty] = step;
-    zero9(h.val + (base + empty) * 9);
+    zero_hv(h.val + (base + empty) * kHV);
     if (empty + 1 > hw) hw = empty + 1;
     high = max(high, empty + 1);
     return empty;
@@ -216,13 +266,13 @@ __global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const S
                 if (depth <= 0.0) continue;
                 const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
                 if (slot < 0) { ++bover; continue; }
-                T* hv = hw.val + ((size_t)ci * kWSlots + slot) * 9;
+                T* hv = hw.val + ((size_t)ci * kWSlots + slot) * kHV;
                 const V3<double> vel = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
                 const V3<double> om =
                     rot_iv(o.qw[w], o.qx[w], o.qy[w], o.qz[w], mk(o.wx[w], o.wy[w], o.wz[w]));
                 const V3<double> off = c.ox ? mk(c.ox[ci], c.oy[ci], c.oz[ci]) : mk(0.0, 0.0, 0.0);
                 V3<T> f, cpl;
-                wall_law<T>(S.pw, T(dt_eff), cvt<T>(out), T(depth), T(rad), T(o.mass[w]), cvt<T>(vel), cvt<T>(om), hv, f,
+                wall_law<T>(mat<T>(S.pw, S.pwf), T(dt_eff), cvt<T>(out), T(depth), T(rad), T(o.mass[w]), cvt<T>(vel), cvt<T>(om), hv, f,
                             cpl);
                 const V3<double> fd = cvt<double>(f);
                 wF = wF + fd;
@@ -372,14 +422,45 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
 }
 
 // ------------------------------------------------------------------ PP law
+// particleContact (:579-706) for one contact of the flat list.  Everything
+// the law reads is loaded before any arithmetic (records through the
+// read-only path, the history slot as vectors), so the loads of a contact
+// are in flight together.
 template <typename T>
 __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict__ sc, Hist<T> hp, Contacts<T> ct,
-                                                Counters k, double dt_eff)
+                                                Counters k, double dt_eff, int nscenes)
 {
     const int total = *k.ct_total;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-        const int4 e = ct.ent[q];
-        const D4 pi = r.pos[e.x], pj = r.pos[e.y];
+        const int4 e = __ldg(&ct.ent[q]);
+        const D4 pi = ldg_d4(&r.pos[e.x]), pj = ldg_d4(&r.pos[e.y]);
+        const int s = nscenes > 1 ? __ldg(&r.meta[e.x].w) : 0;
+        T h[9];
+        T* hv = hp.val + (size_t)e.z * kHV;
+        hv_load(hv, h);
+        V3<T> erv, mrv, ewi, ewj, mwi, mwj;
+        T mi_, mj_;
+        if constexpr (sizeof(T) == sizeof(double)) {
+            const D4 vi = ldg_d4(&r.v[e.x]), vj = ldg_d4(&r.v[e.y]);
+            const D4 ui = ldg_d4(&r.vm[e.x]), uj = ldg_d4(&r.vm[e.y]);
+            const D4 wi = ldg_d4(&r.w[e.x]), wj = ldg_d4(&r.w[e.y]);
+            const D4 xi = ldg_d4(&r.wm[e.x]), xj = ldg_d4(&r.wm[e.y]);
+            erv = d3(vj) - d3(vi);
+            mrv = d3(uj) - d3(ui);
+            ewi = d3(wi); ewj = d3(wj);
+            mwi = d3(xi); mwj = d3(xj);
+            mi_ = vi.w; mj_ = vj.w;
+        } else {
+            const float4 vi = __ldg(&r.vf[e.x]), vj = __ldg(&r.vf[e.y]);
+            const float4 ui = __ldg(&r.vmf[e.x]), uj = __ldg(&r.vmf[e.y]);
+            const float4 wi = __ldg(&r.wf[e.x]), wj = __ldg(&r.wf[e.y]);
+            const float4 xi = __ldg(&r.wmf[e.x]), xj = __ldg(&r.wmf[e.y]);
+            erv = f3(vj) - f3(vi);
+            mrv = f3(uj) - f3(ui);
+            ewi = f3(wi); ewj = f3(wj);
+            mwi = f3(xi); mwj = f3(xj);
+            mi_ = vi.w; mj_ = vj.w;
+        }
         const V3<double> delta = mk(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
         const double d2 = distance_squared(delta);
         const double rs = pi.w + pj.w;
@@ -398,33 +479,20 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
             depth = (float)num / ((float)rs + df);
             n = cvt<float>(delta) * (1.0f / df);
         }
-        V3<T> erv, mrv, ewi, ewj, mwi, mwj;
-        T mi_, mj_;
-        if constexpr (sizeof(T) == sizeof(double)) {
-            const D4 vi = r.v[e.x], vj = r.v[e.y];
-            const D4 ui = r.vm[e.x], uj = r.vm[e.y];
-            erv = d3(vj) - d3(vi);
-            mrv = d3(uj) - d3(ui);
-            ewi = d3(r.w[e.x]); ewj = d3(r.w[e.y]);
-            mwi = d3(r.wm[e.x]); mwj = d3(r.wm[e.y]);
-            mi_ = vi.w; mj_ = vj.w;
-        } else {
-            const float4 vi = r.vf[e.x], vj = r.vf[e.y];
-            const float4 ui = r.vmf[e.x], uj = r.vmf[e.y];
-            erv = f3(vj) - f3(vi);
-            mrv = f3(uj) - f3(ui);
-            ewi = f3(r.wf[e.x]); ewj = f3(r.wf[e.y]);
-            mwi = f3(r.wmf[e.x]); mwj = f3(r.wmf[e.y]);
-            mi_ = vi.w; mj_ = vj.w;
-        }
-        const int s = r.meta[e.x].w;
-        T* hv = hp.val + (size_t)e.z * 9;
+        const SceneC& S = sc[s];
         V3<T> f, cpl;
-        pp_law<T>(sc[s].pp, T(dt_eff), n, d, depth, T(d2), T(pi.w), T(pj.w), mi_, mj_, erv, mrv, ewi, ewj, mwi, mwj, hv,
-                  f, cpl);
+        pp_law<T>(mat<T>(S.pp, S.ppf), T(dt_eff), n, d, depth, T(d2), T(pi.w), T(pj.w), mi_, mj_, erv, mrv, ewi, ewj,
+                  mwi, mwj, h, f, cpl);
+        hv_store(hv, h);
         if (r.off) cpl = cpl + cross(cvt<T>(d3(r.off[e.x])), f);
         T* out = ct.res + 6 * (size_t)e.w;
-        out[0] = f.x; out[1] = f.y; out[2] = f.z; out[3] = cpl.x; out[4] = cpl.y; out[5] = cpl.z;
+        if constexpr (sizeof(T) == sizeof(double)) {
+            double2* o2 = reinterpret_cast<double2*>(out);
+            o2[0] = make_double2(f.x, f.y); o2[1] = make_double2(f.z, cpl.x); o2[2] = make_double2(cpl.y, cpl.z);
+        } else {
+            float2* o2 = reinterpret_cast<float2*>(out);
+            o2[0] = make_float2(f.x, f.y); o2[1] = make_float2(f.z, cpl.x); o2[2] = make_float2(cpl.y, cpl.z);
+        }
     }
 }
 
@@ -548,7 +616,7 @@ __global__ void __launch_bounds__(128) k_pt(Comps c, Owners o, Recs r, const Sce
             const double md = wd / tot;
             const int slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh);
             if (slot < 0) { ++bover; continue; }
-            T* hv = hb.val + ((size_t)ci * kBSlots + slot) * 9;
+            T* hv = hb.val + ((size_t)ci * kBSlots + slot) * kHV;
             const V3<double> center = mk(bodies.c[3 * b], bodies.c[3 * b + 1], bodies.c[3 * b + 2]);
             const double* bq = bodies.q + 4 * b;
             const V3<double> wb = rot_iv(bq[0], bq[1], bq[2], bq[3], mk(bodies.w[3 * b], bodies.w[3 * b + 1], bodies.w[3 * b + 2]));
@@ -905,7 +973,7 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
     (void)block;
     if (stage & 1) k_expire_walls<T, TB><<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, hp, hw, hb, ct, k, dt_eff);
     if (stage & 2) k_sweep<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, ct, k, c.n);
-    if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff);
+    if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
         launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);
         k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list, ct.pt_index,

@@ -83,6 +83,11 @@ __host__ __device__ inline void unpack_cell(uint64_t k, int& x, int& y, int& z)
 struct MatC {
     double kN, kS, logN, logS, denN, denS, mu, muT, muR, beta, coh, dt;
 };
+// The same constants rounded once to FP32 (the values the FP32 laws would
+// otherwise convert per contact).
+struct MatF {
+    float kN, kS, logN, logS, denN, denS, mu, muT, muR, beta, coh, dt;
+};
 
 // ---------------------------------------------------------------- history
 // transportTangentHistory (:245-256)
@@ -158,7 +163,7 @@ template <typename T> DEM_DEV void hstore(T* v, int cat, V3<T> x)
 
 // Damping coefficients of the reference's restitution model (:619-632).
 template <typename T> struct LawC { T kN, kS, cN, cS, kT, cT, kR, cR, brs; };
-template <typename T> DEM_DEV LawC<T> law_constants(const MatC& m, T mred, T radius_term)
+template <typename T, typename M> DEM_DEV LawC<T> law_constants(const M& m, T mred, T radius_term)
 {
     LawC<T> c;
     c.kN = T(m.kN);
@@ -177,14 +182,14 @@ template <typename T> DEM_DEV LawC<T> law_constants(const MatC& m, T mred, T rad
 // particleContact (:579-706) after the overlap test and slot acquisition.
 // n: unit direction i->j; erv/mrv: endpoint/midpoint velocity of j minus i;
 // h: history slot values [roll, tangent, twist] updated in place.
-template <typename T>
-DEM_DEV void pp_law(const MatC& m, T dt, V3<T> n, T d, T depth, T d2, T ri, T rj, T mi, T mj, V3<T> erv, V3<T> mrv,
+template <typename T, typename M>
+DEM_DEV void pp_law(const M& m, T dt, V3<T> n, T d, T depth, T d2, T ri, T rj, T mi, T mj, V3<T> erv, V3<T> mrv,
                     V3<T> ewi, V3<T> ewj, V3<T> mwi, V3<T> mwj, T* h, V3<T>& force, V3<T>& couple)
 {
     const T mred = mi * mj / (mi + mj);
     const T rs = ri + rj;
     const T reff = ri * rj / rs;
-    const LawC<T> c = law_constants<T>(m, mred, reff);
+    const LawC<T> c = law_constants<T, M>(m, mred, reff);
     V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(erv, n));
     fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
     const T li = (ri * ri - rj * rj + d2) / (T(2.0) * d);
@@ -215,8 +220,8 @@ DEM_DEV void pp_law(const MatC& m, T dt, V3<T> n, T d, T depth, T d2, T ri, T rj
 
 // ---------------------------------------------------------- wall contact
 // wallContact (:975-1063) after the slot acquisition; out = outward normal.
-template <typename T>
-DEM_DEV void wall_law(const MatC& m, T dt, V3<T> out, T depth, T r, T mass, V3<T> vel, V3<T> om, T* h, V3<T>& force,
+template <typename T, typename M>
+DEM_DEV void wall_law(const M& m, T dt, V3<T> out, T depth, T r, T mass, V3<T> vel, V3<T> om, T* h, V3<T>& force,
                       V3<T>& couple)
 {
     const V3<T> n = out * T(-1.0);
@@ -228,7 +233,7 @@ DEM_DEV void wall_law(const MatC& m, T dt, V3<T> out, T depth, T r, T mass, V3<T
     const V3<T> twr = n * dot(rw, n);
     V3<T> rlr = rw - twr;
     if (fabs(lever) > T(1.0e-30)) rlr = rlr + cross(n, tv) * (T(0.5) / lever);
-    const LawC<T> c = law_constants<T>(m, mass, r);
+    const LawC<T> c = law_constants<T, M>(m, mass, r);
     const V3<T> en = n * (-c.kN * depth);
     const V3<T> dn = n * (c.cN * dot(rv, n));
     const V3<T> fn = en + dn;

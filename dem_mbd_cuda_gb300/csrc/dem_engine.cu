@@ -72,6 +72,12 @@ private:
     size_t bytes_ = 0;
 };
 
+static MatF to_float(const MatC& c)
+{
+    return MatF{(float)c.kN, (float)c.kS, (float)c.logN, (float)c.logS, (float)c.denN, (float)c.denS, (float)c.mu,
+                (float)c.muT, (float)c.muR, (float)c.beta, (float)c.coh, (float)c.dt};
+}
+
 static MatC make_mat(const dem_mech& m, double dt)
 {
     MatC c;
@@ -196,6 +202,7 @@ public:
                     throw DemError(DEM_ERR_INVALID, "each CUDA owner requires 1 to 8 components");
             SceneC& S = sc[s];
             S.pp = make_mat(x.pp, x.dt); S.pt = make_mat(x.pt, x.dt); S.pw = make_mat(x.pw, x.dt);
+            S.ppf = to_float(S.pp); S.ptf = to_float(S.pt); S.pwf = to_float(S.pw);
             S.mesh = cell_factor_ * scene_rmax[s];
             if (!(S.mesh > 0.0)) throw DemError(DEM_ERR_INVALID, "invalid mesh size");
             S.inv_mesh = 1.0 / S.mesh;
@@ -449,11 +456,11 @@ public:
         const size_t n = (size_t)nc_ * slots;
         h.key = arena_.alloc<uint64_t>(n, "history keys");
         h.last = arena_.alloc<int>(n, "history last seen");
-        h.val = arena_.alloc<H>(n * 9, "history values");
+        h.val = arena_.alloc<H>(n * kHV, "history values");
         h.hw = arena_.alloc<int>(nc_, "history hw");
         check(cudaMemsetAsync(h.key, 0, n * sizeof(uint64_t), s), "clear history keys");
         check(cudaMemsetAsync(h.last, 0xff, n * sizeof(int), s), "clear history age");
-        check(cudaMemsetAsync(h.val, 0, n * 9 * sizeof(H), s), "clear history values");
+        check(cudaMemsetAsync(h.val, 0, n * kHV * sizeof(H), s), "clear history values");
         check(cudaMemsetAsync(h.hw, 0, nc_ * sizeof(int), s), "clear history hw");
     }
 
@@ -931,9 +938,10 @@ public:
         if (keys) check(cudaMemcpy(keys, h.key, n * sizeof(uint64_t), cudaMemcpyDeviceToHost), "download keys");
         if (last) check(cudaMemcpy(last, h.last, n * sizeof(int), cudaMemcpyDeviceToHost), "download last");
         if (val) {
-            std::vector<T> v(n * 9);
-            check(cudaMemcpy(v.data(), h.val, n * 9 * sizeof(T), cudaMemcpyDeviceToHost), "download values");
-            for (size_t k = 0; k < n * 9; ++k) val[k] = (double)v[k];
+            std::vector<T> v(n * kHV);
+            check(cudaMemcpy(v.data(), h.val, n * kHV * sizeof(T), cudaMemcpyDeviceToHost), "download values");
+            for (size_t k = 0; k < n; ++k)
+                for (int a = 0; a < 9; ++a) val[9 * k + a] = (double)v[kHV * k + a];
         }
     }
     void download_history(int kind, uint64_t* keys, int* last, double* val)
@@ -956,9 +964,10 @@ public:
     {
         const size_t n = (size_t)nc_ * slots;
         check(cudaMemcpy(h.key, keys, n * sizeof(uint64_t), cudaMemcpyHostToDevice), "upload keys");
-        std::vector<T> v(n * 9);
-        for (size_t k = 0; k < n * 9; ++k) v[k] = (T)val[k];
-        check(cudaMemcpy(h.val, v.data(), n * 9 * sizeof(T), cudaMemcpyHostToDevice), "upload values");
+        std::vector<T> v(n * kHV, T(0));
+        for (size_t k = 0; k < n; ++k)
+            for (int a = 0; a < 9; ++a) v[kHV * k + a] = (T)val[9 * k + a];
+        check(cudaMemcpy(h.val, v.data(), n * kHV * sizeof(T), cudaMemcpyHostToDevice), "upload values");
         check(cudaMemset(h.last, 0xff, n * sizeof(int)), "reset history age");
         std::vector<int> hw(nc_, 0);
         for (int c = 0; c < nc_; ++c)

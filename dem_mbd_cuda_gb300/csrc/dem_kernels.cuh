@@ -53,6 +53,7 @@ struct Comps {
 // Per-scene constants.
 struct SceneC {
     MatC pp, pt, pw;
+    MatF ppf, ptf, pwf;
     double g[3];
     // Cell edge (cell factor x the scene's largest component radius), its
     // inverse and the triangle-grid padding (the largest radius): each scene
@@ -96,6 +97,11 @@ struct Recs {
     int4* cell;                             // cx, cy, cz, lin
     float4* relf;                           // position relative to the cell origin, radius
 };
+
+// History values: 9 per slot (roll, tangent, twist vectors), stored with a
+// stride of 12 so a slot starts on a 16-byte boundary and moves as three
+// float4 (FP32) or five double2 (FP64) accesses.
+constexpr int kHV = 12;
 
 template <typename T> struct Hist {
     uint64_t* key;

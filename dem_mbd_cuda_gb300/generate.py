@@ -2,10 +2,12 @@
 
 The reference ships no benchmark inputs beyond its 1704-particle validation
 cases, so every workload is generated here from a fixed seed.  Beds are built
-on a jittered simple-cubic lattice; radii are drawn from the stated
-distribution and then clipped, in lattice-wavefront order, so that no pair
-overlaps by more than ``overlap`` metres.  That gives a resting bed with
-gentle initial contacts (a settled-bed contact count without a settling run).
+either on a jittered simple-cubic lattice (``bed``: radii drawn from the
+stated distribution and clipped, in lattice-wavefront order, so that no pair
+overlaps by more than ``overlap`` metres; layers start apart and the bed
+falls) or as vertical columns in force balance (``column_bed``: every sphere
+rests on the one below with the overlap its load needs, so the bed is
+settled at step 0).
 All MECH fields are set explicitly (the reference's defaults enable cohesion).
 
 Meshes follow the reference's convention: faces are 1-based vertex triples
@@ -252,26 +254,92 @@ def pure_dem(n=20000, seed=1000, rmin=1.8e-3, rmax=2.2e-3, box=(0.2, 0.2, 0.4), 
                  wall_normal=wn, name=name)
 
 
+def column_bed(n, col_xy, base_z, radius_fn, rng, cap, g, kN, kN_base, density=DENSITY, kmax=None):
+    """A bed of vertical sphere columns in static equilibrium under gravity.
+
+    Column c stands at ``col_xy[c]``; its lowest sphere rests on the support
+    ``base_z(xy, r) -> z`` (centre height of a sphere of radius r touching
+    the support, vectorised over columns) and every sphere rests on the one
+    below it.  Radii come from ``radius_fn`` capped at ``cap`` (half the
+    smallest lateral gap between column axes), so spheres of neighbouring
+    columns never touch.  The n lowest spheres (by top height) are kept, and
+    each contact is then given the overlap that carries the weight above it
+    (g * sum of masses above / kN, kN_base for the support): every particle
+    starts at rest in force balance with its contacts closed, which a plain
+    lattice (gaps between layers) does not give.  Returns positions, radii
+    and the column index of every sphere."""
+    m = len(col_xy)
+    kmax = kmax or int(np.ceil(3.0 * n / max(m, 1))) + 8
+    r = np.minimum(radius_fn(rng, m * kmax).reshape(m, kmax), cap)
+    z0 = base_z(col_xy, r[:, 0])
+    ok = np.isfinite(z0)
+    z = np.empty_like(r)
+    z[:, 0] = z0
+    z[:, 1:] = z0[:, None] + np.cumsum(r[:, :-1] + r[:, 1:], axis=1)
+    top = z + r
+    top[~ok] = np.inf
+    flat = np.argsort(top, axis=None, kind="stable")[:n]
+    if not np.isfinite(top.flat[flat[-1]]):
+        raise ValueError("column bed: not enough room for %d spheres" % n)
+    keep = np.zeros(m * kmax, bool)
+    keep[flat] = True
+    keep = keep.reshape(m, kmax)
+    # a column keeps a contiguous run from its base (top heights increase
+    # along a column), so the counts give the kept spheres directly
+    cnt = keep.sum(axis=1)
+    assert np.array_equal(keep, np.arange(kmax)[None, :] < cnt[:, None])
+    mass = density * (4.0 / 3.0) * np.pi * r ** 3 * keep
+    above = np.cumsum(mass[:, ::-1], axis=1)[:, ::-1]   # weight carried by each sphere's lower contact
+    delta = g * above / kN
+    delta[:, 0] = g * above[:, 0] / kN_base
+    z = z - np.cumsum(delta, axis=1)
+    sel = keep.ravel()
+    cols = np.repeat(np.arange(m), kmax)[sel]
+    pos = np.column_stack([col_xy[cols, 0], col_xy[cols, 1], z.ravel()[sel]])
+    return pos, r.ravel()[sel], cols
+
+
+def column_grid(lo, hi, pitch, jitter, rng):
+    """Column axes on a square lattice covering [lo, hi] (2-D), jittered."""
+    nx = int(np.floor((hi[0] - lo[0]) / pitch)) + 1
+    ny = int(np.floor((hi[1] - lo[1]) / pitch)) + 1
+    ox = lo[0] + 0.5 * ((hi[0] - lo[0]) - (nx - 1) * pitch)
+    oy = lo[1] + 0.5 * ((hi[1] - lo[1]) - (ny - 1) * pitch)
+    gx, gy = np.meshgrid(ox + pitch * np.arange(nx), oy + pitch * np.arange(ny), indexing="ij")
+    xy = np.column_stack([gx.ravel(), gy.ravel()])
+    return xy + rng.uniform(-jitter, jitter, size=xy.shape)
+
+
 def mbd_blade_plate(n=200000, seed=1001, rmin=1.5e-3, rmax=2.5e-3, box=0.4, dt=5e-6, name="c1_dem_mbd"):
     """Config 1: spheres r ~ U[1.5, 2.5] mm in a 0.4 m box with a rotating
-    blade (prescribed, omega_z = 3) and a 1 kg dynamic plate
-    (inertia 1e-3 I) resting on the bed; wall/triangle friction 0.4."""
-    pitch = 2.0 * rmin + 0.3e-3
+    blade (prescribed, omega_z = 3) buried in the bed and a 1 kg dynamic
+    plate (inertia 1e-3 I) resting on it; wall/triangle friction 0.4.
+
+    The bed is the settled state of the dropped spheres: vertical columns
+    in force balance (``column_bed``) on the floor, and on the blade's top
+    face where a column stands over the blade."""
+    rng = np.random.default_rng(seed)
+    g = 9.81
+    pitch, jitter = 2.0 * rmax + 0.3e-3, 0.1e-3
+    cap = 0.5 * pitch - jitter - 1e-6
     lo = np.array([-box / 2, -box / 2, 0.0])
     hi = np.array([box / 2, box / 2, box])
-    per = int((box - 2 * rmax) // pitch)
-    span = (per - 1) * pitch
-    origin = np.array([-span / 2, -span / 2, rmax + 0.3e-3])
+    edge = rmax + 0.3e-3
+    xy = column_grid(lo[:2] + edge, hi[:2] - edge, pitch, jitter, rng)
     blade_half = (0.12, 0.006, 0.05)
     blade_center = np.array([0.0, 0.0, 0.06])
     blade_v, blade_f = box_mesh(blade_half, (32, 2, 13))
+    blade_top = blade_center[2] + blade_half[2]
+    on_blade = (np.abs(xy[:, 0]) < blade_half[0]) & (np.abs(xy[:, 1]) < blade_half[1])
+    near_blade = (np.abs(xy[:, 0]) < blade_half[0] + rmax + 0.5e-3) & \
+                 (np.abs(xy[:, 1]) < blade_half[1] + rmax + 0.5e-3)
+    xy = xy[on_blade | ~near_blade]
+    on_blade = (np.abs(xy[:, 0]) < blade_half[0]) & (np.abs(xy[:, 1]) < blade_half[1])
 
-    def in_blade(p):
-        d = np.abs(p - blade_center)
-        return (d[:, 0] < blade_half[0] + rmax + 0.5e-3) & (d[:, 1] < blade_half[1] + rmax + 0.5e-3) & \
-               (d[:, 2] < blade_half[2] + rmax + 0.5e-3)
+    def base_z(p, r):
+        return np.where(on_blade, blade_top + r, r)
 
-    pos, rad, _ = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed, inside=in_blade)
+    pos, rad, _ = column_bed(n, xy, base_z, lambda rg, k: rg.uniform(rmin, rmax, size=k), rng, cap, g, 1e5, 1e5)
     plate_half = (0.05, 0.05, 0.002)
     plate_xy = np.array([0.08, 0.08])
     under = (np.abs(pos[:, 0] - plate_xy[0]) < plate_half[0]) & (np.abs(pos[:, 1] - plate_xy[1]) < plate_half[1])
@@ -287,39 +355,58 @@ def mbd_blade_plate(n=200000, seed=1001, rmin=1.5e-3, rmax=2.5e-3, box=0.4, dt=5
               dict(vertices=plate_v, faces=plate_f, mass=1.0, center=plate_center,
                    inertia=[1e-3, 0, 0, 0, 1e-3, 0, 0, 0, 1e-3], state=0)]
     _attach(kw, bodies)
-    return Scene(**kw, pp=pp, pt=pt, pw=pt, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
+    return Scene(**kw, pp=pp, pt=pt, pw=pt, dt=dt, gravity=(0.0, 0.0, -g), gravity_enabled=1, wall_origin=wo,
                  wall_normal=wn, name=name), [(blade_v, blade_f), (plate_v, plate_f)]
 
 
 def drum(n=2000000, seed=1002, radius=0.3, length=0.5, omega=2.0, dt=2e-6, name="c2_drum", ntheta=160, nx=50,
-         nrings=6):
+         nrings=6, pitch=3.1e-3):
     """Config 2: lognormal radii (median 1 mm, sigma 0.25, clipped to
     [0.5, 2] mm) in a rotating closed cylinder (axis x, inward normals,
-    prescribed omega_x), friction 0.5, restitution 0.3, kN 1e5."""
+    prescribed omega_x), friction 0.5, restitution 0.3, kN 1e5.
 
-    def radius_fn(rng, k):
-        return np.clip(np.exp(np.log(1e-3) + 0.25 * rng.standard_normal(k)), 0.5e-3, 2.0e-3)
+    The bed is settled and turning with the drum: vertical columns in force
+    balance (``column_bed``) standing on the cylinder's facets, every
+    sphere moving with the drum's rigid rotation (v = omega x p, spin =
+    omega), so the wall does not slip under the bed at the start.  The
+    column pitch caps the radii at 1.5 mm (about 5% of the lognormal draws
+    lie above it)."""
+    rng = np.random.default_rng(seed)
+    g = 9.81
 
-    rmax = 2.0e-3
-    pitch = 2.15e-3
-    inner = radius - rmax - 1e-3
-    ny = int(2 * inner / pitch)
-    nxl = int((length - 2 * rmax - 2e-3) / pitch)
+    def radius_fn(rg, k):
+        return np.clip(np.exp(np.log(1e-3) + 0.25 * rg.standard_normal(k)), 0.5e-3, 2.0e-3)
 
-    def outside(p):
-        return (p[:, 1] ** 2 + p[:, 2] ** 2) > inner ** 2
+    jitter = 0.05e-3
+    cap = 0.5 * pitch - jitter - 1e-6
+    half_len = length / 2 - cap - 0.5e-3
+    inner = radius * np.cos(np.pi / ntheta)          # facet plane distance from the axis
+    reach = np.sqrt((inner - cap) ** 2 - (0.5 * inner) ** 2)
+    xy = column_grid(np.array([-half_len, -reach]), np.array([half_len, reach]), pitch, jitter, rng)
+    # facets of the lower half: plane (cos a, sin a) . (y, z) = inner at the
+    # facet's mid angle a (sin a < 0); a sphere of radius r inside has
+    # (cos a, sin a) . (y, z) <= inner - r for every facet, so on the
+    # vertical line at y its lowest centre is the largest of the bounds.
+    mids = (np.arange(ntheta) + 0.5) * (2 * np.pi / ntheta)
+    lower = mids[np.sin(mids) < -0.3]
+    ca, sa = np.cos(lower), np.sin(lower)
 
-    origin = np.array([-(nxl - 1) * pitch / 2, -(ny - 1) * pitch / 2, -inner + 0.2e-3])
-    aspect = (nxl / ny, 1.0, None)
-    pos, rad, _ = bed(n, 0.5e-3, rmax, pitch, origin, aspect=aspect, seed=seed, jitter=0.1e-3, radius_fn=radius_fn,
-                      inside=outside)
-    kw = make_spheres(pos, rad, DENSITY)
+    def base_z(p, r):
+        y = p[:, 1][:, None]
+        zc = ((inner - r[:, None]) - ca[None, :] * y) / sa[None, :]
+        return zc.max(axis=1)
+
+    pos, rad, _ = column_bed(n, xy, base_z, radius_fn, rng, cap, g, 1e5, 1e5)
+    w = np.array([omega, 0.0, 0.0])
+    vel = np.cross(w[None, :], pos)
+    kw = make_spheres(pos, rad, DENSITY, vel=vel)
+    kw["omega"] = np.tile(w, (len(pos), 1))
     v, f = cylinder_mesh(radius, length, ntheta, nx, nrings)
     m = mech(kN=1e5, epsN=0.3, epsS=0.3, mu=0.5)
     bodies = [dict(vertices=v, faces=f, mass=100.0, center=[0, 0, 0], omega=[omega, 0, 0],
                    inertia=[10, 0, 0, 0, 10, 0, 0, 0, 10], state=2)]
     _attach(kw, bodies)
-    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, name=name), [(v, f)]
+    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -g), gravity_enabled=1, name=name), [(v, f)]
 
 
 def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5):
