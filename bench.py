@@ -120,7 +120,7 @@ def launches_per_step(scene):
     if scene.comp_owner is not None:
         k += 1
     if scene.n_bodies:
-        k += 1 + 6 + 5 + 2       # triangle transform, triangle grid, PT compaction + PT, body reduction
+        k += 1 + 6 + 10 + 2      # triangle transform, triangle grid, PT compactions + probe + law, body reduction
     return k
 
 

@@ -514,7 +514,6 @@ __global__ void k_pt_compact(Grid g, Recs r, int* pt_flag, int* pt_pos, int* pt_
 }
 
 // ------------------------------------------------------------------- PT
-constexpr int kTriCache = 24;
 
 // bodyTriangleAreaScale (:380-407); also returns distance along the outward
 // normal.
@@ -550,37 +549,260 @@ __device__ double tri_area_scale(const double* W, V3<double> p, double r, double
     return sc > 1.0e-12 ? sc : 0.0;
 }
 
+// Conservative FP32 rejection of a particle-triangle pair: false only when
+// tri_area_scale is certainly 0 (the particle is not strictly above the
+// triangle's plane within its radius, or the contact disk cannot reach the
+// triangle).  tol bounds the FP32 error of the plane distance; it scales
+// with the coordinates' magnitude.
+struct PtProbe {
+    float px, py, pz, r, tol;
+};
+__device__ __forceinline__ PtProbe pt_probe(V3<double> p, double r)
+{
+    PtProbe q;
+    q.px = (float)p.x; q.py = (float)p.y; q.pz = (float)p.z; q.r = (float)r;
+    q.tol = 1e-6f + 1e-6f * (fabsf(q.px) + fabsf(q.py) + fabsf(q.pz));
+    return q;
+}
+__device__ __forceinline__ bool pt_may_touch(const float4* __restrict__ tf, int tri, const PtProbe& q)
+{
+    const float4 A = __ldg(&tf[2 * (size_t)tri]);
+    const float tol = q.tol + 1e-6f * fabsf(A.w);
+    const float dist = fmaf(A.x, q.px, fmaf(A.y, q.py, A.z * q.pz)) - A.w;
+    if (dist <= -tol || dist >= q.r + tol) return false;
+    const float4 B = __ldg(&tf[2 * (size_t)tri + 1]);
+    const float dlo = fmaxf(dist - tol, 0.f);
+    const float reach = sqrtf(fmaxf(q.r * q.r - dlo * dlo, 0.f)) + B.w + 4.f * tol;
+    const float cx = B.x - (q.px - A.x * dist), cy = B.y - (q.py - A.y * dist), cz = B.z - (q.pz - A.z * dist);
+    return cx * cx + cy * cy + cz * cz <= reach * reach;
+}
+
+// Per PT item: can any triangle of its cell give a nonzero area scale (the
+// condition of a manifold, :1154-1183)?  One warp per item, one lane per
+// triangle, FP32 rejection only: the flag may be set for an item without a
+// manifold (the law kernel then finds none), never cleared for one with.
+__global__ void __launch_bounds__(256) k_pt_probe(Recs r, Tris tris, int* pt_list, int* pt_total, int* cflag)
+{
+    const int total = *pt_total;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < total; item += warps) {
+        const int t = pt_list[item];
+        const D4 p4 = r.pos[t];
+        const PtProbe q = pt_probe(d3(p4), p4.w);
+        const int lin = r.cell[t].w;
+        const int tb = tris.tcell_start[lin];
+        const int te = min(tris.tcell_start[lin + 1], tris.capacity);
+        bool hit = false;
+        for (int e0 = tb; e0 < te && !hit; e0 += 32) {
+            const int e = e0 + lane;
+            hit = __any_sync(0xffffffffu, e < te && pt_may_touch(tris.tf, tris.ttri[e], q));
+        }
+        if (lane == 0) cflag[item] = hit ? 1 : 0;
+    }
+}
+
+// Contact items in PT-item order; pt_index maps a component to its contact
+// item (-1 when it touches no triangle).
+__global__ void k_pt_compact_contacts(Recs r, int* pt_list, int* pt_total, int* cflag, int* cpos, int* clist,
+                                      int* pt_index, int* ctotal)
+{
+    const int total = *pt_total;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *ctotal = cpos[total];
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
+        const int ci = r.meta[pt_list[item]].x;
+        if (cflag[item]) {
+            clist[cpos[item]] = item;
+            pt_index[ci] = cpos[item];
+        } else {
+            pt_index[ci] = -1;
+        }
+    }
+}
+
+// ---------------------------------------------------------- PT laws
+// The particle-side inputs of one contact item and the body-side inputs of
+// one body, and the three pieces of the reference's body contact that both
+// PT kernels below share.
+struct PtItem {
+    V3<double> p, ev, mv, ew, mw, off;
+    double rad, mass;
+};
+struct PtBody {
+    V3<double> center, wb, bv;
+    const double* bq;
+};
+
+__device__ __forceinline__ PtItem pt_item(const Comps& c, const Owners& o, const Recs& r, int t, int ci, int w,
+                                          double dt_eff)
+{
+    PtItem it;
+    const D4 p4 = r.pos[t];
+    it.p = d3(p4);
+    it.rad = p4.w;
+    it.mass = o.mass[w];
+    // FP64 velocities straight from the state (the mixed form keeps FP32
+    // rows only for the particle-particle law).
+    const bool mid = dt_eff > 0.0 && o.status[w] != -1;
+    it.ev = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
+    it.mv = mid ? mk(c.vhx[ci], c.vhy[ci], c.vhz[ci]) : it.ev;
+    const double oqw = o.qw[w], oqx = o.qx[w], oqy = o.qy[w], oqz = o.qz[w];
+    it.ew = rot_iv(oqw, oqx, oqy, oqz, mk(o.wx[w], o.wy[w], o.wz[w]));
+    it.mw = mid ? rot_iv(oqw, oqx, oqy, oqz, mk(o.whx[w], o.why[w], o.whz[w])) : it.ew;
+    it.off = r.off ? d3(r.off[t]) : mk(0.0, 0.0, 0.0);
+    return it;
+}
+
+__device__ __forceinline__ PtBody pt_body(const Bodies& bodies, int b)
+{
+    PtBody bd;
+    bd.center = mk(bodies.c[3 * b], bodies.c[3 * b + 1], bodies.c[3 * b + 2]);
+    bd.bq = bodies.q + 4 * b;
+    bd.wb = rot_iv(bd.bq[0], bd.bq[1], bd.bq[2], bd.bq[3], mk(bodies.w[3 * b], bodies.w[3 * b + 1], bodies.w[3 * b + 2]));
+    bd.bv = mk(bodies.v[3 * b], bodies.v[3 * b + 1], bodies.v[3 * b + 2]);
+    return bd;
+}
+
+// advanceBodyManifoldHistory (:855-949): the manifold (normal mn, centre mc,
+// distance md) updates the history h in place.
+template <typename T>
+__device__ void pt_manifold_history(const MatC& m, const PtItem& it, const PtBody& bd, V3<double> mn, V3<double> mc,
+                                    double md, double dt_eff, T* h, bool& slide, bool& twist)
+{
+    const V3<double> arm = mc - bd.center;
+    const V3<double> bvel = bd.bv + cross(bd.wb, arm);
+    const V3<T> erv = cvt<T>(bvel - it.ev), mrv = cvt<T>(bvel - it.mv);
+    const V3<T> n = cvt<T>(mn);
+    const LawC<T> c = law_constants<T>(m, T(it.mass), T(it.rad));
+    const T depth = T(it.rad - md);
+    V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(erv, n));
+    fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
+    V3<T> tv = mrv - n * dot(mrv, n);
+    tv = tv + cross(n, cvt<T>(it.mw)) * T(md);
+    V3<T> st;
+    limited_rates<T>(tv, tv, c.kS, c.cS, T(dt_eff), transport_tangent(hload(h, 1), n), T(m.mu) * norm(fn), st, slide);
+    hstore(h, 1, st);
+    const V3<T> rw = cvt<T>(bd.wb - it.mw);
+    const V3<T> twr = n * dot(rw, n);
+    const V3<T> rlr = (rw - twr) + cross(n, tv) * (T(0.5) / fmax(T(md), T(1.0e-14)));
+    const T ms = T(m.beta) * T(it.rad) * norm(fn);
+    limited_rates<T>(twr, twr, c.kT, c.cT, T(dt_eff), transport_axial(hload(h, 2), n), T(m.mu) * T(m.muT) * ms, st,
+                     twist);
+    hstore(h, 2, st);
+    bool dummy;
+    limited_rates<T>(rlr, rlr, c.kR, c.cR, T(dt_eff), transport_tangent(hload(h, 0), n), T(m.muR) * ms, st, dummy);
+    hstore(h, 0, st);
+}
+
+// bodyContact (:708-853) for one triangle with read-only history: the
+// particle load pf/ptq, the body-side force rf and torque bt, and the six
+// body-side terms for the optional detail output.
+struct PtTri {
+    V3<double> pf, ptq, rf, bt, v[6];
+};
+template <typename T>
+__device__ void pt_triangle_load(const MatC& m, const LawC<T>& c, const PtItem& it, const PtBody& bd, const double* W,
+                                 double as, double dist, V3<T> hroll, V3<T> htan, V3<T> htw, PtTri& o)
+{
+    const double depthd = it.rad - dist;
+    const V3<double> nout = mk(W[12], W[13], W[14]);
+    const V3<double> ce = it.p - nout * dist;
+    const V3<double> arm = ce - bd.center;
+    const V3<double> bvel = bd.bv + cross(bd.wb, arm);
+    const V3<T> n = cvt<T>(nout * -1.0);
+    const V3<T> rv = cvt<T>(bvel - it.ev);
+    const V3<T> wp = cvt<T>(it.ew);
+    const T depth = T(depthd), distT = T(dist);
+    V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(rv, n));
+    fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
+    V3<T> tv = rv - n * dot(rv, n);
+    tv = tv + cross(n, wp) * distT;
+    V3<T> st;
+    bool y;
+    const V3<T> fr = limited_rates<T>(tv, tv, c.kS, c.cS, T(0), transport_tangent(htan, n), T(m.mu) * norm(fn), st, y);
+    const V3<T> rw = cvt<T>(bd.wb) - wp;
+    const V3<T> twr = n * dot(rw, n);
+    const V3<T> rlr = (rw - twr) + cross(n, tv) * (T(0.5) / fmax(distT, T(1.0e-14)));
+    const T ms = T(m.beta) * T(it.rad) * norm(fn);
+    const V3<T> tw = limited_rates<T>(twr, twr, c.kT, c.cT, T(0), transport_axial(htw, n), T(m.mu) * T(m.muT) * ms,
+                                      st, y);
+    const V3<T> rl = limited_rates<T>(rlr, rlr, c.kR, c.cR, T(0), transport_tangent(hroll, n), T(m.muR) * ms, st, y);
+    const V3<double> fnd = cvt<double>(fn), frd = cvt<double>(fr);
+    o.pf = (fnd + frd) * as;
+    const V3<double> nd = cvt<double>(n);
+    const V3<double> cm = cvt<double>(tw) + cvt<double>(rl);
+    const V3<double> cpl = (cm + cross(nd, frd) * dist) * as;
+    o.ptq = cpl + cross(it.off, o.pf);
+    const V3<double> bnf = fnd * (-as), bfr = frd * (-as);
+    const V3<double> bnt = cross(arm, fnd) * (-as), bft = cross(arm, frd) * (-as);
+    const V3<double> btw = cvt<double>(tw) * (-as), brl = cvt<double>(rl) * (-as);
+    o.bt = (bnt + bft) + (btw + brl);
+    o.rf = mk(bnf.x + bfr.x, bnf.y + bfr.y, bnf.z + bfr.z);
+    o.v[0] = bnf; o.v[1] = bfr; o.v[2] = bnt; o.v[3] = bft; o.v[4] = btw; o.v[5] = brl;
+}
+
+// observeBodyMicrostateKernel (:1226-1356) for one manifold, fused; th and
+// twh are the updated tangent and twist history.
+__device__ void pt_microstate(const MatC& m, const PtItem& it, const PtBody& bd, V3<double> mn, V3<double> mc,
+                              double md, double tot, V3<double> th, V3<double> twh, double* mcr)
+{
+    const double rad = it.rad;
+    const V3<double> arm = mc - bd.center;
+    const V3<double> bvel = bd.bv + cross(bd.wb, arm);
+    const V3<double> rv = bvel - it.ev;
+    const double cN = -2.0 * m.logN * sqrt(m.kN * it.mass / m.denN);
+    const double brs = m.beta * rad * m.beta * rad;
+    const double depth = rad - md;
+    V3<double> fn = mn * (-m.kN * depth) + mn * (cN * dot(rv, mn));
+    fn = fn + mn * (m.coh * 4.0 * brs);
+    const double fnn = norm(fn);
+    const double ms = m.beta * rad * fnn;
+    const double tl = m.mu * fnn;
+    const double twl = m.mu * m.muT * ms;
+    const V3<double> az = rot_iv(bd.bq[0], bd.bq[1], bd.bq[2], bd.bq[3], mk(0.0, 0.0, 1.0));
+    const V3<double> radial = arm - az * dot(arm, az);
+    const double tu = tl > 1.0e-30 ? fmin(1.0, norm(th) / tl) : 0.0;
+    const double twu = twl > 1.0e-30 ? fmin(1.0, norm(twh) / twl) : 0.0;
+    const V3<double> btw = twh * (-tot), bnl = fn * (-tot), bth = th * (-tot);
+    const V3<double> btt = cross(arm, bth);
+    mcr[0] = fnn * tot; mcr[1] = fnn * rad * tot; mcr[2] = fnn * norm(radial) * tot;
+    mcr[3] = btw.x; mcr[4] = btw.y; mcr[5] = btw.z;
+    mcr[6] = norm(twh) * tot; mcr[7] = twl * tot; mcr[8] = norm(th) * tot; mcr[9] = tl * tot;
+    mcr[10] = twu * tot; mcr[11] = tu * tot; mcr[12] = tot;
+    mcr[13] = bnl.x; mcr[14] = bnl.y; mcr[15] = bnl.z;
+    mcr[16] = bth.x; mcr[17] = bth.y; mcr[18] = bth.z;
+    mcr[19] = btt.x; mcr[20] = btt.y; mcr[21] = btt.z;
+}
+
+// Contact items at or below Counters::pt_warp_items run one warp per item
+// (latency bound: few items, many triangles each); above it one thread per
+// item (FP64 throughput bound).  Both kernels are launched; the count on the
+// device picks the one that works.
+
+// ---------------------------------------------------- PT, thread per item
+constexpr int kTriCache = 24;
+
 template <typename TC, typename T>
-__global__ void __launch_bounds__(128) k_pt(Comps c, Owners o, Recs r, const SceneC* __restrict__ sc, Tris tris,
-                                            Bodies bodies, Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff)
+__global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, const SceneC* __restrict__ sc, Tris tris,
+                                                   Bodies bodies, Hist<T> hb, Contacts<TC> ct, Counters k,
+                                                   double dt_eff)
 {
     const int step = *k.step;
-    const int total = *ct.pt_total_ptr;
+    const int total = *ct.pt_ctotal_ptr;
+    if (total <= k.pt_warp_items) return;
     int bover = 0, bhigh = 0;
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
-        const int t = ct.pt_list[item];
+        const int t = ct.pt_list[ct.pt_clist[item]];
         const int4 meta = r.meta[t];
-        const int ci = meta.x, s = meta.w;
-        const SceneC S = sc[s];
-        const D4 p4 = r.pos[t];
-        const V3<double> p = d3(p4);
-        const double rad = p4.w;
-        // FP64 velocities straight from the state (the mixed form keeps FP32
-        // rows only for the particle-particle law).
-        const int w = meta.y;
-        const double mass = o.mass[w];
-        const bool mid = dt_eff > 0.0 && o.status[w] != -1;
-        const V3<double> ev = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
-        const V3<double> mv = mid ? mk(c.vhx[ci], c.vhy[ci], c.vhz[ci]) : ev;
-        const double oqw = o.qw[w], oqx = o.qx[w], oqy = o.qy[w], oqz = o.qz[w];
-        const V3<double> ew = rot_iv(oqw, oqx, oqy, oqz, mk(o.wx[w], o.wy[w], o.wz[w]));
-        const V3<double> mw = mid ? rot_iv(oqw, oqx, oqy, oqz, mk(o.whx[w], o.why[w], o.whz[w])) : ew;
-        const V3<double> off = r.off ? d3(r.off[t]) : mk(0.0, 0.0, 0.0);
+        const int ci = meta.x;
+        const SceneC& S = sc[meta.w];
+        const PtItem it = pt_item(c, o, r, t, ci, meta.y, dt_eff);
         const int lin = r.cell[t].w;
         const int tb = tris.tcell_start[lin];
         const int te = min(tris.tcell_start[lin + 1], tris.capacity);
         V3<double> bF = mk(0.0, 0.0, 0.0), bT = mk(0.0, 0.0, 0.0);
         int bhw = hb.hw[ci];
+        const PtProbe pq = pt_probe(it.p, it.rad);
         for (int j = 0; j < S.body_count; ++j) {
             const int b = S.body_begin + j;
             double* rec = ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord;
@@ -596,13 +818,13 @@ __global__ void __launch_bounds__(128) k_pt(Comps c, Owners o, Recs r, const Sce
             V3<double> wn = mk(0.0, 0.0, 0.0), wc = mk(0.0, 0.0, 0.0);
             for (int e = tb; e < te; ++e) {
                 const int tri = tris.ttri[e];
-                if (tris.body[tri] != b) continue;
+                if (tris.body[tri] != b || !pt_may_touch(tris.tf, tri, pq)) continue;
                 const double* W = tris.world + 16 * (size_t)tri;
                 double dist;
-                const double as = tri_area_scale<T>(W, p, rad, dist);
+                const double as = tri_area_scale<T>(W, it.p, it.rad, dist);
                 if (as <= 0.0) continue;
                 const V3<double> out = mk(W[12], W[13], W[14]);
-                const V3<double> ce = p - out * dist;
+                const V3<double> ce = it.p - out * dist;
                 tot += as;
                 wn = wn + out * (-as);
                 wc = wc + ce * as;
@@ -617,46 +839,18 @@ __global__ void __launch_bounds__(128) k_pt(Comps c, Owners o, Recs r, const Sce
             const int slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh);
             if (slot < 0) { ++bover; continue; }
             T* hv = hb.val + ((size_t)ci * kBSlots + slot) * kHV;
-            const V3<double> center = mk(bodies.c[3 * b], bodies.c[3 * b + 1], bodies.c[3 * b + 2]);
-            const double* bq = bodies.q + 4 * b;
-            const V3<double> wb = rot_iv(bq[0], bq[1], bq[2], bq[3], mk(bodies.w[3 * b], bodies.w[3 * b + 1], bodies.w[3 * b + 2]));
-            const V3<double> bv = mk(bodies.v[3 * b], bodies.v[3 * b + 1], bodies.v[3 * b + 2]);
+            T h[9];
+            hv_load(hv, h);
+            const PtBody bd = pt_body(bodies, b);
             const MatC& m = S.pt;
-            // advanceBodyManifoldHistory (:855-949)
             bool slide = false, twist = false;
-            {
-                const V3<double> arm = mc - center;
-                const V3<double> bvel = bv + cross(wb, arm);
-                const V3<T> erv = cvt<T>(bvel - ev), mrv = cvt<T>(bvel - mv);
-                const V3<T> n = cvt<T>(mn);
-                const LawC<T> c = law_constants<T>(m, T(mass), T(rad));
-                const T depth = T(rad - md);
-                V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(erv, n));
-                fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
-                V3<T> tv = mrv - n * dot(mrv, n);
-                tv = tv + cross(n, cvt<T>(mw)) * T(md);
-                V3<T> st;
-                limited_rates<T>(tv, tv, c.kS, c.cS, T(dt_eff), transport_tangent(hload(hv, 1), n), T(m.mu) * norm(fn),
-                                 st, slide);
-                hstore(hv, 1, st);
-                const V3<T> rw = cvt<T>(wb - mw);
-                const V3<T> twr = n * dot(rw, n);
-                const V3<T> rlr = (rw - twr) + cross(n, tv) * (T(0.5) / fmax(T(md), T(1.0e-14)));
-                const T ms = T(m.beta) * T(rad) * norm(fn);
-                limited_rates<T>(twr, twr, c.kT, c.cT, T(dt_eff), transport_axial(hload(hv, 2), n),
-                                 T(m.mu) * T(m.muT) * ms, st, twist);
-                hstore(hv, 2, st);
-                bool dummy;
-                limited_rates<T>(rlr, rlr, c.kR, c.cR, T(dt_eff), transport_tangent(hload(hv, 0), n), T(m.muR) * ms, st,
-                                 dummy);
-                hstore(hv, 0, st);
-            }
+            pt_manifold_history<T>(m, it, bd, mn, mc, md, dt_eff, h, slide, twist);
+            hv_store(hv, h);
             rec[9] = (double)(1 | (slide ? 2 : 0) | (twist ? 4 : 0));
-            // per-triangle loads with read-only history (bodyContact, :708-853)
             double maxdepth = 0.0;
             int tcount = 0;
-            const LawC<T> c = law_constants<T>(m, T(mass), T(rad));
-            const V3<T> hroll = hload(hv, 0), htan = hload(hv, 1), htw = hload(hv, 2);
+            const LawC<T> lc = law_constants<T>(m, T(it.mass), T(it.rad));
+            const V3<T> hroll = hload(h, 0), htan = hload(h, 1), htw = hload(h, 2);
             const int nloop = spill ? (te - tb) : ncache;
             for (int qi = 0; qi < nloop; ++qi) {
                 int tri;
@@ -666,103 +860,209 @@ __global__ void __launch_bounds__(128) k_pt(Comps c, Owners o, Recs r, const Sce
                     tri = ctri[qi];
                     as = cas[qi];
                     W = tris.world + 16 * (size_t)tri;
-                    dist = dot(mk(W[12], W[13], W[14]), p - mk(W[3], W[4], W[5]));
+                    dist = dot(mk(W[12], W[13], W[14]), it.p - mk(W[3], W[4], W[5]));
                 } else {
                     tri = tris.ttri[tb + qi];
-                    if (tris.body[tri] != b) continue;
+                    if (tris.body[tri] != b || !pt_may_touch(tris.tf, tri, pq)) continue;
                     W = tris.world + 16 * (size_t)tri;
-                    as = tri_area_scale<T>(W, p, rad, dist);
+                    as = tri_area_scale<T>(W, it.p, it.rad, dist);
                     if (as <= 0.0) continue;
                 }
-                const double depthd = rad - dist;
+                const double depthd = it.rad - dist;
                 if (dist <= 0.0 || depthd <= 0.0) continue;
-                const V3<double> nout = mk(W[12], W[13], W[14]);
-                const V3<double> ce = p - nout * dist;
-                const V3<double> arm = ce - center;
-                const V3<double> bvel = bv + cross(wb, arm);
-                const V3<T> n = cvt<T>(nout * -1.0);
-                const V3<T> rv = cvt<T>(bvel - ev);
-                const V3<T> wp = cvt<T>(ew);
-                const T depth = T(depthd), distT = T(dist);
-                V3<T> fn = n * (-c.kN * depth) + n * (c.cN * dot(rv, n));
-                fn = fn + n * (T(m.coh) * T(4.0) * c.brs);
-                V3<T> tv = rv - n * dot(rv, n);
-                tv = tv + cross(n, wp) * distT;
-                V3<T> st;
-                bool y;
-                const V3<T> fr = limited_rates<T>(tv, tv, c.kS, c.cS, T(0), transport_tangent(htan, n), T(m.mu) * norm(fn),
-                                                  st, y);
-                const V3<T> rw = cvt<T>(wb) - wp;
-                const V3<T> twr = n * dot(rw, n);
-                const V3<T> rlr = (rw - twr) + cross(n, tv) * (T(0.5) / fmax(distT, T(1.0e-14)));
-                const T ms = T(m.beta) * T(rad) * norm(fn);
-                const V3<T> tw = limited_rates<T>(twr, twr, c.kT, c.cT, T(0), transport_axial(htw, n),
-                                                  T(m.mu) * T(m.muT) * ms, st, y);
-                const V3<T> rl = limited_rates<T>(rlr, rlr, c.kR, c.cR, T(0), transport_tangent(hroll, n), T(m.muR) * ms,
-                                                  st, y);
-                const V3<double> fnd = cvt<double>(fn), frd = cvt<double>(fr);
-                const V3<double> pf = (fnd + frd) * as;
-                const V3<double> nd = cvt<double>(n);
-                const V3<double> cm = cvt<double>(tw) + cvt<double>(rl);
-                const V3<double> cpl = (cm + cross(nd, frd) * dist) * as;
-                const V3<double> ptq = cpl + cross(off, pf);
-                const V3<double> bnf = fnd * (-as), bfr = frd * (-as);
-                const V3<double> bnt = cross(arm, fnd) * (-as), bft = cross(arm, frd) * (-as);
-                const V3<double> btw = cvt<double>(tw) * (-as), brl = cvt<double>(rl) * (-as);
-                const V3<double> bt = (bnt + bft) + (btw + brl);
-                bF = bF + pf;
-                bT = bT + ptq;
-                rec[0] += bnf.x + bfr.x; rec[1] += bnf.y + bfr.y; rec[2] += bnf.z + bfr.z;
-                rec[3] += bt.x; rec[4] += bt.y; rec[5] += bt.z;
-                rec[8] += bnf.z + bfr.z;
+                PtTri pr;
+                pt_triangle_load<T>(m, lc, it, bd, W, as, dist, hroll, htan, htw, pr);
+                bF = bF + pr.pf;
+                bT = bT + pr.ptq;
+                rec[0] += pr.rf.x; rec[1] += pr.rf.y; rec[2] += pr.rf.z;
+                rec[3] += pr.bt.x; rec[4] += pr.bt.y; rec[5] += pr.bt.z;
+                rec[8] += pr.rf.z;
                 ++tcount;
                 maxdepth = fmax(maxdepth, depthd);
                 if (outd) {
-                    outd[0] += pf.x; outd[1] += pf.y; outd[2] += pf.z; outd[3] += ptq.x; outd[4] += ptq.y; outd[5] += ptq.z;
-                    const V3<double> vals[6] = {bnf, bfr, bnt, bft, btw, brl};
+                    outd[0] += pr.pf.x; outd[1] += pr.pf.y; outd[2] += pr.pf.z;
+                    outd[3] += pr.ptq.x; outd[4] += pr.ptq.y; outd[5] += pr.ptq.z;
                     for (int gq = 0; gq < 6; ++gq) {
-                        outd[6 + 3 * gq] += vals[gq].x; outd[7 + 3 * gq] += vals[gq].y; outd[8 + 3 * gq] += vals[gq].z;
+                        outd[6 + 3 * gq] += pr.v[gq].x; outd[7 + 3 * gq] += pr.v[gq].y; outd[8 + 3 * gq] += pr.v[gq].z;
                     }
                     outd[24] = fmax(outd[24], depthd);
                 }
             }
             rec[6] = (double)tcount;
             rec[7] = maxdepth;
-            // observeBodyMicrostateKernel (:1226-1356), fused
-            {
-                const V3<double> arm = mc - center;
-                const V3<double> bvel = bv + cross(wb, arm);
-                const V3<double> rv = bvel - ev;
-                const double logN = m.logN;
-                const double cN = -2.0 * logN * sqrt(m.kN * mass / m.denN);
-                const double brs = m.beta * rad * m.beta * rad;
-                const double depth = rad - md;
-                V3<double> fn = mn * (-m.kN * depth) + mn * (cN * dot(rv, mn));
-                fn = fn + mn * (m.coh * 4.0 * brs);
-                const double fnn = norm(fn);
-                const double ms = m.beta * rad * fnn;
-                const double tl = m.mu * fnn;
-                const double twl = m.mu * m.muT * ms;
-                const V3<double> th = cvt<double>(hload(hv, 1)), twh = cvt<double>(hload(hv, 2));
-                const V3<double> az = rot_iv(bq[0], bq[1], bq[2], bq[3], mk(0.0, 0.0, 1.0));
-                const V3<double> radial = arm - az * dot(arm, az);
-                const double tu = tl > 1.0e-30 ? fmin(1.0, norm(th) / tl) : 0.0;
-                const double twu = twl > 1.0e-30 ? fmin(1.0, norm(twh) / twl) : 0.0;
-                const V3<double> btw = twh * (-tot), bnl = fn * (-tot), bth = th * (-tot);
-                const V3<double> btt = cross(arm, bth);
-                double* mcr = rec + 10;
-                mcr[0] = fnn * tot; mcr[1] = fnn * rad * tot; mcr[2] = fnn * norm(radial) * tot;
-                mcr[3] = btw.x; mcr[4] = btw.y; mcr[5] = btw.z;
-                mcr[6] = norm(twh) * tot; mcr[7] = twl * tot; mcr[8] = norm(th) * tot; mcr[9] = tl * tot;
-                mcr[10] = twu * tot; mcr[11] = tu * tot; mcr[12] = tot;
-                mcr[13] = bnl.x; mcr[14] = bnl.y; mcr[15] = bnl.z;
-                mcr[16] = bth.x; mcr[17] = bth.y; mcr[18] = bth.z;
-                mcr[19] = btt.x; mcr[20] = btt.y; mcr[21] = btt.z;
-            }
+            pt_microstate(m, it, bd, mn, mc, md, tot, cvt<double>(hload(h, 1)), cvt<double>(hload(h, 2)), rec + 10);
         }
         hb.hw[ci] = bhw;
         double* pr = ct.pt_res + 6 * (size_t)ci;
         pr[0] = bF.x; pr[1] = bF.y; pr[2] = bF.z; pr[3] = bT.x; pr[4] = bT.y; pr[5] = bT.z;
+    }
+    block_add(k.bover, bover);
+    block_max(k.bhigh, bhigh);
+}
+
+// ------------------------------------------------------ PT, warp per item
+// The lanes share the triangles of the item's cell; the per-manifold work
+// (history update, microstate) is computed by every lane alike and written
+// by lane 0.  Sums are taken in triangle order, each term fetched from its
+// lane by shuffles, so every lane holds totals bit-identical to the serial
+// loops of k_pt_thread.
+constexpr int kPtTriCache = 128;  // per-warp cache of (area scale, distance) between the two passes
+
+__device__ __forceinline__ V3<double> shfl3(V3<double> v, int src)
+{
+    return mk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+              __shfl_sync(0xffffffffu, v.z, src));
+}
+
+template <typename TC, typename T>
+__global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, const SceneC* __restrict__ sc, Tris tris,
+                                                 Bodies bodies, Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff)
+{
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ double2 s_ad[4][kPtTriCache];
+    const int step = *k.step;
+    const int total = *ct.pt_ctotal_ptr;
+    if (total > k.pt_warp_items) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    int bover = 0, bhigh = 0;
+    for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < total; item += warps) {
+        const int t = ct.pt_list[ct.pt_clist[item]];
+        const int4 meta = r.meta[t];
+        const int ci = meta.x;
+        const SceneC& S = sc[meta.w];
+        const PtItem it = pt_item(c, o, r, t, ci, meta.y, dt_eff);
+        const int lin = r.cell[t].w;
+        const int tb = tris.tcell_start[lin];
+        const int te = min(tris.tcell_start[lin + 1], tris.capacity);
+        V3<double> bF = mk(0.0, 0.0, 0.0), bT = mk(0.0, 0.0, 0.0);
+        int bhw = hb.hw[ci];
+        const PtProbe pq = pt_probe(it.p, it.rad);
+        for (int j = 0; j < S.body_count; ++j) {
+            const int b = S.body_begin + j;
+            double* rec = ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord;
+            for (int f = lane; f < kPtRecord; f += 32) rec[f] = 0.0;
+            double* outd = ct.pt_out ? ct.pt_out + ((size_t)item * ct.nbs + j) * 25 : nullptr;
+            if (outd) for (int f = lane; f < 25; f += 32) outd[f] = 0.0;
+            __syncwarp();
+            // pass 1: manifold sums over the component's own cell (:1154-1183)
+            double tot = 0.0, wd = 0.0;
+            V3<double> wn = mk(0.0, 0.0, 0.0), wc = mk(0.0, 0.0, 0.0);
+            for (int e0 = tb; e0 < te; e0 += 32) {
+                const int e = e0 + lane;
+                double as = 0.0, dist = 0.0;
+                int tri = 0;
+                if (e < te) {
+                    tri = tris.ttri[e];
+                    if (tris.body[tri] == b && pt_may_touch(tris.tf, tri, pq))
+                        as = tri_area_scale<T>(tris.world + 16 * (size_t)tri, it.p, it.rad, dist);
+                    if (e - tb < kPtTriCache) s_ad[wib][e - tb] = make_double2(as, dist);
+                }
+                unsigned msk = __ballot_sync(FULL, as > 0.0);
+                while (msk) {
+                    const int src = __ffs(msk) - 1;
+                    msk &= msk - 1;
+                    const double a_ = __shfl_sync(FULL, as, src), d_ = __shfl_sync(FULL, dist, src);
+                    const double* W = tris.world + 16 * (size_t)__shfl_sync(FULL, tri, src);
+                    const V3<double> out = mk(W[12], W[13], W[14]);
+                    const V3<double> ce = it.p - out * d_;
+                    tot += a_;
+                    wn = wn + out * (-a_);
+                    wc = wc + ce * a_;
+                    wd += d_ * a_;
+                }
+            }
+            if (tot <= 0.0) continue;
+            const V3<double> mn = normalized(wn);
+            const V3<double> mc = wc * (1.0 / tot);
+            const double md = wd / tot;
+            int slot = 0;
+            if (lane == 0) slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh);
+            slot = __shfl_sync(FULL, slot, 0);
+            bhw = __shfl_sync(FULL, bhw, 0);
+            if (slot < 0) {
+                if (lane == 0) ++bover;
+                continue;
+            }
+            T* hv = hb.val + ((size_t)ci * kBSlots + slot) * kHV;
+            T h[9];
+            hv_load(hv, h);
+            const PtBody bd = pt_body(bodies, b);
+            const MatC& m = S.pt;
+            bool slide = false, twist = false;
+            pt_manifold_history<T>(m, it, bd, mn, mc, md, dt_eff, h, slide, twist);
+            if (lane == 0) hv_store(hv, h);
+            // pass 2: per-triangle loads, the terms summed in triangle order
+            double maxdepth = 0.0;
+            int tcount = 0;
+            V3<double> rF = mk(0.0, 0.0, 0.0), rT = mk(0.0, 0.0, 0.0);
+            double rFz = 0.0;
+            const LawC<T> lc = law_constants<T>(m, T(it.mass), T(it.rad));
+            const V3<T> hroll = hload(h, 0), htan = hload(h, 1), htw = hload(h, 2);
+            for (int e0 = tb; e0 < te; e0 += 32) {
+                const int e = e0 + lane;
+                double as = 0.0, dist = 0.0;
+                int tri = 0;
+                if (e < te) {
+                    tri = tris.ttri[e];
+                    if (e - tb < kPtTriCache) {
+                        const double2 ad = s_ad[wib][e - tb];
+                        as = ad.x;
+                        dist = ad.y;
+                    } else if (tris.body[tri] == b && pt_may_touch(tris.tf, tri, pq)) {
+                        as = tri_area_scale<T>(tris.world + 16 * (size_t)tri, it.p, it.rad, dist);
+                    }
+                }
+                const double depthd = it.rad - dist;
+                const bool on = as > 0.0 && dist > 0.0 && depthd > 0.0;
+                PtTri pr;
+                if (on) pt_triangle_load<T>(m, lc, it, bd, tris.world + 16 * (size_t)tri, as, dist, hroll, htan, htw, pr);
+                unsigned msk = __ballot_sync(FULL, on);
+                while (msk) {
+                    const int src = __ffs(msk) - 1;
+                    msk &= msk - 1;
+                    const V3<double> pf_ = shfl3(pr.pf, src), ptq_ = shfl3(pr.ptq, src);
+                    const V3<double> rf_ = shfl3(pr.rf, src), bt_ = shfl3(pr.bt, src);
+                    const double dd_ = __shfl_sync(FULL, depthd, src);
+                    bF = bF + pf_;
+                    bT = bT + ptq_;
+                    rF = rF + rf_;
+                    rT = rT + bt_;
+                    rFz += rf_.z;
+                    ++tcount;
+                    maxdepth = fmax(maxdepth, dd_);
+                    if (outd) {
+                        // optional per-particle detail, accumulated by lane 0
+                        V3<double> v_[6];
+#pragma unroll
+                        for (int gq = 0; gq < 6; ++gq) v_[gq] = shfl3(pr.v[gq], src);
+                        if (lane == 0) {
+                            outd[0] += pf_.x; outd[1] += pf_.y; outd[2] += pf_.z;
+                            outd[3] += ptq_.x; outd[4] += ptq_.y; outd[5] += ptq_.z;
+#pragma unroll
+                            for (int gq = 0; gq < 6; ++gq) {
+                                outd[6 + 3 * gq] += v_[gq].x; outd[7 + 3 * gq] += v_[gq].y; outd[8 + 3 * gq] += v_[gq].z;
+                            }
+                            outd[24] = fmax(outd[24], dd_);
+                        }
+                    }
+                }
+            }
+            if (lane == 0) {
+                rec[0] = rF.x; rec[1] = rF.y; rec[2] = rF.z;
+                rec[3] = rT.x; rec[4] = rT.y; rec[5] = rT.z;
+                rec[6] = (double)tcount;
+                rec[7] = maxdepth;
+                rec[8] = rFz;
+                rec[9] = (double)(1 | (slide ? 2 : 0) | (twist ? 4 : 0));
+                pt_microstate(m, it, bd, mn, mc, md, tot, cvt<double>(hload(h, 1)), cvt<double>(hload(h, 2)), rec + 10);
+            }
+        }
+        if (lane == 0) {
+            hb.hw[ci] = bhw;
+            double* pr = ct.pt_res + 6 * (size_t)ci;
+            pr[0] = bF.x; pr[1] = bF.y; pr[2] = bF.z; pr[3] = bT.x; pr[4] = bT.y; pr[5] = bT.z;
+        }
     }
     block_add(k.bover, bover);
     block_max(k.bhigh, bhigh);
@@ -885,7 +1185,7 @@ template <typename T>
 __global__ void k_body_partial(Recs r, const SceneC* __restrict__ sc, Bodies bodies, Contacts<T> ct, BodyOut bo)
 {
     const int b = blockIdx.y;
-    const int total = *ct.pt_total_ptr;
+    const int total = *ct.pt_ctotal_ptr;
     const int chunk = (total + bo.groups - 1) / bo.groups;
     const int beg = blockIdx.x * chunk, end = min(total, beg + chunk);
     const int bs = bodies.scene[b];
@@ -893,7 +1193,7 @@ __global__ void k_body_partial(Recs r, const SceneC* __restrict__ sc, Bodies bod
     double acc[kBodyFields];
     for (int f = 0; f < kBodyFields; ++f) acc[f] = 0.0;
     for (int item = beg + threadIdx.x; item < end; item += blockDim.x) {
-        const int t = ct.pt_list[item];
+        const int t = ct.pt_list[ct.pt_clist[item]];
         if (r.meta[t].w != bs) continue;
         accumulate_record(acc, ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord);
     }
@@ -978,7 +1278,12 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
         launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);
         k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list, ct.pt_index,
                                                   ct.pt_total_ptr);
-        k_pt<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
+        k_pt_probe<<<sm_count * 16, 256, 0, s>>>(r, t, ct.pt_list, ct.pt_total_ptr, ct.pt_cflag);
+        launch_scan(ct.pt_cflag, ct.pt_cpos, ct.pt_total_ptr, g.tile_sums, sm_count, s);
+        k_pt_compact_contacts<<<sm_count * 8, 256, 0, s>>>(r, ct.pt_list, ct.pt_total_ptr, ct.pt_cflag, ct.pt_cpos,
+                                                           ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr);
+        k_pt_warp<T, TB><<<sm_count * 8, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
+        k_pt_thread<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
     }
 }
 

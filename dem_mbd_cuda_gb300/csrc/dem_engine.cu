@@ -72,6 +72,9 @@ private:
     size_t bytes_ = 0;
 };
 
+// Contact items up to which the PT law runs one warp per item.
+constexpr int kDefaultPtWarpItems = 3072;
+
 static MatF to_float(const MatC& c)
 {
     return MatF{(float)c.kN, (float)c.kS, (float)c.logN, (float)c.logS, (float)c.denN, (float)c.denS, (float)c.mu,
@@ -381,6 +384,7 @@ public:
             T_.local = upd(tloc, "tri local");
             T_.world = arena_.alloc<double>(16 * (size_t)nt_, "tri world");
             T_.aabb = arena_.alloc<double>(6 * (size_t)nt_, "tri aabb");
+            T_.tf = arena_.alloc<float4>(2 * (size_t)nt_, "tri fp32 planes");
             // rotation-invariant bound of the cells a padded triangle box covers
             long long tcap = 0;
             for (int t = 0; t < nt_; ++t) {
@@ -413,6 +417,8 @@ public:
         check(cudaMemsetAsync(cnt, 0, sizeof(int) * 16, s), "clear counters");
         K_.pcontacts = cnt; K_.pover = cnt + 1; K_.bover = cnt + 2; K_.phigh = cnt + 3; K_.bhigh = cnt + 4;
         K_.tgover = cnt + 5; K_.ct_total = cnt + 6; K_.pt_total = cnt + 7; K_.step = cnt + 8;
+        K_.pt_ctotal = cnt + 9;
+        K_.pt_warp_items = kDefaultPtWarpItems;
 
         // ---- scene constants
         scenes_h_ = sc;
@@ -490,6 +496,10 @@ public:
         if (nb_ > 0 && nt_ > 0) {
             ct.pt_pos = arena_.alloc<int>(nc_ + 2, "pt pos");
             ct.pt_list = arena_.alloc<int>(nc_, "pt list");
+            ct.pt_cflag = arena_.alloc<int>(nc_ + 1, "pt contact flag");
+            ct.pt_cpos = arena_.alloc<int>(nc_ + 2, "pt contact pos");
+            ct.pt_clist = arena_.alloc<int>(nc_, "pt contact list");
+            ct.pt_ctotal_ptr = K_.pt_ctotal;
             ct.pt_res = arena_.alloc<double>((size_t)nc_ * 6, "pt results");
             ct.pt_body = arena_.alloc<double>((size_t)nc_ * ct.nbs * kPtRecord, "pt body records");
             if (keep_bp_ || keep_bd_) ct.pt_out = arena_.alloc<double>((size_t)nc_ * ct.nbs * 25, "pt outputs");
@@ -824,6 +834,16 @@ public:
         check(cudaStreamEndCapture(stream_, &g), "end capture");
         check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
         cudaGraphDestroy(g);
+    }
+    // Crossover of the two PT kernels (contact items); captured graphs hold
+    // the old value, so they are rebuilt on the next graph launch.
+    void set_pt_warp_items(int n)
+    {
+        need_init();
+        check(cudaStreamSynchronize(stream_), "sync");
+        K_.pt_warp_items = n;
+        for (cudaGraphExec_t* g : {&graph_fa_, &graph_f_, &graph_mbd_fa_, &graph_mbd_f_})
+            if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
     }
     void ensure_graphs(bool mbd)
     {
@@ -1376,6 +1396,11 @@ int dem_x_time_steps(dem_engine* e, int steps, float* ms)
 int dem_x_download_half(dem_engine* e, double* vh, double* wh, double* hdq, double* acc, double* aacc)
 {
     return guarded([&] { NEED(e); e->e.download_half(vh, wh, hdq, acc, aacc); });
+}
+
+int dem_x_set_pt_warp_items(dem_engine* e, int n)
+{
+    return guarded([&] { NEED(e); e->e.set_pt_warp_items(n); });
 }
 
 int dem_x_synchronize(dem_engine* e)

@@ -324,6 +324,11 @@ __global__ void k_tri_transform(Tris t, Bodies b)
             r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
         }
         W[15] = sqrt(r2) * (1.0 + 1e-12) + 1e-15;
+        if (t.tf) {
+            const double na = nn.x * W[3] + nn.y * W[4] + nn.z * W[5];
+            t.tf[2 * (size_t)i] = make_float4((float)nn.x, (float)nn.y, (float)nn.z, (float)na);
+            t.tf[2 * (size_t)i + 1] = make_float4((float)gx, (float)gy, (float)gz, (float)W[15]);
+        }
     }
     double* A = t.aabb + 6 * (size_t)i;
     double mnx = W[0], mny = W[1], mnz = W[2], mxx = W[0], mxy = W[1], mxz = W[2];

@@ -120,6 +120,7 @@ struct Tris {
     double* local;  // [t][15]
     double* world;  // [t][16] v1..v4, normal, pad
     double* aabb;   // [t][6]
+    float4* tf;     // [t][2] FP32 copies for prefilters: (normal, normal . v2), (centroid of v2..v4, circumradius)
     int* scene;     // per triangle
     int capacity;   // triangle grid entry capacity
     int *tcell_count, *tcell_cursor, *tcell_start, *ttri, *ttri_tmp, *tlin_tmp;
@@ -140,7 +141,9 @@ struct Counters {
     int* tgover;        // per build
     int* ct_total;      // contacts this step
     int* pt_total;      // PT components this step
+    int* pt_ctotal;     // PT components touching a triangle this step
     int* step;          // contact step index
+    int pt_warp_items;  // PT: warp-per-item kernel up to this many contact items
 };
 
 template <typename T> struct Contacts {
@@ -150,14 +153,18 @@ template <typename T> struct Contacts {
     int capacity;
     double* wres;   // [c][6] wall force/torque per component (valid where wflag)
     unsigned char* wflag;  // per component: nonzero wall force/torque this step
-    int* pt_index;  // per component: PT item or -1
+    int* pt_index;  // per component: contact item or -1
     int* pt_flag;   // per sorted position
     int* pt_pos;    // scan of pt_flag
     int* pt_list;   // item -> sorted position
     int* pt_total_ptr;  // [1] PT items this step
-    double* pt_res; // [k][6]
-    double* pt_body;    // [k][nbs][kPtRecord]
-    double* pt_out;     // [k][nbs][25] optional output detail
+    int* pt_cflag;      // per PT item: touches a triangle (some body has a manifold)
+    int* pt_cpos;       // scan of pt_cflag
+    int* pt_clist;      // contact item k -> PT item
+    int* pt_ctotal_ptr; // [1] contact items this step
+    double* pt_res; // [component][6] particle-side PT load (valid where pt_index >= 0)
+    double* pt_body;    // [contact item][nbs][kPtRecord]
+    double* pt_out;     // [contact item][nbs][25] optional output detail
     int nbs;            // max bodies per scene
 };
 

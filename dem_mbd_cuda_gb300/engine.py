@@ -57,6 +57,7 @@ _SIGS = {
     "dem_x_time_steps": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "dem_x_download_half": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),
     "dem_x_synchronize": ([C.c_void_p], C.c_int),
+    "dem_x_set_pt_warp_items": ([C.c_void_p, C.c_int], C.c_int),
 }
 
 
@@ -258,6 +259,13 @@ class CudaDemSolver:
         cnt = C.c_int()
         self._check(self.lib.dem_last_phase_times(self.h, ms, 16, C.byref(cnt)))
         return [ms[k] for k in range(cnt.value)]
+
+    def set_pt_warp_items(self, n):
+        """Crossover of the two particle-triangle kernels: up to n contact
+        items one warp per item, above one thread per item (tests force
+        either path with 1 << 30 or -1)."""
+        self._check(self.lib.dem_x_set_pt_warp_items(self.h, int(n)))
+        return self
 
     def time_steps(self, steps):
         ms = C.c_float()
