@@ -108,10 +108,49 @@ def hbm_peak():
 
 
 def algorithmic_bytes(n, nc, contacts, wall_contacts, body_manifolds, triangles, h):
-    """Per-step algorithmic bytes (the survey's B_step):
+    """Per-step algorithmic bytes of the whole pipeline:
     N*412 + Nc*24 + (C_pp + C_pw + C_pb)*2*(8 + 9h) + T*288, with C_pp the
     unordered particle contacts (= contact sides / 2)."""
     return n * 412 + nc * 24 + (contacts / 2 + wall_contacts + body_manifolds) * 2 * (8 + 9 * h) + triangles * 288
+
+
+# Algorithmic DRAM bytes of one launch of the single-kernel phases, from the
+# data each must move once (records, cell rows, history, contact list), for
+# n particles with s contact sides; hv = bytes of one history slot.
+KERNEL_BYTES = {
+    # own record (relf, pos, meta, cell) 80 + 9 cell-row boundaries 144 +
+    # counters 12 + history keys 8/slot; contact list entry 16 + key 8 per side
+    "sweep": ("k_sweep", lambda n, s, hv: n * 236 + s * 24),
+    # per side: list entry 16, history slot read + write, result row 24;
+    # per particle: its FP64 position 32 and four FP32 rows 64
+    "pp_law": ("k_pp_law", lambda n, s, hv: s * (16 + 2 * hv + 24) + n * 96),
+    # per owner: count, flags, field force, inverse mass and inertia,
+    # quaternion, omega, accelerations; result rows 24 per side
+    "owner_sum": ("k_owner_sum", lambda n, s, hv: n * 196 + s * 24),
+    # per component: position and radius 32, three slot arrays' high-water
+    # marks 12, key and age scan 12/slot, wall flag and result 8
+    "expire+walls": ("k_expire_walls", lambda n, s, hv: n * 52 + s * 12),
+}
+
+
+def dominant_kernel(phases, n, sides, hv):
+    """The single-kernel phase that takes longest and its roofline inputs."""
+    times = dict(zip(PHASES, phases))
+    name = max(KERNEL_BYTES, key=lambda k: times.get(k, 0.0))
+    kernel, fn = KERNEL_BYTES[name]
+    return name, kernel, times[name], fn(n, sides, hv)
+
+
+def measured_traffic(kernel, n):
+    """DRAM bytes of one launch, from the committed ncu capture of the kernel
+    (profiles/traffic.json: read + write bytes per particle at a stated
+    scene size), scaled to n particles; None when there is no capture."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            rec = json.load(f)[kernel]
+        return rec["bytes_per_particle"] * n, rec["source"]
+    except Exception:
+        return None, None
 
 
 def launches_per_step(scene):
@@ -131,7 +170,10 @@ def run_engine(scene, precision, steps, warmup):
     with ClockSampler() as clk:
         ms = e.time_steps(steps)
     stats = e.stepStats()
-    phases = e.compute_forces_timed(diag=True)
+    # per-kernel times: CUDA events on the engine stream around each phase
+    # of five force evaluations after the timed region, averaged
+    runs = [e.compute_forces_timed(diag=(k == 4)) for k in range(5)]
+    phases = [sum(r[k] for r in runs) / len(runs) for k in range(len(runs[0]))]
     stats_after = e.stepStats()
     return e, ms, clk.summary(), stats, phases, stats_after
 
@@ -202,6 +244,23 @@ def load_error(scene, evaluations=3):
     return out
 
 
+def drum_summary(steps, warmup):
+    """The 2,000,000-sphere drum in both precisions and the mixed form's
+    error against FP64: the scene the engine's headline target is set on."""
+    scene, desc = make_scene("c2")
+    out = {"workload": desc, "particles": scene.n}
+    for prec in ("mixed", "fp64"):
+        e, ms, clocks, stats, phases, _ = run_engine(scene, prec, steps, warmup)
+        out[prec] = {"value": scene.n * steps / (ms / 1000.0), "ms_per_step": ms / steps,
+                     "contact_sides_per_step": stats["particle_contacts"],
+                     "body_manifolds": stats["body_contacts"], "phase_ms": dict(zip(PHASES, phases)),
+                     "clocks": clocks}
+        del e
+    out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["load_error_vs_fp64"] = load_error(scene)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -211,6 +270,7 @@ def main():
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-drum", action="store_true", help="skip the embedded 2M-sphere drum summary")
     ap.add_argument("--particles", type=int, default=None,
                     help="particle count of the generated scene (profiling captures of a smaller case)")
     ap.add_argument("--single", action="store_true",
@@ -280,15 +340,22 @@ def main():
         return
     errs = load_error(scene)
     h = 4 if args.precision == "mixed" else 8
+    hv = 3 * h * 4            # one history slot: 9 values padded to 12
     contacts = stats["particle_contacts"]
-    bbytes = algorithmic_bytes(scene.n, scene.n_components, contacts, 0, stats["body_contacts"], scene.n_triangles, h)
     peak, peak_kind = hbm_peak()
-    achieved = bbytes / (per_step_ms / 1000.0) / 1e9
+    pname, kernel, kms, kbytes = dominant_kernel(phases, scene.n, contacts, hv)
+    achieved = kbytes / (kms / 1000.0) / 1e9
+    traffic, traffic_src = measured_traffic(kernel, scene.n)
+    step_bytes = algorithmic_bytes(scene.n, scene.n_components, contacts, 0, stats["body_contacts"],
+                                   scene.n_triangles, h)
     cpu = None
     if not args.no_cpu_baseline:
         v, cores, done, dt = cpu_baseline(scene)
         cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                "sample": f"{done} steps of the same workload on {cores} threads ({dt:.1f} s)"}
+    drum = None
+    if args.config != "c2" and not args.no_drum:
+        drum = drum_summary(args.steps, args.warmup)
     nb = scene.n_bodies
     line = {
         "metric": "particle-steps/s",
@@ -312,13 +379,19 @@ def main():
         "load_error_vs_fp64": errs,
         "phase_ms": dict(zip(PHASES, phases)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "whole step (algorithmic B_step / step time)", "peak_kind": peak_kind},
+                     "traffic": traffic, "kernel": kernel, "phase": pname, "kernel_ms": kms,
+                     "algorithmic_bytes": kbytes, "traffic_source": traffic_src,
+                     "peak_kind": peak_kind + " (hbm_gbs)",
+                     "step": {"algorithmic_bytes": step_bytes,
+                              "achieved": step_bytes / (per_step_ms / 1000.0) / 1e9}},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 13 * 8 * nb,
                 "d2h_bytes_per_step": 38 * 8 * nb + 16 * 4},
         "gpu_launches": launches_per_step(scene) * args.steps,
         "clocks": clocks,
     }
+    if drum:
+        line["drum_2m"] = drum
     print(json.dumps(line))
 
 

@@ -211,9 +211,10 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
         } else {
             // mixed form: FP32 rows; the world-frame rotation of omega is part
             // of the per-contact FP32 arithmetic.
-            r.vf[t] = make_float4((float)vx, (float)vy, (float)vz, (float)o.mass[w]);
+            const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+            r.vf[t] = make_float4(fvx, fvy, fvz, (float)o.mass[w]);
             r.vmf[t] = mid ? make_float4((float)c.vhx[ci], (float)c.vhy[ci], (float)c.vhz[ci], 0.f)
-                           : make_float4((float)vx, (float)vy, (float)vz, 0.f);
+                           : make_float4(fvx, fvy, fvz, 0.f);
             const float qw = (float)o.qw[w], qx = (float)o.qx[w], qy = (float)o.qy[w], qz = (float)o.qz[w];
             const V3<float> ew = rot_ivf(qw, qx, qy, qz, mk((float)o.wx[w], (float)o.wy[w], (float)o.wz[w]));
             r.wf[t] = make_float4(ew.x, ew.y, ew.z, 0.f);
@@ -226,8 +227,8 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
         r.meta[t] = make_int4(ci, w, c.cid[ci], o.scene[w]);
         r.cell[t] = make_int4(cx, cy, cz, g.clin[ci]);
         const double mesh = g.sc[o.scene[w]].mesh;
-        r.relf[t] = make_float4((float)(x - cx * mesh), (float)(y - cy * mesh), (float)(z - cz * mesh),
-                                (float)rad);
+        r.relf[t] = make_float4((float)(__fma_rn(-(double)cx, mesh, x)), (float)(__fma_rn(-(double)cy, mesh, y)),
+                                (float)(__fma_rn(-(double)cz, mesh, z)), (float)rad);
     }
 }
 
@@ -252,16 +253,19 @@ __global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const S
         if (S.wall_count > 0) {
             const V3<double> p = mk(c.x[ci], c.y[ci], c.z[ci]);
             const double rad = c.radius[ci];
+            // FP32 prefilter on the wall planes: a wall is skipped only when
+            // the particle is certainly clear of it; tol bounds the FP32
+            // error of the plane distance for these coordinates.
+            const float pfx = (float)p.x, pfy = (float)p.y, pfz = (float)p.z, rf = (float)rad;
+            const float tol = 1e-6f + 1e-6f * (fabsf(pfx) + fabsf(pfy) + fabsf(pfz));
             int whw = hw.hw[ci];
             for (int wl = 0; wl < S.wall_count; ++wl) {
                 const int wg = S.wall_begin + wl;
+                const float4 pl = walls.plane[wg];
+                const float distf = fmaf(pl.x, pfx, fmaf(pl.y, pfy, pl.z * pfz)) - pl.w;
+                if (distf - rf > tol + 1e-6f * fabsf(pl.w)) continue;
                 const V3<double> out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
                 const V3<double> org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
-                // FP32 prefilter, conservative by 1e-4 of the wall distance
-                // scale plus a micrometre
-                const V3<float> dpf = cvt<float>(p - org);
-                const float distf = dot(dpf, cvt<float>(out));
-                if (distf - (float)rad > 1e-4f * fabsf(distf) + 1e-6f) continue;
                 const double depth = rad - dot(p - org, out);
                 if (depth <= 0.0) continue;
                 const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
@@ -294,6 +298,7 @@ __global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const S
 // ------------------------------------------------------------- particle sweep
 constexpr int kMaxContacts = kPSlots;
 constexpr int kCandidates = 96;  // FP32-prefilter survivors held before the exact pass
+constexpr int kCertain = 1 << 30;  // staged candidate flag: contact decided by the FP32 test
 
 // Exact part of the reference's overlap test for one candidate (:587-597):
 // same owner skipped, FP64 d^2 with the reference's contraction, strict
@@ -348,12 +353,23 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
         int phw = hp.hw[ci];
         int pending = 0;  // candidates in stage_t[count .. count + pending)
+        // Phase 2 over the staged candidates, in order.  A candidate staged
+        // with kCertain passed the FP32 test with the rounding margin to
+        // spare on both sides (d < r_i + r_j and d > 0 hold in FP64 too), so
+        // only the owner check and its key need the record.
         auto exact_pass = [&]() {
             const int first = count, last = count + pending;
             for (int q = first; q < last; ++q) {
-                const int u = stage_t[q];
+                const int su = stage_t[q];
+                const int u = su & ~kCertain;
                 int cid;
-                if (!exact_contact(r.pos, r.meta, u, owner, pi.x, pi.y, pi.z, pi.w, cid)) continue;
+                if (su & kCertain) {
+                    const int4 mj = r.meta[u];
+                    if (mj.y == owner) continue;
+                    cid = mj.z;
+                } else if (!exact_contact(r.pos, r.meta, u, owner, pi.x, pi.y, pi.z, pi.w, cid)) {
+                    continue;
+                }
                 if (count >= kMaxContacts) { ++pover; continue; }
                 const int slot = acquire(hp, kPSlots, ci, (uint64_t)(uint32_t)cid + 1ull, step, phw, phigh);
                 if (slot < 0) { ++pover; continue; }
@@ -372,28 +388,35 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
                 if (ny < lay[1] || ny >= lay[1] + lay[4]) continue;
                 const float oy = offy[dy + 1];
                 const int row = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] - lay[2];
-                // boundaries of the z-cells z0..z1 of this column
-                int bnd[4];
-                for (int z = z0; z <= z1 + 1; ++z) bnd[z - z0] = g.cell_start[row + z];
-                for (int zc = z0; zc <= z1; ++zc) {
-                    const float oz = offz[zc - cell.z + 1];
-                    const int e = bnd[zc - z0 + 1];
-                    // four candidates per iteration: their loads are issued
-                    // together, the survivors are appended in order
-                    for (int u0 = bnd[zc - z0]; u0 < e; u0 += 4) {
-                        float4 fj[4];
+                // the z-cells z0..z1 of this column are one contiguous range
+                // [b0, e) of the sorted order, split at b1 and b2
+                const int b0 = g.cell_start[row + z0];
+                const int e = g.cell_start[row + z1 + 1];
+                const int b1 = z1 >= z0 + 1 ? g.cell_start[row + z0 + 1] : e;
+                const int b2 = z1 >= z0 + 2 ? g.cell_start[row + z0 + 2] : e;
+                const float oz0 = offz[z0 - cell.z + 1];
+                const float oz1 = z1 >= z0 + 1 ? offz[z0 - cell.z + 2] : 0.f;
+                const float oz2 = z1 >= z0 + 2 ? offz[z0 - cell.z + 3] : 0.f;
+                // four candidates per iteration: their loads are issued
+                // together, the survivors are appended in order
+                for (int u0 = b0; u0 < e; u0 += 4) {
+                    float4 fj[4];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            fj[q] = (u0 + q < e) ? r.relf[u0 + q] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+                    for (int q = 0; q < 4; ++q)
+                        fj[q] = (u0 + q < e) ? r.relf[u0 + q] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const float ddx = fj[q].x + ox, ddy = fj[q].y + oy, ddz = fj[q].z + oz;
-                            const float rsf = fj[q].w + fi.w + margin_f;
-                            if (ddx * ddx + ddy * ddy + ddz * ddz >= rsf * rsf) continue;
-                            if (count + pending == kCandidates) exact_pass();
-                            stage_t[count + pending] = u0 + q;
-                            ++pending;
-                        }
+                    for (int q = 0; q < 4; ++q) {
+                        const int u = u0 + q;
+                        const float oz = u < b1 ? oz0 : (u < b2 ? oz1 : oz2);
+                        const float ddx = fj[q].x + ox, ddy = fj[q].y + oy, ddz = fj[q].z + oz;
+                        const float rsf = fj[q].w + fi.w + margin_f;
+                        const float dd2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        if (dd2 >= rsf * rsf) continue;
+                        const float rin = rsf - 2.f * margin_f;
+                        const bool certain = dd2 < rin * rin && dd2 > 4.f * margin_f * margin_f;
+                        if (count + pending == kCandidates) exact_pass();
+                        stage_t[count + pending] = certain ? (u | kCertain) : u;
+                        ++pending;
                     }
                 }
             }
@@ -431,6 +454,7 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
                                                 Counters k, double dt_eff, int nscenes)
 {
     const int total = *k.ct_total;
+    const T dtT = T(dt_eff);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
         const int4 e = __ldg(&ct.ent[q]);
         const D4 pi = ldg_d4(&r.pos[e.x]), pj = ldg_d4(&r.pos[e.y]);
@@ -481,8 +505,8 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
         }
         const SceneC& S = sc[s];
         V3<T> f, cpl;
-        pp_law<T>(mat<T>(S.pp, S.ppf), T(dt_eff), n, d, depth, T(d2), T(pi.w), T(pj.w), mi_, mj_, erv, mrv, ewi, ewj,
-                  mwi, mwj, h, f, cpl);
+        pp_law<T>(mat<T>(S.pp, S.ppf), dtT, n, d, depth, cv<T>(d2), cv<T>(pi.w), cv<T>(pj.w), mi_, mj_, erv, mrv, ewi,
+                  ewj, mwi, mwj, h, f, cpl);
         hv_store(hv, h);
         if (r.off) cpl = cpl + cross(cvt<T>(d3(r.off[e.x])), f);
         T* out = ct.res + 6 * (size_t)e.w;
@@ -1134,6 +1158,30 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
     }
     const double im = o.inv_mass[i];
     o.ax[i] = TF.x * im; o.ay[i] = TF.y * im; o.az[i] = TF.z * im;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        // mixed form: the body-frame rotation of the torque and the Euler
+        // equations in FP32, like the per-contact arithmetic they follow
+        const float qw = (float)o.qw[i], qx = (float)o.qx[i], qy = (float)o.qy[i], qz = (float)o.qz[i];
+        const V3<float> Tq = cvt<float>(TT);
+        const float tx = (1.f - 2.f * (qy * qy + qz * qz)) * Tq.x + 2.f * (qx * qy + qw * qz) * Tq.y +
+                         2.f * (qx * qz - qw * qy) * Tq.z;
+        const float ty = 2.f * (qx * qy - qw * qz) * Tq.x + (1.f - 2.f * (qx * qx + qz * qz)) * Tq.y +
+                         2.f * (qy * qz + qw * qx) * Tq.z;
+        const float tz = 2.f * (qx * qz + qw * qy) * Tq.x + 2.f * (qy * qz - qw * qx) * Tq.y +
+                         (1.f - 2.f * (qx * qx + qy * qy)) * Tq.z;
+        const float ix = (float)o.inv_ix[i], iy = (float)o.inv_iy[i], iz = (float)o.inv_iz[i];
+        const double Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
+        if (Ix == Iy && Iy == Iz) {
+            o.awx[i] = (double)(tx * ix); o.awy[i] = (double)(ty * iy); o.awz[i] = (double)(tz * iz);
+            return;
+        }
+        const float wx = (float)o.wx[i], wy = (float)o.wy[i], wz = (float)o.wz[i];
+        const float fx = (float)Ix, fy = (float)Iy, fz = (float)Iz;
+        o.awx[i] = (double)((tx - (fz - fy) * wz * wy) * ix);
+        o.awy[i] = (double)((ty - (fx - fz) * wx * wz) * iy);
+        o.awz[i] = (double)((tz - (fy - fx) * wy * wx) * iz);
+        return;
+    }
     const double qw = o.qw[i], qx = o.qx[i], qy = o.qy[i], qz = o.qz[i];
     const double tx = (1.0 - 2.0 * (qy * qy + qz * qz)) * TT.x + 2.0 * (qx * qy + qw * qz) * TT.y + 2.0 * (qx * qz - qw * qy) * TT.z;
     const double ty = 2.0 * (qx * qy - qw * qz) * TT.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * TT.y + 2.0 * (qy * qz + qw * qx) * TT.z;

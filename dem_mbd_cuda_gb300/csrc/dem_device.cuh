@@ -42,7 +42,12 @@ template <typename T> DEM_DEV V3<T> normalized(V3<T> a)
     const T l = norm(a);
     return l > T(1.0e-14) ? a * (T(1) / l) : mk<T>(0, 0, 0);
 }
-template <typename T, typename S> DEM_DEV V3<T> cvt(V3<S> a) { return {T(a.x), T(a.y), T(a.z)}; }
+// Precision conversions.  On GB300 every 64-bit conversion issues on the
+// FP64 pipe (about 2 per clock per SM, the rate of a DFMA), so the mixed
+// form keeps their number per particle and per contact small.
+template <typename T> DEM_DEV T cv(double x) { return static_cast<T>(x); }
+template <typename T> DEM_DEV T cv(float x) { return static_cast<T>(x); }
+template <typename T, typename S> DEM_DEV V3<T> cvt(V3<S> a) { return {cv<T>(a.x), cv<T>(a.y), cv<T>(a.z)}; }
 
 // Overlap predicate operand with a fixed contraction pattern so the contact
 // set is decided by the same bits as the oracle and the reference build:

@@ -245,6 +245,8 @@ public:
             gvec_.push_back({x.gravity[0], x.gravity[1], x.gravity[2]});
         }
         n_ = (int)oid.size();
+        if (cown.size() >= (size_t)1 << 30)
+            throw DemError(DEM_ERR_CAPACITY, "more than 2^30 components: sorted positions carry a flag in bit 30");
         nc_ = (int)cown.size();
         nw_ = (int)wo.size() / 3;
         nb_ = (int)bmass.size();
@@ -373,6 +375,14 @@ public:
 
         // ---- walls, bodies, triangles
         W_.o = upd(wo, "wall origin"); W_.n = upd(wn, "wall normal");
+        {
+            std::vector<float4> pl(wo.size() / 3);
+            for (size_t k = 0; k < pl.size(); ++k) {
+                const double nd = wn[3 * k] * wo[3 * k] + wn[3 * k + 1] * wo[3 * k + 1] + wn[3 * k + 2] * wo[3 * k + 2];
+                pl[k] = make_float4((float)wn[3 * k], (float)wn[3 * k + 1], (float)wn[3 * k + 2], (float)nd);
+            }
+            W_.plane = arena_.upload(pl.data(), pl.size(), "wall planes", s);
+        }
         B_.nb = nb_;
         B_.c = arena_.upload(bc.data(), bc.size(), "body c", s); B_.q = arena_.upload(bq.data(), bq.size(), "body q", s);
         B_.v = arena_.upload(bv.data(), bv.size(), "body v", s); B_.w = arena_.upload(bw.data(), bw.size(), "body w", s);

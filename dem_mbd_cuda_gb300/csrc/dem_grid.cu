@@ -14,6 +14,7 @@
 // Step 4 makes the result equal to a stable sort of the keys over component
 // indices, i.e. the reference's sortedCellKey / sortedEntityId, and the scan
 // is the cell start/end table the contact kernels index directly.
+#include "../../include/dem_gb300.h"
 #include "dem_kernels.cuh"
 
 #include <climits>
@@ -378,39 +379,48 @@ __device__ bool tri_range_valid(const Tris& t, const Grid& g, int i)
     return true;
 }
 
+// One warp per triangle, the lanes over the cells of its padded AABB.
 __global__ void k_tri_count(Tris t, Grid g, int* tgover)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= t.nt) return;
     if (!tri_range_valid(t, g, i)) {
-        atomicAdd(tgover, 1);
-        atomicOr(g.err, kErrTriRange);
+        if (lane == 0) {
+            atomicAdd(tgover, 1);
+            atomicOr(g.err, kErrTriRange);
+        }
         return;
     }
     int lo[3], hi[3];
     const int* lay;
     if (!tri_cell_range(t, g, i, lo, hi, lay)) return;
-    for (int x = lo[0]; x <= hi[0]; ++x)
-        for (int y = lo[1]; y <= hi[1]; ++y)
-            for (int z = lo[2]; z <= hi[2]; ++z) atomicAdd(t.tcell_count + cell_lin(lay, x, y, z), 1);
+    const int ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    const int cells = (hi[0] - lo[0] + 1) * ny * nz;
+    for (int k = lane; k < cells; k += 32) {
+        const int x = lo[0] + k / (ny * nz), y = lo[1] + (k / nz) % ny, z = lo[2] + k % nz;
+        atomicAdd(t.tcell_count + cell_lin(lay, x, y, z), 1);
+    }
 }
 
 __global__ void k_tri_fill(Tris t, Grid g)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= t.nt) return;
     if (!tri_range_valid(t, g, i)) return;
     int lo[3], hi[3];
     const int* lay;
     if (!tri_cell_range(t, g, i, lo, hi, lay)) return;
-    for (int x = lo[0]; x <= hi[0]; ++x)
-        for (int y = lo[1]; y <= hi[1]; ++y)
-            for (int z = lo[2]; z <= hi[2]; ++z) {
-                const int lin = cell_lin(lay, x, y, z);
-                const int pos = t.tcell_start[lin] + atomicAdd(t.tcell_cursor + lin, 1);
-                if (pos < t.capacity) { t.ttri_tmp[pos] = i; t.tlin_tmp[pos] = lin; }
-                else atomicOr(g.err, kErrTriCapacity);
-            }
+    const int ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    const int cells = (hi[0] - lo[0] + 1) * ny * nz;
+    for (int k = lane; k < cells; k += 32) {
+        const int x = lo[0] + k / (ny * nz), y = lo[1] + (k / nz) % ny, z = lo[2] + k % nz;
+        const int lin = cell_lin(lay, x, y, z);
+        const int pos = t.tcell_start[lin] + atomicAdd(t.tcell_cursor + lin, 1);
+        if (pos < t.capacity) { t.ttri_tmp[pos] = i; t.tlin_tmp[pos] = lin; }
+        else atomicOr(g.err, kErrTriCapacity);
+    }
 }
 
 // Triangle-cell entries in ascending triangle order per cell (the order of
@@ -617,9 +627,9 @@ void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s)
 void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover, int sm_count, cudaStream_t s)
 {
     if (t.nt <= 0) return;
-    k_tri_count<<<blocks(t.nt, 128), 128, 0, s>>>(t, g, tgover);
+    k_tri_count<<<blocks(32 * t.nt, 128), 128, 0, s>>>(t, g, tgover);
     launch_scan(t.tcell_count, t.tcell_start, g.total_cells, g.tile_sums, sm_count, s);
-    k_tri_fill<<<blocks(t.nt, 128), 128, 0, s>>>(t, g);
+    k_tri_fill<<<blocks(32 * t.nt, 128), 128, 0, s>>>(t, g);
     k_tri_place<<<sm_count * 8, 256, 0, s>>>(t, g);
 }
 

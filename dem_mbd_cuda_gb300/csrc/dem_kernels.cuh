@@ -112,6 +112,7 @@ template <typename T> struct Hist {
 
 struct Walls {
     double *o, *n;  // [nw][3]
+    float4* plane;  // [nw] FP32 (normal, normal . origin) for the prefilter
 };
 
 struct Tris {
