@@ -32,7 +32,7 @@ import numpy as np  # noqa: E402
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # pipeline phases timed with CUDA events in one force evaluation
-PHASES = ["grid", "triangles+gather", "expire+walls", "sweep", "pp_law", "pt", "owner_sum", "body_reduce"]
+PHASES = ["grid", "triangles+gather", "sweep", "walls", "pp_law", "pt", "owner_sum", "body_reduce"]
 
 
 def make_scene(config, particles=None):
@@ -119,17 +119,17 @@ def algorithmic_bytes(n, nc, contacts, wall_contacts, body_manifolds, triangles,
 # n particles with s contact sides; hv = bytes of one history slot.
 KERNEL_BYTES = {
     # own record (relf, pos, meta, cell) 80 + 9 cell-row boundaries 144 +
-    # counters 12 + history keys 8/slot; contact list entry 16 + key 8 per side
-    "sweep": ("k_sweep", lambda n, s, hv: n * 236 + s * 24),
+    # counters 12 + three high-water marks 12 + history key and age 12/slot;
+    # contact list entry 16 + key and age 12 per side
+    "sweep": ("k_sweep", lambda n, s, hv: n * 260 + s * 28),
     # per side: list entry 16, history slot read + write, result row 24;
     # per particle: its FP64 position 32 and four FP32 rows 64
     "pp_law": ("k_pp_law", lambda n, s, hv: s * (16 + 2 * hv + 24) + n * 96),
     # per owner: count, flags, field force, inverse mass and inertia,
     # quaternion, omega, accelerations; result rows 24 per side
     "owner_sum": ("k_owner_sum", lambda n, s, hv: n * 196 + s * 24),
-    # per component: position and radius 32, three slot arrays' high-water
-    # marks 12, key and age scan 12/slot, wall flag and result 8
-    "expire+walls": ("k_expire_walls", lambda n, s, hv: n * 52 + s * 12),
+    # per component: owner and scene 8, position and radius 32, wall flag 1
+    "walls": ("k_walls", lambda n, s, hv: n * 41),
 }
 
 

@@ -233,60 +233,105 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
 }
 
 // ------------------------------------------------------ expiry and walls
-// Per component in input order: expireHistory for the three slot arrays
-// (:1109-1117), then the planar walls of its scene (wallContact, :975-1063).
-template <typename T, typename TB>
-__global__ void __launch_bounds__(256) k_expire_walls(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
-                                                      Hist<T> hp, Hist<T> hw, Hist<TB> hb, Contacts<T> ct, Counters k,
-                                                      double dt_eff)
+// wallContact (:975-1063) for wall wl of the component's scene: the exact
+// FP64 depth, slot acquisition and the wall law; the load is added to wF/wT.
+template <typename T>
+__device__ __noinline__ void wall_contact(const Comps& c, const Owners& o, const SceneC& S, const Walls& walls,
+                                          Hist<T> hw, int ci, int w, int wl, V3<double> p, double rad, int step,
+                                          double dt_eff, int& whw, int& bhigh, int& bover, V3<double>& wF,
+                                          V3<double>& wT)
+{
+    const int wg = S.wall_begin + wl;
+    const V3<double> out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
+    const V3<double> org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
+    const double depth = rad - dot(p - org, out);
+    if (depth <= 0.0) return;
+    const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
+    if (slot < 0) { ++bover; return; }
+    T* hv = hw.val + ((size_t)ci * kWSlots + slot) * kHV;
+    const V3<double> vel = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
+    const V3<double> om = rot_iv(o.qw[w], o.qx[w], o.qy[w], o.qz[w], mk(o.wx[w], o.wy[w], o.wz[w]));
+    const V3<double> off = c.ox ? mk(c.ox[ci], c.oy[ci], c.oz[ci]) : mk(0.0, 0.0, 0.0);
+    V3<T> f, cpl;
+    wall_law<T>(mat<T>(S.pw, S.pwf), T(dt_eff), cvt<T>(out), T(depth), T(rad), T(o.mass[w]), cvt<T>(vel), cvt<T>(om),
+                hv, f, cpl);
+    const V3<double> fd = cvt<double>(f);
+    wF = wF + fd;
+    wT = wT + (cvt<double>(cpl) + cross(off, fd));
+}
+
+// Planar walls (wallContact, :975-1063) in two passes.  The components'
+// wall slots were expired by the sweep, which runs first; wall, particle and
+// body slots are separate arrays, so the slots each acquires are those of
+// the reference's order (all expiries, then walls, particles, bodies).
+//
+// Pass 1, per component in input order: FP32 rejection on the wall planes
+// (a wall is skipped only when the particle is certainly clear of it; tol
+// bounds the FP32 error of the plane distance for these coordinates).  The
+// components with a wall that may touch go to a compact list with their
+// candidate mask (walls past the 32nd are always candidates: a scene with
+// more than 32 walls lists every component by setting bit 31, which only
+// adds wall 31 to the exact test); every wall
+// flag of the step starts cleared.  The list's order does not matter: pass
+// 2 handles each component whole, in one thread, so the FP64 work runs in
+// full warps instead of one lane in every warp that holds a wall particle.
+__global__ void __launch_bounds__(256) k_walls_probe(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
+                                                     unsigned char* wflag, int2* wlist, int* wl_total)
+{
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned cand = 0u;
+    if (ci < c.n) {
+        wflag[ci] = 0;
+        const SceneC& S = sc[o.scene[c.owner[ci]]];
+        if (S.wall_count > 0) {
+            const float pfx = (float)c.x[ci], pfy = (float)c.y[ci], pfz = (float)c.z[ci], rf = (float)c.radius[ci];
+            const float tol = 1e-6f + 1e-6f * (fabsf(pfx) + fabsf(pfy) + fabsf(pfz));
+            const int nw32 = min(S.wall_count, 32);
+            for (int wl = 0; wl < nw32; ++wl) {
+                const float4 pl = walls.plane[S.wall_begin + wl];
+                const float distf = fmaf(pl.x, pfx, fmaf(pl.y, pfy, pl.z * pfz)) - pl.w;
+                if (distf - rf <= tol + 1e-6f * fabsf(pl.w)) cand |= 1u << wl;
+            }
+            if (S.wall_count > 32) cand |= 0x80000000u;
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, cand != 0u);
+    if (m) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(wl_total, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (cand) wlist[base + __popc(m & ((1u << lane) - 1u))] = make_int2(ci, (int)cand);
+    }
+}
+
+// Pass 2, one thread per listed component: the exact FP64 depth, slot
+// acquisition and wall law for its candidate walls in ascending order.
+template <typename T>
+__global__ void __launch_bounds__(128) k_walls_law(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
+                                                   Hist<T> hw, Contacts<T> ct, Counters k, double dt_eff)
 {
     const int step = *k.step;
-    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    const int total = *k.wl_total;
     int bover = 0, bhigh = 0;
-    if (ci < c.n) {
-        expire(hp, kPSlots, ci, step);
-        expire(hw, kWSlots, ci, step);
-        expire(hb, kBSlots, ci, step);
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
+        const int2 e = ct.wlist[item];
+        const int ci = e.x;
+        unsigned cand = (unsigned)e.y;
         const int w = c.owner[ci];
         const SceneC& S = sc[o.scene[w]];
+        const V3<double> p = mk(c.x[ci], c.y[ci], c.z[ci]);
+        const double rad = c.radius[ci];
         V3<double> wF = mk(0.0, 0.0, 0.0), wT = mk(0.0, 0.0, 0.0);
-        if (S.wall_count > 0) {
-            const V3<double> p = mk(c.x[ci], c.y[ci], c.z[ci]);
-            const double rad = c.radius[ci];
-            // FP32 prefilter on the wall planes: a wall is skipped only when
-            // the particle is certainly clear of it; tol bounds the FP32
-            // error of the plane distance for these coordinates.
-            const float pfx = (float)p.x, pfy = (float)p.y, pfz = (float)p.z, rf = (float)rad;
-            const float tol = 1e-6f + 1e-6f * (fabsf(pfx) + fabsf(pfy) + fabsf(pfz));
-            int whw = hw.hw[ci];
-            for (int wl = 0; wl < S.wall_count; ++wl) {
-                const int wg = S.wall_begin + wl;
-                const float4 pl = walls.plane[wg];
-                const float distf = fmaf(pl.x, pfx, fmaf(pl.y, pfy, pl.z * pfz)) - pl.w;
-                if (distf - rf > tol + 1e-6f * fabsf(pl.w)) continue;
-                const V3<double> out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
-                const V3<double> org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
-                const double depth = rad - dot(p - org, out);
-                if (depth <= 0.0) continue;
-                const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
-                if (slot < 0) { ++bover; continue; }
-                T* hv = hw.val + ((size_t)ci * kWSlots + slot) * kHV;
-                const V3<double> vel = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
-                const V3<double> om =
-                    rot_iv(o.qw[w], o.qx[w], o.qy[w], o.qz[w], mk(o.wx[w], o.wy[w], o.wz[w]));
-                const V3<double> off = c.ox ? mk(c.ox[ci], c.oy[ci], c.oz[ci]) : mk(0.0, 0.0, 0.0);
-                V3<T> f, cpl;
-                wall_law<T>(mat<T>(S.pw, S.pwf), T(dt_eff), cvt<T>(out), T(depth), T(rad), T(o.mass[w]), cvt<T>(vel), cvt<T>(om), hv, f,
-                            cpl);
-                const V3<double> fd = cvt<double>(f);
-                wF = wF + fd;
-                wT = wT + (cvt<double>(cpl) + cross(off, fd));
-            }
-            hw.hw[ci] = whw;
-        }
+        int whw = hw.hw[ci];
+        for (; cand; cand &= cand - 1u)
+            wall_contact<T>(c, o, S, walls, hw, ci, w, __ffs(cand) - 1, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT);
+        for (int wl = 32; wl < S.wall_count; ++wl)
+            wall_contact<T>(c, o, S, walls, hw, ci, w, wl, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT);
+        hw.hw[ci] = whw;
         const bool hit = wF.x != 0.0 || wF.y != 0.0 || wF.z != 0.0 || wT.x != 0.0 || wT.y != 0.0 || wT.z != 0.0;
-        ct.wflag[ci] = hit ? 1 : 0;
         if (hit) {
+            ct.wflag[ci] = 1;
             double* wr = ct.wres + 6 * (size_t)ci;
             wr[0] = wF.x; wr[1] = wF.y; wr[2] = wF.z; wr[3] = wT.x; wr[4] = wT.y; wr[5] = wT.z;
         }
@@ -327,9 +372,9 @@ __device__ __noinline__ bool exact_contact(const D4* __restrict__ pos, const int
 // FP64 test and the history slot acquisition (acquireHistorySlot, :190-215)
 // on them in order.  Contacts go to a flat list; results are stored per
 // (slot rank, component) so the owner sum reads them coalesced.
-template <typename T>
+template <typename T, typename TB>
 __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __restrict__ sc, Tris tris, Hist<T> hp,
-                                               Contacts<T> ct, Counters k, int nc)
+                                               Hist<T> hw, Hist<TB> hb, Contacts<T> ct, Counters k, int nc)
 {
     const int step = *k.step;
     const int nvalid = *g.nvalid;
@@ -351,6 +396,11 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         const float offy[3] = {-mesh_f - fi.y, -fi.y, mesh_f - fi.y};
         const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
         const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
+        // expireHistory (:1109-1117) for the component's three slot arrays,
+        // before any slot of this step is acquired
+        expire(hp, kPSlots, ci, step);
+        expire(hw, kWSlots, ci, step);
+        expire(hb, kBSlots, ci, step);
         int phw = hp.hw[ci];
         int pending = 0;  // candidates in stage_t[count .. count + pending)
         // Phase 2 over the staged candidates, in order.  A candidate staged
@@ -1095,12 +1145,115 @@ __global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, cons
 // --------------------------------------------------------------- owner sum
 // Per owner: the reference's accumulators (:1082-1094, 1211-1220) and the
 // acceleration / Euler equations (src/cuda/cuda_particle_backend.cu:71-101).
+// Euler's equations of an owner (src/cuda/cuda_particle_backend.cu:71-101):
+// the world-frame torque TT rotated into the body frame, the angular
+// acceleration in the body frame.  The gyroscopic terms vanish for isotropic
+// inertia (the flag is precomputed); the general case is kept out of line so
+// its FP64 work is not issued for spheres.
+__device__ __noinline__ void euler_aniso_f64(Owners o, int i, double tx, double ty, double tz)
+{
+    const double Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
+    const double wx = o.wx[i], wy = o.wy[i], wz = o.wz[i];
+    o.awx[i] = (tx - (Iz - Iy) * wz * wy) * o.inv_ix[i];
+    o.awy[i] = (ty - (Ix - Iz) * wx * wz) * o.inv_iy[i];
+    o.awz[i] = (tz - (Iy - Ix) * wy * wx) * o.inv_iz[i];
+}
+__device__ __forceinline__ void euler_f64(Owners o, int i, V3<double> TT)
+{
+    const double qw = o.qw[i], qx = o.qx[i], qy = o.qy[i], qz = o.qz[i];
+    const double tx = (1.0 - 2.0 * (qy * qy + qz * qz)) * TT.x + 2.0 * (qx * qy + qw * qz) * TT.y + 2.0 * (qx * qz - qw * qy) * TT.z;
+    const double ty = 2.0 * (qx * qy - qw * qz) * TT.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * TT.y + 2.0 * (qy * qz + qw * qx) * TT.z;
+    const double tz = 2.0 * (qx * qz + qw * qy) * TT.x + 2.0 * (qy * qz - qw * qx) * TT.y + (1.0 - 2.0 * (qx * qx + qy * qy)) * TT.z;
+    if (o.iso[i]) {
+        o.awx[i] = tx * o.inv_ix[i];
+        o.awy[i] = ty * o.inv_iy[i];
+        o.awz[i] = tz * o.inv_iz[i];
+        return;
+    }
+    euler_aniso_f64(o, i, tx, ty, tz);
+}
+// Mixed form: the rotation and Euler's equations in FP32, like the
+// per-contact arithmetic they follow; the result is stored in FP64.
+__device__ __noinline__ void euler_aniso_f32(Owners o, int i, float tx, float ty, float tz)
+{
+    const float ix = (float)o.inv_ix[i], iy = (float)o.inv_iy[i], iz = (float)o.inv_iz[i];
+    const float wx = (float)o.wx[i], wy = (float)o.wy[i], wz = (float)o.wz[i];
+    const float fx = (float)o.ix[i], fy = (float)o.iy[i], fz = (float)o.iz[i];
+    o.awx[i] = (double)((tx - (fz - fy) * wz * wy) * ix);
+    o.awy[i] = (double)((ty - (fx - fz) * wx * wz) * iy);
+    o.awz[i] = (double)((tz - (fy - fx) * wy * wx) * iz);
+}
+__device__ __forceinline__ void euler_f32(Owners o, int i, V3<float> Tq)
+{
+    const float qw = (float)o.qw[i], qx = (float)o.qx[i], qy = (float)o.qy[i], qz = (float)o.qz[i];
+    const float tx = (1.f - 2.f * (qy * qy + qz * qz)) * Tq.x + 2.f * (qx * qy + qw * qz) * Tq.y +
+                     2.f * (qx * qz - qw * qy) * Tq.z;
+    const float ty = 2.f * (qx * qy - qw * qz) * Tq.x + (1.f - 2.f * (qx * qx + qz * qz)) * Tq.y +
+                     2.f * (qy * qz + qw * qx) * Tq.z;
+    const float tz = 2.f * (qx * qz + qw * qy) * Tq.x + 2.f * (qy * qz - qw * qx) * Tq.y +
+                     (1.f - 2.f * (qx * qx + qy * qy)) * Tq.z;
+    if (o.iso[i]) {
+        const float ii = o.inv_i_f[i];
+        o.awx[i] = (double)(tx * ii); o.awy[i] = (double)(ty * ii); o.awz[i] = (double)(tz * ii);
+        return;
+    }
+    euler_aniso_f32(o, i, tx, ty, tz);
+}
+
+// Mixed form, one sphere per owner, no force outputs: the particle rows are
+// summed in FP32 (as in the general path), the translational total in FP64;
+// a torque with only particle terms goes to the FP32 Euler step without a
+// round trip through FP64.  The wall and body terms, when present, are added
+// in FP64 in the general path's order.
+template <typename T>
+__device__ __forceinline__ void owner_sum_sphere_f32(Owners o, Contacts<T> ct, int i)
+{
+    const int cnt = ct.cnt[i];
+    V3<float> sf = mk(0.f, 0.f, 0.f), st = mk(0.f, 0.f, 0.f);
+    for (int q = 0; q < cnt; ++q) {
+        const float* rr = reinterpret_cast<const float*>(ct.res) + 6 * ((size_t)q * o.n + i);
+        sf = sf + mk(rr[0], rr[1], rr[2]);
+        st = st + mk(rr[3], rr[4], rr[5]);
+    }
+    const V3<double> fF = mk(o.mg[3 * (size_t)i], o.mg[3 * (size_t)i + 1], o.mg[3 * (size_t)i + 2]);
+    V3<double> cF = cvt<double>(sf);
+    V3<double> TF = cF + (o.ugx ? fF + mk(o.ugx[i], o.ugy[i], o.ugz[i]) : fF);
+    const bool wall = ct.wflag[i] != 0;
+    const int pk = ct.pt_index[i];
+    V3<float> Tq = st;
+    if (wall || pk >= 0) {
+        V3<double> wF = mk(0.0, 0.0, 0.0), wT = wF, bF = wF, bT = wF;
+        if (wall) {
+            const double* wr = ct.wres + 6 * (size_t)i;
+            wF = mk(wr[0], wr[1], wr[2]);
+            wT = mk(wr[3], wr[4], wr[5]);
+        }
+        if (pk >= 0) {
+            const double* pr = ct.pt_res + 6 * (size_t)i;
+            bF = mk(pr[0], pr[1], pr[2]);
+            bT = mk(pr[3], pr[4], pr[5]);
+        }
+        const V3<double> cT = cvt<double>(st);
+        TF = TF + (wall ? (pk >= 0 ? wF + bF : wF) : bF);
+        Tq = cvt<float>(wall ? (pk >= 0 ? cT + (wT + bT) : cT + wT) : cT + bT);
+    }
+    const double im = o.inv_mass[i];
+    o.ax[i] = TF.x * im; o.ay[i] = TF.y * im; o.az[i] = TF.z * im;
+    euler_f32(o, i, Tq);
+}
+
 template <typename T>
 __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Contacts<T> ct, int outputs, double* fc,
                             double* ff, double* fw, double* ft)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= o.n) return;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (c.sphere && !outputs) {
+            owner_sum_sphere_f32(o, ct, i);
+            return;
+        }
+    }
     // field force m*g (precomputed per owner, the same products as
     // :1090-1094) plus universal gravitation when enabled
     V3<double> fF = mk(o.mg[3 * (size_t)i], o.mg[3 * (size_t)i + 1], o.mg[3 * (size_t)i + 2]);
@@ -1158,48 +1311,9 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
     }
     const double im = o.inv_mass[i];
     o.ax[i] = TF.x * im; o.ay[i] = TF.y * im; o.az[i] = TF.z * im;
-    if constexpr (sizeof(T) == sizeof(float)) {
-        // mixed form: the body-frame rotation of the torque and the Euler
-        // equations in FP32, like the per-contact arithmetic they follow
-        const float qw = (float)o.qw[i], qx = (float)o.qx[i], qy = (float)o.qy[i], qz = (float)o.qz[i];
-        const V3<float> Tq = cvt<float>(TT);
-        const float tx = (1.f - 2.f * (qy * qy + qz * qz)) * Tq.x + 2.f * (qx * qy + qw * qz) * Tq.y +
-                         2.f * (qx * qz - qw * qy) * Tq.z;
-        const float ty = 2.f * (qx * qy - qw * qz) * Tq.x + (1.f - 2.f * (qx * qx + qz * qz)) * Tq.y +
-                         2.f * (qy * qz + qw * qx) * Tq.z;
-        const float tz = 2.f * (qx * qz + qw * qy) * Tq.x + 2.f * (qy * qz - qw * qx) * Tq.y +
-                         (1.f - 2.f * (qx * qx + qy * qy)) * Tq.z;
-        const float ix = (float)o.inv_ix[i], iy = (float)o.inv_iy[i], iz = (float)o.inv_iz[i];
-        const double Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
-        if (Ix == Iy && Iy == Iz) {
-            o.awx[i] = (double)(tx * ix); o.awy[i] = (double)(ty * iy); o.awz[i] = (double)(tz * iz);
-            return;
-        }
-        const float wx = (float)o.wx[i], wy = (float)o.wy[i], wz = (float)o.wz[i];
-        const float fx = (float)Ix, fy = (float)Iy, fz = (float)Iz;
-        o.awx[i] = (double)((tx - (fz - fy) * wz * wy) * ix);
-        o.awy[i] = (double)((ty - (fx - fz) * wx * wz) * iy);
-        o.awz[i] = (double)((tz - (fy - fx) * wy * wx) * iz);
-        return;
-    }
-    const double qw = o.qw[i], qx = o.qx[i], qy = o.qy[i], qz = o.qz[i];
-    const double tx = (1.0 - 2.0 * (qy * qy + qz * qz)) * TT.x + 2.0 * (qx * qy + qw * qz) * TT.y + 2.0 * (qx * qz - qw * qy) * TT.z;
-    const double ty = 2.0 * (qx * qy - qw * qz) * TT.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * TT.y + 2.0 * (qy * qz + qw * qx) * TT.z;
-    const double tz = 2.0 * (qx * qz + qw * qy) * TT.x + 2.0 * (qy * qz - qw * qx) * TT.y + (1.0 - 2.0 * (qx * qx + qy * qy)) * TT.z;
-    const double Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
-    if (Ix == Iy && Iy == Iz) {
-        // isotropic inertia: the gyroscopic terms are exactly zero
-        o.awx[i] = tx * o.inv_ix[i];
-        o.awy[i] = ty * o.inv_iy[i];
-        o.awz[i] = tz * o.inv_iz[i];
-        return;
-    }
-    const double wx = o.wx[i], wy = o.wy[i], wz = o.wz[i];
-    o.awx[i] = (tx - (Iz - Iy) * wz * wy) * o.inv_ix[i];
-    o.awy[i] = (ty - (Ix - Iz) * wx * wz) * o.inv_iy[i];
-    o.awz[i] = (tz - (Iy - Ix) * wy * wx) * o.inv_iz[i];
+    if constexpr (sizeof(T) == sizeof(float)) euler_f32(o, i, cvt<float>(TT));
+    else euler_f64(o, i, TT);
 }
-
 // ------------------------------------------------------------ body reduce
 // Level 1: blocks (group g, body b) reduce a contiguous item range in a
 // fixed order; level 2 reduces the groups in order.  Fields: [0..5] load,
@@ -1319,8 +1433,11 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
                      const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s, int stage)
 {
     (void)block;
-    if (stage & 1) k_expire_walls<T, TB><<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, hp, hw, hb, ct, k, dt_eff);
-    if (stage & 2) k_sweep<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, ct, k, c.n);
+    if (stage & 2) k_sweep<T, TB><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, hw, hb, ct, k, c.n);
+    if ((stage & 1) && w.count > 0) {
+        k_walls_probe<<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, ct.wflag, ct.wlist, k.wl_total);
+        k_walls_law<T><<<sm_count * 4, 128, 0, s>>>(c, o, sc, w, hw, ct, k, dt_eff);
+    }
     if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
         launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);

@@ -297,6 +297,15 @@ public:
                 for (int i = 0; i < n_; ++i) inv[i] = 1.0 / oin[3 * (size_t)i + a];
                 (a == 0 ? O_.inv_ix : (a == 1 ? O_.inv_iy : O_.inv_iz)) = upd(inv, "inverse inertia");
             }
+            std::vector<unsigned char> iso(n_);
+            std::vector<float> iif(n_);
+            for (int i = 0; i < n_; ++i) {
+                const double* I = &oin[3 * (size_t)i];
+                iso[i] = (I[0] == I[1] && I[1] == I[2]) ? 1 : 0;
+                iif[i] = (float)(1.0 / I[0]);
+            }
+            O_.iso = arena_.upload(iso.data(), iso.size(), "isotropic flags", s);
+            O_.inv_i_f = arena_.upload(iif.data(), iif.size(), "fp32 inverse inertia", s);
         }
         double** zeros[] = {&O_.ax, &O_.ay, &O_.az, &O_.awx, &O_.awy, &O_.awz, &O_.vhx, &O_.vhy, &O_.vhz,
                             &O_.whx, &O_.why, &O_.whz, &O_.hqw, &O_.hqx, &O_.hqy, &O_.hqz};
@@ -374,6 +383,7 @@ public:
         R_.relf = arena_.alloc<float4>(nc_, "rec relf");
 
         // ---- walls, bodies, triangles
+        W_.count = (int)(wo.size() / 3);
         W_.o = upd(wo, "wall origin"); W_.n = upd(wn, "wall normal");
         {
             std::vector<float4> pl(wo.size() / 3);
@@ -428,6 +438,7 @@ public:
         K_.pcontacts = cnt; K_.pover = cnt + 1; K_.bover = cnt + 2; K_.phigh = cnt + 3; K_.bhigh = cnt + 4;
         K_.tgover = cnt + 5; K_.ct_total = cnt + 6; K_.pt_total = cnt + 7; K_.step = cnt + 8;
         K_.pt_ctotal = cnt + 9;
+        K_.wl_total = cnt + 10;
         K_.pt_warp_items = kDefaultPtWarpItems;
 
         // ---- scene constants
@@ -495,6 +506,7 @@ public:
         check(cudaMemsetAsync(ct.off, 0, nc_ * sizeof(int), s), "clear");
         ct.wres = arena_.alloc<double>((size_t)nc_ * 6, "wall results");
         ct.wflag = arena_.alloc<unsigned char>(nc_, "wall flags");
+        ct.wlist = arena_.alloc<int2>(nc_, "wall candidates");
         check(cudaMemsetAsync(ct.wflag, 0, nc_, s), "clear");
         check(cudaMemsetAsync(ct.wres, 0, (size_t)nc_ * 6 * sizeof(double), s), "clear");
         ct.pt_index = arena_.alloc<int>(nc_, "pt index");
@@ -532,7 +544,8 @@ public:
         if (O_.ugx) launch_universal_gravity(O_, s);
         launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
         mark();
-        for (int stage : {1, 2, 4, 8}) {
+        // sweep (with the history expiry), walls, particle law, bodies
+        for (int stage : {2, 1, 4, 8}) {
             launch_contacts<T, TB>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, s,
                                    stage);
             mark();

@@ -585,7 +585,7 @@ __global__ void k_step_counter(Counters k, int reset)
 {
     if (threadIdx.x != 0) return;
     if (reset) {
-        *k.pcontacts = 0; *k.phigh = 0; *k.bhigh = 0; *k.ct_total = 0; *k.tgover = 0;
+        *k.pcontacts = 0; *k.phigh = 0; *k.bhigh = 0; *k.ct_total = 0; *k.tgover = 0; *k.wl_total = 0;
     } else {
         *k.step += 1;
     }

@@ -38,6 +38,8 @@ struct Owners {
     double *mass, *ix, *iy, *iz, *radius;
     double *inv_mass, *inv_ix, *inv_iy, *inv_iz;
     double* mg;  // [n][3] field force m*g of the owner's scene (0 without gravity)
+    unsigned char* iso;  // isotropic inertia (Ix == Iy == Iz): no gyroscopic terms
+    float* inv_i_f;      // FP32 inverse inertia of isotropic owners (mixed form)
     int *id, *status, *scene;
     double *ugx, *ugy, *ugz;  // universal-gravitation field force (optional)
 };
@@ -111,6 +113,7 @@ template <typename T> struct Hist {
 };
 
 struct Walls {
+    int count;      // walls of all scenes
     double *o, *n;  // [nw][3]
     float4* plane;  // [nw] FP32 (normal, normal . origin) for the prefilter
 };
@@ -143,6 +146,7 @@ struct Counters {
     int* ct_total;      // contacts this step
     int* pt_total;      // PT components this step
     int* pt_ctotal;     // PT components touching a triangle this step
+    int* wl_total;      // components with a candidate wall this step
     int* step;          // contact step index
     int pt_warp_items;  // PT: warp-per-item kernel up to this many contact items
 };
@@ -154,6 +158,7 @@ template <typename T> struct Contacts {
     int capacity;
     double* wres;   // [c][6] wall force/torque per component (valid where wflag)
     unsigned char* wflag;  // per component: nonzero wall force/torque this step
+    int2* wlist;           // components with a candidate wall: (component, wall mask)
     int* pt_index;  // per component: contact item or -1
     int* pt_flag;   // per sorted position
     int* pt_pos;    // scan of pt_flag
