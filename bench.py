@@ -128,8 +128,6 @@ KERNEL_BYTES = {
     # per owner: count, flags, field force, inverse mass and inertia,
     # quaternion, omega, accelerations; result rows 24 per side
     "owner_sum": ("k_owner_sum", lambda n, s, hv: n * 196 + s * 24),
-    # per component: owner and scene 8, position and radius 32, wall flag 1
-    "walls": ("k_walls", lambda n, s, hv: n * 41),
 }
 
 
