@@ -40,6 +40,11 @@ def make_scene(config, particles=None):
     if config == "c0":
         n = particles or 20000
         return G.pure_dem(n=n, seed=1000), "pure DEM, %d spheres r~U[1.8,2.2] mm on a lattice, 5 walls, dt 1e-5" % n
+    if config == "c4":
+        scenes = G.batch(settled=True)
+        n = sum(sc.n for sc in scenes)
+        return scenes, ("256 independent box scenes (0.1 x 0.1 x 0.4 m, 5 walls), N_s ~ U[2000, 40000], "
+                        "%d spheres in total, per-scene friction and restitution, settled in columns, one engine" % n)
     if config == "c2":
         n = particles or 2000000
         sc, _ = G.drum(n=n, seed=1002)
@@ -259,16 +264,32 @@ def drum_summary(steps, warmup):
     return out
 
 
+def batch_summary(steps, warmup):
+    """The 256-scene batch (config 4) in both precisions: every scene advances
+    in the same graph launch per step."""
+    scenes, desc = make_scene("c4")
+    n = sum(sc.n for sc in scenes)
+    out = {"workload": desc, "scenes": len(scenes), "particles": n}
+    for prec in ("mixed", "fp64"):
+        e, ms, clocks, stats, phases, _ = run_engine(scenes, prec, steps, warmup)
+        out[prec] = {"value": n * steps / (ms / 1000.0), "ms_per_step": ms / steps,
+                     "contact_sides_per_step": stats["particle_contacts"], "phase_ms": dict(zip(PHASES, phases)),
+                     "clocks": clocks}
+        del e
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c4"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-drum", action="store_true", help="skip the embedded 2M-sphere drum summary")
+    ap.add_argument("--no-batch", action="store_true", help="skip the embedded 256-scene batch summary")
     ap.add_argument("--particles", type=int, default=None,
                     help="particle count of the generated scene (profiling captures of a smaller case)")
     ap.add_argument("--single", action="store_true",
@@ -284,6 +305,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
     scene, desc = make_scene(args.config, args.particles)
+    if isinstance(scene, list) and not args.single:
+        ap.error("--config c4 runs with --single; the default line carries it as batch_256")
 
     if args.impl == "reference":
         # The reference's own hot path is CUDA-only; its CPU implementation of
@@ -317,7 +340,8 @@ def main():
         dist.barrier()
     e, ms, clocks, stats, phases, _ = run_engine(scene, args.precision, args.steps, args.warmup)
     if args.single:
-        print(json.dumps({"metric": "particle-steps/s", "value": scene.n * args.steps / (ms / 1000.0),
+        n_total = sum(sc.n for sc in scene) if isinstance(scene, list) else scene.n
+        print(json.dumps({"metric": "particle-steps/s", "value": n_total * args.steps / (ms / 1000.0),
                           "ms_per_step": ms / args.steps, "precision": args.precision,
                           "phase_ms": dict(zip(PHASES, phases)),
                           "contact_sides_per_step": stats["particle_contacts"], "clocks": clocks}))
@@ -354,6 +378,9 @@ def main():
     drum = None
     if args.config != "c2" and not args.no_drum:
         drum = drum_summary(args.steps, args.warmup)
+    batch = None
+    if args.config != "c4" and not args.no_batch:
+        batch = batch_summary(args.steps, args.warmup)
     nb = scene.n_bodies
     line = {
         "metric": "particle-steps/s",
@@ -390,6 +417,8 @@ def main():
     }
     if drum:
         line["drum_2m"] = drum
+    if batch:
+        line["batch_256"] = batch
     print(json.dumps(line))
 
 

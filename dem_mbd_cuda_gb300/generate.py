@@ -409,16 +409,44 @@ def drum(n=2000000, seed=1002, radius=0.3, length=0.5, omega=2.0, dt=2e-6, name=
     return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -g), gravity_enabled=1, name=name), [(v, f)]
 
 
-def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5):
+def box_columns(n, seed, rmin=1.8e-3, rmax=2.2e-3, box=(0.1, 0.1, 0.4), dt=1e-5, kN=1e5, epsN=0.5, mu=0.3,
+                name="box_columns"):
+    """A settled bed of n spheres r ~ U[rmin, rmax] in a box of 5 walls
+    (floor + 4 sides): vertical columns in force balance on the floor
+    (``column_bed``)."""
+    rng = np.random.default_rng(seed)
+    g = 9.81
+    pitch, jitter = 2.0 * rmax + 0.2e-3, 0.05e-3
+    cap = 0.5 * pitch - jitter - 1e-6
+    lo = np.array([-box[0] / 2, -box[1] / 2, 0.0])
+    hi = np.array([box[0] / 2, box[1] / 2, box[2]])
+    edge = rmax + 0.2e-3
+    xy = column_grid(lo[:2] + edge, hi[:2] - edge, pitch, jitter, rng)
+    pos, rad, _ = column_bed(n, xy, lambda p, r: r, lambda rg, k: rg.uniform(rmin, rmax, size=k), rng, cap, g, kN, kN)
+    if (pos[:, 2] + rad).max() > hi[2]:
+        raise ValueError("column bed exceeds the box height")
+    kw = make_spheres(pos, rad, DENSITY)
+    wo, wn = box_walls(lo, hi)
+    m = mech(kN=kN, epsN=epsN, epsS=epsN, mu=mu)
+    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -g), gravity_enabled=1, wall_origin=wo,
+                 wall_normal=wn, name=name)
+
+
+def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5, settled=False):
     """Config 4: independent box scenes with N_s ~ U[2k, 40k], per-scene
-    friction ~ U[0.1, 0.7] and restitution ~ U[0.2, 0.8]."""
+    friction ~ U[0.1, 0.7] and restitution ~ U[0.2, 0.8], in 0.1 x 0.1 x
+    0.4 m boxes: lattice beds at rest (``settled=False``, they settle during
+    the run) or settled column beds."""
     rng = np.random.default_rng(seed)
     out = []
     for s in range(nscenes):
         ns = int(rng.integers(nmin, nmax + 1))
         mu = float(rng.uniform(0.1, 0.7))
         e = float(rng.uniform(0.2, 0.8))
-        sc = pure_dem(n=ns, seed=seed * 1000 + s, box=(0.1, 0.1, 0.4), dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}")
+        if settled:
+            sc = box_columns(ns, seed * 1000 + s, dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}")
+        else:
+            sc = pure_dem(n=ns, seed=seed * 1000 + s, box=(0.1, 0.1, 0.4), dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}")
         out.append(sc)
     return out
 
