@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdemgb300.so")
-SOURCES = ["dem_grid.cu", "dem_contact.cu", "dem_engine.cu", "dem_static_sort.cu"]
+SOURCES = ["dem_grid.cu", "dem_contact.cu", "dem_engine.cu", "dem_static_sort.cu", "dem_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wno-format-truncation",
          "--expt-relaxed-constexpr"]

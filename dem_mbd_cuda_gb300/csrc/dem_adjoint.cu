@@ -1,0 +1,371 @@
+// dem_adjoint.cu -- reverse sweep of the FP64 step: kernels.
+//
+// One step of the engine maps the owner state S_s (29 values per owner,
+// layout below) and the contact history to S_{s+1}:
+//   advance  x1 = x + vh dt, q1 = N(q + hq dt), v1 = vh + a dt/2, w1 = wh + aw dt/2
+//            (advancePositionKernel, src/cuda/cuda_particle_backend.cu:212-237)
+//   forces   a1, aw1 from the contact laws at (x1, q1, v1, w1) with the
+//            midpoint velocities (vh, wh) (computeContactsKernel and
+//            accelerationKernel, src/cuda/cuda_contact_backend.cu:1082-1220,
+//            src/cuda/cuda_particle_backend.cu:71-101)
+//   finish   vh1 = vh + a1 dt, wh1 = wh + aw1 dt,
+//            hq1 = G(N(q1 + dt/2 G(q1, w1)), wh1)  (advanceHalfVelocityKernel,
+//            :239-265)
+// The reverse sweep runs, per step: k_adj_finish (finish^T and the owner
+// part of forces^T), k_adj_pp and k_adj_pw (the contact laws, scattering
+// into the owners with FP64 atomics), k_adj_advance (advance^T).  The
+// history adjoints live in the reference's slot layout, so a contact that
+// persists keeps its slot and its adjoint; a slot acquired new in the step
+// gets a zero adjoint before it.  Spheres only (one component per owner,
+// isotropic inertia), no rigid bodies.
+#include "dem_adjoint.cuh"
+#include "dem_kernels.cuh"
+
+namespace demgb {
+
+namespace {
+
+inline int nblocks(int n, int b) { return (n + b - 1) / b; }
+
+__device__ __forceinline__ D3 ld3(const double* A, int f, int n, int i)
+{
+    return mk(A[(size_t)f * n + i], A[(size_t)(f + 1) * n + i], A[(size_t)(f + 2) * n + i]);
+}
+__device__ __forceinline__ void st3(double* A, int f, int n, int i, D3 v)
+{
+    A[(size_t)f * n + i] = v.x; A[(size_t)(f + 1) * n + i] = v.y; A[(size_t)(f + 2) * n + i] = v.z;
+}
+__device__ __forceinline__ void ld4(const double* A, int f, int n, int i, double q[4])
+{
+    for (int k = 0; k < 4; ++k) q[k] = A[(size_t)(f + k) * n + i];
+}
+__device__ __forceinline__ void st4(double* A, int f, int n, int i, const double q[4])
+{
+    for (int k = 0; k < 4; ++k) A[(size_t)(f + k) * n + i] = q[k];
+}
+__device__ __forceinline__ void add3(double* A, int f, int n, int i, D3 v)
+{
+    atomicAdd(A + (size_t)f * n + i, v.x);
+    atomicAdd(A + (size_t)(f + 1) * n + i, v.y);
+    atomicAdd(A + (size_t)(f + 2) * n + i, v.z);
+}
+__device__ __forceinline__ void add4(double* A, int f, int n, int i, const double q[4])
+{
+    for (int k = 0; k < 4; ++k) atomicAdd(A + (size_t)(f + k) * n + i, q[k]);
+}
+__device__ __forceinline__ void normq(double q[4])
+{
+    const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (n2 <= 1.0e-24) { q[0] = 1.0; q[1] = q[2] = q[3] = 0.0; return; }
+    const double inv = rsqrt(n2);
+    for (int k = 0; k < 4; ++k) q[k] *= inv;
+}
+
+// The post-advance state of owner i from S_s (and the midpoint velocities
+// the laws use: vh, wh, or the endpoint ones when there is no midpoint).
+__device__ void post_advance(const double* S, int n, int i, double dt, bool moves, bool mid, D3& x1, double q1[4], D3& v1,
+                             D3& w1, D3& mv, D3& mw)
+{
+    const D3 x = ld3(S, kAdjX, n, i), vh = ld3(S, kAdjVH, n, i), wh = ld3(S, kAdjWH, n, i);
+    double q[4], hq[4];
+    ld4(S, kAdjQ, n, i, q);
+    ld4(S, kAdjHQ, n, i, hq);
+    if (moves) {
+        x1 = x + vh * dt;
+        for (int k = 0; k < 4; ++k) q1[k] = q[k] + hq[k] * dt;
+        normq(q1);
+        v1 = vh + ld3(S, kAdjA, n, i) * (0.5 * dt);
+        w1 = wh + ld3(S, kAdjAW, n, i) * (0.5 * dt);
+    } else {
+        x1 = x;
+        for (int k = 0; k < 4; ++k) q1[k] = q[k];
+        v1 = ld3(S, kAdjV, n, i);
+        w1 = ld3(S, kAdjW, n, i);
+    }
+    mv = mid ? vh : v1;
+    mw = mid ? wh : w1;
+}
+
+}  // namespace
+
+// Owner state of the engine -> [29][n].
+__global__ void k_adj_snapshot(Owners o, double* S)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = o.n;
+    if (i >= n) return;
+    const double* src[kAdjFields] = {o.px, o.py, o.pz, o.qw, o.qx, o.qy, o.qz, o.vx, o.vy, o.vz, o.wx,
+                                     o.wy, o.wz, o.vhx, o.vhy, o.vhz, o.whx, o.why, o.whz, o.hqw, o.hqx, o.hqy,
+                                     o.hqz, o.ax, o.ay, o.az, o.awx, o.awy, o.awz};
+    for (int f = 0; f < kAdjFields; ++f) S[(size_t)f * n + i] = src[f][i];
+}
+__global__ void k_adj_restore(Owners o, const double* S)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = o.n;
+    if (i >= n) return;
+    double* dst[kAdjFields] = {o.px, o.py, o.pz, o.qw, o.qx, o.qy, o.qz, o.vx, o.vy, o.vz, o.wx,
+                               o.wy, o.wz, o.vhx, o.vhy, o.vhz, o.whx, o.why, o.whz, o.hqw, o.hqx, o.hqy,
+                               o.hqz, o.ax, o.ay, o.az, o.awx, o.awy, o.awz};
+    for (int f = 0; f < kAdjFields; ++f) dst[f][i] = S[(size_t)f * n + i];
+}
+
+// finish^T and the owner part of forces^T for step s: S = S_s, S1 = S_{s+1},
+// L = adjoint of S_{s+1} (in), Lp = adjoint of S_s (vh, wh partials out),
+// P = post-advance state, T = adjoints of the post-advance state, of the
+// midpoint velocities (zeroed, filled by the contact kernels), and of the
+// total force and torque.  With init = 1 the step is the first evaluation
+// (dt = 0, no advance, no midpoint) followed by initializeLeapfrogKernel
+// (:185-210) with half step h: L is then the adjoint of S_0.
+__global__ void k_adj_finish(Owners o, const double* S, const double* S1, const double* L, double* Lp, double* P,
+                             double* T, double dt, int init)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = o.n;
+    if (i >= n) return;
+    const bool moves = !init && o.status[i] != -1;
+    const bool mid = !init && o.status[i] != -1;
+    D3 x1, v1, w1, mv, mw;
+    double q1[4];
+    post_advance(S, n, i, dt, moves, mid, x1, q1, v1, w1, mv, mw);
+    st3(P, kPX, n, i, x1); st4(P, kPQ, n, i, q1); st3(P, kPV, n, i, v1); st3(P, kPW, n, i, w1);
+    st3(P, kPMV, n, i, mv); st3(P, kPMW, n, i, mw);
+    // S1's finish half: the half step h = dt/2 of the finish, or the
+    // leapfrog start's half step (dt holds it when init)
+    const double h = init ? dt : 0.5 * dt;
+    const double dtv = dt;  // velocity increment: the step, or the start's half step when init
+    const D3 wh1 = ld3(S1, kAdjWH, n, i);
+    double lhq[4], lp[4] = {0, 0, 0, 0}, ls[4] = {0, 0, 0, 0}, lq1[4];
+    ld4(L, kAdjHQ, n, i, lhq);
+    // hq1 = G(p, wh1), p = N(s), s = q1 + h G(q1, w1)
+    double s[4], g[4];
+    quatd(q1, w1, g);
+    for (int k = 0; k < 4; ++k) s[k] = q1[k] + g[k] * h;
+    double p[4] = {s[0], s[1], s[2], s[3]};
+    normq(p);
+    D3 lwh1 = ld3(L, kAdjWH, n, i);
+    quatd_vjp(p, wh1, lhq, lp, lwh1);
+    normq_vjp(s, lp, ls);
+    ld4(L, kAdjQ, n, i, lq1);
+    D3 lw1 = ld3(L, kAdjW, n, i);
+    for (int k = 0; k < 4; ++k) lq1[k] += ls[k];
+    double lsh[4];
+    for (int k = 0; k < 4; ++k) lsh[k] = ls[k] * h;
+    quatd_vjp(q1, w1, lsh, lq1, lw1);
+    // vh1 = vh + a1 dt (or v0 + a0 h), wh1 likewise
+    const D3 lvh1 = ld3(L, kAdjVH, n, i);
+    const D3 la1 = ld3(L, kAdjA, n, i) + lvh1 * dtv;
+    const D3 law1 = ld3(L, kAdjAW, n, i) + lwh1 * dtv;
+    D3 lv1 = ld3(L, kAdjV, n, i);
+    if (init) {
+        // the start adds vh0 = v0 + a0 h, wh0 = w0 + aw0 h
+        lv1 = lv1 + lvh1;
+        lw1 = lw1 + lwh1;
+        st3(Lp, kAdjVH, n, i, z3());
+        st3(Lp, kAdjWH, n, i, z3());
+    } else {
+        st3(Lp, kAdjVH, n, i, lvh1);
+        st3(Lp, kAdjWH, n, i, lwh1);
+    }
+    // forces^T, owner part: a1 = F / m, aw1 = R(q1)^T tau / I (isotropic)
+    const double m = o.mass[i], I = o.ix[i];
+    const D3 lF = la1 * (1.0 / m);
+    const D3 aw1 = ld3(S1, kAdjAW, n, i);
+    const D3 tau = rotq(q1, aw1) * I;
+    D3 ltau = z3();
+    rotq_t_vjp(q1, tau, law1 * (1.0 / I), lq1, ltau);
+    st3(T, kTX, n, i, ld3(L, kAdjX, n, i));
+    st4(T, kTQ, n, i, lq1);
+    st3(T, kTV, n, i, lv1);
+    st3(T, kTW, n, i, lw1);
+    st3(T, kTMV, n, i, z3());
+    st3(T, kTMW, n, i, z3());
+    st3(T, kTF, n, i, lF);
+    st3(T, kTTau, n, i, ltau);
+}
+
+// Particle contact sides of one step (tape entries), reverse.
+__global__ void k_adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTape tp, int count, const double* P,
+                         double* T, double* lhist, double dt_eff, double* grads)
+{
+    const int n = o.n;
+    __shared__ double sg[kAdjParams];
+    if (threadIdx.x < kAdjParams) sg[threadIdx.x] = 0.0;
+    __syncthreads();
+    MatGrad gsum = {0, 0, 0, 0, 0, 0};
+    const MatC& m = sc[0].pp;   // one scene (checked by the engine)
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int4 e = tp.pp[k];
+        const int i = e.x, j = e.y;
+        D3 xi = ld3(P, kPX, n, i), xj = ld3(P, kPX, n, j);
+        double qi[4], qj[4];
+        ld4(P, kPQ, n, i, qi);
+        ld4(P, kPQ, n, j, qj);
+        const D3 vi = ld3(P, kPV, n, i), vj = ld3(P, kPV, n, j), wi = ld3(P, kPW, n, i), wj = ld3(P, kPW, n, j);
+        const D3 mvi = ld3(P, kPMV, n, i), mvj = ld3(P, kPMV, n, j), mwbi = ld3(P, kPMW, n, i), mwbj = ld3(P, kPMW, n, j);
+        PPIn in;
+        in.delta = xj - xi;
+        in.ri = c.radius[i]; in.rj = c.radius[j]; in.mi = o.mass[i]; in.mj = o.mass[j];
+        in.erv = vj - vi;
+        in.mrv = mvj - mvi;
+        in.ewi = rotq(qi, wi); in.ewj = rotq(qj, wj);
+        in.mwi = rotq(qi, mwbi); in.mwj = rotq(qj, mwbj);
+        for (int a = 0; a < 9; ++a) in.h[a] = tp.pp_h[(size_t)k * kHV + a];
+        double* lh = lhist + (size_t)e.z * kHV;
+        double lho[9];
+        for (int a = 0; a < 9; ++a) lho[a] = lh[a];
+        PPAdj ad;
+        ad.delta = ad.erv = ad.mrv = ad.ewi = ad.ewj = ad.mwi = ad.mwj = z3();
+        for (int a = 0; a < 9; ++a) ad.h[a] = 0.0;
+        pp_law_vjp(m, dt_eff, in, ld3(T, kTF, n, i), ld3(T, kTTau, n, i), lho, ad, gsum);
+        for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : ad.h[a];
+        add3(T, kTX, n, j, ad.delta);
+        add3(T, kTX, n, i, ad.delta * -1.0);
+        add3(T, kTV, n, j, ad.erv);
+        add3(T, kTV, n, i, ad.erv * -1.0);
+        add3(T, kTMV, n, j, ad.mrv);
+        add3(T, kTMV, n, i, ad.mrv * -1.0);
+        double lq[4] = {0, 0, 0, 0};
+        D3 lw = z3(), lmw = z3();
+        rotq_vjp(qi, wi, ad.ewi, lq, lw);
+        rotq_vjp(qi, mwbi, ad.mwi, lq, lmw);
+        add4(T, kTQ, n, i, lq);
+        add3(T, kTW, n, i, lw);
+        add3(T, kTMW, n, i, lmw);
+        double lqj[4] = {0, 0, 0, 0};
+        D3 lwj = z3(), lmwj = z3();
+        rotq_vjp(qj, wj, ad.ewj, lqj, lwj);
+        rotq_vjp(qj, mwbj, ad.mwj, lqj, lmwj);
+        add4(T, kTQ, n, j, lqj);
+        add3(T, kTW, n, j, lwj);
+        add3(T, kTMW, n, j, lmwj);
+    }
+    const double gv[kAdjParams] = {gsum.kN, gsum.mu, gsum.logN, gsum.logS, gsum.muT, gsum.muR};
+    for (int f = 0; f < kAdjParams; ++f) atomicAdd(sg + f, gv[f]);
+    __syncthreads();
+    if (threadIdx.x < kAdjParams) atomicAdd(grads + threadIdx.x, sg[threadIdx.x]);
+}
+
+__device__ void pw_one(const Comps& c, const Owners& o, const SceneC& S, const Walls& walls, const StepTape& tp, int k,
+                       const double* P, double* T, double* lhist, double dt_eff, MatGrad& g)
+{
+    const int n = o.n;
+    const int4 e = tp.pw[k];
+    const int i = e.x;
+    const int wg = S.wall_begin + e.y;
+    const D3 out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
+    const D3 org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
+    const D3 x1 = ld3(P, kPX, n, i), v1 = ld3(P, kPV, n, i), w1 = ld3(P, kPW, n, i);
+    double q1[4];
+    ld4(P, kPQ, n, i, q1);
+    const double r = c.radius[i];
+    const double depth = r - dot(x1 - org, out);
+    const D3 om = rotq(q1, w1);
+    double hin[9], lho[9];
+    for (int a = 0; a < 9; ++a) hin[a] = tp.pw_h[(size_t)k * kHV + a];
+    double* lh = lhist + (size_t)e.z * kHV;
+    for (int a = 0; a < 9; ++a) lho[a] = lh[a];
+    PWAdj ad;
+    ad.p = ad.vel = ad.om = z3();
+    for (int a = 0; a < 9; ++a) ad.h[a] = 0.0;
+    pw_law_vjp(S.pw, dt_eff, out, depth, r, o.mass[i], v1, om, hin, ld3(T, kTF, n, i), ld3(T, kTTau, n, i), lho, ad, g);
+    for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : ad.h[a];
+    add3(T, kTX, n, i, ad.p);
+    add3(T, kTV, n, i, ad.vel);
+    double lq[4] = {0, 0, 0, 0};
+    D3 lw = z3();
+    rotq_vjp(q1, w1, ad.om, lq, lw);
+    add4(T, kTQ, n, i, lq);
+    add3(T, kTW, n, i, lw);
+}
+
+// Wall contacts of one step (tape entries), reverse.
+__global__ void k_adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls, StepTape tp, int count,
+                         const double* P, double* T, double* lhist, double dt_eff, double* grads)
+{
+    const int n = o.n;
+    __shared__ double sg[kAdjParams];
+    if (threadIdx.x < kAdjParams) sg[threadIdx.x] = 0.0;
+    __syncthreads();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    MatGrad g = {0, 0, 0, 0, 0, 0};
+    if (k < count) pw_one(c, o, sc[0], walls, tp, k, P, T, lhist, dt_eff, g);
+    const double gv[kAdjParams] = {g.kN, g.mu, g.logN, g.logS, g.muT, g.muR};
+    for (int f = 0; f < kAdjParams; ++f) atomicAdd(sg + f, gv[f]);
+    __syncthreads();
+    if (threadIdx.x < kAdjParams) atomicAdd(grads + kAdjParams + threadIdx.x, sg[threadIdx.x]);
+}
+
+
+// advance^T: T (complete) and the vh, wh partials of Lp -> Lp = adjoint of
+// S_s.  With init = 1 (the first evaluation, no advance): Lp = adjoint of
+// the initial x, q, v, w.
+__global__ void k_adj_advance(Owners o, const double* S, const double* T, double* Lp, double dt, int init)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = o.n;
+    if (i >= n) return;
+    const D3 lx1 = ld3(T, kTX, n, i), lv1 = ld3(T, kTV, n, i), lw1 = ld3(T, kTW, n, i);
+    const D3 lmv = ld3(T, kTMV, n, i), lmw = ld3(T, kTMW, n, i);
+    double lq1[4];
+    ld4(T, kTQ, n, i, lq1);
+    const bool moves = !init && o.status[i] != -1;
+    double zero4[4] = {0, 0, 0, 0};
+    if (!moves) {
+        // no advance and no midpoint: the laws saw x, q, v, w themselves
+        st3(Lp, kAdjX, n, i, lx1);
+        st4(Lp, kAdjQ, n, i, lq1);
+        st3(Lp, kAdjV, n, i, lv1 + lmv);
+        st3(Lp, kAdjW, n, i, lw1 + lmw);
+        if (!init) {
+            st3(Lp, kAdjVH, n, i, ld3(Lp, kAdjVH, n, i));
+            st3(Lp, kAdjWH, n, i, ld3(Lp, kAdjWH, n, i));
+        }
+        st4(Lp, kAdjHQ, n, i, zero4);
+        st3(Lp, kAdjA, n, i, z3());
+        st3(Lp, kAdjAW, n, i, z3());
+        return;
+    }
+    double q[4], hq[4];
+    ld4(S, kAdjQ, n, i, q);
+    ld4(S, kAdjHQ, n, i, hq);
+    double r[4], lr[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; ++k) r[k] = q[k] + hq[k] * dt;
+    normq_vjp(r, lq1, lr);
+    D3 lvh = ld3(Lp, kAdjVH, n, i) + lmv + lx1 * dt + lv1;
+    D3 lwh = ld3(Lp, kAdjWH, n, i) + lmw + lw1;
+    st3(Lp, kAdjX, n, i, lx1);
+    st4(Lp, kAdjQ, n, i, lr);
+    double lhq[4];
+    for (int k = 0; k < 4; ++k) lhq[k] = lr[k] * dt;
+    st4(Lp, kAdjHQ, n, i, lhq);
+    st3(Lp, kAdjV, n, i, z3());
+    st3(Lp, kAdjW, n, i, z3());
+    st3(Lp, kAdjVH, n, i, lvh);
+    st3(Lp, kAdjWH, n, i, lwh);
+    st3(Lp, kAdjA, n, i, lv1 * (0.5 * dt));
+    st3(Lp, kAdjAW, n, i, lw1 * (0.5 * dt));
+}
+
+// ---------------------------------------------------------- launchers
+void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s)
+{
+    if (o.n > 0) k_adj_snapshot<<<nblocks(o.n, 256), 256, 0, s>>>(o, S);
+}
+void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s)
+{
+    if (o.n > 0) k_adj_restore<<<nblocks(o.n, 256), 256, 0, s>>>(o, S);
+}
+void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
+                     int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
+                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int sm_count,
+                     cudaStream_t s)
+{
+    if (o.n <= 0) return;
+    k_adj_finish<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init);
+    if (npp > 0) k_adj_pp<<<min(nblocks(npp, 128), sm_count * 16), 128, 0, s>>>(c, o, sc, tp, npp, P, T, lh_pp, dt_eff, grads);
+    if (npw > 0) k_adj_pw<<<nblocks(npw, 128), 128, 0, s>>>(c, o, sc, w, tp, npw, P, T, lh_pw, dt_eff, grads);
+    k_adj_advance<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, T, Lp, dt, init);
+}
+
+}  // namespace demgb

@@ -152,8 +152,9 @@ template <typename T> __device__ void expire(Hist<T> h, int slots, int c, int st
 // acquireHistorySlot (:190-215): the matching key, else the first empty slot.
 // Returns the slot index within the component, -1 on overflow.
 template <typename T>
-__device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int& hw, int& high)
+__device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int& hw, int& high, bool* fresh = nullptr)
 {
+    if (fresh) *fresh = false;
     const size_t base = (size_t)c * slots;
     int empty = -1;
     for (int s = 0; s < hw; ++s) {
@@ -172,6 +173,7 @@ __device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int&
     h.key[base + empty] = key;
     h.last[base + empty] = step;
     zero_hv(h.val + (base + empty) * kHV);
+    if (fresh) *fresh = true;
     if (empty + 1 > hw) hw = empty + 1;
     high = max(high, empty + 1);
     return empty;
@@ -239,16 +241,26 @@ template <typename T>
 __device__ __noinline__ void wall_contact(const Comps& c, const Owners& o, const SceneC& S, const Walls& walls,
                                           Hist<T> hw, int ci, int w, int wl, V3<double> p, double rad, int step,
                                           double dt_eff, int& whw, int& bhigh, int& bover, V3<double>& wF,
-                                          V3<double>& wT)
+                                          V3<double>& wT, const StepTape& tape)
 {
     const int wg = S.wall_begin + wl;
     const V3<double> out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
     const V3<double> org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
     const double depth = rad - dot(p - org, out);
     if (depth <= 0.0) return;
-    const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh);
+    bool fresh;
+    const int slot = acquire(hw, kWSlots, ci, (uint64_t)wl + 1ull, step, whw, bhigh, &fresh);
     if (slot < 0) { ++bover; return; }
     T* hv = hw.val + ((size_t)ci * kWSlots + slot) * kHV;
+    if (tape.pw) {
+        const int k = atomicAdd(tape.pw_count, 1);
+        if (k < tape.pw_cap) {
+            tape.pw[k] = make_int4(ci, wl, ci * kWSlots + slot, fresh ? 1 : 0);
+            for (int a = 0; a < kHV; ++a) tape.pw_h[(size_t)k * kHV + a] = (double)hv[a];
+        } else {
+            atomicOr(tape.overflow, 2);
+        }
+    }
     const V3<double> vel = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
     const V3<double> om = rot_iv(o.qw[w], o.qx[w], o.qy[w], o.qz[w], mk(o.wx[w], o.wy[w], o.wz[w]));
     const V3<double> off = c.ox ? mk(c.ox[ci], c.oy[ci], c.oz[ci]) : mk(0.0, 0.0, 0.0);
@@ -325,9 +337,10 @@ __global__ void __launch_bounds__(128) k_walls_law(Comps c, Owners o, const Scen
         V3<double> wF = mk(0.0, 0.0, 0.0), wT = mk(0.0, 0.0, 0.0);
         int whw = hw.hw[ci];
         for (; cand; cand &= cand - 1u)
-            wall_contact<T>(c, o, S, walls, hw, ci, w, __ffs(cand) - 1, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT);
+            wall_contact<T>(c, o, S, walls, hw, ci, w, __ffs(cand) - 1, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT,
+                            ct.tape);
         for (int wl = 32; wl < S.wall_count; ++wl)
-            wall_contact<T>(c, o, S, walls, hw, ci, w, wl, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT);
+            wall_contact<T>(c, o, S, walls, hw, ci, w, wl, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT, ct.tape);
         hw.hw[ci] = whw;
         const bool hit = wF.x != 0.0 || wF.y != 0.0 || wF.z != 0.0 || wT.x != 0.0 || wT.y != 0.0 || wT.z != 0.0;
         if (hit) {
@@ -338,6 +351,23 @@ __global__ void __launch_bounds__(128) k_walls_law(Comps c, Owners o, const Scen
     }
     block_add(k.bover, bover);
     block_max(k.bhigh, bhigh);
+}
+
+// Adjoint tape of the particle contacts of this step (FP64 form), between
+// the sweep and the law: component, partner, history slot index, new flag,
+// and the slot's history before the law updates it.
+template <typename T>
+__global__ void k_tape_pp(Recs r, Hist<T> hp, Contacts<T> ct, Counters k)
+{
+    const int total = *k.ct_total;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && total > ct.tape.pp_cap) atomicOr(ct.tape.overflow, 1);
+    const int n = min(total, ct.tape.pp_cap);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int4 e = ct.ent[q];
+        ct.tape.pp[q] = make_int4(r.meta[e.x].x, r.meta[e.y].x, e.z, ct.tape.pp_new[q]);
+        const T* hv = hp.val + (size_t)e.z * kHV;
+        for (int a = 0; a < kHV; ++a) ct.tape.pp_h[(size_t)q * kHV + a] = (double)hv[a];
+    }
 }
 
 // ------------------------------------------------------------- particle sweep
@@ -421,10 +451,11 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
                     continue;
                 }
                 if (count >= kMaxContacts) { ++pover; continue; }
-                const int slot = acquire(hp, kPSlots, ci, (uint64_t)(uint32_t)cid + 1ull, step, phw, phigh);
+                bool fresh;
+                const int slot = acquire(hp, kPSlots, ci, (uint64_t)(uint32_t)cid + 1ull, step, phw, phigh, &fresh);
                 if (slot < 0) { ++pover; continue; }
                 stage_t[count] = u;
-                stage_s[count] = slot;
+                stage_s[count] = slot | (fresh ? 0x100 : 0);
                 ++count;
             }
             pending = 0;
@@ -487,8 +518,10 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     if (threadIdx.x == 0) s_base = total ? atomicAdd(k.ct_total, total) : 0;
     __syncthreads();
     const int base = s_base + ex;
-    for (int q = 0; q < count; ++q)
-        ct.ent[base + q] = make_int4(t, stage_t[q], ci * kPSlots + stage_s[q], q * nc + ci);
+    for (int q = 0; q < count; ++q) {
+        ct.ent[base + q] = make_int4(t, stage_t[q], ci * kPSlots + (stage_s[q] & 0xff), q * nc + ci);
+        if (ct.tape.pp_new) ct.tape.pp_new[base + q] = (unsigned char)(stage_s[q] >> 8);
+    }
     block_add(k.pcontacts, count);
     block_add(k.pover, pover);
     block_max(k.phigh, phigh);
@@ -1433,7 +1466,10 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
                      const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s, int stage)
 {
     (void)block;
-    if (stage & 2) k_sweep<T, TB><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, hw, hb, ct, k, c.n);
+    if (stage & 2) {
+        k_sweep<T, TB><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, hw, hb, ct, k, c.n);
+        if (ct.tape.pp) k_tape_pp<T><<<sm_count * 8, 256, 0, s>>>(r, hp, ct, k);
+    }
     if ((stage & 1) && w.count > 0) {
         k_walls_probe<<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, ct.wflag, ct.wlist, k.wl_total);
         k_walls_law<T><<<sm_count * 4, 128, 0, s>>>(c, o, sc, w, hw, ct, k, dt_eff);

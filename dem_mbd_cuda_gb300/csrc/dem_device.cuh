@@ -12,7 +12,10 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#define DEM_DEV __device__ __forceinline__
+// Law helpers compile for the host too, so their adjoints can be checked
+// against finite differences on the CPU; only the overlap predicate, which
+// pins a device contraction, is device-only.
+#define DEM_DEV __host__ __device__ __forceinline__
 
 namespace demgb {
 
@@ -52,7 +55,7 @@ template <typename T, typename S> DEM_DEV V3<T> cvt(V3<S> a) { return {cv<T>(a.x
 // Overlap predicate operand with a fixed contraction pattern so the contact
 // set is decided by the same bits as the oracle and the reference build:
 // fma(dz, dz, fma(dy, dy, dx * dx)).
-DEM_DEV double distance_squared(V3<double> d)
+__device__ __forceinline__ double distance_squared(V3<double> d)
 {
     return __fma_rn(d.z, d.z, __fma_rn(d.y, d.y, __dmul_rn(d.x, d.x)));
 }

@@ -305,6 +305,7 @@ public:
                 iif[i] = (float)(1.0 / I[0]);
             }
             O_.iso = arena_.upload(iso.data(), iso.size(), "isotropic flags", s);
+            oin_host_ = oin;
             O_.inv_i_f = arena_.upload(iif.data(), iif.size(), "fp32 inverse inertia", s);
         }
         double** zeros[] = {&O_.ax, &O_.ay, &O_.az, &O_.awx, &O_.awy, &O_.awz, &O_.vhx, &O_.vhy, &O_.vhz,
@@ -1146,6 +1147,244 @@ public:
         if (!sphere_) { launch_update_components(C_, O_, stream_); check(cudaStreamSynchronize(stream_), "sync"); }
     }
 
+    // --------------------------------------------------- reverse mode
+    // Gradients of the FP64 step by a hand-written adjoint (dem_adjoint.cu):
+    // the forward run keeps checkpoints every K steps; the backward run
+    // recomputes each segment from its checkpoint with a per-step tape and
+    // sweeps it in reverse.  Spheres, walls and particle contacts in one
+    // scene; no rigid bodies.
+    struct AdjCkpt {
+        double* S = nullptr;                       // owner state [29][n]
+        uint64_t *pk = nullptr, *wk = nullptr;     // history keys
+        int *pl = nullptr, *wl = nullptr;          // last seen
+        double *pv = nullptr, *wv = nullptr;       // values
+        int *phw = nullptr, *whw = nullptr;        // high-water marks
+        int* step = nullptr;                       // device step counter
+        int step_index = 0;
+        bool started = false;
+    };
+    struct Adjoint {
+        bool ready = false;
+        int steps = 0, K = 0, nseg = 0, cap_pp = 0, cap_pw = 0;
+        std::vector<AdjCkpt> ck;                   // [0] before the first evaluation, [1 + k] after segment k - 1
+        double *S = nullptr;                       // tape of owner states [K + 1][29][n]
+        unsigned char* pp_new = nullptr;
+        int4 *pp = nullptr, *pw = nullptr;         // [K + 1][cap]
+        double *pp_h = nullptr, *pw_h = nullptr;
+        int *pp_cnt = nullptr, *pw_cnt = nullptr, *overflow = nullptr;
+        double *L = nullptr, *Lp = nullptr, *P = nullptr, *T = nullptr, *lh_pp = nullptr, *lh_pw = nullptr;
+        double* grads = nullptr;
+    };
+
+    void adj_require() const
+    {
+        need_init();
+        if (precision_ != DEM_PRECISION_FP64)
+            throw DemError(DEM_ERR_INVALID, "the adjoint runs on the FP64 form (precision DEM_PRECISION_FP64)");
+        if (nb_ > 0) throw DemError(DEM_ERR_INVALID, "the adjoint does not cover rigid bodies");
+        if (!sphere_) throw DemError(DEM_ERR_INVALID, "the adjoint covers spheres (one component per owner)");
+        if (S_ != 1) throw DemError(DEM_ERR_INVALID, "the adjoint covers one scene per engine");
+        for (int i = 0; i < n_; ++i)
+            if (!(oin_host_[3 * (size_t)i] == oin_host_[3 * (size_t)i + 1] &&
+                  oin_host_[3 * (size_t)i + 1] == oin_host_[3 * (size_t)i + 2]))
+                throw DemError(DEM_ERR_INVALID, "the adjoint covers isotropic inertia");
+    }
+    AdjCkpt adj_alloc_ckpt()
+    {
+        AdjCkpt c;
+        const size_t ps = (size_t)nc_ * kPSlots, ws = (size_t)nc_ * kWSlots;
+        c.S = adj_arena_.alloc<double>((size_t)kAdjFields * n_, "adjoint checkpoint");
+        c.pk = adj_arena_.alloc<uint64_t>(ps, "adjoint checkpoint"); c.pl = adj_arena_.alloc<int>(ps, "adjoint checkpoint");
+        c.pv = adj_arena_.alloc<double>(ps * kHV, "adjoint checkpoint"); c.phw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
+        c.wk = adj_arena_.alloc<uint64_t>(ws, "adjoint checkpoint"); c.wl = adj_arena_.alloc<int>(ws, "adjoint checkpoint");
+        c.wv = adj_arena_.alloc<double>(ws * kHV, "adjoint checkpoint"); c.whw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
+        c.step = adj_arena_.alloc<int>(1, "adjoint checkpoint");
+        return c;
+    }
+    void adj_copy_hist(AdjCkpt& c, bool save)
+    {
+        cudaStream_t s = stream_;
+        const size_t ps = (size_t)nc_ * kPSlots, ws = (size_t)nc_ * kWSlots;
+        auto cp = [&](void* ck, void* live, size_t bytes) {
+            check(cudaMemcpyAsync(save ? ck : live, save ? live : ck, bytes, cudaMemcpyDeviceToDevice, s), "adjoint checkpoint");
+        };
+        cp(c.pk, hp64_.key, ps * 8); cp(c.pl, hp64_.last, ps * 4); cp(c.pv, hp64_.val, ps * kHV * 8); cp(c.phw, hp64_.hw, (size_t)nc_ * 4);
+        cp(c.wk, hw64_.key, ws * 8); cp(c.wl, hw64_.last, ws * 4); cp(c.wv, hw64_.val, ws * kHV * 8); cp(c.whw, hw64_.hw, (size_t)nc_ * 4);
+        cp(c.step, K_.step, 4);
+    }
+    void adj_save(AdjCkpt& c)
+    {
+        launch_adj_snapshot(O_, c.S, stream_);
+        adj_copy_hist(c, true);
+        c.step_index = step_index_;
+        c.started = started_;
+    }
+    void adj_restore(AdjCkpt& c)
+    {
+        launch_adj_restore(O_, c.S, stream_);
+        adj_copy_hist(c, false);
+        step_index_ = c.step_index;
+        started_ = c.started;
+    }
+
+    // dem_adjoint_forward: the first evaluation, the leapfrog start and
+    // `steps` steps, keeping a checkpoint every K steps.
+    void adjoint_forward(int steps, int K)
+    {
+        adj_require();
+        if (steps < 1 || K < 1) throw DemError(DEM_ERR_INVALID, "adjoint forward: steps and K must be positive");
+        if (started_ || step_index_ != 0)
+            throw DemError(DEM_ERR_STATE, "adjoint forward starts from a freshly initialized engine");
+        adj_arena_.release();
+        adj_ = Adjoint{};
+        Adjoint& A = adj_;
+        A.steps = steps; A.K = std::min(K, steps); A.nseg = (steps + A.K - 1) / A.K;
+        A.cap_pp = 16 * nc_ + 1024;
+        A.cap_pw = 2 * nc_ + 1024;
+        for (int k = 0; k < A.nseg + 2; ++k) A.ck.push_back(adj_alloc_ckpt());
+        const size_t slots = (size_t)A.K + 1;
+        A.S = adj_arena_.alloc<double>(slots * kAdjFields * n_, "adjoint tape");
+        A.pp_new = adj_arena_.alloc<unsigned char>((size_t)nc_ * kPSlots, "adjoint tape");
+        A.pp = adj_arena_.alloc<int4>(slots * A.cap_pp, "adjoint tape");
+        A.pp_h = adj_arena_.alloc<double>(slots * A.cap_pp * kHV, "adjoint tape");
+        A.pw = adj_arena_.alloc<int4>(slots * A.cap_pw, "adjoint tape");
+        A.pw_h = adj_arena_.alloc<double>(slots * A.cap_pw * kHV, "adjoint tape");
+        A.pp_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
+        A.pw_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
+        A.overflow = adj_arena_.alloc<int>(1, "adjoint tape");
+        A.L = adj_arena_.alloc<double>((size_t)kAdjFields * n_, "adjoint state");
+        A.Lp = adj_arena_.alloc<double>((size_t)kAdjFields * n_, "adjoint state");
+        A.P = adj_arena_.alloc<double>((size_t)kPFields * n_, "adjoint state");
+        A.T = adj_arena_.alloc<double>((size_t)kTFields * n_, "adjoint state");
+        A.lh_pp = adj_arena_.alloc<double>((size_t)nc_ * kPSlots * kHV, "adjoint history");
+        A.lh_pw = adj_arena_.alloc<double>((size_t)nc_ * kWSlots * kHV, "adjoint history");
+        A.grads = adj_arena_.alloc<double>(2 * kAdjParams, "adjoint parameters");
+        adj_save(A.ck[0]);
+        run_steps(0);
+        adj_save(A.ck[1]);
+        for (int k = 0; k < A.nseg; ++k) {
+            run_steps(std::min(A.K, A.steps - k * A.K));
+            adj_save(A.ck[k + 2]);
+        }
+        check(cudaStreamSynchronize(stream_), "adjoint forward");
+        A.ready = true;
+    }
+
+    // One recomputed force evaluation with its tape in slot `sl`.
+    void adj_tape_forces(int sl)
+    {
+        Adjoint& A = adj_;
+        check(cudaMemsetAsync(A.pw_cnt + sl, 0, sizeof(int), stream_), "adjoint tape");
+        StepTape tp{};
+        tp.pp_new = A.pp_new;
+        tp.pp = A.pp + (size_t)sl * A.cap_pp; tp.pp_h = A.pp_h + (size_t)sl * A.cap_pp * kHV; tp.pp_cap = A.cap_pp;
+        tp.pw = A.pw + (size_t)sl * A.cap_pw; tp.pw_h = A.pw_h + (size_t)sl * A.cap_pw * kHV; tp.pw_cap = A.cap_pw;
+        tp.pw_count = A.pw_cnt + sl;
+        tp.overflow = A.overflow;
+        ct64_.tape = tp;
+        const double dt_eff = step_index_ == 0 ? 0.0 : dt_;
+        forces(dt_eff);
+        ct64_.tape = StepTape{};
+        ++step_index_;
+        check(cudaMemcpyAsync(A.pp_cnt + sl, K_.ct_total, sizeof(int), cudaMemcpyDeviceToDevice, stream_), "adjoint tape");
+    }
+
+    // dem_adjoint_backward: the adjoint of the final positions and velocities
+    // in, those of the initial state and of the materials out.
+    void adjoint_backward(const double* dl_dpos, const double* dl_dvel, double* dl_dpos0, double* dl_dvel0,
+                          double* dl_domega0, double* dl_dparams)
+    {
+        adj_require();
+        Adjoint& A = adj_;
+        if (!A.ready) throw DemError(DEM_ERR_STATE, "adjoint backward needs dem_adjoint_forward first");
+        cudaStream_t s = stream_;
+        const size_t N = (size_t)n_;
+        check(cudaMemsetAsync(A.L, 0, sizeof(double) * kAdjFields * N, s), "adjoint");
+        check(cudaMemsetAsync(A.lh_pp, 0, sizeof(double) * (size_t)nc_ * kPSlots * kHV, s), "adjoint");
+        check(cudaMemsetAsync(A.lh_pw, 0, sizeof(double) * (size_t)nc_ * kWSlots * kHV, s), "adjoint");
+        check(cudaMemsetAsync(A.grads, 0, sizeof(double) * 2 * kAdjParams, s), "adjoint");
+        check(cudaMemsetAsync(A.overflow, 0, sizeof(int), s), "adjoint");
+        {
+            std::vector<double> h(kAdjFields * N, 0.0);
+            for (size_t i = 0; i < N; ++i)
+                for (int a = 0; a < 3; ++a) {
+                    if (dl_dpos) h[(kAdjX + a) * N + i] = dl_dpos[3 * i + a];
+                    if (dl_dvel) h[(kAdjV + a) * N + i] = dl_dvel[3 * i + a];
+                }
+            check(cudaMemcpyAsync(A.L, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s), "adjoint");
+            check(cudaStreamSynchronize(s), "adjoint");
+        }
+        auto tape_of = [&](int sl) {
+            StepTape tp{};
+            tp.pp = A.pp + (size_t)sl * A.cap_pp; tp.pp_h = A.pp_h + (size_t)sl * A.cap_pp * kHV;
+            tp.pw = A.pw + (size_t)sl * A.cap_pw; tp.pw_h = A.pw_h + (size_t)sl * A.cap_pw * kHV;
+            return tp;
+        };
+        std::vector<int> npp(A.K + 1), npw(A.K + 1);
+        auto counts = [&](int k) {
+            int of = 0;
+            check(cudaMemcpyAsync(npp.data(), A.pp_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
+            check(cudaMemcpyAsync(npw.data(), A.pw_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
+            check(cudaMemcpyAsync(&of, A.overflow, sizeof(int), cudaMemcpyDeviceToHost, s), "adjoint counts");
+            check(cudaStreamSynchronize(s), "adjoint counts");
+            if (of) throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
+            for (int j = 0; j < k; ++j) { npp[j] = std::min(npp[j], A.cap_pp); npw[j] = std::min(npw[j], A.cap_pw); }
+        };
+        for (int seg = A.nseg - 1; seg >= 0; --seg) {
+            const int ks = std::min(A.K, A.steps - seg * A.K);
+            adj_restore(A.ck[seg + 1]);
+            for (int sl = 0; sl < ks; ++sl) {
+                launch_adj_snapshot(O_, A.S + (size_t)sl * kAdjFields * N, s);
+                launch_advance(O_, dt_, s);
+                adj_tape_forces(sl);
+                launch_finish(O_, dt_, s);
+            }
+            launch_adj_snapshot(O_, A.S + (size_t)ks * kAdjFields * N, s);
+            counts(ks);
+            for (int sl = ks - 1; sl >= 0; --sl) {
+                launch_adj_step(C_, O_, d_sc_, W_, tape_of(sl), npp[sl], npw[sl], A.S + (size_t)sl * kAdjFields * N,
+                                A.S + (size_t)(sl + 1) * kAdjFields * N, A.L, A.Lp, A.P, A.T, A.lh_pp, A.lh_pw, dt_, dt_,
+                                0, A.grads, sm_count_, s);
+                std::swap(A.L, A.Lp);
+            }
+        }
+        // the first evaluation (dt = 0) and the leapfrog start
+        adj_restore(A.ck[0]);
+        adj_tape_forces(0);
+        launch_leapfrog_init(O_, 0.5 * dt_, s);
+        launch_adj_snapshot(O_, A.S, s);
+        counts(1);
+        launch_adj_step(C_, O_, d_sc_, W_, tape_of(0), npp[0], npw[0], A.S, A.S, A.L, A.Lp, A.P, A.T, A.lh_pp, A.lh_pw,
+                        0.5 * dt_, 0.0, 1, A.grads, sm_count_, s);
+        check(cudaGetLastError(), "adjoint backward");
+        std::vector<double> h(kAdjFields * N);
+        double g[2 * kAdjParams];
+        check(cudaMemcpyAsync(h.data(), A.Lp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s), "adjoint");
+        check(cudaMemcpyAsync(g, A.grads, sizeof g, cudaMemcpyDeviceToHost, s), "adjoint");
+        check(cudaStreamSynchronize(s), "adjoint");
+        for (size_t i = 0; i < N; ++i)
+            for (int a = 0; a < 3; ++a) {
+                if (dl_dpos0) dl_dpos0[3 * i + a] = h[(kAdjX + a) * N + i];
+                if (dl_dvel0) dl_dvel0[3 * i + a] = h[(kAdjV + a) * N + i];
+                if (dl_domega0) dl_domega0[3 * i + a] = h[(kAdjW + a) * N + i];
+            }
+        if (dl_dparams) {
+            const MatC* mats[2] = {&scenes_h_[0].pp, &scenes_h_[0].pw};
+            for (int c = 0; c < 2; ++c) {
+                const double* gc = g + c * kAdjParams;
+                double* o = dl_dparams + c * kAdjParams;
+                // kN, mu, epsN (log epsN = logN), epsS, muT, muR
+                o[0] = gc[0]; o[1] = gc[1];
+                o[2] = gc[2] / std::exp(mats[c]->logN);
+                o[3] = gc[3] / std::exp(mats[c]->logS);
+                o[4] = gc[4]; o[5] = gc[5];
+            }
+        }
+        // leave the engine at the end of the forward run
+        adj_restore(A.ck[A.nseg + 1]);
+        check(cudaStreamSynchronize(s), "adjoint backward");
+    }
+
     // -------------------------------------------------------------- misc
     void need_init() const
     {
@@ -1163,7 +1402,9 @@ public:
     cudaStream_t stream_ = nullptr;
     std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;
-    DeviceArena arena_, arena_tmp_;
+    DeviceArena arena_, arena_tmp_, adj_arena_;
+    Adjoint adj_;
+    std::vector<double> oin_host_;  // owner principal inertia [n][3] (host copy)
     void* pinned_ = nullptr;
     size_t pinned_bytes_ = 0;
     cudaGraphExec_t graph_fa_ = nullptr, graph_f_ = nullptr, graph_mbd_fa_ = nullptr, graph_mbd_f_ = nullptr;
@@ -1424,6 +1665,17 @@ int dem_x_download_half(dem_engine* e, double* vh, double* wh, double* hdq, doub
 int dem_x_set_pt_warp_items(dem_engine* e, int n)
 {
     return guarded([&] { NEED(e); e->e.set_pt_warp_items(n); });
+}
+
+int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every)
+{
+    return guarded([&] { NEED(e); e->e.adjoint_forward(steps, checkpoint_every); });
+}
+
+int dem_adjoint_backward(dem_engine* e, const double* dl_dpos, const double* dl_dvel, double* dl_dpos0,
+                         double* dl_dvel0, double* dl_domega0, double* dl_dparams)
+{
+    return guarded([&] { NEED(e); e->e.adjoint_backward(dl_dpos, dl_dvel, dl_dpos0, dl_dvel0, dl_domega0, dl_dparams); });
 }
 
 int dem_x_synchronize(dem_engine* e)

@@ -151,6 +151,35 @@ struct Counters {
     int pt_warp_items;  // PT: warp-per-item kernel up to this many contact items
 };
 
+// Reverse sweep (dem_adjoint.cu).  Owner state S of one step, [field][owner]:
+// x 3, q 4, v 3, w (body frame) 3, vh 3, wh 3, hq 4, a 3, aw 3.
+constexpr int kAdjX = 0, kAdjQ = 3, kAdjV = 7, kAdjW = 10, kAdjVH = 13, kAdjWH = 16, kAdjHQ = 19, kAdjA = 23,
+              kAdjAW = 26, kAdjFields = 29;
+// post-advance state the laws see: x1, q1, v1, w1, midpoint v and w
+constexpr int kPX = 0, kPQ = 3, kPV = 7, kPW = 10, kPMV = 13, kPMW = 16, kPFields = 19;
+// adjoints of the post-advance state, of the midpoint velocities, and of the
+// total force and world torque of each owner
+constexpr int kTX = 0, kTQ = 3, kTV = 7, kTW = 10, kTMV = 13, kTMW = 16, kTF = 19, kTTau = 22, kTFields = 25;
+// material adjoints per contact class: kN, mu, log epsN, log epsS, muT, muR
+constexpr int kAdjParams = 6;
+
+// Adjoint tape of one step (FP64 form, written only while the engine tapes a
+// recomputed step): per particle contact side (component, partner component,
+// history slot index, 1 if the slot was acquired this step) and the slot's
+// history before the law; the same for wall contacts (component, wall,
+// slot index, new).
+struct StepTape {
+    unsigned char* pp_new;  // per contact list entry, written by the sweep
+    int4* pp;
+    double* pp_h;           // [entry][kHV]
+    int pp_cap;
+    int4* pw;
+    double* pw_h;
+    int pw_cap;
+    int* pw_count;
+    int* overflow;
+};
+
 template <typename T> struct Contacts {
     int4* ent;      // ti, tj, slot, -
     T* res;         // [k][6]
@@ -172,6 +201,7 @@ template <typename T> struct Contacts {
     double* pt_body;    // [contact item][nbs][kPtRecord]
     double* pt_out;     // [contact item][nbs][25] optional output detail
     int nbs;            // max bodies per scene
+    StepTape tape;      // adjoint tape (all null when not taping)
 };
 
 struct BodyOut {
@@ -197,6 +227,13 @@ void launch_finish(const Owners& o, double dt, cudaStream_t s);
 void launch_finish_advance(const Owners& o, double dt, cudaStream_t s);
 // reset != 0: clear the per-step counters; 0: advance the contact step index.
 void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
+
+void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s);
+void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s);
+void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
+                     int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
+                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int sm_count,
+                     cudaStream_t s);
 
 template <typename T>
 void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,

@@ -58,6 +58,8 @@ _SIGS = {
     "dem_x_download_half": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),
     "dem_x_synchronize": ([C.c_void_p], C.c_int),
     "dem_x_set_pt_warp_items": ([C.c_void_p, C.c_int], C.c_int),
+    "dem_adjoint_forward": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
+    "dem_adjoint_backward": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
 }
 
 
@@ -259,6 +261,29 @@ class CudaDemSolver:
         cnt = C.c_int()
         self._check(self.lib.dem_last_phase_times(self.h, ms, 16, C.byref(cnt)))
         return [ms[k] for k in range(cnt.value)]
+
+    def adjoint_forward(self, steps, checkpoint_every=100):
+        """The reference's step sequence from a fresh engine (first
+        evaluation, leapfrog start, `steps` steps) with checkpoints for the
+        reverse sweep (FP64 form, spheres, no bodies)."""
+        self._check(self.lib.dem_adjoint_forward(self.h, int(steps), int(checkpoint_every)))
+        return self
+
+    def adjoint_backward(self, dl_dpos=None, dl_dvel=None):
+        """Gradient of a scalar loss given its adjoint w.r.t. the final
+        positions / velocities ([n, 3]).  Returns a dict with dl_dpos0,
+        dl_dvel0, dl_domega0 ([n, 3]) and dl_dparams ({"pp": ..., "pw": ...}
+        each {kN, mu, epsN, epsS, muT, muR})."""
+        n = self.n
+        a = None if dl_dpos is None else np.ascontiguousarray(dl_dpos, dtype=np.float64).reshape(n, 3)
+        b = None if dl_dvel is None else np.ascontiguousarray(dl_dvel, dtype=np.float64).reshape(n, 3)
+        x0, v0, w0 = (np.zeros((n, 3)) for _ in range(3))
+        p = np.zeros(12)
+        self._check(self.lib.dem_adjoint_backward(self.h, _p(a) if a is not None else None,
+                                                  _p(b) if b is not None else None, _p(x0), _p(v0), _p(w0), _p(p)))
+        keys = ("kN", "mu", "epsN", "epsS", "muT", "muR")
+        return {"dl_dpos0": x0, "dl_dvel0": v0, "dl_domega0": w0,
+                "dl_dparams": {"pp": dict(zip(keys, p[:6])), "pw": dict(zip(keys, p[6:]))}}
 
     def set_pt_warp_items(self, n):
         """Crossover of the two particle-triangle kernels: up to n contact

@@ -278,6 +278,31 @@ int dem_cell_sort_static(const double* x, const double* y, const double* z,
                          int n, double mesh_size, uint64_t* sorted_key,
                          int* sorted_id, void* stream);
 
+/* ---- reverse mode (the shape a torch.autograd.Function wraps) ----------
+ * No counterpart in the reference, which has no gradients.  A hand-written
+ * adjoint of each step of the FP64 form: within a step the contact set is
+ * the one the forward step found, and at the Coulomb / twisting / rolling
+ * caps the derivative is that of the branch taken.  Covers one scene of
+ * spheres with walls and particle contacts (no rigid bodies), precision
+ * DEM_PRECISION_FP64; other engines return DEM_ERR_INVALID.
+ *
+ * dem_adjoint_forward runs the reference's step sequence from a freshly
+ * initialized engine: the first evaluation (dt = 0), the leapfrog start and
+ * `steps` steps, keeping a checkpoint every `checkpoint_every` steps.
+ *
+ * dem_adjoint_backward takes the adjoint of a scalar loss with respect to
+ * the final positions and velocities ([n][3] each, owner order; either may
+ * be NULL for zero) and returns its gradient with respect to the initial
+ * positions, velocities and angular velocities ([n][3]; NULL to skip) and
+ * to the materials (dl_dparams[2][6]: particle-particle then particle-wall,
+ * each d/dkN, d/dmu, d/depsN, d/depsS, d/dmuT, d/dmuR).  It recomputes each
+ * segment from its checkpoint and leaves the engine at the end of the
+ * forward run. */
+int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every);
+int dem_adjoint_backward(dem_engine* e, const double* dl_dpos, const double* dl_dvel,
+                         double* dl_dpos0, double* dl_dvel0, double* dl_domega0,
+                         double* dl_dparams);
+
 #ifdef __cplusplus
 }
 #endif
