@@ -87,15 +87,15 @@ def clip_radii(idx, pos, radius, counts, overlap, keep=None):
 
 
 def bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=0, jitter=0.2e-3, overlap=1e-7, radius_fn=None,
-        inside=None, center_xy=True):
+        inside=None, center_xy=True, nxy=None):
     """Lattice bed of about ``n`` spheres; ``inside(pos) -> bool mask`` removes
     sites (e.g. the volume of a body).  With ``center_xy`` the lattice is
     centred on x = y = 0 and ``origin`` only sets its lowest z."""
     rng = np.random.default_rng(seed)
     ax, ay = aspect[0], aspect[1]
     base = (n / (ax * ay)) ** (1.0 / 3.0)
-    nx = max(1, int(round(base * ax)))
-    ny = max(1, int(round(base * ay)))
+    nx = max(1, int(round(base * ax))) if nxy is None else nxy
+    ny = max(1, int(round(base * ay))) if nxy is None else nxy
     nz = max(1, int(np.ceil(n / (nx * ny))))
     counts = (nx, ny, nz)
     origin = np.array(origin, float)
@@ -235,7 +235,7 @@ def _attach(kw, bodies):
 
 
 def pure_dem(n=20000, seed=1000, rmin=1.8e-3, rmax=2.2e-3, box=(0.2, 0.2, 0.4), dt=1e-5, kN=1e5, epsN=0.5, mu=0.3,
-             pitch=None, name="c0_pure_dem"):
+             pitch=None, name="c0_pure_dem", fill_width=False):
     """Config 0: spheres r ~ U[rmin, rmax] on a jittered lattice in a box of 5
     walls (floor + 4 sides), kN 1e5, restitution 0.5, friction 0.3."""
     pitch = pitch if pitch is not None else 2.0 * rmin + 0.1e-3
@@ -245,7 +245,7 @@ def pure_dem(n=20000, seed=1000, rmin=1.8e-3, rmax=2.2e-3, box=(0.2, 0.2, 0.4), 
     per = int(width // pitch)
     origin = lo + np.array([rmax, rmax, rmax]) + (width - (per - 1) * pitch) / 2 * np.array([1, 1, 0])
     origin[2] = rmax + 0.3e-3
-    pos, rad, _ = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed)
+    pos, rad, _ = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed, nxy=per if fill_width else None)
     assert pos[:, 0].max() + rad.max() < hi[0] and pos[:, 1].max() + rad.max() < hi[1], "bed exceeds the box"
     kw = make_spheres(pos, rad, DENSITY)
     wo, wn = box_walls(lo, hi)
@@ -449,6 +449,16 @@ def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5, settled=False)
             sc = pure_dem(n=ns, seed=seed * 1000 + s, box=(0.1, 0.1, 0.4), dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}")
         out.append(sc)
     return out
+
+
+def adjoint_settle(n=50000, seed=1003, dt=1e-5, vel_std=0.05, name="c3_adjoint"):
+    """Config 3 without its plate: spheres r ~ U[1.8, 2.2] mm on a lattice in
+    a 0.1 m box of 5 walls (open top, walls 0.6 m high), seeded normal
+    initial velocities (std 0.05 m/s); the bed settles during the run."""
+    sc = pure_dem(n=n, seed=seed, box=(0.1, 0.1, 0.6), dt=dt, name=name, fill_width=True)
+    rng = np.random.default_rng(seed + 1)
+    sc.vel = rng.normal(0.0, vel_std, size=sc.vel.shape)
+    return sc
 
 
 def small_mbd(n=400, seed=7, dt=2e-5, caps=True, name="small_mbd"):
