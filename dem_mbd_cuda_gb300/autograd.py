@@ -1,0 +1,59 @@
+"""torch.autograd.Function over the engine's reverse mode.
+
+``simulate(scene, steps, pp, pw, vel0)`` runs the reference's step sequence
+(FP64 form) from ``scene`` with the particle-particle and particle-wall
+materials ``pp`` / ``pw`` (tensors [kN, mu, epsN, epsS, muT, muR]) and initial
+velocities ``vel0`` ([n, 3]), and returns the final positions and velocities.
+Gradients flow back to the materials and the initial velocities through
+dem_adjoint_forward / dem_adjoint_backward, so material calibration is an
+ordinary torch optimisation loop.  Tensors live on the host; the engine keeps
+its own device state.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+import torch
+
+from .engine import CudaDemSolver
+
+FIELDS = ("kN", "mu", "epsN", "epsS", "muT", "muR")
+
+
+def _with_materials(scene, pp, pw, vel0):
+    def mech(m, v):
+        return dataclasses.replace(m, **{f: float(x) for f, x in zip(FIELDS, v)})
+    return dataclasses.replace(scene, pp=mech(scene.pp, pp), pw=mech(scene.pw, pw), pt=dataclasses.replace(scene.pt),
+                               vel=np.asarray(vel0, dtype=np.float64).reshape(-1, 3).copy())
+
+
+class DemRun(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pp, pw, vel0, scene, steps, checkpoint_every):
+        sc = _with_materials(scene, pp.detach().cpu().numpy(), pw.detach().cpu().numpy(), vel0.detach().cpu().numpy())
+        e = CudaDemSolver().initialize(sc, precision="fp64").adjoint_forward(steps, checkpoint_every)
+        st = e.downloadParticleState()
+        ctx.engine = e
+        ctx.dtype = pp.dtype
+        return (torch.as_tensor(st["pos"], dtype=vel0.dtype), torch.as_tensor(st["vel"], dtype=vel0.dtype))
+
+    @staticmethod
+    def backward(ctx, gpos, gvel):
+        g = ctx.engine.adjoint_backward(None if gpos is None else gpos.detach().cpu().numpy(),
+                                        None if gvel is None else gvel.detach().cpu().numpy())
+        pp = torch.tensor([g["dl_dparams"]["pp"][f] for f in FIELDS], dtype=ctx.dtype)
+        pw = torch.tensor([g["dl_dparams"]["pw"][f] for f in FIELDS], dtype=ctx.dtype)
+        dv = torch.as_tensor(g["dl_dvel0"], dtype=gpos.dtype if gpos is not None else gvel.dtype)
+        return pp, pw, dv, None, None, None
+
+
+def materials(m):
+    """A scene's Mech as the [kN, mu, epsN, epsS, muT, muR] tensor."""
+    return torch.tensor([getattr(m, f) for f in FIELDS], dtype=torch.float64)
+
+
+def simulate(scene, steps, pp, pw, vel0, checkpoint_every=100):
+    """Final (positions, velocities) of `steps` steps, differentiable with
+    respect to pp, pw and vel0."""
+    return DemRun.apply(pp, pw, vel0, scene, int(steps), int(checkpoint_every))

@@ -121,3 +121,38 @@ def test_adjoint_scope_errors():
     e = engine_for(G.small_mbd(), precision="fp64")
     with pytest.raises(RuntimeError, match="rigid bodies"):
         e.adjoint_forward(5, 5)
+
+
+def test_autograd_function_and_calibration_step():
+    """The torch.autograd.Function returns the engine's gradients, and one
+    gradient step on the restitution reduces a calibration loss (final mean
+    height against a target made with another restitution)."""
+    torch = pytest.importorskip("torch")
+    from dem_mbd_cuda_gb300.autograd import materials, simulate
+    sc = _scene()
+    pw = materials(sc.pw)
+    v0 = torch.tensor(sc.vel)
+    target_pp = materials(sc.pp)
+    target_pp[2] = 0.6
+    with torch.no_grad():
+        target = simulate(sc, STEPS, target_pp, pw, v0)[0][:, 2].mean()
+
+    def loss_of(pp):
+        pos, _ = simulate(sc, STEPS, pp, pw, v0)
+        return (pos[:, 2].mean() - target) ** 2
+
+    pp = materials(sc.pp).requires_grad_(True)
+    loss = loss_of(pp)
+    loss.backward()
+    # the autograd gradient is the engine's backward result
+    e = engine_for(sc, precision="fp64").adjoint_forward(STEPS, 100)
+    n = e.n
+    z = torch.tensor(e.downloadParticleState()["pos"][:, 2]).mean()
+    dpos = np.zeros((n, 3)); dpos[:, 2] = float(2.0 * (z - target)) / n
+    g = e.adjoint_backward(dpos, None)
+    assert pp.grad[2].item() == pytest.approx(g["dl_dparams"]["pp"]["epsN"], rel=1e-12)
+    # half a Newton step on L = r^2 (d eps = -L / L') lowers the loss
+    with torch.no_grad():
+        pp2 = pp.detach().clone()
+        pp2[2] -= float(loss.detach()) / pp.grad[2]
+    assert float(loss_of(pp2)) < 0.5 * float(loss.detach())
