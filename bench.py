@@ -345,6 +345,13 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
             "fd_check": fd}
 
 
+def autotune_summary(scene, precision):
+    """The autotuner's choice of cell factor and particle-triangle crossover
+    on the workload (dem_mbd_cuda_gb300/autotune.py)."""
+    from dem_mbd_cuda_gb300.autotune import autotune
+    return autotune(scene, precision=precision)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -357,6 +364,7 @@ def main():
     ap.add_argument("--no-drum", action="store_true", help="skip the embedded 2M-sphere drum summary")
     ap.add_argument("--no-batch", action="store_true", help="skip the embedded 256-scene batch summary")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the embedded config-3 adjoint summary")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the embedded autotuner summary")
     ap.add_argument("--adjoint-only", action="store_true", help="print the config-3 adjoint summary alone")
     ap.add_argument("--particles", type=int, default=None,
                     help="particle count of the generated scene (profiling captures of a smaller case)")
@@ -455,6 +463,7 @@ def main():
     if args.config != "c4" and not args.no_batch:
         batch = batch_summary(args.steps, args.warmup)
     adjoint = None if args.no_adjoint else adjoint_summary()
+    tuned = None if args.no_autotune else autotune_summary(scene, args.precision)
     nb = scene.n_bodies
     line = {
         "metric": "particle-steps/s",
@@ -495,6 +504,8 @@ def main():
         line["batch_256"] = batch
     if adjoint:
         line["adjoint_c3"] = adjoint
+    if tuned:
+        line["autotuned"] = tuned
     print(json.dumps(line))
 
 
