@@ -162,7 +162,7 @@ def launches_per_step(scene):
     if scene.comp_owner is not None:
         k += 1
     if scene.n_bodies:
-        k += 1 + 6 + 10 + 2      # triangle transform, triangle grid, PT compactions + probe + law, body reduction
+        k += 1 + 6 + 7 + 2       # triangle transform, triangle grid, PT probe + scan + compaction + law, body reduction
     return k
 
 

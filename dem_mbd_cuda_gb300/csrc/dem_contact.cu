@@ -505,12 +505,6 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         exact_pass();
         hp.hw[ci] = phw;
         ct.cnt[ci] = count;
-        int pt_flag = 0;
-        if (tris.nt > 0 && sc[s].body_count > 0) {
-            const int lin = cell.w;
-            pt_flag = tris.tcell_start[lin + 1] > tris.tcell_start[lin] ? 1 : 0;
-        }
-        ct.pt_flag[t] = pt_flag;
     }
     int total;
     const int ex = block_exclusive_scan_c(count, total);
@@ -603,22 +597,6 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
     }
 }
 
-// PT list in sorted order: item index = exclusive scan of the flags.
-__global__ void k_pt_compact(Grid g, Recs r, int* pt_flag, int* pt_pos, int* pt_list,
-                             int* pt_index, int* pt_total)
-{
-    const int nvalid = *g.nvalid;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *pt_total = pt_pos[nvalid];
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
-        const int ci = r.meta[t].x;
-        if (pt_flag[t]) {
-            pt_list[pt_pos[t]] = t;
-            pt_index[ci] = pt_pos[t];
-        } else {
-            pt_index[ci] = -1;
-        }
-    }
-}
 
 // ------------------------------------------------------------------- PT
 
@@ -684,43 +662,39 @@ __device__ __forceinline__ bool pt_may_touch(const float4* __restrict__ tf, int 
     return cx * cx + cy * cy + cz * cz <= reach * reach;
 }
 
-// Per PT item: can any triangle of its cell give a nonzero area scale (the
-// condition of a manifold, :1154-1183)?  One warp per item, one lane per
-// triangle, FP32 rejection only: the flag may be set for an item without a
-// manifold (the law kernel then finds none), never cleared for one with.
-__global__ void __launch_bounds__(256) k_pt_probe(Recs r, Tris tris, int* pt_list, int* pt_total, int* cflag)
+// Per sorted position: can any triangle of its cell give a nonzero area
+// scale (the condition of a manifold, :1154-1183)?  FP32 rejection only: the
+// flag may be set for a component without a manifold (the law kernel then
+// finds none), never cleared for one with.  Components in cells without
+// triangles leave at once.
+__global__ void __launch_bounds__(256) k_pt_probe(Grid g, Recs r, Tris tris, int* cflag)
 {
-    const int total = *pt_total;
-    const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < total; item += warps) {
-        const int t = pt_list[item];
-        const D4 p4 = r.pos[t];
-        const PtProbe q = pt_probe(d3(p4), p4.w);
+    const int nvalid = *g.nvalid;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
         const int lin = r.cell[t].w;
         const int tb = tris.tcell_start[lin];
         const int te = min(tris.tcell_start[lin + 1], tris.capacity);
-        bool hit = false;
-        for (int e0 = tb; e0 < te && !hit; e0 += 32) {
-            const int e = e0 + lane;
-            hit = __any_sync(0xffffffffu, e < te && pt_may_touch(tris.tf, tris.ttri[e], q));
+        int hit = 0;
+        if (te > tb) {
+            const D4 p4 = r.pos[t];
+            const PtProbe q = pt_probe(d3(p4), p4.w);
+            for (int e = tb; e < te && !hit; ++e) hit = pt_may_touch(tris.tf, tris.ttri[e], q) ? 1 : 0;
         }
-        if (lane == 0) cflag[item] = hit ? 1 : 0;
+        cflag[t] = hit;
     }
 }
 
-// Contact items in PT-item order; pt_index maps a component to its contact
-// item (-1 when it touches no triangle).
-__global__ void k_pt_compact_contacts(Recs r, int* pt_list, int* pt_total, int* cflag, int* cpos, int* clist,
-                                      int* pt_index, int* ctotal)
+// Contact items in sorted order (clist holds sorted positions); pt_index
+// maps a component to its contact item, -1 when it touches no triangle.
+__global__ void k_pt_compact_contacts(Grid g, Recs r, int* cflag, int* cpos, int* clist, int* pt_index, int* ctotal)
 {
-    const int total = *pt_total;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *ctotal = cpos[total];
-    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
-        const int ci = r.meta[pt_list[item]].x;
-        if (cflag[item]) {
-            clist[cpos[item]] = item;
-            pt_index[ci] = cpos[item];
+    const int nvalid = *g.nvalid;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *ctotal = cpos[nvalid];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
+        const int ci = r.meta[t].x;
+        if (cflag[t]) {
+            clist[cpos[t]] = t;
+            pt_index[ci] = cpos[t];
         } else {
             pt_index[ci] = -1;
         }
@@ -899,7 +873,7 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
     if (total <= k.pt_warp_items) return;
     int bover = 0, bhigh = 0;
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
-        const int t = ct.pt_list[ct.pt_clist[item]];
+        const int t = ct.pt_clist[item];
         const int4 meta = r.meta[t];
         const int ci = meta.x;
         const SceneC& S = sc[meta.w];
@@ -1034,7 +1008,7 @@ __global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, cons
     const int warps = (gridDim.x * blockDim.x) >> 5;
     int bover = 0, bhigh = 0;
     for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < total; item += warps) {
-        const int t = ct.pt_list[ct.pt_clist[item]];
+        const int t = ct.pt_clist[item];
         const int4 meta = r.meta[t];
         const int ci = meta.x;
         const SceneC& S = sc[meta.w];
@@ -1348,73 +1322,96 @@ __global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Co
     else euler_f64(o, i, TT);
 }
 // ------------------------------------------------------------ body reduce
-// Level 1: blocks (group g, body b) reduce a contiguous item range in a
-// fixed order; level 2 reduces the groups in order.  Fields: [0..5] load,
+// Level 1: warps (group g, body b) reduce a contiguous range of contact
+// items in order; level 2 reduces the groups in order.  Fields: [0..5] load,
 // [6] triangle contacts, [7] max depth, [8] Fz, [9..15] regime counters,
 // [16..37] microstate -> stored as kPtRecord + 6 doubles.
 constexpr int kBodyFields = kBodyFieldCount;
 
-__device__ void accumulate_record(double* acc, const double* rec)
+// Regime counter f (9..15) of one record from its flags rec[9]
+// (accumulateBodyRegimeKernel, :530-567): active, slide/twist class, slide,
+// twist, both.
+__device__ __forceinline__ double regime_field(int f, int st)
 {
-    for (int f = 0; f < 6; ++f) acc[f] += rec[f];
-    acc[6] += rec[6];
-    acc[7] = fmax(acc[7], rec[7]);
-    acc[8] += rec[8];
-    const int st = (int)rec[9];
-    if (st & 1) {
-        const bool sl = (st & 2) != 0, tw = (st & 4) != 0;
-        acc[9] += 1.0;
-        acc[9 + (tw ? 3 : (sl ? 2 : 1))] += 1.0;
-        if (sl) acc[13] += 1.0;
-        if (tw) acc[14] += 1.0;
-        if (sl && tw) acc[15] += 1.0;
-        for (int f = 0; f < kMicro; ++f) acc[16 + f] += rec[10 + f];
-    }
+    if (!(st & 1)) return 0.0;
+    const bool sl = (st & 2) != 0, tw = (st & 4) != 0;
+    if (f == 9) return 1.0;
+    if (f < 13) return (9 + (tw ? 3 : (sl ? 2 : 1))) == f ? 1.0 : 0.0;
+    if (f == 13) return sl ? 1.0 : 0.0;
+    if (f == 14) return tw ? 1.0 : 0.0;
+    return (sl && tw) ? 1.0 : 0.0;
 }
-__device__ void combine(double* a, const double* b)
-{
-    for (int f = 0; f < kBodyFields; ++f) a[f] = (f == 7) ? fmax(a[f], b[f]) : a[f] + b[f];
-}
+__device__ __forceinline__ double fold(double acc, double v, int f) { return f == 7 ? fmax(acc, v) : acc + v; }
 
+// Level 1: one warp per (group, body); the group's contact items are taken
+// in order, each lane folding one or two of the 38 body fields: loads, count,
+// max depth and Fz straight from rec[0..8], the regime counters from the
+// flags rec[9], the microstate from rec[10..31] of active manifolds.  A
+// record is read coalesced across the lanes, four items in flight at a time.
 template <typename T>
 __global__ void k_body_partial(Recs r, const SceneC* __restrict__ sc, Bodies bodies, Contacts<T> ct, BodyOut bo)
 {
+    const int lane = threadIdx.x & 31;
+    const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int b = blockIdx.y;
+    if (g >= bo.groups) return;
     const int total = *ct.pt_ctotal_ptr;
     const int chunk = (total + bo.groups - 1) / bo.groups;
-    const int beg = blockIdx.x * chunk, end = min(total, beg + chunk);
+    const int beg = g * chunk, end = min(total, beg + chunk);
     const int bs = bodies.scene[b];
     const int j = b - sc[bs].body_begin;
-    double acc[kBodyFields];
-    for (int f = 0; f < kBodyFields; ++f) acc[f] = 0.0;
-    for (int item = beg + threadIdx.x; item < end; item += blockDim.x) {
-        const int t = ct.pt_list[ct.pt_clist[item]];
-        if (r.meta[t].w != bs) continue;
-        accumulate_record(acc, ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord);
+    const int f1 = lane, f2 = lane + 32;
+    const bool two = f2 < kBodyFields;
+    // record index of each field (-1: derived from the flags)
+    const int i1 = f1 < 9 ? f1 : (f1 >= 16 ? f1 - 6 : -1);
+    const int i2 = two ? f2 - 6 : -1;
+    double a1 = 0.0, a2 = 0.0;
+    for (int i0 = beg; i0 < end; i0 += 4) {
+        double v1[4], v2[4], st[4];
+        bool use[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int item = i0 + q;
+            use[q] = item < end && r.meta[ct.pt_clist[item]].w == bs;
+            v1[q] = v2[q] = st[q] = 0.0;
+            if (use[q]) {
+                const double* rec = ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord;
+                st[q] = rec[9];
+                if (i1 >= 0) v1[q] = rec[i1];
+                if (i2 >= 0) v2[q] = rec[i2];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (!use[q]) continue;
+            const int sq = (int)st[q];
+            const double c1 = f1 < 9 ? v1[q] : (f1 < 16 ? regime_field(f1, sq) : ((sq & 1) ? v1[q] : 0.0));
+            a1 = fold(a1, c1, f1);
+            if (two && (sq & 1)) a2 += v2[q];
+        }
     }
-    __shared__ double sh[128][kBodyFields + 1];
-    for (int f = 0; f < kBodyFields; ++f) sh[threadIdx.x][f] = acc[f];
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) combine(sh[threadIdx.x], sh[threadIdx.x + w]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        double* out = bo.partial + ((size_t)b * bo.groups + blockIdx.x) * kBodyFields;
-        for (int f = 0; f < kBodyFields; ++f) out[f] = sh[0][f];
-    }
+    double* out = bo.partial + ((size_t)b * bo.groups + g) * kBodyFields;
+    out[f1] = a1;
+    if (two) out[f2] = a2;
 }
 
-// One block per body, one thread per field, groups summed in a fixed order.
+// Level 2: one block per (field, body); thread k folds the groups k, k +
+// 256, ... in order, then a fixed-shape tree over the threads.
 __global__ void k_body_final(BodyOut bo, int interval)
 {
-    const int b = blockIdx.x, f = threadIdx.x;
-    if (f >= kBodyFields) return;
+    const int f = blockIdx.x, b = blockIdx.y;
+    __shared__ double sh[256];
     double acc = 0.0;
-    for (int g = 0; g < bo.groups; ++g) {
-        const double v = bo.partial[((size_t)b * bo.groups + g) * kBodyFields + f];
-        acc = (f == 7) ? fmax(acc, v) : acc + v;
+    const double* p = bo.partial + (size_t)b * bo.groups * kBodyFields + f;
+    for (int g = threadIdx.x; g < bo.groups; g += blockDim.x) acc = fold(acc, p[(size_t)g * kBodyFields], f);
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] = fold(sh[threadIdx.x], sh[threadIdx.x + w], f);
+        __syncthreads();
     }
+    if (threadIdx.x != 0) return;
+    acc = sh[0];
     bo.result[(size_t)b * kBodyFields + f] = acc;
     if (interval) {
         if (f >= 9 && f < 9 + kRegime) bo.reg_int[b * kRegime + (f - 9)] += (unsigned long long)acc;
@@ -1476,13 +1473,10 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
     }
     if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
-        launch_scan(ct.pt_flag, ct.pt_pos, g.nvalid, g.tile_sums, sm_count, s);
-        k_pt_compact<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_flag, ct.pt_pos, ct.pt_list, ct.pt_index,
-                                                  ct.pt_total_ptr);
-        k_pt_probe<<<sm_count * 16, 256, 0, s>>>(r, t, ct.pt_list, ct.pt_total_ptr, ct.pt_cflag);
-        launch_scan(ct.pt_cflag, ct.pt_cpos, ct.pt_total_ptr, g.tile_sums, sm_count, s);
-        k_pt_compact_contacts<<<sm_count * 8, 256, 0, s>>>(r, ct.pt_list, ct.pt_total_ptr, ct.pt_cflag, ct.pt_cpos,
-                                                           ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr);
+        k_pt_probe<<<sm_count * 8, 256, 0, s>>>(g, r, t, ct.pt_cflag);
+        launch_scan(ct.pt_cflag, ct.pt_cpos, g.nvalid, g.tile_sums, sm_count, s);
+        k_pt_compact_contacts<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_cflag, ct.pt_cpos, ct.pt_clist, ct.pt_index,
+                                                           ct.pt_ctotal_ptr);
         k_pt_warp<T, TB><<<sm_count * 8, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
         k_pt_thread<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
     }
@@ -1500,8 +1494,8 @@ void launch_body_reduce(const Recs& r, const SceneC* sc, const Bodies& b, Contac
                         cudaStream_t s)
 {
     if (b.nb <= 0) return;
-    k_body_partial<T><<<dim3(bo.groups, b.nb), 128, 0, s>>>(r, sc, b, ct, bo);
-    k_body_final<<<b.nb, 64, 0, s>>>(bo, interval ? 1 : 0);
+    k_body_partial<T><<<dim3((bo.groups + 3) / 4, b.nb), 128, 0, s>>>(r, sc, b, ct, bo);
+    k_body_final<<<dim3(kBodyFields, b.nb), 256, 0, s>>>(bo, interval ? 1 : 0);
 }
 
 template <typename T>

@@ -437,7 +437,7 @@ public:
         int* cnt = arena_.alloc<int>(16, "counters");
         check(cudaMemsetAsync(cnt, 0, sizeof(int) * 16, s), "clear counters");
         K_.pcontacts = cnt; K_.pover = cnt + 1; K_.bover = cnt + 2; K_.phigh = cnt + 3; K_.bhigh = cnt + 4;
-        K_.tgover = cnt + 5; K_.ct_total = cnt + 6; K_.pt_total = cnt + 7; K_.step = cnt + 8;
+        K_.tgover = cnt + 5; K_.ct_total = cnt + 6; K_.step = cnt + 8;
         K_.pt_ctotal = cnt + 9;
         K_.wl_total = cnt + 10;
         K_.pt_warp_items = kDefaultPtWarpItems;
@@ -455,7 +455,7 @@ public:
 
         // ---- body reduction
         if (nb_ > 0) {
-            BO_.groups = std::max(1, std::min(sm_count_ * 2, (nc_ + 4095) / 4096));
+            BO_.groups = std::max(1, std::min(sm_count_ * 16, (nc_ + 1023) / 1024));
             BO_.partial = arena_.alloc<double>((size_t)nb_ * BO_.groups * kBodyFieldCount, "body partial");
             BO_.result = arena_.alloc<double>((size_t)nb_ * kBodyFieldCount, "body result");
             check(cudaMemsetAsync(BO_.result, 0, sizeof(double) * nb_ * kBodyFieldCount, s), "clear");
@@ -512,13 +512,8 @@ public:
         check(cudaMemsetAsync(ct.wres, 0, (size_t)nc_ * 6 * sizeof(double), s), "clear");
         ct.pt_index = arena_.alloc<int>(nc_, "pt index");
         check(cudaMemsetAsync(ct.pt_index, 0xff, nc_ * sizeof(int), s), "clear");
-        ct.pt_flag = arena_.alloc<int>(nc_ + 1, "pt flag");
-        check(cudaMemsetAsync(ct.pt_flag, 0, (nc_ + 1) * sizeof(int), s), "clear");
-        ct.pt_total_ptr = K_.pt_total;
         ct.nbs = std::max(nbs_, 1);
         if (nb_ > 0 && nt_ > 0) {
-            ct.pt_pos = arena_.alloc<int>(nc_ + 2, "pt pos");
-            ct.pt_list = arena_.alloc<int>(nc_, "pt list");
             ct.pt_cflag = arena_.alloc<int>(nc_ + 1, "pt contact flag");
             ct.pt_cpos = arena_.alloc<int>(nc_ + 2, "pt contact pos");
             ct.pt_clist = arena_.alloc<int>(nc_, "pt contact list");

@@ -144,7 +144,6 @@ struct Counters {
     int* bhigh;         // per step
     int* tgover;        // per build
     int* ct_total;      // contacts this step
-    int* pt_total;      // PT components this step
     int* pt_ctotal;     // PT components touching a triangle this step
     int* wl_total;      // components with a candidate wall this step
     int* step;          // contact step index
@@ -189,13 +188,9 @@ template <typename T> struct Contacts {
     unsigned char* wflag;  // per component: nonzero wall force/torque this step
     int2* wlist;           // components with a candidate wall: (component, wall mask)
     int* pt_index;  // per component: contact item or -1
-    int* pt_flag;   // per sorted position
-    int* pt_pos;    // scan of pt_flag
-    int* pt_list;   // item -> sorted position
-    int* pt_total_ptr;  // [1] PT items this step
-    int* pt_cflag;      // per PT item: touches a triangle (some body has a manifold)
+    int* pt_cflag;      // per sorted position: may touch a triangle of its cell
     int* pt_cpos;       // scan of pt_cflag
-    int* pt_clist;      // contact item k -> PT item
+    int* pt_clist;      // contact item k -> sorted position
     int* pt_ctotal_ptr; // [1] contact items this step
     double* pt_res; // [component][6] particle-side PT load (valid where pt_index >= 0)
     double* pt_body;    // [contact item][nbs][kPtRecord]
