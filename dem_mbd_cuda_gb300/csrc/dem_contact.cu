@@ -600,6 +600,12 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
 
 // ------------------------------------------------------------------- PT
 
+__device__ __noinline__ double circle_triangle_area_fp64(V3<double> n, V3<double> ra, V3<double> rb, V3<double> rc,
+                                                        double r)
+{
+    return circle_triangle_area<double>(n, ra, rb, rc, r);
+}
+
 // bodyTriangleAreaScale (:380-407); also returns distance along the outward
 // normal.
 template <typename T>
@@ -626,8 +632,13 @@ __device__ double tri_area_scale(const double* W, V3<double> p, double r, double
     if constexpr (sizeof(T) == sizeof(double)) {
         area = circle_triangle_area<double>(n, ra, rb, rc, sqrt(c2));
     } else {
+        // FP32 area, except where it decides the threshold: a scale below
+        // 1e-4 (a disk that grazes the triangle, where FP32 cancellation
+        // noise exceeds the 1e-12 cut) is recomputed in FP64, so the set of
+        // manifolds is the FP64 one
         area = (double)circle_triangle_area<float>(cvt<float>(n), cvt<float>(ra), cvt<float>(rb), cvt<float>(rc),
                                                    sqrtf((float)c2));
+        if (!(area >= 1.0e-4 * kPi * c2)) area = circle_triangle_area_fp64(n, ra, rb, rc, sqrt(c2));
     }
     if (area <= 0.0) return 0.0;
     const double sc = fmin(1.0, area / (kPi * c2));

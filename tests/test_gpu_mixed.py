@@ -49,13 +49,18 @@ def test_mixed_first_evaluation(maker):
 
 def test_mixed_pt_fp32_option():
     """With the particle-triangle law in FP32 too, body loads carry FP32
-    error (bar 1e-4 relative)."""
+    error (bar 1e-4 relative), but the set of manifolds is the FP64 one:
+    areas that decide the 1e-12 cut are recomputed in FP64."""
     sc = G.small_mbd()
     e = engine_for(sc, precision="mixed", pt_fp32=True)
     o = Oracle(sc)
     le = e.computeForces(0.0, sc.body_states(), True, True)
     lo = o.compute_forces(sc.body_states())
     assert np.abs(le - lo).max() <= 1e-4 * np.abs(lo).max()
+    assert e.stepStats()["body_contacts"] == o.stats()["body_contacts"]
+    k1, _, _ = e.history(2)
+    k2, _, _ = o.history(2)
+    np.testing.assert_array_equal(k1, k2)
 
 
 def test_mixed_trajectory_stays_close():
