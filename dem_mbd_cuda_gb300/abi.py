@@ -26,6 +26,7 @@ class CStepStats(C.Structure):
         ("body_history_overflows", C.c_int), ("particle_history_high_water", C.c_int),
         ("body_history_high_water", C.c_int), ("triangle_grid_overflows", C.c_int),
         ("cell_table_overflows", C.c_int), ("body_regime_interval_native_steps", C.c_uint64),
+        ("body_candidate_items", C.c_int), ("wall_candidates", C.c_int),
     ]
 
     def to_dict(self):

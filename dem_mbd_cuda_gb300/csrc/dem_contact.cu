@@ -287,12 +287,16 @@ __device__ __noinline__ void wall_contact(const Comps& c, const Owners& o, const
 // flag of the step starts cleared.  The list's order does not matter: pass
 // 2 handles each component whole, in one thread, so the FP64 work runs in
 // full warps instead of one lane in every warp that holds a wall particle.
+template <typename T>
 __global__ void __launch_bounds__(256) k_walls_probe(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
-                                                     unsigned char* wflag, int2* wlist, int* wl_total)
+                                                     Hist<T> hw, Counters k, unsigned char* wflag, int2* wlist)
 {
     const int ci = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned cand = 0u;
     if (ci < c.n) {
+        // expireHistory (:1109-1117) of the wall slots, before pass 2
+        // acquires any for this step
+        expire(hw, kWSlots, ci, *k.step);
         wflag[ci] = 0;
         const SceneC& S = sc[o.scene[c.owner[ci]]];
         if (S.wall_count > 0) {
@@ -311,7 +315,7 @@ __global__ void __launch_bounds__(256) k_walls_probe(Comps c, Owners o, const Sc
     if (m) {
         const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
         int base = 0;
-        if (lane == leader) base = atomicAdd(wl_total, __popc(m));
+        if (lane == leader) base = atomicAdd(k.wl_total, __popc(m));
         base = __shfl_sync(0xffffffffu, base, leader);
         if (cand) wlist[base + __popc(m & ((1u << lane) - 1u))] = make_int2(ci, (int)cand);
     }
@@ -402,9 +406,9 @@ __device__ __noinline__ bool exact_contact(const D4* __restrict__ pos, const int
 // FP64 test and the history slot acquisition (acquireHistorySlot, :190-215)
 // on them in order.  Contacts go to a flat list; results are stored per
 // (slot rank, component) so the owner sum reads them coalesced.
-template <typename T, typename TB>
-__global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __restrict__ sc, Tris tris, Hist<T> hp,
-                                               Hist<T> hw, Hist<TB> hb, Contacts<T> ct, Counters k, int nc)
+template <typename T>
+__global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __restrict__ sc, Hist<T> hp,
+                                               Contacts<T> ct, Counters k, int nc)
 {
     const int step = *k.step;
     const int nvalid = *g.nvalid;
@@ -426,11 +430,10 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         const float offy[3] = {-mesh_f - fi.y, -fi.y, mesh_f - fi.y};
         const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
         const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
-        // expireHistory (:1109-1117) for the component's three slot arrays,
-        // before any slot of this step is acquired
+        // expireHistory (:1109-1117) for the component's particle slots,
+        // before any slot of this step is acquired (the wall and body slots
+        // expire in their own probes)
         expire(hp, kPSlots, ci, step);
-        expire(hw, kWSlots, ci, step);
-        expire(hb, kBSlots, ci, step);
         int phw = hp.hw[ci];
         int pending = 0;  // candidates in stage_t[count .. count + pending)
         // Phase 2 over the staged candidates, in order.  A candidate staged
@@ -678,10 +681,15 @@ __device__ __forceinline__ bool pt_may_touch(const float4* __restrict__ tf, int 
 // flag may be set for a component without a manifold (the law kernel then
 // finds none), never cleared for one with.  Components in cells without
 // triangles leave at once.
-__global__ void __launch_bounds__(256) k_pt_probe(Grid g, Recs r, Tris tris, int* cflag)
+template <typename TB>
+__global__ void __launch_bounds__(256) k_pt_probe(Grid g, Recs r, Tris tris, Hist<TB> hb, Counters k, int* cflag)
 {
     const int nvalid = *g.nvalid;
+    const int step = *k.step;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
+        // expireHistory (:1109-1117) of the body slots, before the law
+        // kernels acquire any for this step
+        expire(hb, kBSlots, g.sorted_id[t], step);
         const int lin = r.cell[t].w;
         const int tb = tris.tcell_start[lin];
         const int te = min(tris.tcell_start[lin + 1], tris.capacity);
@@ -1475,17 +1483,17 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
 {
     (void)block;
     if (stage & 2) {
-        k_sweep<T, TB><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, t, hp, hw, hb, ct, k, c.n);
+        k_sweep<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, hp, ct, k, c.n);
         if (ct.tape.pp) k_tape_pp<T><<<sm_count * 8, 256, 0, s>>>(r, hp, ct, k);
     }
     if ((stage & 1) && w.count > 0) {
-        k_walls_probe<<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, ct.wflag, ct.wlist, k.wl_total);
+        k_walls_probe<T><<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, hw, k, ct.wflag, ct.wlist);
         k_walls_law<T><<<sm_count * 4, 128, 0, s>>>(c, o, sc, w, hw, ct, k, dt_eff);
     }
     if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
-        k_pt_probe<<<sm_count * 8, 256, 0, s>>>(g, r, t, ct.pt_cflag);
-        launch_scan(ct.pt_cflag, ct.pt_cpos, g.nvalid, g.tile_sums, sm_count, s);
+        k_pt_probe<TB><<<sm_count * 8, 256, 0, s>>>(g, r, t, hb, k, ct.pt_cflag);
+        launch_scan(ct.pt_cflag, ct.pt_cpos, g.nvalid, ct.pt_tile_sums, sm_count, s);
         k_pt_compact_contacts<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_cflag, ct.pt_cpos, ct.pt_clist, ct.pt_index,
                                                            ct.pt_ctotal_ptr);
         k_pt_warp<T, TB><<<sm_count * 8, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);

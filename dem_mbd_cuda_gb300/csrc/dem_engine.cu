@@ -102,8 +102,10 @@ public:
         for (cudaGraphExec_t g : {graph_fa_, graph_f_, graph_mbd_fa_, graph_mbd_f_})
             if (g) cudaGraphExecDestroy(g);
         for (auto* e : ev_) if (e) cudaEventDestroy(e);
+        for (auto* e : fork_ev_) if (e) cudaEventDestroy(e);
         arena_.release();
         if (pinned_) cudaFreeHost(pinned_);
+        for (auto* b : branch_) if (b) cudaStreamDestroy(b);
         if (stream_) cudaStreamDestroy(stream_);
     }
 
@@ -131,6 +133,8 @@ public:
         check(cudaMemGetInfo(&free_before_, &total_mem), "cudaMemGetInfo");
         check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         for (auto*& e : ev_) check(cudaEventCreate(&e), "cudaEventCreate");
+        for (auto*& b : branch_) check(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto*& e : fork_ev_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
 
         S_ = nscenes;
         dt_ = scenes[0].dt;
@@ -431,6 +435,7 @@ public:
             T_.tcell_start = arena_.alloc<int>(cap + 2, "tri cell start");
             check(cudaMemsetAsync(T_.tcell_count, 0, sizeof(int) * (cap + 1), s), "clear");
             check(cudaMemsetAsync(T_.tcell_cursor, 0, sizeof(int) * (cap + 1), s), "clear");
+            T_.tile_sums = arena_.alloc<int>(cap / 4096 + 64, "tri tile sums");
         }
 
         // ---- counters
@@ -518,6 +523,7 @@ public:
             ct.pt_cpos = arena_.alloc<int>(nc_ + 2, "pt contact pos");
             ct.pt_clist = arena_.alloc<int>(nc_, "pt contact list");
             ct.pt_ctotal_ptr = K_.pt_ctotal;
+            ct.pt_tile_sums = arena_.alloc<int>((size_t)nc_ / 4096 + 64, "pt tile sums");
             ct.pt_res = arena_.alloc<double>((size_t)nc_ * 6, "pt results");
             ct.pt_body = arena_.alloc<double>((size_t)nc_ * ct.nbs * kPtRecord, "pt body records");
             if (keep_bp_ || keep_bd_) ct.pt_out = arena_.alloc<double>((size_t)nc_ * ct.nbs * 25, "pt outputs");
@@ -531,27 +537,75 @@ public:
         cudaStream_t s = stream_;
         int e = 0;
         auto mark = [&]() { if (timed && e < (int)ev_.size()) check(cudaEventRecord(ev_[e++], s), "event"); };
-        mark();
+        auto contacts = [&](int stage, cudaStream_t on) {
+            launch_contacts<T, TB>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, on,
+                                   stage);
+        };
+        const bool walls = W_.count > 0, pt = nb_ > 0 && nt_ > 0;
+        if (timed) {
+            // one stream, phase by phase, for the phase timers
+            mark();
+            launch_step_counter(K_, 1, s);
+            if (!sphere_) launch_update_components(C_, O_, s);
+            launch_grid_layout(C_, O_, G_, s);
+            launch_grid_sort(C_, O_, G_, sm_count_, s);
+            mark();
+            if (pt) launch_tri_build(T_, B_, G_, K_.tgover, sm_count_, s);
+            if (O_.ugx) launch_universal_gravity(O_, s);
+            launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
+            mark();
+            for (int stage : {2, 1, 4, 8}) {
+                contacts(stage, s);
+                mark();
+            }
+            launch_owner_sum<T>(C_, O_, d_sc_, ct, false, nullptr, nullptr, nullptr, nullptr, s);
+            mark();
+            if (nb_ > 0) launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
+            launch_step_counter(K_, 0, s);
+            mark();
+            n_marks_ = e;
+            return;
+        }
+        // Three branches (a DAG when captured into the step graph).  The
+        // walls need only the component state; the triangle grid only the
+        // cell layout; the PT law the gathered records and the triangle
+        // grid; the owner sum all three.  Each branch touches its own
+        // history array and result buffers (the wall and body slots expire in
+        // their own probes), so the branches are independent.
+        cudaStream_t bw = branch_[0], bt = branch_[1];
+        auto link = [&](cudaStream_t from, cudaStream_t to, int ev) {
+            check(cudaEventRecord(fork_ev_[ev], from), "fork event");
+            check(cudaStreamWaitEvent(to, fork_ev_[ev], 0), "fork wait");
+        };
         launch_step_counter(K_, 1, s);
         if (!sphere_) launch_update_components(C_, O_, s);
-        launch_grid_build(C_, O_, G_, sm_count_, s);
-        mark();
-        if (nb_ > 0 && nt_ > 0) launch_tri_build(T_, B_, G_, K_.tgover, sm_count_, s);
+        if (walls) {
+            link(s, bw, 0);
+            contacts(1, bw);
+        }
+        launch_grid_layout(C_, O_, G_, s);
+        if (pt) {
+            link(s, bt, 1);
+            launch_tri_build(T_, B_, G_, K_.tgover, sm_count_, bt);
+        }
+        launch_grid_sort(C_, O_, G_, sm_count_, s);
         if (O_.ugx) launch_universal_gravity(O_, s);
         launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
-        mark();
-        // sweep (with the history expiry), walls, particle law, bodies
-        for (int stage : {2, 1, 4, 8}) {
-            launch_contacts<T, TB>(C_, O_, G_, R_, d_sc_, W_, T_, B_, hp, hw, hb, ct, K_, dt_eff, block_, sm_count_, s,
-                                   stage);
-            mark();
+        if (pt) {
+            link(s, bt, 2);
+            contacts(8, bt);
+        }
+        contacts(2, s);
+        contacts(4, s);
+        if (walls) link(bw, s, 3);
+        if (pt) {
+            link(bt, s, 4);
+            launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, bt);
         }
         launch_owner_sum<T>(C_, O_, d_sc_, ct, false, nullptr, nullptr, nullptr, nullptr, s);
-        mark();
-        if (nb_ > 0) launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
+        if (pt) link(bt, s, 5);
+        else if (nb_ > 0) launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
         launch_step_counter(K_, 0, s);
-        mark();
-        n_marks_ = e;
     }
 
     void forces(double dt_eff, bool timed = false)
@@ -657,6 +711,8 @@ public:
         st.triangle_grid_overflows = cnt[5];
         st.cell_table_overflows = (err & kErrCellCapacity) ? 1 : 0;
         st.body_regime_interval_native_steps = native;
+        st.body_candidate_items = cnt[9];
+        st.wall_candidates = cnt[10];
         reg_inst_.assign((size_t)kRegime * nb_, 0ull);
         reg_int_.assign(rint.begin(), rint.begin() + (size_t)kRegime * nb_);
         micro_inst_.assign((size_t)kMicro * nb_, 0.0);
@@ -1395,6 +1451,10 @@ public:
     int step_index_ = 0;
     size_t free_before_ = 0;
     cudaStream_t stream_ = nullptr;
+    // Branches of a force evaluation: [0] walls, [1] triangle grid + PT +
+    // body reduction; forked from and joined back into stream_ by events.
+    std::array<cudaStream_t, 2> branch_{};
+    std::array<cudaEvent_t, 6> fork_ev_{};
     std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;
     DeviceArena arena_, arena_tmp_, adj_arena_;

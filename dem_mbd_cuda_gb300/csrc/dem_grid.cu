@@ -608,11 +608,16 @@ void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int 
     k_scan_apply<<<g, kScanBlock, 0, s>>>(in, out, n_dev, tile_sums);
 }
 
-void launch_grid_build(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s)
+void launch_grid_layout(const Comps& c, const Owners& o, const Grid& g, cudaStream_t s)
 {
     if (c.n <= 0) return;
     k_cell_keys<<<blocks(c.n, 256), 256, 0, s>>>(c, o, g);
     k_layout<<<1, 256, 0, s>>>(g);
+}
+
+void launch_grid_sort(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s)
+{
+    if (c.n <= 0) return;
     k_cell_count<<<blocks(c.n, 256), 256, 0, s>>>(c, o, g);
     launch_scan(g.cell_count, g.cell_start, g.total_cells, g.tile_sums, sm_count, s);
     k_scatter<<<blocks(c.n, 256), 256, 0, s>>>(c, g);
@@ -628,7 +633,7 @@ void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover
 {
     if (t.nt <= 0) return;
     k_tri_count<<<blocks(32 * t.nt, 128), 128, 0, s>>>(t, g, tgover);
-    launch_scan(t.tcell_count, t.tcell_start, g.total_cells, g.tile_sums, sm_count, s);
+    launch_scan(t.tcell_count, t.tcell_start, g.total_cells, t.tile_sums, sm_count, s);
     k_tri_fill<<<blocks(32 * t.nt, 128), 128, 0, s>>>(t, g);
     k_tri_place<<<sm_count * 8, 256, 0, s>>>(t, g);
 }

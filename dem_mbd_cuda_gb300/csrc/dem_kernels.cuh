@@ -128,6 +128,7 @@ struct Tris {
     int* scene;     // per triangle
     int capacity;   // triangle grid entry capacity
     int *tcell_count, *tcell_cursor, *tcell_start, *ttri, *ttri_tmp, *tlin_tmp;
+    int* tile_sums;  // scan scratch of the triangle grid (it builds beside the particle grid)
 };
 
 struct Bodies {
@@ -192,6 +193,7 @@ template <typename T> struct Contacts {
     int* pt_cpos;       // scan of pt_cflag
     int* pt_clist;      // contact item k -> sorted position
     int* pt_ctotal_ptr; // [1] contact items this step
+    int* pt_tile_sums;  // scan scratch of the contact-item compaction
     double* pt_res; // [component][6] particle-side PT load (valid where pt_index >= 0)
     double* pt_body;    // [contact item][nbs][kPtRecord]
     double* pt_out;     // [contact item][nbs][25] optional output detail
@@ -210,7 +212,10 @@ struct BodyOut {
 
 // ------------------------------------------------------------- launchers
 void launch_update_components(const Comps& c, const Owners& o, cudaStream_t s);
-void launch_grid_build(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s);
+// The particle grid in two parts: cell keys and the per-scene cell layout
+// (all the triangle grid needs), then the counting sort.
+void launch_grid_layout(const Comps& c, const Owners& o, const Grid& g, cudaStream_t s);
+void launch_grid_sort(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s);
 void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int sm_count, cudaStream_t s);
 void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s);
 void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover, int sm_count, cudaStream_t s);

@@ -135,6 +135,10 @@ typedef struct dem_step_stats {
     int triangle_grid_overflows;
     int cell_table_overflows;      /* engine-only: dense cell table capacity */
     uint64_t body_regime_interval_native_steps;
+    int body_candidate_items;      /* engine-only: (particle, cell) items that the
+                                      FP32 particle-triangle probe passed */
+    int wall_candidates;           /* engine-only: particle-wall pairs that the
+                                      FP32 plane test passed */
 } dem_step_stats;
 
 typedef struct dem_engine dem_engine;

@@ -43,8 +43,30 @@ def test_struct_layouts_match_header():
     from dem_mbd_cuda_gb300.scene import CMech, CScene
     assert C.sizeof(CMech) == 8 * 8
     assert C.sizeof(COptions) == 32
-    assert C.sizeof(CStepStats) == 56
+    assert C.sizeof(CStepStats) == 64
     assert C.sizeof(CScene) % 8 == 0
+
+
+def test_struct_sizes_match_compiled_header(tmp_path):
+    """The ctypes mirrors against sizeof() of the header's structs as the C
+    compiler lays them out."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    from dem_mbd_cuda_gb300.abi import COptions, CStepStats
+    from dem_mbd_cuda_gb300.scene import CMech, CScene
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = Path(__file__).resolve().parents[1] / "include"
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "dem_gb300.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu\\n", sizeof(dem_mech), sizeof(dem_options),'
+                   ' sizeof(dem_step_stats), sizeof(dem_scene));return 0;}\n')
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == [C.sizeof(CMech), C.sizeof(COptions), C.sizeof(CStepStats), C.sizeof(CScene)]
 
 
 def test_scene_struct_roundtrip():
