@@ -103,6 +103,7 @@ public:
             if (g) cudaGraphExecDestroy(g);
         for (auto* e : ev_) if (e) cudaEventDestroy(e);
         for (auto* e : fork_ev_) if (e) cudaEventDestroy(e);
+        if (body_ready_) cudaEventDestroy(body_ready_);
         arena_.release();
         if (pinned_) cudaFreeHost(pinned_);
         for (auto* b : branch_) if (b) cudaStreamDestroy(b);
@@ -135,6 +136,7 @@ public:
         for (auto*& e : ev_) check(cudaEventCreate(&e), "cudaEventCreate");
         for (auto*& b : branch_) check(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking), "cudaStreamCreate");
         for (auto*& e : fork_ev_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        check(cudaEventCreateWithFlags(&body_ready_, cudaEventDisableTiming), "cudaEventCreate");
 
         S_ = nscenes;
         dt_ = scenes[0].dt;
@@ -399,8 +401,19 @@ public:
             W_.plane = arena_.upload(pl.data(), pl.size(), "wall planes", s);
         }
         B_.nb = nb_;
-        B_.c = arena_.upload(bc.data(), bc.size(), "body c", s); B_.q = arena_.upload(bq.data(), bq.size(), "body q", s);
-        B_.v = arena_.upload(bv.data(), bv.size(), "body v", s); B_.w = arena_.upload(bw.data(), bw.size(), "body w", s);
+        {
+            // c, q, v, w of all bodies in one block, in the pinned staging
+            // layout, so a step's body state moves in one copy
+            std::vector<double> st;
+            st.insert(st.end(), bc.begin(), bc.end());
+            st.insert(st.end(), bq.begin(), bq.end());
+            st.insert(st.end(), bv.begin(), bv.end());
+            st.insert(st.end(), bw.begin(), bw.end());
+            st.resize(13 * (size_t)std::max(nb_, 1), 0.0);
+            B_.c = arena_.upload(st.data(), st.size(), "body state", s);
+            const size_t m = (size_t)std::max(nb_, 1);
+            B_.q = B_.c + 3 * m; B_.v = B_.c + 7 * m; B_.w = B_.c + 10 * m;
+        }
         B_.scene = arena_.upload(bscene.data(), bscene.size(), "body scene", s);
         T_.nt = nt_;
         if (nt_ > 0) {
@@ -408,7 +421,7 @@ public:
             T_.scene = arena_.upload(tscene.data(), tscene.size(), "tri scene", s);
             T_.local = upd(tloc, "tri local");
             T_.world = arena_.alloc<double>(16 * (size_t)nt_, "tri world");
-            T_.aabb = arena_.alloc<double>(6 * (size_t)nt_, "tri aabb");
+            T_.trange = arena_.alloc<int>(6 * (size_t)nt_, "tri cell range");
             T_.tf = arena_.alloc<float4>(2 * (size_t)nt_, "tri fp32 planes");
             // rotation-invariant bound of the cells a padded triangle box covers
             long long tcap = 0;
@@ -477,7 +490,7 @@ public:
         // host MBD state
         hbhv_.assign(3 * nb_, 0.0); hbhw_.assign(3 * nb_, 0.0); hbhq_.assign(4 * nb_, 0.0); hbhdq_.assign(4 * nb_, 0.0);
         hbacc_.assign(3 * nb_, 0.0); hbdom_.assign(3 * nb_, 0.0); hbloads_.assign(6 * nb_, 0.0);
-        if (nb_ > 0) launch_tri_transform(T_, B_, s);
+        if (nb_ > 0) launch_tri_transform(T_, B_, d_sc_, s);
         if (!sphere_) launch_update_components(C_, O_, s);
         check(cudaStreamSynchronize(s), "initialize");
         initialized_ = true;
@@ -531,8 +544,15 @@ public:
     }
 
     // ----------------------------------------------------------- pipeline
+    // Work a force evaluation carries at its ends: the body-frame triangle
+    // transform before it, the body-result download after the body
+    // reduction (with the event the host waits on for the MBD step), and
+    // the leapfrog finish (or finish + next advance) after the owner sum.
+    enum : unsigned { kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kTailFinishAdvance = 8 };
+
     template <typename T, typename TB>
-    void enqueue_forces(double dt_eff, Hist<T>& hp, Hist<T>& hw, Hist<TB>& hb, Contacts<T>& ct, bool timed)
+    void enqueue_forces(double dt_eff, Hist<T>& hp, Hist<T>& hw, Hist<TB>& hb, Contacts<T>& ct, bool timed,
+                        unsigned tail)
     {
         cudaStream_t s = stream_;
         int e = 0;
@@ -542,6 +562,22 @@ public:
                                    stage);
         };
         const bool walls = W_.count > 0, pt = nb_ > 0 && nt_ > 0;
+        auto integrate = [&](cudaStream_t on) {
+            if (tail & kTailFinishAdvance) launch_finish_advance(O_, dt_, on);
+            else if (tail & kTailFinish) launch_finish(O_, dt_, on);
+        };
+        auto download = [&](cudaStream_t on) {
+            if (!(tail & kTailD2H) || nb_ <= 0) return;
+            check(cudaMemcpyAsync(pin_body_result(), BO_.result, sizeof(double) * nb_ * kBodyFieldCount,
+                                  cudaMemcpyDeviceToHost, on), "download body result");
+            // in a captured graph the record must be an event node of its own
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            check(cudaStreamIsCapturing(on, &cs), "capture status");
+            check(cudaEventRecordWithFlags(body_ready_, on,
+                                           cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u),
+                  "body result event");
+        };
+        if ((tail & kTailTransform) && nb_ > 0 && (timed || !pt)) launch_tri_transform(T_, B_, d_sc_, s);
         if (timed) {
             // one stream, phase by phase, for the phase timers
             mark();
@@ -564,6 +600,8 @@ public:
             launch_step_counter(K_, 0, s);
             mark();
             n_marks_ = e;
+            download(s);
+            integrate(s);
             return;
         }
         // Three branches (a DAG when captured into the step graph).  The
@@ -577,6 +615,10 @@ public:
             check(cudaEventRecord(fork_ev_[ev], from), "fork event");
             check(cudaStreamWaitEvent(to, fork_ev_[ev], 0), "fork wait");
         };
+        if (pt && (tail & kTailTransform)) {
+            link(s, bt, 6);
+            launch_tri_transform(T_, B_, d_sc_, bt);
+        }
         launch_step_counter(K_, 1, s);
         if (!sphere_) launch_update_components(C_, O_, s);
         if (walls) {
@@ -601,20 +643,27 @@ public:
         if (pt) {
             link(bt, s, 4);
             launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, bt);
+            download(bt);
         }
         launch_owner_sum<T>(C_, O_, d_sc_, ct, false, nullptr, nullptr, nullptr, nullptr, s);
+        if (!pt && nb_ > 0) {
+            launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
+            download(s);
+        }
+        // the integrator needs only the owner sum: it overlaps the body
+        // reduction and the download the host waits for
+        integrate(s);
         if (pt) link(bt, s, 5);
-        else if (nb_ > 0) launch_body_reduce<T>(R_, d_sc_, B_, ct, BO_, dt_eff > 0.0, s);
         launch_step_counter(K_, 0, s);
     }
 
-    void forces(double dt_eff, bool timed = false)
+    void forces(double dt_eff, bool timed = false, unsigned tail = 0)
     {
         if (precision_ == DEM_PRECISION_MIXED) {
-            if (pt_fp32_) enqueue_forces<float, float>(dt_eff, hp32_, hw32_, hb32_, ct32_, timed);
-            else enqueue_forces<float, double>(dt_eff, hp32_, hw32_, hb64_, ct32_, timed);
+            if (pt_fp32_) enqueue_forces<float, float>(dt_eff, hp32_, hw32_, hb32_, ct32_, timed, tail);
+            else enqueue_forces<float, double>(dt_eff, hp32_, hw32_, hb64_, ct32_, timed, tail);
         } else {
-            enqueue_forces<double, double>(dt_eff, hp64_, hw64_, hb64_, ct64_, timed);
+            enqueue_forces<double, double>(dt_eff, hp64_, hw64_, hb64_, ct64_, timed, tail);
         }
         check(cudaGetLastError(), "force pipeline launch");
     }
@@ -635,15 +684,8 @@ public:
     void enqueue_body_h2d()
     {
         double* p = pin_body_state();
-        check(cudaMemcpyAsync(B_.c, p, sizeof(double) * 3 * nb_, cudaMemcpyHostToDevice, stream_), "upload body c");
-        check(cudaMemcpyAsync(B_.q, p + 3 * nb_, sizeof(double) * 4 * nb_, cudaMemcpyHostToDevice, stream_), "upload body q");
-        check(cudaMemcpyAsync(B_.v, p + 7 * nb_, sizeof(double) * 3 * nb_, cudaMemcpyHostToDevice, stream_), "upload body v");
-        check(cudaMemcpyAsync(B_.w, p + 10 * nb_, sizeof(double) * 3 * nb_, cudaMemcpyHostToDevice, stream_), "upload body w");
-    }
-    void enqueue_body_d2h()
-    {
-        check(cudaMemcpyAsync(pin_body_result(), BO_.result, sizeof(double) * nb_ * kBodyFieldCount,
-                              cudaMemcpyDeviceToHost, stream_), "download body result");
+        check(cudaMemcpyAsync(B_.c, p, sizeof(double) * 13 * std::max(nb_, 1), cudaMemcpyHostToDevice, stream_),
+              "upload body state");
     }
     void body_forces_from_pinned(double* out)
     {
@@ -667,11 +709,9 @@ public:
             std::memcpy(hbw_.data(), bodies->omega, sizeof(double) * 3 * nb_);
             upload_body_state_async();
         }
-        if (nb_ > 0) launch_tri_transform(T_, B_, s);
         const double dt_eff = step_index_ == 0 ? 0.0 : dt_;
-        forces(dt_eff, timed);
+        forces(dt_eff, timed, kTailTransform | (nb_ > 0 && (body_forces || diag) ? kTailD2H : 0u));
         ++step_index_;
-        if (nb_ > 0 && (body_forces || diag)) enqueue_body_d2h();
         if (diag) return collect_diagnostics(body_forces);
         if (body_forces && nb_ > 0) {
             check(cudaStreamSynchronize(s), "compute forces");
@@ -877,12 +917,14 @@ public:
             check(cudaGraphLaunch(g, stream_), "cudaGraphLaunch");
             ++step_index_;
             if (mbd) {
-                check(cudaStreamSynchronize(stream_), "mbd step");
+                // the loads are on the host once the download's event fires;
+                // the particle integrator may still be running
+                check(cudaEventSynchronize(body_ready_), "mbd step");
                 body_forces_from_pinned(hbloads_.data());
                 body_half_update(false, dt_);
             }
         }
-        if (!mbd) check(cudaStreamSynchronize(stream_), "run steps");
+        check(cudaStreamSynchronize(stream_), "run steps");
     }
 
     // Captured force evaluation with dt, optionally with the body upload /
@@ -893,14 +935,8 @@ public:
         cudaGraph_t g = nullptr;
         check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
         try {
-            if (mbd) {
-                enqueue_body_h2d();
-                launch_tri_transform(T_, B_, stream_);
-            }
-            forces(dt_, false);
-            if (mbd) enqueue_body_d2h();
-            if (fused) launch_finish_advance(O_, dt_, stream_);
-            else launch_finish(O_, dt_, stream_);
+            if (mbd) enqueue_body_h2d();
+            forces(dt_, false, (mbd ? kTailTransform | kTailD2H : 0u) | (fused ? kTailFinishAdvance : kTailFinish));
         } catch (...) {
             cudaStreamEndCapture(stream_, &g);
             if (g) cudaGraphDestroy(g);
@@ -1454,7 +1490,8 @@ public:
     // Branches of a force evaluation: [0] walls, [1] triangle grid + PT +
     // body reduction; forked from and joined back into stream_ by events.
     std::array<cudaStream_t, 2> branch_{};
-    std::array<cudaEvent_t, 6> fork_ev_{};
+    std::array<cudaEvent_t, 7> fork_ev_{};
+    cudaEvent_t body_ready_ = nullptr;  // recorded after the body-result download
     std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;
     DeviceArena arena_, arena_tmp_, adj_arena_;

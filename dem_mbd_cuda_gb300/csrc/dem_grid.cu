@@ -300,7 +300,7 @@ __global__ void k_scan_apply(const int* in, int* out, const int* n_dev, const in
 
 // ------------------------------------------------------------- triangles
 // transformTrianglesKernel (src/cuda/cuda_body_backend.cu:71-112).
-__global__ void k_tri_transform(Tris t, Bodies b)
+__global__ void k_tri_transform(Tris t, Bodies b, const SceneC* __restrict__ sc)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= t.nt) return;
@@ -331,53 +331,46 @@ __global__ void k_tri_transform(Tris t, Bodies b)
             t.tf[2 * (size_t)i + 1] = make_float4((float)gx, (float)gy, (float)gz, (float)W[15]);
         }
     }
-    double* A = t.aabb + 6 * (size_t)i;
-    double mnx = W[0], mny = W[1], mnz = W[2], mxx = W[0], mxy = W[1], mxz = W[2];
-    for (int k = 1; k < 4; ++k) {
-        mnx = fmin(mnx, W[3 * k]); mny = fmin(mny, W[3 * k + 1]); mnz = fmin(mnz, W[3 * k + 2]);
-        mxx = fmax(mxx, W[3 * k]); mxy = fmax(mxy, W[3 * k + 1]); mxz = fmax(mxz, W[3 * k + 2]);
+    // Padded-AABB cell range (countTriangleCellsKernel,
+    // src/cuda/cuda_contact_backend.cu:409-452): floor((min - pad) / mesh)
+    // .. floor((max + pad) / mesh) per axis, the same range check as a
+    // particle key.  Computed once per triangle here; the grid kernels clip
+    // it to the cell layout with integer arithmetic only.
+    double mn[3] = {W[0], W[1], W[2]}, mx[3] = {W[0], W[1], W[2]};
+    for (int k = 1; k < 4; ++k)
+        for (int a = 0; a < 3; ++a) { mn[a] = fmin(mn[a], W[3 * k + a]); mx[a] = fmax(mx[a], W[3 * k + a]); }
+    const SceneC& S = sc[t.scene[i]];
+    const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
+    int* R = t.trange + 6 * (size_t)i;
+    bool ok = true;
+    int lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        const double l = floor((mn[a] - S.pad) * S.inv_mesh);
+        const double h = floor((mx[a] + S.pad) * S.inv_mesh);
+        if (!isfinite(l) || !isfinite(h) || l < minCell || h > maxCell) ok = false;
+        lo[a] = ok ? (int)l : 0;
+        hi[a] = ok ? (int)h : 0;
     }
-    A[0] = mnx; A[1] = mny; A[2] = mnz; A[3] = mxx; A[4] = mxy; A[5] = mxz;
+    for (int a = 0; a < 3; ++a) { R[a] = lo[a]; R[3 + a] = hi[a]; }
+    if (!ok) R[0] = INT_MAX;
 }
 
-// Padded-AABB cell range of a triangle (countTriangleCellsKernel,
-// src/cuda/cuda_contact_backend.cu:409-452), clipped to the particle cell box
-// of its scene: only those cells are ever looked up.
+// The stored cell range of triangle i clipped to the particle cell box of
+// its scene: only those cells are ever looked up.
 __device__ bool tri_cell_range(const Tris& t, const Grid& g, int i, int lo[3], int hi[3], const int*& lay)
 {
-    const double* A = t.aabb + 6 * (size_t)i;
-    const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
-    const SceneC& S = g.sc[t.scene[i]];
-    const double pad = S.pad, inv_mesh = S.inv_mesh;
-    for (int a = 0; a < 3; ++a) {
-        const double mn = floor((A[a] - pad) * inv_mesh);
-        const double mx = floor((A[3 + a] + pad) * inv_mesh);
-        if (!isfinite(mn) || !isfinite(mx) || mn < minCell || mx > maxCell) return false;
-        lo[a] = (int)mn;
-        hi[a] = (int)mx;
-    }
+    const int* R = t.trange + 6 * (size_t)i;
     lay = g.scene_layout + 8 * t.scene[i];
     if (lay[7] == 0) return false;
     for (int a = 0; a < 3; ++a) {
-        lo[a] = max(lo[a], lay[a]);
-        hi[a] = min(hi[a], lay[a] + lay[3 + a] - 1);
+        lo[a] = max(R[a], lay[a]);
+        hi[a] = min(R[3 + a], lay[a] + lay[3 + a] - 1);
         if (lo[a] > hi[a]) return false;
     }
     return true;
 }
 
-__device__ bool tri_range_valid(const Tris& t, const Grid& g, int i)
-{
-    const double* A = t.aabb + 6 * (size_t)i;
-    const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
-    const SceneC& S = g.sc[t.scene[i]];
-    for (int a = 0; a < 3; ++a) {
-        const double mn = floor((A[a] - S.pad) * S.inv_mesh);
-        const double mx = floor((A[3 + a] + S.pad) * S.inv_mesh);
-        if (!isfinite(mn) || !isfinite(mx) || mn < minCell || mx > maxCell) return false;
-    }
-    return true;
-}
+__device__ __forceinline__ bool tri_range_valid(const Tris& t, int i) { return t.trange[6 * (size_t)i] != INT_MAX; }
 
 // One warp per triangle, the lanes over the cells of its padded AABB.
 __global__ void k_tri_count(Tris t, Grid g, int* tgover)
@@ -385,7 +378,7 @@ __global__ void k_tri_count(Tris t, Grid g, int* tgover)
     const int lane = threadIdx.x & 31;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= t.nt) return;
-    if (!tri_range_valid(t, g, i)) {
+    if (!tri_range_valid(t, i)) {
         if (lane == 0) {
             atomicAdd(tgover, 1);
             atomicOr(g.err, kErrTriRange);
@@ -408,7 +401,7 @@ __global__ void k_tri_fill(Tris t, Grid g)
     const int lane = threadIdx.x & 31;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= t.nt) return;
-    if (!tri_range_valid(t, g, i)) return;
+    if (!tri_range_valid(t, i)) return;
     int lo[3], hi[3];
     const int* lay;
     if (!tri_cell_range(t, g, i, lo, hi, lay)) return;
@@ -624,9 +617,9 @@ void launch_grid_sort(const Comps& c, const Owners& o, const Grid& g, int sm_cou
     k_place<<<blocks(c.n, 256), 256, 0, s>>>(c, g);
 }
 
-void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s)
+void launch_tri_transform(const Tris& t, const Bodies& b, const SceneC* sc, cudaStream_t s)
 {
-    if (t.nt > 0) k_tri_transform<<<blocks(t.nt, 128), 128, 0, s>>>(t, b);
+    if (t.nt > 0) k_tri_transform<<<blocks(t.nt, 128), 128, 0, s>>>(t, b, sc);
 }
 
 void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover, int sm_count, cudaStream_t s)

@@ -123,7 +123,7 @@ struct Tris {
     int* body;
     double* local;  // [t][15]
     double* world;  // [t][16] v1..v4, normal, pad
-    double* aabb;   // [t][6]
+    int* trange;    // [t][6] padded-AABB cell range (lo xyz, hi xyz); lo.x = INT_MAX outside the key range
     float4* tf;     // [t][2] FP32 copies for prefilters: (normal, normal . v2), (centroid of v2..v4, circumradius)
     int* scene;     // per triangle
     int capacity;   // triangle grid entry capacity
@@ -217,7 +217,7 @@ void launch_update_components(const Comps& c, const Owners& o, cudaStream_t s);
 void launch_grid_layout(const Comps& c, const Owners& o, const Grid& g, cudaStream_t s);
 void launch_grid_sort(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s);
 void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int sm_count, cudaStream_t s);
-void launch_tri_transform(const Tris& t, const Bodies& b, cudaStream_t s);
+void launch_tri_transform(const Tris& t, const Bodies& b, const SceneC* sc, cudaStream_t s);
 void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover, int sm_count, cudaStream_t s);
 void launch_universal_gravity(const Owners& o, cudaStream_t s);
 void launch_leapfrog_init(const Owners& o, double half_dt, cudaStream_t s);
