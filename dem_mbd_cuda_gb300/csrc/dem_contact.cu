@@ -1006,7 +1006,14 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
 // by lane 0.  Sums are taken in triangle order, each term fetched from its
 // lane by shuffles, so every lane holds totals bit-identical to the serial
 // loops of k_pt_thread.
-constexpr int kPtTriCache = 128;  // per-warp cache of (area scale, distance) between the two passes
+//
+// An FP64 warp instruction costs the same with one active lane as with 32,
+// so the warp first compacts the cell's triangles that pass the FP32 test
+// (in triangle order) and runs the FP64 area and law over that list, 32 at
+// a time: one pass for any realistic contact instead of one per 32 cell
+// triangles.  A list longer than the per-warp cache takes the uncompacted
+// loops (same sums, recomputed areas).
+constexpr int kPtTriCache = 128;  // per-warp candidate list: triangle, (area scale, distance)
 
 __device__ __forceinline__ V3<double> shfl3(V3<double> v, int src)
 {
@@ -1020,6 +1027,7 @@ __global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, cons
 {
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ double2 s_ad[4][kPtTriCache];
+    __shared__ int s_tri[4][kPtTriCache];
     const int step = *k.step;
     const int total = *ct.pt_ctotal_ptr;
     if (total > k.pt_warp_items) return;
@@ -1044,19 +1052,47 @@ __global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, cons
             for (int f = lane; f < kPtRecord; f += 32) rec[f] = 0.0;
             double* outd = ct.pt_out ? ct.pt_out + ((size_t)item * ct.nbs + j) * 25 : nullptr;
             if (outd) for (int f = lane; f < 25; f += 32) outd[f] = 0.0;
-            __syncwarp();
-            // pass 1: manifold sums over the component's own cell (:1154-1183)
-            double tot = 0.0, wd = 0.0;
-            V3<double> wn = mk(0.0, 0.0, 0.0), wc = mk(0.0, 0.0, 0.0);
+            // candidates of body b: the cell's triangles that pass the FP32
+            // test, in triangle order
+            int ncand = 0;
             for (int e0 = tb; e0 < te; e0 += 32) {
                 const int e = e0 + lane;
-                double as = 0.0, dist = 0.0;
                 int tri = 0;
+                bool cand = false;
                 if (e < te) {
                     tri = tris.ttri[e];
-                    if (tris.body[tri] == b && pt_may_touch(tris.tf, tri, pq))
-                        as = tri_area_scale<T>(tris.world + 16 * (size_t)tri, it.p, it.rad, dist);
-                    if (e - tb < kPtTriCache) s_ad[wib][e - tb] = make_double2(as, dist);
+                    cand = tris.body[tri] == b && pt_may_touch(tris.tf, tri, pq);
+                }
+                const unsigned m = __ballot_sync(FULL, cand);
+                const int at = ncand + __popc(m & ((1u << lane) - 1u));
+                if (cand && at < kPtTriCache) s_tri[wib][at] = tri;
+                ncand += __popc(m);
+            }
+            __syncwarp();
+            const bool listed = ncand <= kPtTriCache;
+            // the lane's triangle of the chunk starting at k0: from the list,
+            // or (unlisted) the cell entry filtered again
+            auto lane_tri = [&](int k0, int& tri) -> bool {
+                if (listed) {
+                    if (k0 + lane >= ncand) return false;
+                    tri = s_tri[wib][k0 + lane];
+                    return true;
+                }
+                const int e = tb + k0 + lane;
+                if (e >= te) return false;
+                tri = tris.ttri[e];
+                return tris.body[tri] == b && pt_may_touch(tris.tf, tri, pq);
+            };
+            const int span = listed ? ncand : te - tb;
+            // pass 1: manifold sums (:1154-1183)
+            double tot = 0.0, wd = 0.0;
+            V3<double> wn = mk(0.0, 0.0, 0.0), wc = mk(0.0, 0.0, 0.0);
+            for (int k0 = 0; k0 < span; k0 += 32) {
+                double as = 0.0, dist = 0.0;
+                int tri = 0;
+                if (lane_tri(k0, tri)) {
+                    as = tri_area_scale<T>(tris.world + 16 * (size_t)tri, it.p, it.rad, dist);
+                    if (listed) s_ad[wib][k0 + lane] = make_double2(as, dist);
                 }
                 unsigned msk = __ballot_sync(FULL, as > 0.0);
                 while (msk) {
@@ -1099,19 +1135,18 @@ __global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, cons
             double rFz = 0.0;
             const LawC<T> lc = law_constants<T>(m, T(it.mass), T(it.rad));
             const V3<T> hroll = hload(h, 0), htan = hload(h, 1), htw = hload(h, 2);
-            for (int e0 = tb; e0 < te; e0 += 32) {
-                const int e = e0 + lane;
+            for (int k0 = 0; k0 < span; k0 += 32) {
                 double as = 0.0, dist = 0.0;
                 int tri = 0;
-                if (e < te) {
-                    tri = tris.ttri[e];
-                    if (e - tb < kPtTriCache) {
-                        const double2 ad = s_ad[wib][e - tb];
+                if (listed) {
+                    if (k0 + lane < ncand) {
+                        tri = s_tri[wib][k0 + lane];
+                        const double2 ad = s_ad[wib][k0 + lane];
                         as = ad.x;
                         dist = ad.y;
-                    } else if (tris.body[tri] == b && pt_may_touch(tris.tf, tri, pq)) {
-                        as = tri_area_scale<T>(tris.world + 16 * (size_t)tri, it.p, it.rad, dist);
                     }
+                } else if (lane_tri(k0, tri)) {
+                    as = tri_area_scale<T>(tris.world + 16 * (size_t)tri, it.p, it.rad, dist);
                 }
                 const double depthd = it.rad - dist;
                 const bool on = as > 0.0 && dist > 0.0 && depthd > 0.0;
@@ -1157,6 +1192,7 @@ __global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, cons
                 rec[9] = (double)(1 | (slide ? 2 : 0) | (twist ? 4 : 0));
                 pt_microstate(m, it, bd, mn, mc, md, tot, cvt<double>(hload(h, 1)), cvt<double>(hload(h, 2)), rec + 10);
             }
+            __syncwarp();
         }
         if (lane == 0) {
             hb.hw[ci] = bhw;

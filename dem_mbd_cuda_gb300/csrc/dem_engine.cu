@@ -99,7 +99,7 @@ class Engine {
 public:
     ~Engine()
     {
-        for (cudaGraphExec_t g : {graph_fa_, graph_f_, graph_mbd_fa_, graph_mbd_f_})
+        for (cudaGraphExec_t g : graphs_)
             if (g) cudaGraphExecDestroy(g);
         for (auto* e : ev_) if (e) cudaEventDestroy(e);
         for (auto* e : fork_ev_) if (e) cudaEventDestroy(e);
@@ -218,6 +218,7 @@ public:
             S.pad = scene_rmax[s];
             S.mesh_f = (float)S.mesh;
             S.margin_f = (float)(1.0e-5 * S.mesh);
+            S.inv_mesh_f = (float)S.inv_mesh;
             for (int a = 0; a < 3; ++a) S.g[a] = x.gravity[a];
             S.grav = x.gravity_enabled ? 1 : 0;
             S.wall_begin = (int)wo.size() / 3;
@@ -547,8 +548,14 @@ public:
     // Work a force evaluation carries at its ends: the body-frame triangle
     // transform before it, the body-result download after the body
     // reduction (with the event the host waits on for the MBD step), and
-    // the leapfrog finish (or finish + next advance) after the owner sum.
-    enum : unsigned { kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kTailFinishAdvance = 8 };
+    // the leapfrog finish (or finish + the position part of the next
+    // advance) after the owner sum.
+    // kHeadRest puts the previous step's rotational advance (the second part
+    // of a split finish + advance) at the head, beside the particle grid;
+    // kTailFinishPos ends with the first part.
+    enum : unsigned {
+        kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kHeadRest = 8, kTailFinishPos = 16
+    };
 
     template <typename T, typename TB>
     void enqueue_forces(double dt_eff, Hist<T>& hp, Hist<T>& hw, Hist<TB>& hb, Contacts<T>& ct, bool timed,
@@ -563,9 +570,13 @@ public:
         };
         const bool walls = W_.count > 0, pt = nb_ > 0 && nt_ > 0;
         auto integrate = [&](cudaStream_t on) {
-            if (tail & kTailFinishAdvance) launch_finish_advance(O_, dt_, on);
+            if (tail & kTailFinishPos) launch_finish_advance_pos(O_, dt_, on);
             else if (tail & kTailFinish) launch_finish(O_, dt_, on);
         };
+        // the rotational advance on a branch only for spheres: with clumps the
+        // component update reads the quaternions at once
+        const bool rest_branch = (tail & kHeadRest) && !timed && sphere_;
+        if ((tail & kHeadRest) && !rest_branch) launch_advance_rest(O_, dt_, sm_count_, s);
         auto download = [&](cudaStream_t on) {
             if (!(tail & kTailD2H) || nb_ <= 0) return;
             check(cudaMemcpyAsync(pin_body_result(), BO_.result, sizeof(double) * nb_ * kBodyFieldCount,
@@ -610,11 +621,15 @@ public:
         // grid; the owner sum all three.  Each branch touches its own
         // history array and result buffers (the wall and body slots expire in
         // their own probes), so the branches are independent.
-        cudaStream_t bw = branch_[0], bt = branch_[1];
+        cudaStream_t bw = branch_[0], bt = branch_[1], br = branch_[2];
         auto link = [&](cudaStream_t from, cudaStream_t to, int ev) {
             check(cudaEventRecord(fork_ev_[ev], from), "fork event");
             check(cudaStreamWaitEvent(to, fork_ev_[ev], 0), "fork wait");
         };
+        if (rest_branch) {
+            link(s, br, 7);
+            launch_advance_rest(O_, dt_, sm_count_, br);
+        }
         if (pt && (tail & kTailTransform)) {
             link(s, bt, 6);
             launch_tri_transform(T_, B_, d_sc_, bt);
@@ -623,6 +638,7 @@ public:
         if (!sphere_) launch_update_components(C_, O_, s);
         if (walls) {
             link(s, bw, 0);
+            if (rest_branch) link(br, bw, 8);  // the wall law reads velocities
             contacts(1, bw);
         }
         launch_grid_layout(C_, O_, G_, s);
@@ -632,6 +648,7 @@ public:
         }
         launch_grid_sort(C_, O_, G_, sm_count_, s);
         if (O_.ugx) launch_universal_gravity(O_, s);
+        if (rest_branch) link(br, s, 9);  // the gather reads velocities and quaternions
         launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
         if (pt) {
             link(s, bt, 2);
@@ -895,9 +912,11 @@ public:
     }
 
     // `steps` reference steps after the start: advance, then for every step
-    // the captured force evaluation; all but the last step end with the
-    // fused finish + next advance, the last with finish alone.  With bodies
-    // the host MBD step runs between graph launches.
+    // the captured force evaluation.  All but the last step end with the
+    // finish and the first part of the next advance (positions); the next
+    // step's graph starts with the second part beside its particle grid.
+    // The last step ends with finish alone.  With bodies the host MBD step
+    // runs between graph launches.
     void step_loop(int steps)
     {
         const bool mbd = nb_ > 0;
@@ -905,7 +924,7 @@ public:
         launch_advance(O_, dt_, stream_);
         for (int s = 0; s < steps; ++s) {
             const bool last = s == steps - 1;
-            cudaGraphExec_t g = mbd ? (last ? graph_mbd_f_ : graph_mbd_fa_) : (last ? graph_f_ : graph_fa_);
+            cudaGraphExec_t g = graphs_[graph_index(mbd, s > 0, last)];
             if (mbd) {
                 body_position_update(dt_);
                 double* p = pin_body_state();
@@ -927,16 +946,20 @@ public:
         check(cudaStreamSynchronize(stream_), "run steps");
     }
 
+    static int graph_index(bool mbd, bool head_rest, bool last) { return (mbd ? 4 : 0) | (head_rest ? 2 : 0) | (last ? 1 : 0); }
+
     // Captured force evaluation with dt, optionally with the body upload /
-    // load download around it, followed by finish (+ next advance).
-    void capture(cudaGraphExec_t& ex, bool mbd, bool fused)
+    // load download around it and the previous step's rotational advance at
+    // its head, followed by finish (last) or finish + the position advance.
+    void capture(cudaGraphExec_t& ex, bool mbd, bool head_rest, bool last)
     {
         if (ex) return;
         cudaGraph_t g = nullptr;
         check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
         try {
             if (mbd) enqueue_body_h2d();
-            forces(dt_, false, (mbd ? kTailTransform | kTailD2H : 0u) | (fused ? kTailFinishAdvance : kTailFinish));
+            forces(dt_, false, (mbd ? kTailTransform | kTailD2H : 0u) | (head_rest ? kHeadRest : 0u) |
+                                   (last ? kTailFinish : kTailFinishPos));
         } catch (...) {
             cudaStreamEndCapture(stream_, &g);
             if (g) cudaGraphDestroy(g);
@@ -953,13 +976,14 @@ public:
         need_init();
         check(cudaStreamSynchronize(stream_), "sync");
         K_.pt_warp_items = n;
-        for (cudaGraphExec_t* g : {&graph_fa_, &graph_f_, &graph_mbd_fa_, &graph_mbd_f_})
-            if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
+        for (cudaGraphExec_t& g : graphs_)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     }
     void ensure_graphs(bool mbd)
     {
-        if (mbd) { capture(graph_mbd_fa_, true, true); capture(graph_mbd_f_, true, false); }
-        else { capture(graph_fa_, false, true); capture(graph_f_, false, false); }
+        for (int head = 0; head < 2; ++head)
+            for (int last = 0; last < 2; ++last)
+                capture(graphs_[graph_index(mbd, head, last)], mbd, head, last);
     }
 
     // Time `steps` graph-launched steps (pure DEM) on the device; the state is
@@ -1488,9 +1512,10 @@ public:
     size_t free_before_ = 0;
     cudaStream_t stream_ = nullptr;
     // Branches of a force evaluation: [0] walls, [1] triangle grid + PT +
-    // body reduction; forked from and joined back into stream_ by events.
-    std::array<cudaStream_t, 2> branch_{};
-    std::array<cudaEvent_t, 7> fork_ev_{};
+    // body reduction, [2] the previous step's rotational advance; forked
+    // from and joined back into stream_ by events.
+    std::array<cudaStream_t, 3> branch_{};
+    std::array<cudaEvent_t, 10> fork_ev_{};
     cudaEvent_t body_ready_ = nullptr;  // recorded after the body-result download
     std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;
@@ -1499,7 +1524,7 @@ public:
     std::vector<double> oin_host_;  // owner principal inertia [n][3] (host copy)
     void* pinned_ = nullptr;
     size_t pinned_bytes_ = 0;
-    cudaGraphExec_t graph_fa_ = nullptr, graph_f_ = nullptr, graph_mbd_fa_ = nullptr, graph_mbd_f_ = nullptr;
+    std::array<cudaGraphExec_t, 8> graphs_{};  // by graph_index(bodies, rotational head, last step)
 
     Owners O_{};
     Comps C_{};

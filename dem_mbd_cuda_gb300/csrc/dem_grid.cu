@@ -17,6 +17,7 @@
 #include "../../include/dem_gb300.h"
 #include "dem_kernels.cuh"
 
+#include <algorithm>
 #include <climits>
 
 namespace demgb {
@@ -86,6 +87,43 @@ __global__ void k_update_components(Comps c, Owners o)
     c.vhz[i] = o.vhz[w] + hw.x * off.y - hw.y * off.x;
 }
 
+// The reference's cell coordinates, floor(x * inv_mesh) in FP64 per axis,
+// all finite and inside [-2^20, 2^20 - 1].  Out of line, so its FP64 work is
+// issued only by warps with a component that the FP32 estimate leaves open.
+__device__ __noinline__ bool cell_coords_exact(double x, double y, double z, double inv_mesh, int& cx, int& cy,
+                                               int& cz)
+{
+    const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
+    const double fx = floor(x * inv_mesh), fy = floor(y * inv_mesh), fz = floor(z * inv_mesh);
+    const bool ok = isfinite(fx) && isfinite(fy) && isfinite(fz) && fx >= minCell && fx <= maxCell &&
+                    fy >= minCell && fy <= maxCell && fz >= minCell && fz <= maxCell;
+    if (ok) { cx = (int)fx; cy = (int)fy; cz = (int)fz; }
+    return ok;
+}
+
+// FP32 estimate of floor(x * inv_mesh).  q = fl32(fl32(x) * fl32(inv_mesh))
+// is within 1.8e-7 |q| of the FP64 product (three FP32 roundings and one
+// FP64 one), so when q - e and q + e (e = 4e-7 |q|, which also covers the
+// rounding of q -+ e) have the same floor, that floor is the FP64 one.
+// False when open: near a cell face, at 0, or not well inside the key range
+// (|q| < 1e6 < 2^20), non-finite included.
+// floor(q) for |q| < 2^22 with FP32 adds only: adding and removing 1.5 * 2^23
+// rounds q to the nearest integer, which is one too high when above q.
+__device__ __forceinline__ float floor_small(float q)
+{
+    const float r = __fadd_rn(__fadd_rn(q, 12582912.0f), -12582912.0f);
+    return r > q ? r - 1.0f : r;
+}
+__device__ __forceinline__ bool cell_coord_f32(double x, float inv_mesh_f, int& c)
+{
+    const float q = (float)x * inv_mesh_f;
+    const float e = fmaf(4.0e-7f, fabsf(q), 1.0e-30f);
+    const float lo = floor_small(q - e), hi = floor_small(q + e);
+    // the integer of lo (|lo| < 2^22) in the low mantissa bits of lo + 1.5 * 2^23
+    c = __float_as_int(__fadd_rn(lo, 12582912.0f)) - 0x4B400000;
+    return fabsf(q) < 1.0e6f && lo == hi;
+}
+
 // computeComponentKeysKernel (src/cuda/cuda_grid_backend.cu:51-71) plus the
 // per-scene cell box.
 __global__ void k_cell_keys(Comps c, Owners o, Grid g)
@@ -94,16 +132,14 @@ __global__ void k_cell_keys(Comps c, Owners o, Grid g)
     bool ok = false;
     int cx = 0, cy = 0, cz = 0, s = INT_MAX;
     if (i < c.n) {
-        const double minCell = -(double)(1 << 20), maxCell = (double)((1 << 20) - 1);
-        const double inv_mesh = g.sc[o.scene[c.owner[i]]].inv_mesh;
-        const double fx = floor(c.x[i] * inv_mesh);
-        const double fy = floor(c.y[i] * inv_mesh);
-        const double fz = floor(c.z[i] * inv_mesh);
-        ok = isfinite(fx) && isfinite(fy) && isfinite(fz) && fx >= minCell && fx <= maxCell && fy >= minCell &&
-             fy <= maxCell && fz >= minCell && fz <= maxCell;
+        const int sc = o.scene[c.owner[i]];
+        const SceneC& S = g.sc[sc];
+        const double x = c.x[i], y = c.y[i], z = c.z[i];
+        ok = cell_coord_f32(x, S.inv_mesh_f, cx) & cell_coord_f32(y, S.inv_mesh_f, cy) &
+             cell_coord_f32(z, S.inv_mesh_f, cz);
+        if (!ok) ok = cell_coords_exact(x, y, z, S.inv_mesh, cx, cy, cz);
         if (ok) {
-            cx = (int)fx; cy = (int)fy; cz = (int)fz;
-            s = o.scene[c.owner[i]];
+            s = sc;
             g.ckey[i] = pack_cell(cx, cy, cz);
             g.clin[i] = 0;
         } else {
@@ -509,17 +545,30 @@ __global__ void k_finish(Owners d, double dt)
 }
 
 // advanceHalfVelocityKernel of step s followed by advancePositionKernel of
-// step s+1 for one owner, in registers (the two run back to back when no
-// output is taken between steps).
-__global__ void k_finish_advance(Owners d, double dt)
+// step s+1, in two parts, so the next step's particle grid (which reads
+// positions only) need not wait for the rotational FP64 work.
+// Part 1: the half-step velocities of step s and the positions of step s+1.
+__global__ void k_finish_advance_pos(Owners d, double dt)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
-    const double ax = d.ax[i], ay = d.ay[i], az = d.az[i], awx = d.awx[i], awy = d.awy[i], awz = d.awz[i];
-    const double vhx = d.vhx[i] + ax * dt, vhy = d.vhy[i] + ay * dt, vhz = d.vhz[i] + az * dt;
-    const double whx = d.whx[i] + awx * dt, why = d.why[i] + awy * dt, whz = d.whz[i] + awz * dt;
+    const double vhx = d.vhx[i] + d.ax[i] * dt, vhy = d.vhy[i] + d.ay[i] * dt, vhz = d.vhz[i] + d.az[i] * dt;
     d.vhx[i] = vhx; d.vhy[i] = vhy; d.vhz[i] = vhz;
-    d.whx[i] = whx; d.why[i] = why; d.whz[i] = whz;
+    d.whx[i] += d.awx[i] * dt;
+    d.why[i] += d.awy[i] * dt;
+    d.whz[i] += d.awz[i] * dt;
+    if (d.status[i] == -1) return;
+    d.px[i] += vhx * dt;
+    d.py[i] += vhy * dt;
+    d.pz[i] += vhz * dt;
+}
+
+// Part 2 (after part 1): the half-step quaternion rate with the updated
+// half-step spin (k_finish's), then the quaternion of step s+1 and its
+// full-step velocities (k_advance's), on the values part 1 stored.
+__device__ __forceinline__ void advance_rest_one(Owners d, int i, double dt)
+{
+    const double whx = d.whx[i], why = d.why[i], whz = d.whz[i];
     const double h = 0.5 * dt;
     double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
     double pw = qw, px = qx, py = qy, pz = qz, dw, dx, dy, dz;
@@ -530,18 +579,24 @@ __global__ void k_finish_advance(Owners d, double dt)
     quat_derivative(pw, px, py, pz, whx, why, whz, hqw, hqx, hqy, hqz);
     d.hqw[i] = hqw; d.hqx[i] = hqx; d.hqy[i] = hqy; d.hqz[i] = hqz;
     if (d.status[i] == -1) return;
-    d.px[i] += vhx * dt;
-    d.py[i] += vhy * dt;
-    d.pz[i] += vhz * dt;
     qw += hqw * dt; qx += hqx * dt; qy += hqy * dt; qz += hqz * dt;
     normalize_quat(qw, qx, qy, qz);
     d.qw[i] = qw; d.qx[i] = qx; d.qy[i] = qy; d.qz[i] = qz;
-    d.vx[i] = vhx + ax * (0.5 * dt);
-    d.vy[i] = vhy + ay * (0.5 * dt);
-    d.vz[i] = vhz + az * (0.5 * dt);
-    d.wx[i] = whx + awx * (0.5 * dt);
-    d.wy[i] = why + awy * (0.5 * dt);
-    d.wz[i] = whz + awz * (0.5 * dt);
+    d.vx[i] = d.vhx[i] + d.ax[i] * (0.5 * dt);
+    d.vy[i] = d.vhy[i] + d.ay[i] * (0.5 * dt);
+    d.vz[i] = d.vhz[i] + d.az[i] * (0.5 * dt);
+    d.wx[i] = whx + d.awx[i] * (0.5 * dt);
+    d.wy[i] = why + d.awy[i] * (0.5 * dt);
+    d.wz[i] = whz + d.awz[i] * (0.5 * dt);
+}
+
+// One block pair per SM, striding over the owners: the kernel is bound by
+// the FP64 pipe, and the particle grid it runs beside takes the other warp
+// slots of each SM.
+__global__ void __launch_bounds__(256) k_advance_rest(Owners d, double dt)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x)
+        advance_rest_one(d, i, dt);
 }
 
 // Universal gravitation (src/cuda/cuda_contact_backend.cu:1095-1106): the
@@ -648,9 +703,13 @@ void launch_finish(const Owners& o, double dt, cudaStream_t s)
 {
     if (o.n > 0) k_finish<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
 }
-void launch_finish_advance(const Owners& o, double dt, cudaStream_t s)
+void launch_finish_advance_pos(const Owners& o, double dt, cudaStream_t s)
 {
-    if (o.n > 0) k_finish_advance<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+    if (o.n > 0) k_finish_advance_pos<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_advance_rest(const Owners& o, double dt, int sm_count, cudaStream_t s)
+{
+    if (o.n > 0) k_advance_rest<<<std::min(blocks(o.n, 256), 2 * sm_count), 256, 0, s>>>(o, dt);
 }
 void launch_step_counter(const Counters& k, int reset, cudaStream_t s) { k_step_counter<<<1, 32, 0, s>>>(k, reset); }
 

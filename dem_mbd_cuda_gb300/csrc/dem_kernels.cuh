@@ -61,7 +61,7 @@ struct SceneC {
     // inverse and the triangle-grid padding (the largest radius): each scene
     // of a batch is gridded exactly as it would be alone.
     double mesh, inv_mesh, pad;
-    float mesh_f, margin_f;
+    float mesh_f, margin_f, inv_mesh_f;
     int grav;
     int wall_begin, wall_count;
     int body_begin, body_count;
@@ -224,7 +224,10 @@ void launch_leapfrog_init(const Owners& o, double half_dt, cudaStream_t s);
 void launch_advance(const Owners& o, double dt, cudaStream_t s);
 void launch_finish(const Owners& o, double dt, cudaStream_t s);
 // finishParticleStep of one step fused with advanceParticles of the next.
-void launch_finish_advance(const Owners& o, double dt, cudaStream_t s);
+// launch_finish followed by launch_advance, in two parts: positions (what
+// the next particle grid needs), then the rest of the advance.
+void launch_finish_advance_pos(const Owners& o, double dt, cudaStream_t s);
+void launch_advance_rest(const Owners& o, double dt, int sm_count, cudaStream_t s);
 // reset != 0: clear the per-step counters; 0: advance the contact step index.
 void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
 
