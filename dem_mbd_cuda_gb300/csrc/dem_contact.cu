@@ -192,7 +192,10 @@ __device__ __forceinline__ V3<float> rot_ivf(float qw, float qx, float qy, float
 }
 
 // ------------------------------------------------------------------ gather
-template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r, double dt_eff)
+// The records in sorted order, in two parts: the geometry (positions,
+// cells, indices: all the sweep reads, available once the positions are)
+// and the velocities (after the rotational advance).
+__global__ void k_gather_geom(Comps c, Owners o, Grid g, Recs r)
 {
     const int nvalid = *g.nvalid;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
@@ -200,6 +203,24 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
         const int w = c.owner[ci];
         const double x = c.x[ci], y = c.y[ci], z = c.z[ci], rad = c.radius[ci];
         r.pos[t] = d4(x, y, z, rad);
+        if (r.off) r.off[t] = d4(c.ox[ci], c.oy[ci], c.oz[ci], 0.0);
+        int cx, cy, cz;
+        unpack_cell(g.ckey[ci], cx, cy, cz);
+        const int s = o.scene[w];
+        r.meta[t] = make_int4(ci, w, c.cid[ci], s);
+        r.cell[t] = make_int4(cx, cy, cz, g.clin[ci]);
+        const double mesh = g.sc[s].mesh;
+        r.relf[t] = make_float4(f32_rn(__fma_rn(-(double)cx, mesh, x)), f32_rn(__fma_rn(-(double)cy, mesh, y)),
+                                f32_rn(__fma_rn(-(double)cz, mesh, z)), f32_rn(rad));
+    }
+}
+
+template <typename T> __global__ void k_gather_vel(Comps c, Owners o, Grid g, Recs r, double dt_eff)
+{
+    const int nvalid = *g.nvalid;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
+        const int ci = g.sorted_id[t];
+        const int w = c.owner[ci];
         const double vx = c.vx[ci], vy = c.vy[ci], vz = c.vz[ci];
         const bool mid = dt_eff > 0.0 && o.status[w] != -1;
         if constexpr (sizeof(T) == sizeof(double)) {
@@ -213,24 +234,17 @@ template <typename T> __global__ void k_gather(Comps c, Owners o, Grid g, Recs r
         } else {
             // mixed form: FP32 rows; the world-frame rotation of omega is part
             // of the per-contact FP32 arithmetic.
-            const float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
-            r.vf[t] = make_float4(fvx, fvy, fvz, (float)o.mass[w]);
-            r.vmf[t] = mid ? make_float4((float)c.vhx[ci], (float)c.vhy[ci], (float)c.vhz[ci], 0.f)
+            const float fvx = f32_rn(vx), fvy = f32_rn(vy), fvz = f32_rn(vz);
+            r.vf[t] = make_float4(fvx, fvy, fvz, f32_rn(o.mass[w]));
+            r.vmf[t] = mid ? make_float4(f32_rn(c.vhx[ci]), f32_rn(c.vhy[ci]), f32_rn(c.vhz[ci]), 0.f)
                            : make_float4(fvx, fvy, fvz, 0.f);
-            const float qw = (float)o.qw[w], qx = (float)o.qx[w], qy = (float)o.qy[w], qz = (float)o.qz[w];
-            const V3<float> ew = rot_ivf(qw, qx, qy, qz, mk((float)o.wx[w], (float)o.wy[w], (float)o.wz[w]));
+            const float qw = f32_rn(o.qw[w]), qx = f32_rn(o.qx[w]), qy = f32_rn(o.qy[w]), qz = f32_rn(o.qz[w]);
+            const V3<float> ew = rot_ivf(qw, qx, qy, qz, mk(f32_rn(o.wx[w]), f32_rn(o.wy[w]), f32_rn(o.wz[w])));
             r.wf[t] = make_float4(ew.x, ew.y, ew.z, 0.f);
-            const V3<float> mw = mid ? rot_ivf(qw, qx, qy, qz, mk((float)o.whx[w], (float)o.why[w], (float)o.whz[w])) : ew;
+            const V3<float> mw =
+                mid ? rot_ivf(qw, qx, qy, qz, mk(f32_rn(o.whx[w]), f32_rn(o.why[w]), f32_rn(o.whz[w]))) : ew;
             r.wmf[t] = make_float4(mw.x, mw.y, mw.z, 0.f);
         }
-        if (r.off) r.off[t] = d4(c.ox[ci], c.oy[ci], c.oz[ci], 0.0);
-        int cx, cy, cz;
-        unpack_cell(g.ckey[ci], cx, cy, cz);
-        r.meta[t] = make_int4(ci, w, c.cid[ci], o.scene[w]);
-        r.cell[t] = make_int4(cx, cy, cz, g.clin[ci]);
-        const double mesh = g.sc[o.scene[w]].mesh;
-        r.relf[t] = make_float4((float)(__fma_rn(-(double)cx, mesh, x)), (float)(__fma_rn(-(double)cy, mesh, y)),
-                                (float)(__fma_rn(-(double)cz, mesh, z)), (float)rad);
     }
 }
 
@@ -300,7 +314,7 @@ __global__ void __launch_bounds__(256) k_walls_probe(Comps c, Owners o, const Sc
         wflag[ci] = 0;
         const SceneC& S = sc[o.scene[c.owner[ci]]];
         if (S.wall_count > 0) {
-            const float pfx = (float)c.x[ci], pfy = (float)c.y[ci], pfz = (float)c.z[ci], rf = (float)c.radius[ci];
+            const float pfx = f32_rn(c.x[ci]), pfy = f32_rn(c.y[ci]), pfz = f32_rn(c.z[ci]), rf = f32_rn(c.radius[ci]);
             const float tol = 1e-6f + 1e-6f * (fabsf(pfx) + fabsf(pfy) + fabsf(pfz));
             const int nw32 = min(S.wall_count, 32);
             for (int wl = 0; wl < nw32; ++wl) {
@@ -578,9 +592,9 @@ __global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict
         } else {
             // Overlap from the FP64 difference of squares, the rest in FP32.
             const double num = __fma_rn(rs, rs, -d2);
-            const float df = sqrtf((float)d2);
+            const float df = sqrtf(f32_rn(d2));
             d = df;
-            depth = (float)num / ((float)rs + df);
+            depth = f32_rn(num) / (f32_rn(rs) + df);
             n = cvt<float>(delta) * (1.0f / df);
         }
         const SceneC& S = sc[s];
@@ -639,8 +653,8 @@ __device__ double tri_area_scale(const double* W, V3<double> p, double r, double
         // 1e-4 (a disk that grazes the triangle, where FP32 cancellation
         // noise exceeds the 1e-12 cut) is recomputed in FP64, so the set of
         // manifolds is the FP64 one
-        area = (double)circle_triangle_area<float>(cvt<float>(n), cvt<float>(ra), cvt<float>(rb), cvt<float>(rc),
-                                                   sqrtf((float)c2));
+        area = f64_of(circle_triangle_area<float>(cvt<float>(n), cvt<float>(ra), cvt<float>(rb), cvt<float>(rc),
+                                                  sqrtf(f32_rn(c2))));
         if (!(area >= 1.0e-4 * kPi * c2)) area = circle_triangle_area_fp64(n, ra, rb, rc, sqrt(c2));
     }
     if (area <= 0.0) return 0.0;
@@ -659,7 +673,7 @@ struct PtProbe {
 __device__ __forceinline__ PtProbe pt_probe(V3<double> p, double r)
 {
     PtProbe q;
-    q.px = (float)p.x; q.py = (float)p.y; q.pz = (float)p.z; q.r = (float)r;
+    q.px = f32_rn(p.x); q.py = f32_rn(p.y); q.pz = f32_rn(p.z); q.r = f32_rn(r);
     q.tol = 1e-6f + 1e-6f * (fabsf(q.px) + fabsf(q.py) + fabsf(q.pz));
     return q;
 }
@@ -1238,16 +1252,16 @@ __device__ __forceinline__ void euler_f64(Owners o, int i, V3<double> TT)
 // per-contact arithmetic they follow; the result is stored in FP64.
 __device__ __noinline__ void euler_aniso_f32(Owners o, int i, float tx, float ty, float tz)
 {
-    const float ix = (float)o.inv_ix[i], iy = (float)o.inv_iy[i], iz = (float)o.inv_iz[i];
-    const float wx = (float)o.wx[i], wy = (float)o.wy[i], wz = (float)o.wz[i];
-    const float fx = (float)o.ix[i], fy = (float)o.iy[i], fz = (float)o.iz[i];
-    o.awx[i] = (double)((tx - (fz - fy) * wz * wy) * ix);
-    o.awy[i] = (double)((ty - (fx - fz) * wx * wz) * iy);
-    o.awz[i] = (double)((tz - (fy - fx) * wy * wx) * iz);
+    const float ix = f32_rn(o.inv_ix[i]), iy = f32_rn(o.inv_iy[i]), iz = f32_rn(o.inv_iz[i]);
+    const float wx = f32_rn(o.wx[i]), wy = f32_rn(o.wy[i]), wz = f32_rn(o.wz[i]);
+    const float fx = f32_rn(o.ix[i]), fy = f32_rn(o.iy[i]), fz = f32_rn(o.iz[i]);
+    o.awx[i] = f64_of((tx - (fz - fy) * wz * wy) * ix);
+    o.awy[i] = f64_of((ty - (fx - fz) * wx * wz) * iy);
+    o.awz[i] = f64_of((tz - (fy - fx) * wy * wx) * iz);
 }
 __device__ __forceinline__ void euler_f32(Owners o, int i, V3<float> Tq)
 {
-    const float qw = (float)o.qw[i], qx = (float)o.qx[i], qy = (float)o.qy[i], qz = (float)o.qz[i];
+    const float qw = f32_rn(o.qw[i]), qx = f32_rn(o.qx[i]), qy = f32_rn(o.qy[i]), qz = f32_rn(o.qz[i]);
     const float tx = (1.f - 2.f * (qy * qy + qz * qz)) * Tq.x + 2.f * (qx * qy + qw * qz) * Tq.y +
                      2.f * (qx * qz - qw * qy) * Tq.z;
     const float ty = 2.f * (qx * qy - qw * qz) * Tq.x + (1.f - 2.f * (qx * qx + qz * qz)) * Tq.y +
@@ -1256,7 +1270,7 @@ __device__ __forceinline__ void euler_f32(Owners o, int i, V3<float> Tq)
                      (1.f - 2.f * (qx * qx + qy * qy)) * Tq.z;
     if (o.iso[i]) {
         const float ii = o.inv_i_f[i];
-        o.awx[i] = (double)(tx * ii); o.awy[i] = (double)(ty * ii); o.awz[i] = (double)(tz * ii);
+        o.awx[i] = f64_of(tx * ii); o.awy[i] = f64_of(ty * ii); o.awz[i] = f64_of(tz * ii);
         return;
     }
     euler_aniso_f32(o, i, tx, ty, tz);
@@ -1506,10 +1520,15 @@ inline int blocks(int n, int b) { return (n + b - 1) / b; }
 }  // namespace
 
 template <typename T>
-void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
-                   cudaStream_t s)
+void launch_gather_vel(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
+                       cudaStream_t s)
 {
-    k_gather<T><<<sm_count * 8, 256, 0, s>>>(c, o, g, r, dt_eff);
+    k_gather_vel<T><<<sm_count * 8, 256, 0, s>>>(c, o, g, r, dt_eff);
+}
+
+void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, cudaStream_t s)
+{
+    k_gather_geom<<<sm_count * 8, 256, 0, s>>>(c, o, g, r);
 }
 
 template <typename T, typename TB>
@@ -1562,7 +1581,8 @@ void launch_body_outputs(const Comps& c, const Owners& o, const Bodies& b, const
 }
 
 #define DEM_INSTANTIATE(T)                                                                                            \
-    template void launch_gather<T>(const Comps&, const Owners&, const Grid&, const Recs&, double, int, cudaStream_t); \
+    template void launch_gather_vel<T>(const Comps&, const Owners&, const Grid&, const Recs&, double, int,            \
+                                       cudaStream_t);                                                                 \
     template void launch_contacts<T, double>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,   \
                                              const Walls&, const Tris&, const Bodies&, Hist<T>, Hist<T>,             \
                                              Hist<double>, Contacts<T>, const Counters&, double, int, int,            \

@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 // Law helpers compile for the host too, so their adjoints can be checked
@@ -30,6 +31,66 @@ constexpr int kPtRecord = 32;  // doubles per (PT component, body) record
 
 template <typename T> struct V3 { T x, y, z; };
 
+// Double to float, rounded to nearest even, on the integer pipes.  On this
+// GPU every FP64 conversion issues on the FP64 unit (about two lanes per
+// clock per SM, the DFMA rate), so kernels that convert many state values
+// to FP32 rows were bound by it.  From the IEEE-754 formats: rebias the
+// exponent in the high word (1023 - 127 = 896, i.e. 896 << 20), shift the
+// high word left by 3 and bring in the top 3 bits of the low word to get
+// the float's exponent and 23-bit fraction, then round on the 29 dropped
+// bits (ties to even); a carry out of the fraction moves into the exponent
+// as it should, up to infinity.  Results equal the hardware conversion for
+// |x| >= 2^-126; smaller magnitudes (float subnormals) flush to signed zero.
+// Infinities stay infinite, NaNs stay NaN.
+DEM_DEV float f32_rn(double x)
+{
+#ifdef __CUDA_ARCH__
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+#else
+    uint64_t b;
+    std::memcpy(&b, &x, sizeof b);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+#endif
+    const unsigned ahi = hi & 0x7fffffffu;
+    unsigned r = ((ahi - 0x38000000u) << 3) | (lo >> 29);
+    r += ((lo & 0x1fffffffu) + (r & 1u)) > 0x10000000u ? 1u : 0u;
+    if (ahi < 0x38100000u) r = 0u;
+    if (ahi >= 0x47f00000u) r = (ahi > 0x7ff00000u || (ahi == 0x7ff00000u && lo != 0u)) ? 0x7fc00000u : 0x7f800000u;
+    r |= hi & 0x80000000u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(r);
+#else
+    float f;
+    std::memcpy(&f, &r, sizeof f);
+    return f;
+#endif
+}
+
+// Float to double (exact) on the integer pipes: the exponent rebiased by 896
+// and the fraction shifted into place.  Float subnormals become signed zero;
+// infinities and NaNs are kept.
+DEM_DEV double f64_of(float f)
+{
+#ifdef __CUDA_ARCH__
+    const unsigned u = __float_as_uint(f);
+#else
+    unsigned u;
+    std::memcpy(&u, &f, sizeof u);
+#endif
+    const unsigned sign = u & 0x80000000u, a = u & 0x7fffffffu;
+    unsigned hi = sign | ((a >> 3) + 0x38000000u), lo = a << 29;
+    if (a < 0x00800000u) { hi = sign; lo = 0u; }
+    if (a >= 0x7f800000u) { hi = sign | 0x7ff00000u | (a > 0x7f800000u ? 0x00080000u : 0u); lo = 0u; }
+#ifdef __CUDA_ARCH__
+    return __hiloint2double((int)hi, (int)lo);
+#else
+    const uint64_t b = ((uint64_t)hi << 32) | lo;
+    double d;
+    std::memcpy(&d, &b, sizeof d);
+    return d;
+#endif
+}
+
 template <typename T> DEM_DEV V3<T> mk(T x, T y, T z) { return {x, y, z}; }
 template <typename T> DEM_DEV V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 template <typename T> DEM_DEV V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
@@ -45,11 +106,13 @@ template <typename T> DEM_DEV V3<T> normalized(V3<T> a)
     const T l = norm(a);
     return l > T(1.0e-14) ? a * (T(1) / l) : mk<T>(0, 0, 0);
 }
-// Precision conversions.  On GB300 every 64-bit conversion issues on the
-// FP64 pipe (about 2 per clock per SM, the rate of a DFMA), so the mixed
-// form keeps their number per particle and per contact small.
+// Precision conversions, between FP64 and FP32 on the integer pipes
+// (f32_rn, f64_of): on GB300 the hardware conversions issue on the FP64
+// unit at the DFMA rate.
 template <typename T> DEM_DEV T cv(double x) { return static_cast<T>(x); }
 template <typename T> DEM_DEV T cv(float x) { return static_cast<T>(x); }
+template <> DEM_DEV float cv<float>(double x) { return f32_rn(x); }
+template <> DEM_DEV double cv<double>(float x) { return f64_of(x); }
 template <typename T, typename S> DEM_DEV V3<T> cvt(V3<S> a) { return {cv<T>(a.x), cv<T>(a.y), cv<T>(a.z)}; }
 
 // Overlap predicate operand with a fixed contraction pattern so the contact

@@ -599,7 +599,8 @@ public:
             mark();
             if (pt) launch_tri_build(T_, B_, G_, K_.tgover, sm_count_, s);
             if (O_.ugx) launch_universal_gravity(O_, s);
-            launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
+            launch_gather_geom(C_, O_, G_, R_, sm_count_, s);
+            launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
             mark();
             for (int stage : {2, 1, 4, 8}) {
                 contacts(stage, s);
@@ -615,30 +616,33 @@ public:
             integrate(s);
             return;
         }
-        // Three branches (a DAG when captured into the step graph).  The
-        // walls need only the component state; the triangle grid only the
-        // cell layout; the PT law the gathered records and the triangle
-        // grid; the owner sum all three.  Each branch touches its own
-        // history array and result buffers (the wall and body slots expire in
-        // their own probes), so the branches are independent.
+        // Branches (a DAG when captured into the step graph):
+        //   main: cell keys and layout, the sort, the geometry gather, the
+        //     sweep, the particle law, the owner sum, the integrator;
+        //   rotational: the previous step's rotational advance, then (after
+        //     the sort) the velocity gather;
+        //   walls: after the step counter and the rotational advance;
+        //   triangles: transform, triangle grid (after the layout), PT (after
+        //     the geometry gather and the rotational advance), body
+        //     reduction, body-result download.
+        // The particle law waits for the velocity gather, the owner sum for
+        // walls and PT.  Each branch touches its own history array and result
+        // buffers (the wall and body slots expire in their own probes).
         cudaStream_t bw = branch_[0], bt = branch_[1], br = branch_[2];
         auto link = [&](cudaStream_t from, cudaStream_t to, int ev) {
             check(cudaEventRecord(fork_ev_[ev], from), "fork event");
             check(cudaStreamWaitEvent(to, fork_ev_[ev], 0), "fork wait");
         };
-        if (rest_branch) {
-            link(s, br, 7);
-            launch_advance_rest(O_, dt_, sm_count_, br);
-        }
         if (pt && (tail & kTailTransform)) {
             link(s, bt, 6);
             launch_tri_transform(T_, B_, d_sc_, bt);
         }
         launch_step_counter(K_, 1, s);
         if (!sphere_) launch_update_components(C_, O_, s);
+        link(s, br, 7);
+        if (rest_branch) launch_advance_rest(O_, dt_, sm_count_, br);
         if (walls) {
-            link(s, bw, 0);
-            if (rest_branch) link(br, bw, 8);  // the wall law reads velocities
+            link(br, bw, 0);  // the wall law reads velocities
             contacts(1, bw);
         }
         launch_grid_layout(C_, O_, G_, s);
@@ -648,13 +652,17 @@ public:
         }
         launch_grid_sort(C_, O_, G_, sm_count_, s);
         if (O_.ugx) launch_universal_gravity(O_, s);
-        if (rest_branch) link(br, s, 9);  // the gather reads velocities and quaternions
-        launch_gather<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
+        launch_gather_geom(C_, O_, G_, R_, sm_count_, s);
         if (pt) {
+            // PT reads the geometry records and the owner state itself
             link(s, bt, 2);
-            contacts(8, bt);
+            link(br, bt, 10);
         }
+        link(s, br, 9);  // the velocity gather follows the sorted order
+        launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, br);
+        if (pt) contacts(8, bt);
         contacts(2, s);
+        link(br, s, 11);  // the particle law reads the velocity records
         contacts(4, s);
         if (walls) link(bw, s, 3);
         if (pt) {
@@ -1512,10 +1520,10 @@ public:
     size_t free_before_ = 0;
     cudaStream_t stream_ = nullptr;
     // Branches of a force evaluation: [0] walls, [1] triangle grid + PT +
-    // body reduction, [2] the previous step's rotational advance; forked
-    // from and joined back into stream_ by events.
+    // body reduction, [2] the previous step's rotational advance and the
+    // velocity gather; forked from and joined back into stream_ by events.
     std::array<cudaStream_t, 3> branch_{};
-    std::array<cudaEvent_t, 10> fork_ev_{};
+    std::array<cudaEvent_t, 12> fork_ev_{};
     cudaEvent_t body_ready_ = nullptr;  // recorded after the body-result download
     std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;

@@ -116,7 +116,7 @@ __device__ __forceinline__ float floor_small(float q)
 }
 __device__ __forceinline__ bool cell_coord_f32(double x, float inv_mesh_f, int& c)
 {
-    const float q = (float)x * inv_mesh_f;
+    const float q = f32_rn(x) * inv_mesh_f;
     const float e = fmaf(4.0e-7f, fabsf(q), 1.0e-30f);
     const float lo = floor_small(q - e), hi = floor_small(q + e);
     // the integer of lo (|lo| < 2^22) in the low mantissa bits of lo + 1.5 * 2^23

@@ -238,9 +238,12 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
                      double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int sm_count,
                      cudaStream_t s);
 
+// The sorted records: geometry (positions only; all the sweep reads), then
+// velocities (after the rotational advance).
+void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, cudaStream_t s);
 template <typename T>
-void launch_gather(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
-                   cudaStream_t s);
+void launch_gather_vel(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
+                       cudaStream_t s);
 // T: particle-particle and wall law / history type; TB: particle-triangle
 // law, area and body history type.  `stage` selects kernels (1 expiry and
 // walls, 2 sweep, 4 particle law, 8 particle-triangle) so callers can time
