@@ -157,12 +157,22 @@ def measured_traffic(kernel, n):
 
 
 def launches_per_step(scene):
-    """Kernels one graph-launched step issues (see dem_engine.cu enqueue)."""
-    k = 2 + 8 + 1 + 2 + 1 + 2   # counters x2, grid build, gather, broadphase+law, owner sum, advance+finish
+    """Kernels one graph-launched step issues (the force DAG of
+    dem_engine.cu enqueue_forces, steady-state step)."""
+    # counters x2, grid keys + layout + count + scan x3 + scatter + place,
+    # geometry gather, sweep, particle law, owner sum, position advance;
+    # rotational branch: rotational advance, velocity gather
+    k = 2 + 8 + 1 + 1 + 1 + 1 + 1 + 2
     if scene.comp_owner is not None:
+        k += 1                   # component update
+    if scene.universal_gravity_enabled:
         k += 1
-    if scene.n_bodies:
-        k += 1 + 6 + 7 + 2       # triangle transform, triangle grid, PT probe + scan + compaction + law, body reduction
+    if scene.n_walls:
+        k += 2                   # wall probe + law
+    if scene.n_bodies and scene.n_triangles:
+        k += 7 + 7 + 2           # triangle transform + grid, PT probe + scan + compaction + laws, body reduction
+    elif scene.n_bodies:
+        k += 2
     return k
 
 

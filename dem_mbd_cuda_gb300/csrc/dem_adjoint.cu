@@ -88,26 +88,35 @@ __device__ void post_advance(const double* S, int n, int i, double dt, bool move
 
 }  // namespace
 
-// Owner state of the engine -> [29][n].
-__global__ void k_adj_snapshot(Owners o, double* S)
+// Owner state of the engine <-> [29][n], one thread per (field, owner).
+__device__ __forceinline__ double* owner_field(const Owners& o, int f)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    switch (f) {
+    case 0: return o.px; case 1: return o.py; case 2: return o.pz;
+    case 3: return o.qw; case 4: return o.qx; case 5: return o.qy; case 6: return o.qz;
+    case 7: return o.vx; case 8: return o.vy; case 9: return o.vz;
+    case 10: return o.wx; case 11: return o.wy; case 12: return o.wz;
+    case 13: return o.vhx; case 14: return o.vhy; case 15: return o.vhz;
+    case 16: return o.whx; case 17: return o.why; case 18: return o.whz;
+    case 19: return o.hqw; case 20: return o.hqx; case 21: return o.hqy; case 22: return o.hqz;
+    case 23: return o.ax; case 24: return o.ay; case 25: return o.az;
+    case 26: return o.awx; case 27: return o.awy; default: return o.awz;
+    }
+}
+__global__ void k_adj_snapshot(Owners o, double* S, const int* slot)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y;
     const int n = o.n;
     if (i >= n) return;
-    const double* src[kAdjFields] = {o.px, o.py, o.pz, o.qw, o.qx, o.qy, o.qz, o.vx, o.vy, o.vz, o.wx,
-                                     o.wy, o.wz, o.vhx, o.vhy, o.vhz, o.whx, o.why, o.whz, o.hqw, o.hqx, o.hqy,
-                                     o.hqz, o.ax, o.ay, o.az, o.awx, o.awy, o.awz};
-    for (int f = 0; f < kAdjFields; ++f) S[(size_t)f * n + i] = src[f][i];
+    if (slot) S += (size_t)*slot * kAdjFields * n;
+    S[(size_t)f * n + i] = owner_field(o, f)[i];
 }
 __global__ void k_adj_restore(Owners o, const double* S)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y;
     const int n = o.n;
     if (i >= n) return;
-    double* dst[kAdjFields] = {o.px, o.py, o.pz, o.qw, o.qx, o.qy, o.qz, o.vx, o.vy, o.vz, o.wx,
-                               o.wy, o.wz, o.vhx, o.vhy, o.vhz, o.whx, o.why, o.whz, o.hqw, o.hqx, o.hqy,
-                               o.hqz, o.ax, o.ay, o.az, o.awx, o.awy, o.awz};
-    for (int f = 0; f < kAdjFields; ++f) dst[f][i] = S[(size_t)f * n + i];
+    owner_field(o, f)[i] = S[(size_t)f * n + i];
 }
 
 // finish^T and the owner part of forces^T for step s: S = S_s, S1 = S_{s+1},
@@ -118,11 +127,15 @@ __global__ void k_adj_restore(Owners o, const double* S)
 // (dt = 0, no advance, no midpoint) followed by initializeLeapfrogKernel
 // (:185-210) with half step h: L is then the adjoint of S_0.
 __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const double* L, double* Lp, double* P,
-                             double* T, double dt, int init)
+                             double* T, double dt, int init, const int* slot)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = o.n;
     if (i >= n) return;
+    if (slot) {
+        S += (size_t)*slot * kAdjFields * n;
+        S1 = S + (size_t)kAdjFields * n;
+    }
     const bool moves = !init && o.status[i] != -1;
     const bool mid = !init && o.status[i] != -1;
     D3 x1, v1, w1, mv, mw;
@@ -130,6 +143,8 @@ __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const 
     post_advance(S, n, i, dt, moves, mid, x1, q1, v1, w1, mv, mw);
     st3(P, kPX, n, i, x1); st4(P, kPQ, n, i, q1); st3(P, kPV, n, i, v1); st3(P, kPW, n, i, w1);
     st3(P, kPMV, n, i, mv); st3(P, kPMW, n, i, mw);
+    // the world-frame spins every contact of the owner uses
+    st3(P, kPEW, n, i, rotq(q1, w1)); st3(P, kPEMW, n, i, rotq(q1, mw));
     // S1's finish half: the half step h = dt/2 of the finish, or the
     // leapfrog start's half step (dt holds it when init)
     const double h = init ? dt : 0.5 * dt;
@@ -182,34 +197,34 @@ __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const 
     st3(T, kTMW, n, i, z3());
     st3(T, kTF, n, i, lF);
     st3(T, kTTau, n, i, ltau);
+    st3(T, kTEW, n, i, z3());
+    st3(T, kTEMW, n, i, z3());
 }
 
 // Particle contact sides of one step (tape entries), reverse.
-__global__ void k_adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTape tp, int count, const double* P,
-                         double* T, double* lhist, double dt_eff, double* grads)
+__device__ void adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTape tp, int count, const double* P,
+                       double* T, double* lhist, double dt_eff, double* grads, int block, int blocks, double* sg)
 {
     const int n = o.n;
-    __shared__ double sg[kAdjParams];
+    tp = tape_at(tp);
+    if (count < 0) count = min(*tp.pp_count, tp.pp_cap);
     if (threadIdx.x < kAdjParams) sg[threadIdx.x] = 0.0;
     __syncthreads();
     MatGrad gsum = {0, 0, 0, 0, 0, 0};
     const MatC& m = sc[0].pp;   // one scene (checked by the engine)
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    for (int k = block * blockDim.x + threadIdx.x; k < count; k += blocks * blockDim.x) {
         const int4 e = tp.pp[k];
         const int i = e.x, j = e.y;
         D3 xi = ld3(P, kPX, n, i), xj = ld3(P, kPX, n, j);
-        double qi[4], qj[4];
-        ld4(P, kPQ, n, i, qi);
-        ld4(P, kPQ, n, j, qj);
-        const D3 vi = ld3(P, kPV, n, i), vj = ld3(P, kPV, n, j), wi = ld3(P, kPW, n, i), wj = ld3(P, kPW, n, j);
-        const D3 mvi = ld3(P, kPMV, n, i), mvj = ld3(P, kPMV, n, j), mwbi = ld3(P, kPMW, n, i), mwbj = ld3(P, kPMW, n, j);
+        const D3 vi = ld3(P, kPV, n, i), vj = ld3(P, kPV, n, j);
+        const D3 mvi = ld3(P, kPMV, n, i), mvj = ld3(P, kPMV, n, j);
         PPIn in;
         in.delta = xj - xi;
         in.ri = c.radius[i]; in.rj = c.radius[j]; in.mi = o.mass[i]; in.mj = o.mass[j];
         in.erv = vj - vi;
         in.mrv = mvj - mvi;
-        in.ewi = rotq(qi, wi); in.ewj = rotq(qj, wj);
-        in.mwi = rotq(qi, mwbi); in.mwj = rotq(qj, mwbj);
+        in.ewi = ld3(P, kPEW, n, i); in.ewj = ld3(P, kPEW, n, j);
+        in.mwi = ld3(P, kPEMW, n, i); in.mwj = ld3(P, kPEMW, n, j);
         for (int a = 0; a < 9; ++a) in.h[a] = tp.pp_h[(size_t)k * kHV + a];
         double* lh = lhist + (size_t)e.z * kHV;
         double lho[9];
@@ -225,20 +240,10 @@ __global__ void k_adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepT
         add3(T, kTV, n, i, ad.erv * -1.0);
         add3(T, kTMV, n, j, ad.mrv);
         add3(T, kTMV, n, i, ad.mrv * -1.0);
-        double lq[4] = {0, 0, 0, 0};
-        D3 lw = z3(), lmw = z3();
-        rotq_vjp(qi, wi, ad.ewi, lq, lw);
-        rotq_vjp(qi, mwbi, ad.mwi, lq, lmw);
-        add4(T, kTQ, n, i, lq);
-        add3(T, kTW, n, i, lw);
-        add3(T, kTMW, n, i, lmw);
-        double lqj[4] = {0, 0, 0, 0};
-        D3 lwj = z3(), lmwj = z3();
-        rotq_vjp(qj, wj, ad.ewj, lqj, lwj);
-        rotq_vjp(qj, mwbj, ad.mwj, lqj, lmwj);
-        add4(T, kTQ, n, j, lqj);
-        add3(T, kTW, n, j, lwj);
-        add3(T, kTMW, n, j, lmwj);
+        add3(T, kTEW, n, i, ad.ewi);
+        add3(T, kTEW, n, j, ad.ewj);
+        add3(T, kTEMW, n, i, ad.mwi);
+        add3(T, kTEMW, n, j, ad.mwj);
     }
     const double gv[kAdjParams] = {gsum.kN, gsum.mu, gsum.logN, gsum.logS, gsum.muT, gsum.muR};
     for (int f = 0; f < kAdjParams; ++f) atomicAdd(sg + f, gv[f]);
@@ -255,12 +260,10 @@ __device__ void pw_one(const Comps& c, const Owners& o, const SceneC& S, const W
     const int wg = S.wall_begin + e.y;
     const D3 out = mk(walls.n[3 * wg], walls.n[3 * wg + 1], walls.n[3 * wg + 2]);
     const D3 org = mk(walls.o[3 * wg], walls.o[3 * wg + 1], walls.o[3 * wg + 2]);
-    const D3 x1 = ld3(P, kPX, n, i), v1 = ld3(P, kPV, n, i), w1 = ld3(P, kPW, n, i);
-    double q1[4];
-    ld4(P, kPQ, n, i, q1);
+    const D3 x1 = ld3(P, kPX, n, i), v1 = ld3(P, kPV, n, i);
     const double r = c.radius[i];
     const double depth = r - dot(x1 - org, out);
-    const D3 om = rotq(q1, w1);
+    const D3 om = ld3(P, kPEW, n, i);
     double hin[9], lho[9];
     for (int a = 0; a < 9; ++a) hin[a] = tp.pw_h[(size_t)k * kHV + a];
     double* lh = lhist + (size_t)e.z * kHV;
@@ -272,43 +275,71 @@ __device__ void pw_one(const Comps& c, const Owners& o, const SceneC& S, const W
     for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : ad.h[a];
     add3(T, kTX, n, i, ad.p);
     add3(T, kTV, n, i, ad.vel);
-    double lq[4] = {0, 0, 0, 0};
-    D3 lw = z3();
-    rotq_vjp(q1, w1, ad.om, lq, lw);
-    add4(T, kTQ, n, i, lq);
-    add3(T, kTW, n, i, lw);
+    add3(T, kTEW, n, i, ad.om);
 }
 
 // Wall contacts of one step (tape entries), reverse.
-__global__ void k_adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls, StepTape tp, int count,
-                         const double* P, double* T, double* lhist, double dt_eff, double* grads)
+__device__ void adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls, StepTape tp, int count,
+                       const double* P, double* T, double* lhist, double dt_eff, double* grads, int block, int blocks,
+                       double* sg)
 {
-    const int n = o.n;
-    __shared__ double sg[kAdjParams];
+    tp = tape_at(tp);
+    if (count < 0) count = min(*tp.pw_count, tp.pw_cap);
     if (threadIdx.x < kAdjParams) sg[threadIdx.x] = 0.0;
     __syncthreads();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     MatGrad g = {0, 0, 0, 0, 0, 0};
-    if (k < count) pw_one(c, o, sc[0], walls, tp, k, P, T, lhist, dt_eff, g);
+    for (int k = block * blockDim.x + threadIdx.x; k < count; k += blocks * blockDim.x) {
+        MatGrad gk = {0, 0, 0, 0, 0, 0};
+        pw_one(c, o, sc[0], walls, tp, k, P, T, lhist, dt_eff, gk);
+        g.kN += gk.kN; g.mu += gk.mu; g.logN += gk.logN; g.logS += gk.logS; g.muT += gk.muT; g.muR += gk.muR;
+    }
     const double gv[kAdjParams] = {g.kN, g.mu, g.logN, g.logS, g.muT, g.muR};
     for (int f = 0; f < kAdjParams; ++f) atomicAdd(sg + f, gv[f]);
     __syncthreads();
     if (threadIdx.x < kAdjParams) atomicAdd(grads + kAdjParams + threadIdx.x, sg[threadIdx.x]);
 }
 
+// Particle and wall contacts of one step in one launch: blocks [0, bpp) take
+// the particle entries, the rest the wall entries.  Each entry's reverse law
+// is a long serial FP64 chain, and a warp issues one FP64 instruction per
+// about 68 cycles whatever its neighbours do, so with few contacts the two
+// sets cost their longer chain instead of the sum of both.
+__global__ void __launch_bounds__(128) k_adj_contacts(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
+                                                      StepTape tp, int npp, int npw, int bpp, const double* P, double* T,
+                                                      double* lh_pp, double* lh_pw, double dt_eff, double* grads)
+{
+    __shared__ double sg[kAdjParams];
+    if ((int)blockIdx.x < bpp)
+        adj_pp(c, o, sc, tp, npp, P, T, lh_pp, dt_eff, grads, blockIdx.x, bpp, sg);
+    else
+        adj_pw(c, o, sc, walls, tp, npw, P, T, lh_pw, dt_eff, grads, blockIdx.x - bpp, gridDim.x - bpp, sg);
+}
+
 
 // advance^T: T (complete) and the vh, wh partials of Lp -> Lp = adjoint of
 // S_s.  With init = 1 (the first evaluation, no advance): Lp = adjoint of
 // the initial x, q, v, w.
-__global__ void k_adj_advance(Owners o, const double* S, const double* T, double* Lp, double dt, int init)
+__global__ void k_adj_advance(Owners o, const double* S, const double* P, const double* T, double* Lp, double dt,
+                              int init, const int* slot)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = o.n;
     if (i >= n) return;
-    const D3 lx1 = ld3(T, kTX, n, i), lv1 = ld3(T, kTV, n, i), lw1 = ld3(T, kTW, n, i);
-    const D3 lmv = ld3(T, kTMV, n, i), lmw = ld3(T, kTMW, n, i);
+    if (slot) S += (size_t)*slot * kAdjFields * n;
+    const D3 lx1 = ld3(T, kTX, n, i), lv1 = ld3(T, kTV, n, i);
+    D3 lw1 = ld3(T, kTW, n, i);
+    const D3 lmv = ld3(T, kTMV, n, i);
+    D3 lmw = ld3(T, kTMW, n, i);
     double lq1[4];
     ld4(T, kTQ, n, i, lq1);
+    {
+        // the contacts' adjoints of the world-frame spins R(q1) w1 and
+        // R(q1) w_mid, to the quaternion and the body-frame spins
+        double q1[4];
+        ld4(P, kPQ, n, i, q1);
+        rotq_vjp(q1, ld3(P, kPW, n, i), ld3(T, kTEW, n, i), lq1, lw1);
+        rotq_vjp(q1, ld3(P, kPMW, n, i), ld3(T, kTEMW, n, i), lq1, lmw);
+    }
     const bool moves = !init && o.status[i] != -1;
     double zero4[4] = {0, 0, 0, 0};
     if (!moves) {
@@ -348,13 +379,13 @@ __global__ void k_adj_advance(Owners o, const double* S, const double* T, double
 }
 
 // ---------------------------------------------------------- launchers
-void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s)
+void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s, const int* slot)
 {
-    if (o.n > 0) k_adj_snapshot<<<nblocks(o.n, 256), 256, 0, s>>>(o, S);
+    if (o.n > 0) k_adj_snapshot<<<dim3(nblocks(o.n, 256), kAdjFields), 256, 0, s>>>(o, S, slot);
 }
 void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s)
 {
-    if (o.n > 0) k_adj_restore<<<nblocks(o.n, 256), 256, 0, s>>>(o, S);
+    if (o.n > 0) k_adj_restore<<<dim3(nblocks(o.n, 256), kAdjFields), 256, 0, s>>>(o, S);
 }
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
                      int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
@@ -362,10 +393,29 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
                      cudaStream_t s)
 {
     if (o.n <= 0) return;
-    k_adj_finish<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init);
-    if (npp > 0) k_adj_pp<<<min(nblocks(npp, 128), sm_count * 16), 128, 0, s>>>(c, o, sc, tp, npp, P, T, lh_pp, dt_eff, grads);
-    if (npw > 0) k_adj_pw<<<nblocks(npw, 128), 128, 0, s>>>(c, o, sc, w, tp, npw, P, T, lh_pw, dt_eff, grads);
-    k_adj_advance<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, T, Lp, dt, init);
+    // device counts: S, S1 at the tape's slot, fixed grid-stride grids
+    const int* slot = (npp < 0 || npw < 0) ? tp.slot : nullptr;
+    k_adj_finish<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init, slot);
+    const int bpp = npp < 0 ? sm_count * 8 : min(nblocks(npp, 128), sm_count * 8);
+    const int bpw = npw < 0 ? sm_count * 2 : min(nblocks(npw, 128), sm_count * 2);
+    if (bpp + bpw > 0)
+        k_adj_contacts<<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff, grads);
+    k_adj_advance<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, P, T, Lp, dt, init, slot);
+}
+
+__global__ void k_adj_slot_add(int* slot, int delta) { *slot += delta; }
+__global__ void k_adj_tape_begin(int* pw_count, const int* slot) { pw_count[*slot] = 0; }
+__global__ void k_adj_tape_end(int* pp_count, const int* ct_total, int* slot)
+{
+    pp_count[*slot] = *ct_total;
+    *slot += 1;
+}
+
+void launch_adj_slot_add(int* slot, int delta, cudaStream_t s) { k_adj_slot_add<<<1, 1, 0, s>>>(slot, delta); }
+void launch_adj_tape_begin(int* pw_count, const int* slot, cudaStream_t s) { k_adj_tape_begin<<<1, 1, 0, s>>>(pw_count, slot); }
+void launch_adj_tape_end(int* pp_count, const int* ct_total, int* slot, cudaStream_t s)
+{
+    k_adj_tape_end<<<1, 1, 0, s>>>(pp_count, ct_total, slot);
 }
 
 }  // namespace demgb

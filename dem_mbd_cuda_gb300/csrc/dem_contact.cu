@@ -343,6 +343,7 @@ __global__ void __launch_bounds__(128) k_walls_law(Comps c, Owners o, const Scen
 {
     const int step = *k.step;
     const int total = *k.wl_total;
+    const StepTape tape = tape_at(ct.tape);
     int bover = 0, bhigh = 0;
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
         const int2 e = ct.wlist[item];
@@ -356,9 +357,9 @@ __global__ void __launch_bounds__(128) k_walls_law(Comps c, Owners o, const Scen
         int whw = hw.hw[ci];
         for (; cand; cand &= cand - 1u)
             wall_contact<T>(c, o, S, walls, hw, ci, w, __ffs(cand) - 1, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT,
-                            ct.tape);
+                            tape);
         for (int wl = 32; wl < S.wall_count; ++wl)
-            wall_contact<T>(c, o, S, walls, hw, ci, w, wl, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT, ct.tape);
+            wall_contact<T>(c, o, S, walls, hw, ci, w, wl, p, rad, step, dt_eff, whw, bhigh, bover, wF, wT, tape);
         hw.hw[ci] = whw;
         const bool hit = wF.x != 0.0 || wF.y != 0.0 || wF.z != 0.0 || wT.x != 0.0 || wT.y != 0.0 || wT.z != 0.0;
         if (hit) {
@@ -377,14 +378,15 @@ __global__ void __launch_bounds__(128) k_walls_law(Comps c, Owners o, const Scen
 template <typename T>
 __global__ void k_tape_pp(Recs r, Hist<T> hp, Contacts<T> ct, Counters k)
 {
+    const StepTape tp = tape_at(ct.tape);
     const int total = *k.ct_total;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && total > ct.tape.pp_cap) atomicOr(ct.tape.overflow, 1);
-    const int n = min(total, ct.tape.pp_cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && total > tp.pp_cap) atomicOr(tp.overflow, 1);
+    const int n = min(total, tp.pp_cap);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const int4 e = ct.ent[q];
-        ct.tape.pp[q] = make_int4(r.meta[e.x].x, r.meta[e.y].x, e.z, ct.tape.pp_new[q]);
+        tp.pp[q] = make_int4(r.meta[e.x].x, r.meta[e.y].x, e.z, tp.pp_new[q]);
         const T* hv = hp.val + (size_t)e.z * kHV;
-        for (int a = 0; a < kHV; ++a) ct.tape.pp_h[(size_t)q * kHV + a] = (double)hv[a];
+        for (int a = 0; a < kHV; ++a) tp.pp_h[(size_t)q * kHV + a] = (double)hv[a];
     }
 }
 

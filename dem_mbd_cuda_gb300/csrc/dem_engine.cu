@@ -101,6 +101,7 @@ public:
     {
         for (cudaGraphExec_t g : graphs_)
             if (g) cudaGraphExecDestroy(g);
+        adj_release_graphs();
         for (auto* e : ev_) if (e) cudaEventDestroy(e);
         for (auto* e : fork_ev_) if (e) cudaEventDestroy(e);
         if (body_ready_) cudaEventDestroy(body_ready_);
@@ -134,7 +135,16 @@ public:
         check(cudaMemGetInfo(&free_before_, &total_mem), "cudaMemGetInfo");
         check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
         for (auto*& e : ev_) check(cudaEventCreate(&e), "cudaEventCreate");
-        for (auto*& b : branch_) check(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking), "cudaStreamCreate");
+        {
+            // The triangle/PT branch and the rotational branch carry the
+            // critical paths (PT on few-item scenes, the FP64 advance on
+            // large ones): their blocks are scheduled first as SM slots free.
+            int lo = 0, hi = 0;
+            check(cudaDeviceGetStreamPriorityRange(&lo, &hi), "stream priorities");
+            const int prio[3] = {lo, hi, hi};
+            for (int b = 0; b < 3; ++b)
+                check(cudaStreamCreateWithPriority(&branch_[b], cudaStreamNonBlocking, prio[b]), "cudaStreamCreate");
+        }
         for (auto*& e : fork_ev_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
         check(cudaEventCreateWithFlags(&body_ready_, cudaEventDisableTiming), "cudaEventCreate");
 
@@ -1293,7 +1303,17 @@ public:
         int *pp_cnt = nullptr, *pw_cnt = nullptr, *overflow = nullptr;
         double *L = nullptr, *Lp = nullptr, *P = nullptr, *T = nullptr, *lh_pp = nullptr, *lh_pw = nullptr;
         double* grads = nullptr;
+        double* Lb[2] = {nullptr, nullptr};        // the two adjoint-state buffers L and Lp alternate between
+        int* slot = nullptr;                       // device step index within a segment
+        // a taped recompute step and a reverse step (reading Lb[p], writing
+        // Lb[1 - p]), captured once the buffers exist
+        cudaGraphExec_t g_fwd = nullptr, g_rev[2] = {nullptr, nullptr};
     };
+    void adj_release_graphs()
+    {
+        for (cudaGraphExec_t* g : {&adj_.g_fwd, &adj_.g_rev[0], &adj_.g_rev[1]})
+            if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
+    }
 
     void adj_require() const
     {
@@ -1354,6 +1374,7 @@ public:
         if (steps < 1 || K < 1) throw DemError(DEM_ERR_INVALID, "adjoint forward: steps and K must be positive");
         if (started_ || step_index_ != 0)
             throw DemError(DEM_ERR_STATE, "adjoint forward starts from a freshly initialized engine");
+        adj_release_graphs();
         adj_arena_.release();
         adj_ = Adjoint{};
         Adjoint& A = adj_;
@@ -1378,6 +1399,8 @@ public:
         A.lh_pp = adj_arena_.alloc<double>((size_t)nc_ * kPSlots * kHV, "adjoint history");
         A.lh_pw = adj_arena_.alloc<double>((size_t)nc_ * kWSlots * kHV, "adjoint history");
         A.grads = adj_arena_.alloc<double>(2 * kAdjParams, "adjoint parameters");
+        A.slot = adj_arena_.alloc<int>(1, "adjoint slot");
+        A.Lb[0] = A.L; A.Lb[1] = A.Lp;
         adj_save(A.ck[0]);
         run_steps(0);
         adj_save(A.ck[1]);
@@ -1406,6 +1429,60 @@ public:
         ct64_.tape = StepTape{};
         ++step_index_;
         check(cudaMemcpyAsync(A.pp_cnt + sl, K_.ct_total, sizeof(int), cudaMemcpyDeviceToDevice, stream_), "adjoint tape");
+    }
+
+    // The tape of a segment with the step as the device index A.slot.
+    StepTape adj_tape_slotted()
+    {
+        Adjoint& A = adj_;
+        StepTape tp{};
+        tp.pp_new = A.pp_new;
+        tp.pp = A.pp; tp.pp_h = A.pp_h; tp.pp_cap = A.cap_pp;
+        tp.pw = A.pw; tp.pw_h = A.pw_h; tp.pw_cap = A.cap_pw;
+        tp.pw_count = A.pw_cnt; tp.pp_count = A.pp_cnt;
+        tp.overflow = A.overflow;
+        tp.slot = A.slot;
+        return tp;
+    }
+    // A recomputed, taped step (snapshot, advance, forces, finish, counts;
+    // A.slot moves on by one) and the reverse step (A.slot back by one, then
+    // the step's adjoint) as graphs: one launch per step each way.
+    void adj_capture()
+    {
+        Adjoint& A = adj_;
+        if (A.g_fwd) return;
+        auto cap = [&](cudaGraphExec_t& ex, auto&& body) {
+            cudaGraph_t g = nullptr;
+            check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
+            try {
+                body();
+            } catch (...) {
+                ct64_.tape = StepTape{};
+                cudaStreamEndCapture(stream_, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            check(cudaStreamEndCapture(stream_, &g), "end capture");
+            check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
+            cudaGraphDestroy(g);
+        };
+        const StepTape tp = adj_tape_slotted();
+        cap(A.g_fwd, [&] {
+            launch_adj_snapshot(O_, A.S, stream_, A.slot);
+            launch_advance(O_, dt_, stream_);
+            launch_adj_tape_begin(A.pw_cnt, A.slot, stream_);
+            ct64_.tape = tp;
+            forces(dt_);
+            ct64_.tape = StepTape{};
+            launch_finish(O_, dt_, stream_);
+            launch_adj_tape_end(A.pp_cnt, K_.ct_total, A.slot, stream_);
+        });
+        for (int p = 0; p < 2; ++p)
+            cap(A.g_rev[p], [&] {
+                launch_adj_slot_add(A.slot, -1, stream_);
+                launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, A.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T, A.lh_pp,
+                                A.lh_pw, dt_, dt_, 0, A.grads, sm_count_, stream_);
+            });
     }
 
     // dem_adjoint_backward: the adjoint of the final positions and velocities
@@ -1449,24 +1526,28 @@ public:
             if (of) throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
             for (int j = 0; j < k; ++j) { npp[j] = std::min(npp[j], A.cap_pp); npw[j] = std::min(npw[j], A.cap_pw); }
         };
+        adj_capture();
+        int par = A.L == A.Lb[0] ? 0 : 1;  // the buffer that holds the current adjoint
         for (int seg = A.nseg - 1; seg >= 0; --seg) {
             const int ks = std::min(A.K, A.steps - seg * A.K);
             adj_restore(A.ck[seg + 1]);
+            check(cudaMemsetAsync(A.slot, 0, sizeof(int), s), "adjoint slot");
             for (int sl = 0; sl < ks; ++sl) {
-                launch_adj_snapshot(O_, A.S + (size_t)sl * kAdjFields * N, s);
-                launch_advance(O_, dt_, s);
-                adj_tape_forces(sl);
-                launch_finish(O_, dt_, s);
+                check(cudaGraphLaunch(A.g_fwd, s), "adjoint recompute");
+                ++step_index_;
             }
-            launch_adj_snapshot(O_, A.S + (size_t)ks * kAdjFields * N, s);
-            counts(ks);
+            launch_adj_snapshot(O_, A.S, s, A.slot);  // the state after the segment, slot ks
+            int of = 0;
+            check(cudaMemcpyAsync(&of, A.overflow, sizeof(int), cudaMemcpyDeviceToHost, s), "adjoint overflow");
+            check(cudaStreamSynchronize(s), "adjoint recompute");
+            if (of) throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
             for (int sl = ks - 1; sl >= 0; --sl) {
-                launch_adj_step(C_, O_, d_sc_, W_, tape_of(sl), npp[sl], npw[sl], A.S + (size_t)sl * kAdjFields * N,
-                                A.S + (size_t)(sl + 1) * kAdjFields * N, A.L, A.Lp, A.P, A.T, A.lh_pp, A.lh_pw, dt_, dt_,
-                                0, A.grads, sm_count_, s);
-                std::swap(A.L, A.Lp);
+                check(cudaGraphLaunch(A.g_rev[par], s), "adjoint reverse step");
+                par ^= 1;
             }
         }
+        A.L = A.Lb[par];
+        A.Lp = A.Lb[1 - par];
         // the first evaluation (dt = 0) and the leapfrog start
         adj_restore(A.ck[0]);
         adj_tape_forces(0);

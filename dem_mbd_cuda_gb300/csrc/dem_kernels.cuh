@@ -155,11 +155,15 @@ struct Counters {
 // x 3, q 4, v 3, w (body frame) 3, vh 3, wh 3, hq 4, a 3, aw 3.
 constexpr int kAdjX = 0, kAdjQ = 3, kAdjV = 7, kAdjW = 10, kAdjVH = 13, kAdjWH = 16, kAdjHQ = 19, kAdjA = 23,
               kAdjAW = 26, kAdjFields = 29;
-// post-advance state the laws see: x1, q1, v1, w1, midpoint v and w
-constexpr int kPX = 0, kPQ = 3, kPV = 7, kPW = 10, kPMV = 13, kPMW = 16, kPFields = 19;
-// adjoints of the post-advance state, of the midpoint velocities, and of the
-// total force and world torque of each owner
-constexpr int kTX = 0, kTQ = 3, kTV = 7, kTW = 10, kTMV = 13, kTMW = 16, kTF = 19, kTTau = 22, kTFields = 25;
+// post-advance state the laws see: x1, q1, v1, w1 (body frame), midpoint v
+// and w (body frame), and the world-frame spins R(q1) w1 and R(q1) w_mid
+constexpr int kPX = 0, kPQ = 3, kPV = 7, kPW = 10, kPMV = 13, kPMW = 16, kPEW = 19, kPEMW = 22, kPFields = 25;
+// adjoints of the post-advance state, of the midpoint velocities, of the
+// total force and world torque of each owner, and of its two world-frame
+// spins (the contact kernels add these; the owner step turns them into
+// quaternion and spin adjoints)
+constexpr int kTX = 0, kTQ = 3, kTV = 7, kTW = 10, kTMV = 13, kTMW = 16, kTF = 19, kTTau = 22, kTEW = 25, kTEMW = 28,
+              kTFields = 31;
 // material adjoints per contact class: kN, mu, log epsN, log epsS, muT, muR
 constexpr int kAdjParams = 6;
 
@@ -167,7 +171,9 @@ constexpr int kAdjParams = 6;
 // recomputed step): per particle contact side (component, partner component,
 // history slot index, 1 if the slot was acquired this step) and the slot's
 // history before the law; the same for wall contacts (component, wall,
-// slot index, new).
+// slot index, new).  With `slot` set, the arrays hold every step of a
+// segment and the step is the device value *slot (tape_at applies it), so
+// one captured graph serves all steps.
 struct StepTape {
     unsigned char* pp_new;  // per contact list entry, written by the sweep
     int4* pp;
@@ -178,7 +184,26 @@ struct StepTape {
     int pw_cap;
     int* pw_count;
     int* overflow;
+    int* pp_count;          // particle entries of the step (read by the reverse kernels)
+    const int* slot;        // device step index, or null: the pointers are the step's own
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ StepTape tape_at(StepTape t)
+{
+    if (t.slot) {
+        const size_t k = (size_t)*t.slot;
+        t.pp += k * t.pp_cap;
+        t.pp_h += k * t.pp_cap * kHV;
+        t.pw += k * t.pw_cap;
+        t.pw_h += k * t.pw_cap * kHV;
+        t.pw_count += k;
+        if (t.pp_count) t.pp_count += k;
+        t.slot = nullptr;
+    }
+    return t;
+}
+#endif
 
 template <typename T> struct Contacts {
     int4* ent;      // ti, tj, slot, -
@@ -231,12 +256,22 @@ void launch_advance_rest(const Owners& o, double dt, int sm_count, cudaStream_t 
 // reset != 0: clear the per-step counters; 0: advance the contact step index.
 void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
 
-void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s);
+// Owner-state snapshots [29][n]; with `slot`, into S + *slot * 29 n.
+void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s, const int* slot = nullptr);
 void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s);
+// One reverse step.  npp / npw < 0: the counts are the tape's own
+// (pp_count / pw_count at the device slot) and S, S1 are taken at *tp.slot
+// and *tp.slot + 1 of the snapshot array S.
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
                      int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
                      double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int sm_count,
                      cudaStream_t s);
+// Device step index of a taped segment: add `delta`.
+void launch_adj_slot_add(int* slot, int delta, cudaStream_t s);
+// Before a taped step: zero its wall entry count.  After it: record its
+// particle entry count (the contact total) and move to the next step.
+void launch_adj_tape_begin(int* pw_count, const int* slot, cudaStream_t s);
+void launch_adj_tape_end(int* pp_count, const int* ct_total, int* slot, cudaStream_t s);
 
 // The sorted records: geometry (positions only; all the sweep reads), then
 // velocities (after the rotational advance).
