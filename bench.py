@@ -356,8 +356,8 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
 
 
 def autotune_summary(scene, precision):
-    """The autotuner's choice of cell factor and particle-triangle crossover
-    on the workload (dem_mbd_cuda_gb300/autotune.py)."""
+    """The autotuner's choice of cell factor, sweep blocks per SM and
+    particle-triangle crossover on the workload (dem_mbd_cuda_gb300/autotune.py)."""
     from dem_mbd_cuda_gb300.autotune import autotune
     return autotune(scene, precision=precision)
 

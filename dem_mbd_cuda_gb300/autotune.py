@@ -1,11 +1,16 @@
 """Autotuner for the engine's runtime settings on a given scene.
 
-Two settings change the speed of a step without changing its contact physics:
+Three settings change the speed of a step without changing its contact
+physics:
 
 * the cell factor (cell edge = factor x the scene's largest radius): a smaller
   cell means fewer candidates per particle in the sweep but more cells to
   build and visit; the reference's 2.5 is the only value whose sorted cell
   keys match its own, so it stays the default;
+* the sweep's blocks per SM: the sweep runs grid-stride so that the kernels
+  of the step's other branches (particle-triangle law, rotational advance,
+  walls) find free warp slots beside it; the best share depends on how much
+  work those branches carry;
 * the particle-triangle crossover (contact items up to which the PT law runs
   one warp per item instead of one thread per item).
 
@@ -23,6 +28,7 @@ import numpy as np
 from .engine import CudaDemSolver
 
 FACTORS = (2.0, 2.25, 2.5, 3.0, 3.5)
+SWEEP_BLOCKS = (2, 3, 4, 5, 6, 8)
 WARP_ITEMS = (512, 3072, 16384)
 _cache: dict = {}
 
@@ -38,32 +44,42 @@ def _signature(scene, precision):
     return h.hexdigest()
 
 
-def _time(scene, precision, factor, warp_items, steps, warmup):
+def _time(scene, precision, factor, sweep_blocks, warp_items, steps, warmup):
     e = CudaDemSolver().initialize(scene, precision=precision, cell_factor=factor)
+    if sweep_blocks is not None:
+        e.set_sweep_blocks(sweep_blocks)
     if warp_items is not None:
         e.set_pt_warp_items(warp_items)
     e.run(max(1, warmup))
-    return e.time_steps(steps) / steps
+    return min(e.time_steps(steps) / steps for _ in range(2))
 
 
-def autotune(scene, precision="mixed", factors=FACTORS, warp_items=WARP_ITEMS, steps=20, warmup=5):
-    """Fastest (cell_factor, pt_warp_items) for `scene`; returns a dict with
-    the choice, its ms per step, the default's ms per step and the table."""
-    key = (_signature(scene, precision), tuple(factors), tuple(warp_items), steps)
+def autotune(scene, precision="mixed", factors=FACTORS, sweep_blocks=SWEEP_BLOCKS, warp_items=WARP_ITEMS, steps=20,
+             warmup=5):
+    """Fastest (cell_factor, sweep_blocks, pt_warp_items) for `scene`, searched
+    one setting at a time in that order; returns a dict with the choice, its
+    ms per step, the default's ms per step and the table.  None in the choice
+    means the engine's default."""
+    key = (_signature(scene, precision), tuple(factors), tuple(sweep_blocks), tuple(warp_items), steps)
     if key in _cache:
         return _cache[key]
     table = []
-    for f in factors:
-        table.append({"cell_factor": f, "pt_warp_items": None, "ms_per_step": _time(scene, precision, f, None, steps, warmup)})
-    best = min(table, key=lambda r: r["ms_per_step"])
+
+    def row(f, b, w):
+        r = {"cell_factor": f, "sweep_blocks": b, "pt_warp_items": w,
+             "ms_per_step": _time(scene, precision, f, b, w, steps, warmup)}
+        table.append(r)
+        return r
+
+    best = min((row(f, None, None) for f in factors), key=lambda r: r["ms_per_step"])
+    default = next(r["ms_per_step"] for r in table if r["cell_factor"] == 2.5)
+    best = min([best] + [row(best["cell_factor"], b, None) for b in sweep_blocks], key=lambda r: r["ms_per_step"])
     has_bodies = any(s.n_bodies for s in (scene if isinstance(scene, (list, tuple)) else [scene]))
     if has_bodies:
-        for w in warp_items:
-            table.append({"cell_factor": best["cell_factor"], "pt_warp_items": w,
-                          "ms_per_step": _time(scene, precision, best["cell_factor"], w, steps, warmup)})
-        best = min(table, key=lambda r: r["ms_per_step"])
-    default = next(r["ms_per_step"] for r in table if r["cell_factor"] == 2.5 and r["pt_warp_items"] is None)
-    out = {"cell_factor": best["cell_factor"], "pt_warp_items": best["pt_warp_items"], "ms_per_step": best["ms_per_step"],
+        best = min([best] + [row(best["cell_factor"], best["sweep_blocks"], w) for w in warp_items],
+                   key=lambda r: r["ms_per_step"])
+    out = {"cell_factor": best["cell_factor"], "sweep_blocks": best["sweep_blocks"],
+           "pt_warp_items": best["pt_warp_items"], "ms_per_step": best["ms_per_step"],
            "default_ms_per_step": default, "speedup_over_default": default / best["ms_per_step"], "table": table}
     _cache[key] = out
     return out

@@ -18,6 +18,8 @@
 //   body reduce deterministic two-level reduction of the body loads
 #include "dem_kernels.cuh"
 
+#include <algorithm>
+
 #include <climits>
 
 namespace demgb {
@@ -428,8 +430,13 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
 {
     const int step = *k.step;
     const int nvalid = *g.nvalid;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int count = 0, pover = 0, phigh = 0;
+    int pover = 0, phigh = 0, found = 0;
+    __shared__ int s_base;
+    // grid-stride over blocks of sorted positions: the launch may use fewer
+    // blocks than positions so that the kernels beside it find free slots
+    for (int t0 = blockIdx.x * blockDim.x; t0 < nvalid; t0 += gridDim.x * blockDim.x) {
+    const int t = t0 + threadIdx.x;
+    int count = 0;
     int stage_t[kCandidates];
     int stage_s[kMaxContacts];
     int ci = -1;
@@ -527,7 +534,6 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     }
     int total;
     const int ex = block_exclusive_scan_c(count, total);
-    __shared__ int s_base;
     if (threadIdx.x == 0) s_base = total ? atomicAdd(k.ct_total, total) : 0;
     __syncthreads();
     const int base = s_base + ex;
@@ -535,7 +541,10 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         ct.ent[base + q] = make_int4(t, stage_t[q], ci * kPSlots + (stage_s[q] & 0xff), q * nc + ci);
         if (ct.tape.pp_new) ct.tape.pp_new[base + q] = (unsigned char)(stage_s[q] >> 8);
     }
-    block_add(k.pcontacts, count);
+    found += count;
+    __syncthreads();  // s_base is reused by the next pass
+    }
+    block_add(k.pcontacts, found);
     block_add(k.pover, pover);
     block_max(k.phigh, phigh);
 }
@@ -1540,7 +1549,8 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
 {
     (void)block;
     if (stage & 2) {
-        k_sweep<T><<<blocks(c.n, 128), 128, 0, s>>>(g, r, sc, hp, ct, k, c.n);
+        const int nb = blocks(c.n, 128);
+        k_sweep<T><<<k.sweep_bps > 0 ? std::min(nb, sm_count * k.sweep_bps) : nb, 128, 0, s>>>(g, r, sc, hp, ct, k, c.n);
         if (ct.tape.pp) k_tape_pp<T><<<sm_count * 8, 256, 0, s>>>(r, hp, ct, k);
     }
     if ((stage & 1) && w.count > 0) {

@@ -74,6 +74,9 @@ private:
 
 // Contact items up to which the PT law runs one warp per item.
 constexpr int kDefaultPtWarpItems = 3072;
+// Sweep blocks per SM: the sweep leaves warp slots to the PT and rotational
+// branches that run beside it (0 would launch one thread per component).
+constexpr int kDefaultSweepBlocksPerSm = 4;
 
 static MatF to_float(const MatC& c)
 {
@@ -470,6 +473,7 @@ public:
         K_.pt_ctotal = cnt + 9;
         K_.wl_total = cnt + 10;
         K_.pt_warp_items = kDefaultPtWarpItems;
+        K_.sweep_bps = kDefaultSweepBlocksPerSm;
 
         // ---- scene constants
         scenes_h_ = sc;
@@ -996,6 +1000,16 @@ public:
         K_.pt_warp_items = n;
         for (cudaGraphExec_t& g : graphs_)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+    // Sweep blocks per SM (0: one thread per component); graphs rebuilt.
+    void set_sweep_blocks(int n)
+    {
+        need_init();
+        check(cudaStreamSynchronize(stream_), "sync");
+        K_.sweep_bps = std::max(0, n);
+        for (cudaGraphExec_t& g : graphs_)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        adj_release_graphs();
     }
     void ensure_graphs(bool mbd)
     {
@@ -1871,6 +1885,11 @@ int dem_x_download_half(dem_engine* e, double* vh, double* wh, double* hdq, doub
 int dem_x_set_pt_warp_items(dem_engine* e, int n)
 {
     return guarded([&] { NEED(e); e->e.set_pt_warp_items(n); });
+}
+
+int dem_x_set_sweep_blocks(dem_engine* e, int blocks_per_sm)
+{
+    return guarded([&] { NEED(e); e->e.set_sweep_blocks(blocks_per_sm); });
 }
 
 int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every)

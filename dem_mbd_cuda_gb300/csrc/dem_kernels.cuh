@@ -149,6 +149,7 @@ struct Counters {
     int* wl_total;      // components with a candidate wall this step
     int* step;          // contact step index
     int pt_warp_items;  // PT: warp-per-item kernel up to this many contact items
+    int sweep_bps;      // sweep blocks per SM (grid-stride), 0 = one thread per component
 };
 
 // Reverse sweep (dem_adjoint.cu).  Owner state S of one step, [field][owner]:

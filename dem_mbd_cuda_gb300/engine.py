@@ -58,6 +58,7 @@ _SIGS = {
     "dem_x_download_half": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),
     "dem_x_synchronize": ([C.c_void_p], C.c_int),
     "dem_x_set_pt_warp_items": ([C.c_void_p, C.c_int], C.c_int),
+    "dem_x_set_sweep_blocks": ([C.c_void_p, C.c_int], C.c_int),
     "dem_adjoint_forward": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
     "dem_adjoint_backward": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
 }
@@ -290,6 +291,12 @@ class CudaDemSolver:
         items one warp per item, above one thread per item (tests force
         either path with 1 << 30 or -1)."""
         self._check(self.lib.dem_x_set_pt_warp_items(self.h, int(n)))
+        return self
+
+    def set_sweep_blocks(self, blocks_per_sm):
+        """Blocks per SM of the particle sweep (grid-stride); 0 launches one
+        thread per component.  Changes only the speed."""
+        self._check(self.lib.dem_x_set_sweep_blocks(self.h, int(blocks_per_sm)))
         return self
 
     def time_steps(self, steps):

@@ -1,0 +1,58 @@
+"""Speed settings change no result: the sweep's blocks per SM (grid-stride)
+leaves the trajectory, the bodies and the contact histories bit-identical;
+the autotuner returns a setting the engine accepts."""
+import numpy as np
+import pytest
+
+from gpu_helpers import engine_for
+from dem_mbd_cuda_gb300 import generate as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _lib(engine_lib):
+    return engine_lib
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("maker", ["small_dem", "small_mbd"])
+def test_sweep_blocks_do_not_change_results(precision, maker):
+    sc = getattr(G, maker)()
+    runs = []
+    for blocks in (0, 1, 3):
+        e = engine_for(sc, precision=precision).set_sweep_blocks(blocks)
+        e.run(15)
+        runs.append(e)
+    ref = runs[0]
+    st0 = ref.downloadParticleState()
+    for e in runs[1:]:
+        st = e.downloadParticleState()
+        for k in ("pos", "vel", "omega", "quat"):
+            np.testing.assert_array_equal(st[k], st0[k], err_msg=k)
+        for kind in (0, 1, 2):
+            k1, l1, v1 = e.history(kind)
+            k2, l2, v2 = ref.history(kind)
+            np.testing.assert_array_equal(k1, k2)
+            np.testing.assert_array_equal(l1, l2)
+            np.testing.assert_array_equal(v1, v2)
+        if sc.n_bodies:
+            np.testing.assert_array_equal(e.bodies()["loads"], ref.bodies()["loads"])
+
+
+def test_autotune_returns_an_accepted_setting():
+    from dem_mbd_cuda_gb300.autotune import autotune
+    sc = G.small_mbd()
+    out = autotune(sc, factors=(2.5, 3.0), sweep_blocks=(2, 4), warp_items=(512,), steps=3, warmup=2)
+    assert out["cell_factor"] in (2.5, 3.0)
+    assert out["sweep_blocks"] in (None, 2, 4)
+    assert out["pt_warp_items"] in (None, 512)
+    assert out["ms_per_step"] > 0 and out["default_ms_per_step"] > 0
+    assert len(out["table"]) == 2 + 2 + 1
+    e = engine_for(sc, precision="mixed", cell_factor=out["cell_factor"])
+    if out["sweep_blocks"] is not None:
+        e.set_sweep_blocks(out["sweep_blocks"])
+    if out["pt_warp_items"] is not None:
+        e.set_pt_warp_items(out["pt_warp_items"])
+    e.run(3)
+    assert e.stepStats()["particle_contacts"] > 0
