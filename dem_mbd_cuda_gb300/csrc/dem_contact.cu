@@ -702,45 +702,86 @@ __device__ __forceinline__ bool pt_may_touch(const float4* __restrict__ tf, int 
 }
 
 // Per sorted position: can any triangle of its cell give a nonzero area
-// scale (the condition of a manifold, :1154-1183)?  FP32 rejection only: the
-// flag may be set for a component without a manifold (the law kernel then
-// finds none), never cleared for one with.  Components in cells without
-// triangles leave at once.
-template <typename TB>
-__global__ void __launch_bounds__(256) k_pt_probe(Grid g, Recs r, Tris tris, Hist<TB> hb, Counters k, int* cflag)
+// scale (the condition of a manifold, :1154-1183)?  FP32 rejection only: a
+// position may be kept without a manifold (the law kernel then finds none),
+// never dropped with one.  Triangle loads go four at a time.
+__device__ __forceinline__ bool pt_cell_may_touch(const Tris& tris, int tb, int te, const PtProbe& q)
 {
-    const int nvalid = *g.nvalid;
-    const int step = *k.step;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
-        // expireHistory (:1109-1117) of the body slots, before the law
-        // kernels acquire any for this step
-        expire(hb, kBSlots, g.sorted_id[t], step);
-        const int lin = r.cell[t].w;
-        const int tb = tris.tcell_start[lin];
-        const int te = min(tris.tcell_start[lin + 1], tris.capacity);
-        int hit = 0;
-        if (te > tb) {
-            const D4 p4 = r.pos[t];
-            const PtProbe q = pt_probe(d3(p4), p4.w);
-            for (int e = tb; e < te && !hit; ++e) hit = pt_may_touch(tris.tf, tris.ttri[e], q) ? 1 : 0;
-        }
-        cflag[t] = hit;
+    for (int e0 = tb; e0 < te; e0 += 4) {
+        int tri[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) tri[u] = e0 + u < te ? __ldg(&tris.ttri[e0 + u]) : -1;
+        bool hit = false;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) hit |= tri[u] >= 0 && pt_may_touch(tris.tf, tri[u], q);
+        if (hit) return true;
     }
+    return false;
 }
 
-// Contact items in sorted order (clist holds sorted positions); pt_index
-// maps a component to its contact item, -1 when it touches no triangle.
-__global__ void k_pt_compact_contacts(Grid g, Recs r, int* cflag, int* cpos, int* clist, int* pt_index, int* ctotal)
+// The contact items of a step in one launch: per sorted position, the expiry
+// of its body slots (expireHistory, :1109-1117, before the law kernels
+// acquire any) and the probe; then its rank among the kept positions (block
+// scan plus the tiles before it, by single-pass look-back, ScanState) gives
+// the item list in sorted order and each component's item index (-1: none).
+constexpr int kPtTile = 1024;
+
+template <typename TB>
+__global__ void __launch_bounds__(kPtTile) k_pt_items(Grid g, Recs r, Tris tris, Hist<TB> hb, Counters k, int* clist,
+                                                      int* pt_index, int* ctotal, ScanState st, unsigned* err)
 {
+    __shared__ int s_tile, s_prefix;
     const int nvalid = *g.nvalid;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *ctotal = cpos[nvalid];
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
-        const int ci = r.meta[t].x;
-        if (cflag[t]) {
-            clist[cpos[t]] = t;
-            pt_index[ci] = cpos[t];
-        } else {
-            pt_index[ci] = -1;
+    const int step = *k.step;
+    const int ntiles = min((nvalid + kPtTile - 1) / kPtTile, st.max_tiles);
+    const unsigned epoch = st.ctl[2];
+    if (nvalid == 0 && blockIdx.x == 0 && threadIdx.x == 0) *ctotal = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(st.ctl, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= ntiles) break;
+        const int t = tile * kPtTile + threadIdx.x;
+        int hit = 0, ci = -1;
+        if (t < nvalid) {
+            ci = g.sorted_id[t];
+            expire(hb, kBSlots, ci, step);
+            const int lin = r.cell[t].w;
+            const int tb = tris.tcell_start[lin];
+            const int te = min(tris.tcell_start[lin + 1], tris.capacity);
+            if (te > tb) {
+                const D4 p4 = r.pos[t];
+                hit = pt_cell_may_touch(tris, tb, te, pt_probe(d3(p4), p4.w)) ? 1 : 0;
+            }
+        }
+        int total;
+        const int ex = block_exclusive_scan_c(hit, total);
+        if (threadIdx.x == 0) scan_publish(st, tile, total, epoch, tile == 0 ? 2u : 1u);
+        if (threadIdx.x < 32) {
+            const int prefix = tile == 0 ? 0 : scan_lookback(st, tile, epoch, err);
+            if (threadIdx.x == 0) {
+                if (tile > 0) scan_publish(st, tile, prefix + total, epoch, 2u);
+                s_prefix = prefix;
+            }
+        }
+        __syncthreads();
+        if (t < nvalid) {
+            if (hit) {
+                clist[s_prefix + ex] = t;
+                pt_index[ci] = s_prefix + ex;
+            } else {
+                pt_index[ci] = -1;
+            }
+        }
+        if (tile == ntiles - 1 && threadIdx.x == 0) *ctotal = s_prefix + total;
+        __syncthreads();  // s_tile, s_prefix are reused by the next tile
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(st.ctl + 1, 1u) == gridDim.x - 1) {
+            st.ctl[0] = 0u;
+            st.ctl[1] = 0u;
+            atomicAdd(st.ctl + 2, 1u);
         }
     }
 }
@@ -1559,10 +1600,8 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
     }
     if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
-        k_pt_probe<TB><<<sm_count * 8, 256, 0, s>>>(g, r, t, hb, k, ct.pt_cflag);
-        launch_scan(ct.pt_cflag, ct.pt_cpos, g.nvalid, ct.pt_tile_sums, sm_count, s);
-        k_pt_compact_contacts<<<sm_count * 8, 256, 0, s>>>(g, r, ct.pt_cflag, ct.pt_cpos, ct.pt_clist, ct.pt_index,
-                                                           ct.pt_ctotal_ptr);
+        k_pt_items<TB><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 2)), kPtTile, 0, s>>>(
+            g, r, t, hb, k, ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr, ct.pt_scan, g.err);
         k_pt_warp<T, TB><<<sm_count * 8, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
         k_pt_thread<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
     }

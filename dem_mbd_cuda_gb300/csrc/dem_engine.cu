@@ -386,7 +386,7 @@ public:
         G_.scene_layout = arena_.alloc<int>(8 * S_, "scene layout");
         G_.total_cells = arena_.alloc<int>(1, "total cells");
         G_.nvalid = arena_.alloc<int>(1, "nvalid");
-        G_.tile_sums = arena_.alloc<int>(cap / 4096 + 64, "tile sums");
+        G_.scan = alloc_scan(cap + 1, 4096, "cell scan");
         G_.err = arena_.alloc<unsigned>(1, "err");
         check(cudaMemsetAsync(G_.err, 0, sizeof(unsigned), s), "clear err");
 
@@ -462,7 +462,7 @@ public:
             T_.tcell_start = arena_.alloc<int>(cap + 2, "tri cell start");
             check(cudaMemsetAsync(T_.tcell_count, 0, sizeof(int) * (cap + 1), s), "clear");
             check(cudaMemsetAsync(T_.tcell_cursor, 0, sizeof(int) * (cap + 1), s), "clear");
-            T_.tile_sums = arena_.alloc<int>(cap / 4096 + 64, "tri tile sums");
+            T_.scan = alloc_scan(cap + 1, 4096, "triangle scan");
         }
 
         // ---- counters
@@ -547,15 +547,26 @@ public:
         check(cudaMemsetAsync(ct.pt_index, 0xff, nc_ * sizeof(int), s), "clear");
         ct.nbs = std::max(nbs_, 1);
         if (nb_ > 0 && nt_ > 0) {
-            ct.pt_cflag = arena_.alloc<int>(nc_ + 1, "pt contact flag");
-            ct.pt_cpos = arena_.alloc<int>(nc_ + 2, "pt contact pos");
             ct.pt_clist = arena_.alloc<int>(nc_, "pt contact list");
             ct.pt_ctotal_ptr = K_.pt_ctotal;
-            ct.pt_tile_sums = arena_.alloc<int>((size_t)nc_ / 4096 + 64, "pt tile sums");
+            ct.pt_scan = alloc_scan((size_t)nc_ + 1, 1024, "pt item scan");
             ct.pt_res = arena_.alloc<double>((size_t)nc_ * 6, "pt results");
             ct.pt_body = arena_.alloc<double>((size_t)nc_ * ct.nbs * kPtRecord, "pt body records");
             if (keep_bp_ || keep_bd_) ct.pt_out = arena_.alloc<double>((size_t)nc_ * ct.nbs * 25, "pt outputs");
         }
+    }
+
+    // Status words and control words of a single-pass scan over up to n items
+    // in tiles of `tile` (zeroed: epoch 0, nothing published).
+    ScanState alloc_scan(size_t n, int tile, const char* what)
+    {
+        ScanState st;
+        st.max_tiles = (int)(n / tile + 2);
+        st.status = arena_.alloc<unsigned long long>((size_t)st.max_tiles, what);
+        st.ctl = arena_.alloc<unsigned>(4, what);
+        check(cudaMemsetAsync(st.status, 0, sizeof(unsigned long long) * st.max_tiles, stream_), what);
+        check(cudaMemsetAsync(st.ctl, 0, sizeof(unsigned) * 4, stream_), what);
+        return st;
     }
 
     // ----------------------------------------------------------- pipeline
@@ -823,6 +834,7 @@ public:
             throw DemError(DEM_ERR_CAPACITY, "CUDA wall/body contact-history capacity exceeded; increase the configured history slots");
         if (st.triangle_grid_overflows || (err & (kErrTriCapacity | kErrTriRange)))
             throw DemError(DEM_ERR_CAPACITY, "CUDA triangle-grid coordinate/count overflow");
+        if (err & kErrScanWait) throw DemError(DEM_ERR_CUDA, "a single-pass scan gave up waiting for a predecessor tile");
         return DEM_OK;
     }
 

@@ -334,6 +334,66 @@ __global__ void k_scan_apply(const int* in, int* out, const int* n_dev, const in
     }
 }
 
+// ------------------------------------------------------ single-pass scan
+// One launch instead of reduce / tile sums / apply: persistent blocks claim
+// 4096-int tiles in order, sum them, publish the aggregate, look back over
+// the predecessors' status words (ScanState, scan_lookback) and write the
+// tile's exclusive prefixes.
+constexpr int kScan1Block = 512;
+constexpr int kScan1Items = 8;
+constexpr int kScan1Tile = kScan1Block * kScan1Items;
+
+__global__ void __launch_bounds__(kScan1Block) k_scan1(const int* in, int* out, const int* n_dev, ScanState st,
+                                                      unsigned* err)
+{
+    __shared__ int s_tile, s_prefix;
+    const int n = *n_dev;
+    const int ntiles = min((n + kScan1Tile - 1) / kScan1Tile, st.max_tiles);
+    const unsigned epoch = st.ctl[2];
+    if (n == 0 && blockIdx.x == 0 && threadIdx.x == 0) out[0] = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(st.ctl, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= ntiles) break;
+        const int base = tile * kScan1Tile + threadIdx.x * kScan1Items;
+        int v[kScan1Items];
+        int sum = 0;
+#pragma unroll
+        for (int q = 0; q < kScan1Items; ++q) {
+            v[q] = base + q < n ? in[base + q] : 0;
+            sum += v[q];
+        }
+        int total;
+        const int ex = block_exclusive_scan(sum, total);
+        if (threadIdx.x == 0) scan_publish(st, tile, total, epoch, tile == 0 ? 2u : 1u);
+        if (threadIdx.x < 32) {
+            const int prefix = tile == 0 ? 0 : scan_lookback(st, tile, epoch, err);
+            if (threadIdx.x == 0) {
+                if (tile > 0) scan_publish(st, tile, prefix + total, epoch, 2u);
+                s_prefix = prefix;
+            }
+        }
+        __syncthreads();
+        int run = s_prefix + ex;
+#pragma unroll
+        for (int q = 0; q < kScan1Items; ++q) {
+            if (base + q < n) out[base + q] = run;
+            run += v[q];
+        }
+        if (tile == ntiles - 1 && threadIdx.x == 0) out[n] = s_prefix + total;
+        __syncthreads();  // s_tile, s_prefix are reused by the next tile
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(st.ctl + 1, 1u) == gridDim.x - 1) {
+            st.ctl[0] = 0u;
+            st.ctl[1] = 0u;
+            atomicAdd(st.ctl + 2, 1u);
+        }
+    }
+}
+
 // ------------------------------------------------------------- triangles
 // transformTrianglesKernel (src/cuda/cuda_body_backend.cu:71-112).
 __global__ void k_tri_transform(Tris t, Bodies b, const SceneC* __restrict__ sc)
@@ -656,6 +716,12 @@ void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int 
     k_scan_apply<<<g, kScanBlock, 0, s>>>(in, out, n_dev, tile_sums);
 }
 
+void launch_scan1(const int* in, int* out, const int* n_dev, const ScanState& st, unsigned* err, int sm_count,
+                  cudaStream_t s)
+{
+    k_scan1<<<std::max(1, std::min(st.max_tiles, sm_count * 2)), kScan1Block, 0, s>>>(in, out, n_dev, st, err);
+}
+
 void launch_grid_layout(const Comps& c, const Owners& o, const Grid& g, cudaStream_t s)
 {
     if (c.n <= 0) return;
@@ -667,7 +733,7 @@ void launch_grid_sort(const Comps& c, const Owners& o, const Grid& g, int sm_cou
 {
     if (c.n <= 0) return;
     k_cell_count<<<blocks(c.n, 256), 256, 0, s>>>(c, o, g);
-    launch_scan(g.cell_count, g.cell_start, g.total_cells, g.tile_sums, sm_count, s);
+    launch_scan1(g.cell_count, g.cell_start, g.total_cells, g.scan, g.err, sm_count, s);
     k_scatter<<<blocks(c.n, 256), 256, 0, s>>>(c, g);
     k_place<<<blocks(c.n, 256), 256, 0, s>>>(c, g);
 }
@@ -681,7 +747,7 @@ void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover
 {
     if (t.nt <= 0) return;
     k_tri_count<<<blocks(32 * t.nt, 128), 128, 0, s>>>(t, g, tgover);
-    launch_scan(t.tcell_count, t.tcell_start, g.total_cells, t.tile_sums, sm_count, s);
+    launch_scan1(t.tcell_count, t.tcell_start, g.total_cells, t.scan, g.err, sm_count, s);
     k_tri_fill<<<blocks(32 * t.nt, 128), 128, 0, s>>>(t, g);
     k_tri_place<<<sm_count * 8, 256, 0, s>>>(t, g);
 }

@@ -28,7 +28,69 @@ enum : unsigned {
     kErrCellCapacity = 2u,    // dense cell table too small for the cell box
     kErrTriCapacity = 4u,     // triangle grid entries beyond capacity
     kErrTriRange = 8u,        // triangle cell range overflow (reference :422-450)
+    kErrScanWait = 16u,       // a single-pass scan gave up waiting for a predecessor tile
 };
+
+// Single-pass scan state (decoupled look-back).  Tiles are claimed in order
+// through ctl[0]; each publishes a status word (value << 32 | epoch << 2 |
+// flag: 1 aggregate, 2 inclusive prefix); ctl[1] counts finished blocks and
+// the last one resets ctl[0..1] and advances the epoch ctl[2], so the words
+// of an earlier launch read as not ready.  One state per concurrent scan.
+struct ScanState {
+    unsigned long long* status;  // [max_tiles]
+    unsigned* ctl;               // [3]: ticket, blocks done, epoch
+    int max_tiles;
+};
+
+#ifdef __CUDACC__
+constexpr int kScanSpinLimit = 1 << 20;
+
+__device__ __forceinline__ unsigned long long scan_word(int value, unsigned epoch, unsigned flag)
+{
+    return ((unsigned long long)(unsigned)value << 32) | ((unsigned long long)(epoch & 0x3fffffffu) << 2) | flag;
+}
+__device__ __forceinline__ void scan_publish(const ScanState& st, int tile, int value, unsigned epoch, unsigned flag)
+{
+    atomicExch(st.status + tile, scan_word(value, epoch, flag));
+}
+// Exclusive prefix of `tile` (warp 0 of the block, all lanes get it): reads
+// 32 predecessor words at a time, back to the nearest inclusive one.  Every
+// wait is bounded; at the bound it sets kErrScanWait and returns what it has.
+__device__ __forceinline__ int scan_lookback(const ScanState& st, int tile, unsigned epoch, unsigned* err)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int prefix = 0, top = tile - 1, spins = 0;
+    while (true) {
+        const int idx = top - lane;
+        unsigned flag = 2u;  // before tile 0: an inclusive zero
+        int val = 0;
+        if (idx >= 0) {
+            const unsigned long long w = atomicAdd(st.status + idx, 0ull);
+            const bool current = ((w >> 2) & 0x3fffffffu) == (epoch & 0x3fffffffu);
+            flag = current ? (unsigned)(w & 3u) : 0u;
+            val = (int)(unsigned)(w >> 32);
+        }
+        const unsigned incl = __ballot_sync(FULL, flag == 2u);
+        const unsigned waiting = __ballot_sync(FULL, flag == 0u);
+        const int stop = incl ? __ffs(incl) - 1 : 31;
+        const unsigned need = stop == 31 ? FULL : ((1u << (stop + 1)) - 1u);
+        if (waiting & need) {
+            if (++spins > kScanSpinLimit) {
+                if (lane == 0) atomicOr(err, kErrScanWait);
+                return prefix;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        int v = lane <= stop ? val : 0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+        prefix += v;
+        if (incl) return prefix;
+        top -= 32;
+    }
+}
+#endif
 
 struct Owners {
     int n;
@@ -80,8 +142,8 @@ struct Grid {
     int* scene_layout;  // [S][8]: min xyz, n xyz, offset, cells
     int* total_cells;   // [1]
     int* nvalid;        // [1] = cell_start[total_cells]
-    int* tile_sums;
     unsigned* err;
+    ScanState scan;    // the cell start table's single-pass scan
 };
 
 // 32-byte aligned row of four doubles (one full sector per row).
@@ -128,7 +190,7 @@ struct Tris {
     int* scene;     // per triangle
     int capacity;   // triangle grid entry capacity
     int *tcell_count, *tcell_cursor, *tcell_start, *ttri, *ttri_tmp, *tlin_tmp;
-    int* tile_sums;  // scan scratch of the triangle grid (it builds beside the particle grid)
+    ScanState scan;  // the triangle start table's single-pass scan (its own: it builds beside the particle grid)
 };
 
 struct Bodies {
@@ -215,11 +277,9 @@ template <typename T> struct Contacts {
     unsigned char* wflag;  // per component: nonzero wall force/torque this step
     int2* wlist;           // components with a candidate wall: (component, wall mask)
     int* pt_index;  // per component: contact item or -1
-    int* pt_cflag;      // per sorted position: may touch a triangle of its cell
-    int* pt_cpos;       // scan of pt_cflag
     int* pt_clist;      // contact item k -> sorted position
     int* pt_ctotal_ptr; // [1] contact items this step
-    int* pt_tile_sums;  // scan scratch of the contact-item compaction
+    ScanState pt_scan;  // single-pass scan of the contact-item compaction
     double* pt_res; // [component][6] particle-side PT load (valid where pt_index >= 0)
     double* pt_body;    // [contact item][nbs][kPtRecord]
     double* pt_out;     // [contact item][nbs][25] optional output detail
@@ -243,6 +303,9 @@ void launch_update_components(const Comps& c, const Owners& o, cudaStream_t s);
 void launch_grid_layout(const Comps& c, const Owners& o, const Grid& g, cudaStream_t s);
 void launch_grid_sort(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s);
 void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int sm_count, cudaStream_t s);
+// Single-pass exclusive scan of in[0, n) into out[0, n] (out[n] = total).
+void launch_scan1(const int* in, int* out, const int* n_dev, const ScanState& st, unsigned* err, int sm_count,
+                  cudaStream_t s);
 void launch_tri_transform(const Tris& t, const Bodies& b, const SceneC* sc, cudaStream_t s);
 void launch_tri_build(const Tris& t, const Bodies& b, const Grid& g, int* tgover, int sm_count, cudaStream_t s);
 void launch_universal_gravity(const Owners& o, cudaStream_t s);
