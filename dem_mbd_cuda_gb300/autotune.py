@@ -7,10 +7,10 @@ physics:
   cell means fewer candidates per particle in the sweep but more cells to
   build and visit; the reference's 2.5 is the only value whose sorted cell
   keys match its own, so it stays the default;
-* the sweep's blocks per SM: the sweep runs grid-stride so that the kernels
-  of the step's other branches (particle-triangle law, rotational advance,
-  walls) find free warp slots beside it; the best share depends on how much
-  work those branches carry;
+* the blocks per SM of the sweep and of the record gathers: they run
+  grid-stride so that the kernels of the step's other branches
+  (particle-triangle law, rotational advance, walls) find free warp slots
+  beside them; the best share depends on how much work those branches carry;
 * the particle-triangle crossover (contact items up to which the PT law runs
   one warp per item instead of one thread per item).
 
@@ -29,6 +29,7 @@ from .engine import CudaDemSolver
 
 FACTORS = (2.0, 2.25, 2.5, 3.0, 3.5)
 SWEEP_BLOCKS = (2, 3, 4, 5, 6, 8)
+GATHER_BLOCKS = (1, 2, 4, 8)
 WARP_ITEMS = (512, 3072, 16384)
 _cache: dict = {}
 
@@ -44,42 +45,50 @@ def _signature(scene, precision):
     return h.hexdigest()
 
 
-def _time(scene, precision, factor, sweep_blocks, warp_items, steps, warmup):
+def _time(scene, precision, factor, sweep_blocks, gather_blocks, warp_items, steps, warmup):
     e = CudaDemSolver().initialize(scene, precision=precision, cell_factor=factor)
     if sweep_blocks is not None:
         e.set_sweep_blocks(sweep_blocks)
+    if gather_blocks is not None:
+        e.set_gather_blocks(gather_blocks)
     if warp_items is not None:
         e.set_pt_warp_items(warp_items)
     e.run(max(1, warmup))
     return min(e.time_steps(steps) / steps for _ in range(2))
 
 
-def autotune(scene, precision="mixed", factors=FACTORS, sweep_blocks=SWEEP_BLOCKS, warp_items=WARP_ITEMS, steps=20,
-             warmup=5):
-    """Fastest (cell_factor, sweep_blocks, pt_warp_items) for `scene`, searched
-    one setting at a time in that order; returns a dict with the choice, its
-    ms per step, the default's ms per step and the table.  None in the choice
-    means the engine's default."""
-    key = (_signature(scene, precision), tuple(factors), tuple(sweep_blocks), tuple(warp_items), steps)
+def autotune(scene, precision="mixed", factors=FACTORS, sweep_blocks=SWEEP_BLOCKS, gather_blocks=GATHER_BLOCKS,
+             warp_items=WARP_ITEMS, steps=20, warmup=5):
+    """Fastest (cell_factor, sweep_blocks, gather_blocks, pt_warp_items) for
+    `scene`, searched one setting at a time in that order; returns a dict with
+    the choice, its ms per step, the default's ms per step and the table.
+    None in the choice means the engine's default."""
+    key = (_signature(scene, precision), tuple(factors), tuple(sweep_blocks), tuple(gather_blocks), tuple(warp_items),
+           steps)
     if key in _cache:
         return _cache[key]
     table = []
 
-    def row(f, b, w):
-        r = {"cell_factor": f, "sweep_blocks": b, "pt_warp_items": w,
-             "ms_per_step": _time(scene, precision, f, b, w, steps, warmup)}
+    def row(f, b, g, w):
+        r = {"cell_factor": f, "sweep_blocks": b, "gather_blocks": g, "pt_warp_items": w,
+             "ms_per_step": _time(scene, precision, f, b, g, w, steps, warmup)}
         table.append(r)
         return r
 
-    best = min((row(f, None, None) for f in factors), key=lambda r: r["ms_per_step"])
+    def pick(rows):
+        return min(rows, key=lambda r: r["ms_per_step"])
+
+    best = pick([row(f, None, None, None) for f in factors])
     default = next(r["ms_per_step"] for r in table if r["cell_factor"] == 2.5)
-    best = min([best] + [row(best["cell_factor"], b, None) for b in sweep_blocks], key=lambda r: r["ms_per_step"])
+    best = pick([best] + [row(best["cell_factor"], b, None, None) for b in sweep_blocks])
+    best = pick([best] + [row(best["cell_factor"], best["sweep_blocks"], g, None) for g in gather_blocks])
     has_bodies = any(s.n_bodies for s in (scene if isinstance(scene, (list, tuple)) else [scene]))
     if has_bodies:
-        best = min([best] + [row(best["cell_factor"], best["sweep_blocks"], w) for w in warp_items],
-                   key=lambda r: r["ms_per_step"])
+        best = pick([best] + [row(best["cell_factor"], best["sweep_blocks"], best["gather_blocks"], w)
+                              for w in warp_items])
     out = {"cell_factor": best["cell_factor"], "sweep_blocks": best["sweep_blocks"],
-           "pt_warp_items": best["pt_warp_items"], "ms_per_step": best["ms_per_step"],
-           "default_ms_per_step": default, "speedup_over_default": default / best["ms_per_step"], "table": table}
+           "gather_blocks": best["gather_blocks"], "pt_warp_items": best["pt_warp_items"],
+           "ms_per_step": best["ms_per_step"], "default_ms_per_step": default,
+           "speedup_over_default": default / best["ms_per_step"], "table": table}
     _cache[key] = out
     return out

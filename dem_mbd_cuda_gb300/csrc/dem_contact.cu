@@ -724,7 +724,7 @@ __device__ __forceinline__ bool pt_cell_may_touch(const Tris& tris, int tb, int 
 // acquire any) and the probe; then its rank among the kept positions (block
 // scan plus the tiles before it, by single-pass look-back, ScanState) gives
 // the item list in sorted order and each component's item index (-1: none).
-constexpr int kPtTile = 1024;
+constexpr int kPtTile = kPtItemTile;
 
 template <typename TB>
 __global__ void __launch_bounds__(kPtTile) k_pt_items(Grid g, Recs r, Tris tris, Hist<TB> hb, Counters k, int* clist,
@@ -1080,6 +1080,9 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
 // triangles.  A list longer than the per-warp cache takes the uncompacted
 // loops (same sums, recomputed areas).
 constexpr int kPtTriCache = 128;  // per-warp candidate list: triangle, (area scale, distance)
+// One warp per block: a block of this kernel (255 registers a thread) then
+// fits beside the particle law and the sweep that run at the same time.
+constexpr int kPtWarpBlock = 32;
 
 __device__ __forceinline__ V3<double> shfl3(V3<double> v, int src)
 {
@@ -1088,12 +1091,12 @@ __device__ __forceinline__ V3<double> shfl3(V3<double> v, int src)
 }
 
 template <typename TC, typename T>
-__global__ void __launch_bounds__(128) k_pt_warp(Comps c, Owners o, Recs r, const SceneC* __restrict__ sc, Tris tris,
+__global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Recs r, const SceneC* __restrict__ sc, Tris tris,
                                                  Bodies bodies, Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff)
 {
     constexpr unsigned FULL = 0xffffffffu;
-    __shared__ double2 s_ad[4][kPtTriCache];
-    __shared__ int s_tri[4][kPtTriCache];
+    __shared__ double2 s_ad[kPtWarpBlock / 32][kPtTriCache];
+    __shared__ int s_tri[kPtWarpBlock / 32][kPtTriCache];
     const int step = *k.step;
     const int total = *ct.pt_ctotal_ptr;
     if (total > k.pt_warp_items) return;
@@ -1573,14 +1576,15 @@ inline int blocks(int n, int b) { return (n + b - 1) / b; }
 
 template <typename T>
 void launch_gather_vel(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
-                       cudaStream_t s)
+                       int bps, cudaStream_t s)
 {
-    k_gather_vel<T><<<sm_count * 8, 256, 0, s>>>(c, o, g, r, dt_eff);
+    k_gather_vel<T><<<sm_count * bps, 256, 0, s>>>(c, o, g, r, dt_eff);
 }
 
-void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, cudaStream_t s)
+void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, int bps,
+                        cudaStream_t s)
 {
-    k_gather_geom<<<sm_count * 8, 256, 0, s>>>(c, o, g, r);
+    k_gather_geom<<<sm_count * bps, 256, 0, s>>>(c, o, g, r);
 }
 
 template <typename T, typename TB>
@@ -1598,11 +1602,11 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
         k_walls_probe<T><<<blocks(c.n, 256), 256, 0, s>>>(c, o, sc, w, hw, k, ct.wflag, ct.wlist);
         k_walls_law<T><<<sm_count * 4, 128, 0, s>>>(c, o, sc, w, hw, ct, k, dt_eff);
     }
-    if (stage & 4) k_pp_law<T><<<sm_count * 16, 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
+    if (stage & 4) k_pp_law<T><<<sm_count * (k.pp_bps > 0 ? k.pp_bps : 16), 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
-        k_pt_items<TB><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 2)), kPtTile, 0, s>>>(
+        k_pt_items<TB><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 8)), kPtTile, 0, s>>>(
             g, r, t, hb, k, ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr, ct.pt_scan, g.err);
-        k_pt_warp<T, TB><<<sm_count * 8, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
+        k_pt_warp<T, TB><<<sm_count * 32, kPtWarpBlock, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
         k_pt_thread<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
     }
 }
@@ -1632,7 +1636,7 @@ void launch_body_outputs(const Comps& c, const Owners& o, const Bodies& b, const
 }
 
 #define DEM_INSTANTIATE(T)                                                                                            \
-    template void launch_gather_vel<T>(const Comps&, const Owners&, const Grid&, const Recs&, double, int,            \
+    template void launch_gather_vel<T>(const Comps&, const Owners&, const Grid&, const Recs&, double, int, int,       \
                                        cudaStream_t);                                                                 \
     template void launch_contacts<T, double>(const Comps&, const Owners&, const Grid&, const Recs&, const SceneC*,   \
                                              const Walls&, const Tris&, const Bodies&, Hist<T>, Hist<T>,             \

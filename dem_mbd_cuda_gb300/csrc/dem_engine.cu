@@ -76,7 +76,18 @@ private:
 constexpr int kDefaultPtWarpItems = 3072;
 // Sweep blocks per SM: the sweep leaves warp slots to the PT and rotational
 // branches that run beside it (0 would launch one thread per component).
-constexpr int kDefaultSweepBlocksPerSm = 4;
+// Scenes of up to kSmallScene components leave more room (their PT and
+// rotational branches are short chains that must not wait for slots);
+// larger scenes are throughput bound and give the sweep and the gathers
+// more of each SM.  Measured on GB300 (200k- and 2M-sphere scenes); the
+// autotuner refines them per scene.  Six sweep blocks per SM is the sweep's
+// register-limited residency: that grid leaves nothing beside it and was
+// the slowest setting on the 2M drum.
+constexpr int kSmallScene = 500000;
+constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 8;
+// The gathers and the particle law, likewise (blocks of 256 per SM).
+constexpr int kGatherBlocksSmall = 2, kGatherBlocksLarge = 8;
+constexpr int kDefaultPpBlocksPerSm = 16;
 
 static MatF to_float(const MatC& c)
 {
@@ -473,7 +484,9 @@ public:
         K_.pt_ctotal = cnt + 9;
         K_.wl_total = cnt + 10;
         K_.pt_warp_items = kDefaultPtWarpItems;
-        K_.sweep_bps = kDefaultSweepBlocksPerSm;
+        K_.sweep_bps = nc_ <= kSmallScene ? kSweepBlocksSmall : kSweepBlocksLarge;
+        K_.gather_bps = nc_ <= kSmallScene ? kGatherBlocksSmall : kGatherBlocksLarge;
+        K_.pp_bps = kDefaultPpBlocksPerSm;
 
         // ---- scene constants
         scenes_h_ = sc;
@@ -549,7 +562,7 @@ public:
         if (nb_ > 0 && nt_ > 0) {
             ct.pt_clist = arena_.alloc<int>(nc_, "pt contact list");
             ct.pt_ctotal_ptr = K_.pt_ctotal;
-            ct.pt_scan = alloc_scan((size_t)nc_ + 1, 1024, "pt item scan");
+            ct.pt_scan = alloc_scan((size_t)nc_ + 1, kPtItemTile, "pt item scan");
             ct.pt_res = arena_.alloc<double>((size_t)nc_ * 6, "pt results");
             ct.pt_body = arena_.alloc<double>((size_t)nc_ * ct.nbs * kPtRecord, "pt body records");
             if (keep_bp_ || keep_bd_) ct.pt_out = arena_.alloc<double>((size_t)nc_ * ct.nbs * 25, "pt outputs");
@@ -624,8 +637,8 @@ public:
             mark();
             if (pt) launch_tri_build(T_, B_, G_, K_.tgover, sm_count_, s);
             if (O_.ugx) launch_universal_gravity(O_, s);
-            launch_gather_geom(C_, O_, G_, R_, sm_count_, s);
-            launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, s);
+            launch_gather_geom(C_, O_, G_, R_, sm_count_, K_.gather_bps, s);
+            launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, K_.gather_bps, s);
             mark();
             for (int stage : {2, 1, 4, 8}) {
                 contacts(stage, s);
@@ -677,14 +690,14 @@ public:
         }
         launch_grid_sort(C_, O_, G_, sm_count_, s);
         if (O_.ugx) launch_universal_gravity(O_, s);
-        launch_gather_geom(C_, O_, G_, R_, sm_count_, s);
+        launch_gather_geom(C_, O_, G_, R_, sm_count_, K_.gather_bps, s);
         if (pt) {
             // PT reads the geometry records and the owner state itself
             link(s, bt, 2);
             link(br, bt, 10);
         }
         link(s, br, 9);  // the velocity gather follows the sorted order
-        launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, br);
+        launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, K_.gather_bps, br);
         if (pt) contacts(8, bt);
         contacts(2, s);
         link(br, s, 11);  // the particle law reads the velocity records
@@ -1013,12 +1026,16 @@ public:
         for (cudaGraphExec_t& g : graphs_)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     }
-    // Sweep blocks per SM (0: one thread per component); graphs rebuilt.
-    void set_sweep_blocks(int n)
+    // Blocks per SM of the sweep (0: one thread per component), the gathers
+    // and the particle law (0: 16); graphs rebuilt.
+    void set_launch(int what, int n)
     {
         need_init();
         check(cudaStreamSynchronize(stream_), "sync");
-        K_.sweep_bps = std::max(0, n);
+        if (what == 0) K_.sweep_bps = std::max(0, n);
+        else if (what == 1) K_.gather_bps = std::max(1, n);
+        else if (what == 2) K_.pp_bps = std::max(0, n);
+        else throw DemError(DEM_ERR_INVALID, "unknown launch setting");
         for (cudaGraphExec_t& g : graphs_)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         adj_release_graphs();
@@ -1899,9 +1916,9 @@ int dem_x_set_pt_warp_items(dem_engine* e, int n)
     return guarded([&] { NEED(e); e->e.set_pt_warp_items(n); });
 }
 
-int dem_x_set_sweep_blocks(dem_engine* e, int blocks_per_sm)
+int dem_x_set_launch(dem_engine* e, int what, int blocks_per_sm)
 {
-    return guarded([&] { NEED(e); e->e.set_sweep_blocks(blocks_per_sm); });
+    return guarded([&] { NEED(e); e->e.set_launch(what, blocks_per_sm); });
 }
 
 int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every)

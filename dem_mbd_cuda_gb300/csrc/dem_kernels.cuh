@@ -42,6 +42,9 @@ struct ScanState {
     int max_tiles;
 };
 
+// Sorted positions per tile of the particle-triangle item scan.
+constexpr int kPtItemTile = 256;
+
 #ifdef __CUDACC__
 constexpr int kScanSpinLimit = 1 << 20;
 
@@ -212,6 +215,8 @@ struct Counters {
     int* step;          // contact step index
     int pt_warp_items;  // PT: warp-per-item kernel up to this many contact items
     int sweep_bps;      // sweep blocks per SM (grid-stride), 0 = one thread per component
+    int gather_bps;     // gather blocks of 256 per SM (grid-stride)
+    int pp_bps;         // particle-law blocks of 256 per SM (grid-stride), 0 = 16
 };
 
 // Reverse sweep (dem_adjoint.cu).  Owner state S of one step, [field][owner]:
@@ -339,10 +344,12 @@ void launch_adj_tape_end(int* pp_count, const int* ct_total, int* slot, cudaStre
 
 // The sorted records: geometry (positions only; all the sweep reads), then
 // velocities (after the rotational advance).
-void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, cudaStream_t s);
+// bps: blocks of 256 per SM (grid-stride), so the kernels beside them keep slots.
+void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, int bps,
+                        cudaStream_t s);
 template <typename T>
 void launch_gather_vel(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
-                       cudaStream_t s);
+                       int bps, cudaStream_t s);
 // T: particle-particle and wall law / history type; TB: particle-triangle
 // law, area and body history type.  `stage` selects kernels (1 expiry and
 // walls, 2 sweep, 4 particle law, 8 particle-triangle) so callers can time

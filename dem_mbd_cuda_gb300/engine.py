@@ -58,7 +58,7 @@ _SIGS = {
     "dem_x_download_half": ([C.c_void_p] + [C.c_void_p] * 5, C.c_int),
     "dem_x_synchronize": ([C.c_void_p], C.c_int),
     "dem_x_set_pt_warp_items": ([C.c_void_p, C.c_int], C.c_int),
-    "dem_x_set_sweep_blocks": ([C.c_void_p, C.c_int], C.c_int),
+    "dem_x_set_launch": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
     "dem_adjoint_forward": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
     "dem_adjoint_backward": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
 }
@@ -296,7 +296,17 @@ class CudaDemSolver:
     def set_sweep_blocks(self, blocks_per_sm):
         """Blocks per SM of the particle sweep (grid-stride); 0 launches one
         thread per component.  Changes only the speed."""
-        self._check(self.lib.dem_x_set_sweep_blocks(self.h, int(blocks_per_sm)))
+        self._check(self.lib.dem_x_set_launch(self.h, 0, int(blocks_per_sm)))
+        return self
+
+    def set_gather_blocks(self, blocks_per_sm):
+        """Blocks of 256 per SM of the record gathers.  Changes only the speed."""
+        self._check(self.lib.dem_x_set_launch(self.h, 1, int(blocks_per_sm)))
+        return self
+
+    def set_pp_blocks(self, blocks_per_sm):
+        """Blocks of 256 per SM of the particle law (0: 16).  Changes only the speed."""
+        self._check(self.lib.dem_x_set_launch(self.h, 2, int(blocks_per_sm)))
         return self
 
     def time_steps(self, steps):

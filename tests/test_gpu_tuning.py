@@ -1,5 +1,6 @@
-"""Speed settings change no result: the sweep's blocks per SM (grid-stride)
-leaves the trajectory, the bodies and the contact histories bit-identical;
+"""Speed settings change no result: the blocks per SM of the sweep, the
+gathers and the particle law (grid-stride) leave the trajectory, the bodies
+and the contact histories bit-identical;
 the autotuner returns a setting the engine accepts."""
 import numpy as np
 import pytest
@@ -21,7 +22,8 @@ def test_sweep_blocks_do_not_change_results(precision, maker):
     sc = getattr(G, maker)()
     runs = []
     for blocks in (0, 1, 3):
-        e = engine_for(sc, precision=precision).set_sweep_blocks(blocks)
+        e = engine_for(sc, precision=precision).set_sweep_blocks(blocks).set_gather_blocks(1 + blocks)
+        e.set_pp_blocks(2 * blocks)
         e.run(15)
         runs.append(e)
     ref = runs[0]
@@ -43,15 +45,19 @@ def test_sweep_blocks_do_not_change_results(precision, maker):
 def test_autotune_returns_an_accepted_setting():
     from dem_mbd_cuda_gb300.autotune import autotune
     sc = G.small_mbd()
-    out = autotune(sc, factors=(2.5, 3.0), sweep_blocks=(2, 4), warp_items=(512,), steps=3, warmup=2)
+    out = autotune(sc, factors=(2.5, 3.0), sweep_blocks=(2, 4), gather_blocks=(1, 8), warp_items=(512,), steps=3,
+                   warmup=2)
     assert out["cell_factor"] in (2.5, 3.0)
     assert out["sweep_blocks"] in (None, 2, 4)
+    assert out["gather_blocks"] in (None, 1, 8)
     assert out["pt_warp_items"] in (None, 512)
     assert out["ms_per_step"] > 0 and out["default_ms_per_step"] > 0
-    assert len(out["table"]) == 2 + 2 + 1
+    assert len(out["table"]) == 2 + 2 + 2 + 1
     e = engine_for(sc, precision="mixed", cell_factor=out["cell_factor"])
     if out["sweep_blocks"] is not None:
         e.set_sweep_blocks(out["sweep_blocks"])
+    if out["gather_blocks"] is not None:
+        e.set_gather_blocks(out["gather_blocks"])
     if out["pt_warp_items"] is not None:
         e.set_pt_warp_items(out["pt_warp_items"])
     e.run(3)
