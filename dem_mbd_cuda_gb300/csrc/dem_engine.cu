@@ -484,7 +484,8 @@ public:
         K_.pt_ctotal = cnt + 9;
         K_.wl_total = cnt + 10;
         K_.pt_warp_items = kDefaultPtWarpItems;
-        K_.sweep_bps = nc_ <= kSmallScene ? kSweepBlocksSmall : kSweepBlocksLarge;
+        // without triangles no PT branch needs room beside the sweep
+        K_.sweep_bps = nt_ == 0 ? 0 : (nc_ <= kSmallScene ? kSweepBlocksSmall : kSweepBlocksLarge);
         K_.gather_bps = nc_ <= kSmallScene ? kGatherBlocksSmall : kGatherBlocksLarge;
         K_.pp_bps = kDefaultPpBlocksPerSm;
 
