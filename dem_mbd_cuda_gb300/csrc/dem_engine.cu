@@ -119,6 +119,7 @@ public:
         for (auto* e : ev_) if (e) cudaEventDestroy(e);
         for (auto* e : fork_ev_) if (e) cudaEventDestroy(e);
         if (body_ready_) cudaEventDestroy(body_ready_);
+        for (auto* e : adj_ev_) if (e) cudaEventDestroy(e);
         arena_.release();
         if (pinned_) cudaFreeHost(pinned_);
         for (auto* b : branch_) if (b) cudaStreamDestroy(b);
@@ -161,6 +162,7 @@ public:
         }
         for (auto*& e : fork_ev_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
         check(cudaEventCreateWithFlags(&body_ready_, cudaEventDisableTiming), "cudaEventCreate");
+        for (auto*& e : adj_ev_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
 
         S_ = nscenes;
         dt_ = scenes[0].dt;
@@ -1336,27 +1338,34 @@ public:
         int step_index = 0;
         bool started = false;
     };
+    // One segment's tape: owner states, particle and wall entries with their
+    // pre-law histories, per-step counts, the device step index, and the
+    // graphs of a taped recompute step and a reverse step (reading Lb[p],
+    // writing Lb[1 - p]) on it.  Two of them let the recompute of one
+    // segment run while the previous one is swept in reverse.
+    struct AdjTape {
+        double* S = nullptr;                       // [K + 1][29][n]
+        int4 *pp = nullptr, *pw = nullptr;         // [K + 1][cap]
+        double *pp_h = nullptr, *pw_h = nullptr;
+        int *pp_cnt = nullptr, *pw_cnt = nullptr, *slot = nullptr;
+        cudaGraphExec_t g_fwd = nullptr, g_rev[2] = {nullptr, nullptr};
+    };
     struct Adjoint {
         bool ready = false;
         int steps = 0, K = 0, nseg = 0, cap_pp = 0, cap_pw = 0;
         std::vector<AdjCkpt> ck;                   // [0] before the first evaluation, [1 + k] after segment k - 1
-        double *S = nullptr;                       // tape of owner states [K + 1][29][n]
+        AdjTape tb[2];
         unsigned char* pp_new = nullptr;
-        int4 *pp = nullptr, *pw = nullptr;         // [K + 1][cap]
-        double *pp_h = nullptr, *pw_h = nullptr;
-        int *pp_cnt = nullptr, *pw_cnt = nullptr, *overflow = nullptr;
+        int* overflow = nullptr;
         double *L = nullptr, *Lp = nullptr, *P = nullptr, *T = nullptr, *lh_pp = nullptr, *lh_pw = nullptr;
         double* grads = nullptr;
         double* Lb[2] = {nullptr, nullptr};        // the two adjoint-state buffers L and Lp alternate between
-        int* slot = nullptr;                       // device step index within a segment
-        // a taped recompute step and a reverse step (reading Lb[p], writing
-        // Lb[1 - p]), captured once the buffers exist
-        cudaGraphExec_t g_fwd = nullptr, g_rev[2] = {nullptr, nullptr};
     };
     void adj_release_graphs()
     {
-        for (cudaGraphExec_t* g : {&adj_.g_fwd, &adj_.g_rev[0], &adj_.g_rev[1]})
-            if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
+        for (AdjTape& t : adj_.tb)
+            for (cudaGraphExec_t* g : {&t.g_fwd, &t.g_rev[0], &t.g_rev[1]})
+                if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
     }
 
     void adj_require() const
@@ -1427,14 +1436,17 @@ public:
         A.cap_pw = 2 * nc_ + 1024;
         for (int k = 0; k < A.nseg + 2; ++k) A.ck.push_back(adj_alloc_ckpt());
         const size_t slots = (size_t)A.K + 1;
-        A.S = adj_arena_.alloc<double>(slots * kAdjFields * n_, "adjoint tape");
+        for (AdjTape& t : A.tb) {
+            t.S = adj_arena_.alloc<double>(slots * kAdjFields * n_, "adjoint tape");
+            t.pp = adj_arena_.alloc<int4>(slots * A.cap_pp, "adjoint tape");
+            t.pp_h = adj_arena_.alloc<double>(slots * A.cap_pp * kHV, "adjoint tape");
+            t.pw = adj_arena_.alloc<int4>(slots * A.cap_pw, "adjoint tape");
+            t.pw_h = adj_arena_.alloc<double>(slots * A.cap_pw * kHV, "adjoint tape");
+            t.pp_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
+            t.pw_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
+            t.slot = adj_arena_.alloc<int>(1, "adjoint slot");
+        }
         A.pp_new = adj_arena_.alloc<unsigned char>((size_t)nc_ * kPSlots, "adjoint tape");
-        A.pp = adj_arena_.alloc<int4>(slots * A.cap_pp, "adjoint tape");
-        A.pp_h = adj_arena_.alloc<double>(slots * A.cap_pp * kHV, "adjoint tape");
-        A.pw = adj_arena_.alloc<int4>(slots * A.cap_pw, "adjoint tape");
-        A.pw_h = adj_arena_.alloc<double>(slots * A.cap_pw * kHV, "adjoint tape");
-        A.pp_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
-        A.pw_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
         A.overflow = adj_arena_.alloc<int>(1, "adjoint tape");
         A.L = adj_arena_.alloc<double>((size_t)kAdjFields * n_, "adjoint state");
         A.Lp = adj_arena_.alloc<double>((size_t)kAdjFields * n_, "adjoint state");
@@ -1443,7 +1455,6 @@ public:
         A.lh_pp = adj_arena_.alloc<double>((size_t)nc_ * kPSlots * kHV, "adjoint history");
         A.lh_pw = adj_arena_.alloc<double>((size_t)nc_ * kWSlots * kHV, "adjoint history");
         A.grads = adj_arena_.alloc<double>(2 * kAdjParams, "adjoint parameters");
-        A.slot = adj_arena_.alloc<int>(1, "adjoint slot");
         A.Lb[0] = A.L; A.Lb[1] = A.Lp;
         adj_save(A.ck[0]);
         run_steps(0);
@@ -1456,45 +1467,55 @@ public:
         A.ready = true;
     }
 
-    // One recomputed force evaluation with its tape in slot `sl`.
+    // The tape of step `sl` of buffer 0 (the first evaluation), pointers of
+    // its own.
+    StepTape adj_tape_step(int sl)
+    {
+        Adjoint& A = adj_;
+        const AdjTape& t = A.tb[0];
+        StepTape tp{};
+        tp.pp_new = A.pp_new;
+        tp.pp = t.pp + (size_t)sl * A.cap_pp; tp.pp_h = t.pp_h + (size_t)sl * A.cap_pp * kHV; tp.pp_cap = A.cap_pp;
+        tp.pw = t.pw + (size_t)sl * A.cap_pw; tp.pw_h = t.pw_h + (size_t)sl * A.cap_pw * kHV; tp.pw_cap = A.cap_pw;
+        tp.pw_count = t.pw_cnt + sl;
+        tp.overflow = A.overflow;
+        return tp;
+    }
+    // One recomputed force evaluation with its tape in step `sl` of buffer 0.
     void adj_tape_forces(int sl)
     {
         Adjoint& A = adj_;
-        check(cudaMemsetAsync(A.pw_cnt + sl, 0, sizeof(int), stream_), "adjoint tape");
-        StepTape tp{};
-        tp.pp_new = A.pp_new;
-        tp.pp = A.pp + (size_t)sl * A.cap_pp; tp.pp_h = A.pp_h + (size_t)sl * A.cap_pp * kHV; tp.pp_cap = A.cap_pp;
-        tp.pw = A.pw + (size_t)sl * A.cap_pw; tp.pw_h = A.pw_h + (size_t)sl * A.cap_pw * kHV; tp.pw_cap = A.cap_pw;
-        tp.pw_count = A.pw_cnt + sl;
-        tp.overflow = A.overflow;
-        ct64_.tape = tp;
+        check(cudaMemsetAsync(A.tb[0].pw_cnt + sl, 0, sizeof(int), stream_), "adjoint tape");
+        ct64_.tape = adj_tape_step(sl);
         const double dt_eff = step_index_ == 0 ? 0.0 : dt_;
         forces(dt_eff);
         ct64_.tape = StepTape{};
         ++step_index_;
-        check(cudaMemcpyAsync(A.pp_cnt + sl, K_.ct_total, sizeof(int), cudaMemcpyDeviceToDevice, stream_), "adjoint tape");
+        check(cudaMemcpyAsync(A.tb[0].pp_cnt + sl, K_.ct_total, sizeof(int), cudaMemcpyDeviceToDevice, stream_),
+              "adjoint tape");
     }
 
-    // The tape of a segment with the step as the device index A.slot.
-    StepTape adj_tape_slotted()
+    // The tape of buffer b with the step as its device index.
+    StepTape adj_tape_slotted(int b)
     {
         Adjoint& A = adj_;
+        const AdjTape& t = A.tb[b];
         StepTape tp{};
         tp.pp_new = A.pp_new;
-        tp.pp = A.pp; tp.pp_h = A.pp_h; tp.pp_cap = A.cap_pp;
-        tp.pw = A.pw; tp.pw_h = A.pw_h; tp.pw_cap = A.cap_pw;
-        tp.pw_count = A.pw_cnt; tp.pp_count = A.pp_cnt;
+        tp.pp = t.pp; tp.pp_h = t.pp_h; tp.pp_cap = A.cap_pp;
+        tp.pw = t.pw; tp.pw_h = t.pw_h; tp.pw_cap = A.cap_pw;
+        tp.pw_count = t.pw_cnt; tp.pp_count = t.pp_cnt;
         tp.overflow = A.overflow;
-        tp.slot = A.slot;
+        tp.slot = t.slot;
         return tp;
     }
-    // A recomputed, taped step (snapshot, advance, forces, finish, counts;
-    // A.slot moves on by one) and the reverse step (A.slot back by one, then
-    // the step's adjoint) as graphs: one launch per step each way.
+    // Per buffer: a recomputed, taped step (snapshot, advance, forces,
+    // finish, counts; the slot moves on by one) and the reverse step (the
+    // slot back by one, then the step's adjoint) as graphs.
     void adj_capture()
     {
         Adjoint& A = adj_;
-        if (A.g_fwd) return;
+        if (A.tb[0].g_fwd) return;
         auto cap = [&](cudaGraphExec_t& ex, auto&& body) {
             cudaGraph_t g = nullptr;
             check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -1510,23 +1531,26 @@ public:
             check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
             cudaGraphDestroy(g);
         };
-        const StepTape tp = adj_tape_slotted();
-        cap(A.g_fwd, [&] {
-            launch_adj_snapshot(O_, A.S, stream_, A.slot);
-            launch_advance(O_, dt_, stream_);
-            launch_adj_tape_begin(A.pw_cnt, A.slot, stream_);
-            ct64_.tape = tp;
-            forces(dt_);
-            ct64_.tape = StepTape{};
-            launch_finish(O_, dt_, stream_);
-            launch_adj_tape_end(A.pp_cnt, K_.ct_total, A.slot, stream_);
-        });
-        for (int p = 0; p < 2; ++p)
-            cap(A.g_rev[p], [&] {
-                launch_adj_slot_add(A.slot, -1, stream_);
-                launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, A.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T, A.lh_pp,
-                                A.lh_pw, dt_, dt_, 0, A.grads, sm_count_, stream_);
+        for (int b = 0; b < 2; ++b) {
+            AdjTape& t = A.tb[b];
+            const StepTape tp = adj_tape_slotted(b);
+            cap(t.g_fwd, [&] {
+                launch_adj_snapshot(O_, t.S, stream_, t.slot);
+                launch_advance(O_, dt_, stream_);
+                launch_adj_tape_begin(t.pw_cnt, t.slot, stream_);
+                ct64_.tape = tp;
+                forces(dt_);
+                ct64_.tape = StepTape{};
+                launch_finish(O_, dt_, stream_);
+                launch_adj_tape_end(t.pp_cnt, K_.ct_total, t.slot, stream_);
             });
+            for (int p = 0; p < 2; ++p)
+                cap(t.g_rev[p], [&] {
+                    launch_adj_slot_add(t.slot, -1, stream_);
+                    launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, t.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T,
+                                    A.lh_pp, A.lh_pw, dt_, dt_, 0, A.grads, sm_count_, stream_);
+                });
+        }
     }
 
     // dem_adjoint_backward: the adjoint of the final positions and velocities
@@ -1554,52 +1578,67 @@ public:
             check(cudaMemcpyAsync(A.L, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s), "adjoint");
             check(cudaStreamSynchronize(s), "adjoint");
         }
-        auto tape_of = [&](int sl) {
-            StepTape tp{};
-            tp.pp = A.pp + (size_t)sl * A.cap_pp; tp.pp_h = A.pp_h + (size_t)sl * A.cap_pp * kHV;
-            tp.pw = A.pw + (size_t)sl * A.cap_pw; tp.pw_h = A.pw_h + (size_t)sl * A.cap_pw * kHV;
-            return tp;
-        };
         std::vector<int> npp(A.K + 1), npw(A.K + 1);
         auto counts = [&](int k) {
             int of = 0;
-            check(cudaMemcpyAsync(npp.data(), A.pp_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
-            check(cudaMemcpyAsync(npw.data(), A.pw_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
+            check(cudaMemcpyAsync(npp.data(), A.tb[0].pp_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
+            check(cudaMemcpyAsync(npw.data(), A.tb[0].pw_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
             check(cudaMemcpyAsync(&of, A.overflow, sizeof(int), cudaMemcpyDeviceToHost, s), "adjoint counts");
             check(cudaStreamSynchronize(s), "adjoint counts");
             if (of) throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
             for (int j = 0; j < k; ++j) { npp[j] = std::min(npp[j], A.cap_pp); npw[j] = std::min(npw[j], A.cap_pw); }
         };
         adj_capture();
-        int par = A.L == A.Lb[0] ? 0 : 1;  // the buffer that holds the current adjoint
-        for (int seg = A.nseg - 1; seg >= 0; --seg) {
+        // Segment pipeline: the engine stream recomputes segment k - 1 into
+        // one tape while the reverse stream sweeps segment k on the other.
+        // The reverse kernels read only the tapes, the adjoint buffers and
+        // constant owner data (mass, radius, inertia, status), none of which
+        // a recompute writes.
+        cudaStream_t rs = branch_[1];  // a high-priority stream (graphs do not use it once captured)
+        auto recompute = [&](int seg, int b) {
+            AdjTape& t = A.tb[b];
             const int ks = std::min(A.K, A.steps - seg * A.K);
             adj_restore(A.ck[seg + 1]);
-            check(cudaMemsetAsync(A.slot, 0, sizeof(int), s), "adjoint slot");
+            check(cudaMemsetAsync(t.slot, 0, sizeof(int), s), "adjoint slot");
             for (int sl = 0; sl < ks; ++sl) {
-                check(cudaGraphLaunch(A.g_fwd, s), "adjoint recompute");
+                check(cudaGraphLaunch(t.g_fwd, s), "adjoint recompute");
                 ++step_index_;
             }
-            launch_adj_snapshot(O_, A.S, s, A.slot);  // the state after the segment, slot ks
-            int of = 0;
-            check(cudaMemcpyAsync(&of, A.overflow, sizeof(int), cudaMemcpyDeviceToHost, s), "adjoint overflow");
-            check(cudaStreamSynchronize(s), "adjoint recompute");
-            if (of) throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
+            launch_adj_snapshot(O_, t.S, s, t.slot);  // the state after the segment, slot ks
+            check(cudaEventRecord(adj_ev_[b], s), "adjoint event");
+        };
+        int par = A.L == A.Lb[0] ? 0 : 1;  // the buffer that holds the current adjoint
+        check(cudaEventRecord(adj_ev_[2], s), "adjoint event");
+        check(cudaStreamWaitEvent(rs, adj_ev_[2], 0), "adjoint wait");  // the reverse stream after the setup above
+        recompute(A.nseg - 1, 0);
+        bool rev_used[2] = {false, false};
+        for (int seg = A.nseg - 1, b = 0; seg >= 0; --seg, b ^= 1) {
+            if (seg > 0) {
+                // the other tape was last read by the reverse of segment seg + 1
+                if (rev_used[b ^ 1]) check(cudaStreamWaitEvent(s, adj_ev_[3 + (b ^ 1)], 0), "adjoint wait");
+                recompute(seg - 1, b ^ 1);
+            }
+            const int ks = std::min(A.K, A.steps - seg * A.K);
+            check(cudaStreamWaitEvent(rs, adj_ev_[b], 0), "adjoint wait");
             for (int sl = ks - 1; sl >= 0; --sl) {
-                check(cudaGraphLaunch(A.g_rev[par], s), "adjoint reverse step");
+                check(cudaGraphLaunch(A.tb[b].g_rev[par], rs), "adjoint reverse step");
                 par ^= 1;
             }
+            check(cudaEventRecord(adj_ev_[3 + b], rs), "adjoint event");
+            rev_used[b] = true;
         }
+        check(cudaEventRecord(adj_ev_[5], rs), "adjoint event");
+        check(cudaStreamWaitEvent(s, adj_ev_[5], 0), "adjoint wait");
         A.L = A.Lb[par];
         A.Lp = A.Lb[1 - par];
-        // the first evaluation (dt = 0) and the leapfrog start
+        // the first evaluation (dt = 0) and the leapfrog start, on tape 0
         adj_restore(A.ck[0]);
         adj_tape_forces(0);
         launch_leapfrog_init(O_, 0.5 * dt_, s);
-        launch_adj_snapshot(O_, A.S, s);
+        launch_adj_snapshot(O_, A.tb[0].S, s);
         counts(1);
-        launch_adj_step(C_, O_, d_sc_, W_, tape_of(0), npp[0], npw[0], A.S, A.S, A.L, A.Lp, A.P, A.T, A.lh_pp, A.lh_pw,
-                        0.5 * dt_, 0.0, 1, A.grads, sm_count_, s);
+        launch_adj_step(C_, O_, d_sc_, W_, adj_tape_step(0), npp[0], npw[0], A.tb[0].S, A.tb[0].S, A.L, A.Lp, A.P, A.T,
+                        A.lh_pp, A.lh_pw, 0.5 * dt_, 0.0, 1, A.grads, sm_count_, s);
         check(cudaGetLastError(), "adjoint backward");
         std::vector<double> h(kAdjFields * N);
         double g[2 * kAdjParams];
@@ -1650,6 +1689,7 @@ public:
     std::array<cudaStream_t, 3> branch_{};
     std::array<cudaEvent_t, 12> fork_ev_{};
     cudaEvent_t body_ready_ = nullptr;  // recorded after the body-result download
+    std::array<cudaEvent_t, 6> adj_ev_{};  // reverse-mode pipeline: tapes recomputed [2], setup, tapes swept [2], end
     std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;
     DeviceArena arena_, arena_tmp_, adj_arena_;
