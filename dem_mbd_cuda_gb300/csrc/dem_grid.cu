@@ -539,11 +539,37 @@ __device__ __forceinline__ void quat_derivative(double qw, double qx, double qy,
     dy = 0.5 * (qw * wy - qx * wz + qz * wx);
     dz = 0.5 * (qw * wz + qx * wy - qy * wx);
 }
+// q + quatDerivative(q, w) * h with the derivative's factor 0.5 moved onto
+// h: (0.5 s) h and s (0.5 h) are the same product, so the fused result has
+// the same bits, without the four multiplications by 0.5.
+__device__ __forceinline__ void quat_half_step(double& pw, double& px, double& py, double& pz, double wx, double wy,
+                                               double wz, double h)
+{
+    const double qw = pw, qx = px, qy = py, qz = pz, hh = 0.5 * h;
+    pw += (-qx * wx - qy * wy - qz * wz) * hh;
+    px += (qw * wx + qy * wz - qz * wy) * hh;
+    py += (qw * wy - qx * wz + qz * wx) * hh;
+    pz += (qw * wz + qx * wy - qy * wx) * hh;
+}
+// 1/sqrt(n2) away from |n2 - 1| < 2^-20, and the reference's degenerate case
+// (:170-174); out of line so its FP64 work is issued only by warps that need it.
+__device__ __noinline__ double inv_norm_general(double n2) { return n2 <= 1.0e-24 ? 0.0 : rsqrt(n2); }
+
+// A leapfrog quaternion stays within a few ulp of unit length, n2 = 1 + d
+// with tiny d, where 1/sqrt(1 + d) = 1 - d/2 + 3d^2/8 - ... : the quadratic
+// is exact to below 2^-60 for |d| < 2^-20 (the next term is 5|d|^3/16).  The
+// range test reads the exponent of d with integer operations.
 __device__ __forceinline__ void normalize_quat(double& qw, double& qx, double& qy, double& qz)
 {
     const double n2 = qw * qw + qx * qx + qy * qy + qz * qz;
-    if (n2 <= 1.0e-24) { qw = 1.0; qx = qy = qz = 0.0; return; }
-    const double inv = rsqrt(n2);
+    const double d = n2 - 1.0;
+    double inv;
+    if (((unsigned)__double2hiint(d) & 0x7fffffffu) < 0x3eb00000u) {  // |d| < 2^-20
+        inv = fma(d, fma(d, 0.375, -0.5), 1.0);
+    } else {
+        inv = inv_norm_general(n2);
+        if (inv == 0.0) { qw = 1.0; qx = qy = qz = 0.0; return; }
+    }
     qw *= inv; qx *= inv; qy *= inv; qz *= inv;
 }
 
@@ -558,9 +584,8 @@ __global__ void k_leapfrog_init(Owners d, double h)
     d.whx[i] = d.wx[i] + d.awx[i] * h;
     d.why[i] = d.wy[i] + d.awy[i] * h;
     d.whz[i] = d.wz[i] + d.awz[i] * h;
-    double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i], dw, dx, dy, dz;
-    quat_derivative(qw, qx, qy, qz, d.wx[i], d.wy[i], d.wz[i], dw, dx, dy, dz);
-    qw += dw * h; qx += dx * h; qy += dy * h; qz += dz * h;
+    double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
+    quat_half_step(qw, qx, qy, qz, d.wx[i], d.wy[i], d.wz[i], h);
     normalize_quat(qw, qx, qy, qz);
     quat_derivative(qw, qx, qy, qz, d.whx[i], d.why[i], d.whz[i], d.hqw[i], d.hqx[i], d.hqy[i], d.hqz[i]);
 }
@@ -597,9 +622,8 @@ __global__ void k_finish(Owners d, double dt)
     d.why[i] += d.awy[i] * dt;
     d.whz[i] += d.awz[i] * dt;
     const double h = 0.5 * dt;
-    double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i], dw, dx, dy, dz;
-    quat_derivative(qw, qx, qy, qz, d.wx[i], d.wy[i], d.wz[i], dw, dx, dy, dz);
-    qw += dw * h; qx += dx * h; qy += dy * h; qz += dz * h;
+    double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
+    quat_half_step(qw, qx, qy, qz, d.wx[i], d.wy[i], d.wz[i], h);
     normalize_quat(qw, qx, qy, qz);
     quat_derivative(qw, qx, qy, qz, d.whx[i], d.why[i], d.whz[i], d.hqw[i], d.hqx[i], d.hqy[i], d.hqz[i]);
 }
@@ -631,9 +655,8 @@ __device__ __forceinline__ void advance_rest_one(Owners d, int i, double dt)
     const double whx = d.whx[i], why = d.why[i], whz = d.whz[i];
     const double h = 0.5 * dt;
     double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
-    double pw = qw, px = qx, py = qy, pz = qz, dw, dx, dy, dz;
-    quat_derivative(pw, px, py, pz, d.wx[i], d.wy[i], d.wz[i], dw, dx, dy, dz);
-    pw += dw * h; px += dx * h; py += dy * h; pz += dz * h;
+    double pw = qw, px = qx, py = qy, pz = qz;
+    quat_half_step(pw, px, py, pz, d.wx[i], d.wy[i], d.wz[i], h);
     normalize_quat(pw, px, py, pz);
     double hqw, hqx, hqy, hqz;
     quat_derivative(pw, px, py, pz, whx, why, whz, hqw, hqx, hqy, hqz);
