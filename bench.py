@@ -159,10 +159,10 @@ def measured_traffic(kernel, n):
 def launches_per_step(scene):
     """Kernels one graph-launched step issues (the force DAG of
     dem_engine.cu enqueue_forces, steady-state step)."""
-    # counters x2, grid keys + layout + count + scan x3 + scatter + place,
+    # counters x2, grid keys + layout + count + scan + scatter + place,
     # geometry gather, sweep, particle law, owner sum, position advance;
     # rotational branch: rotational advance, velocity gather
-    k = 2 + 8 + 1 + 1 + 1 + 1 + 1 + 2
+    k = 2 + 6 + 1 + 1 + 1 + 1 + 1 + 2
     if scene.comp_owner is not None:
         k += 1                   # component update
     if scene.universal_gravity_enabled:
@@ -170,7 +170,7 @@ def launches_per_step(scene):
     if scene.n_walls:
         k += 2                   # wall probe + law
     if scene.n_bodies and scene.n_triangles:
-        k += 7 + 7 + 2           # triangle transform + grid, PT probe + scan + compaction + laws, body reduction
+        k += 5 + 3 + 2           # triangle transform + grid, PT items + the two law kernels, body reduction
     elif scene.n_bodies:
         k += 2
     return k
