@@ -594,8 +594,10 @@ public:
     // kHeadRest puts the previous step's rotational advance (the second part
     // of a split finish + advance) at the head, beside the particle grid;
     // kTailFinishPos ends with the first part.
+    // kHeadAdvance opens the first step of a run with the advance itself,
+    // split the same way (positions first, the rest on the branch).
     enum : unsigned {
-        kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kHeadRest = 8, kTailFinishPos = 16
+        kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kHeadRest = 8, kTailFinishPos = 16, kHeadAdvance = 32
     };
 
     template <typename T, typename TB>
@@ -616,8 +618,14 @@ public:
         };
         // the rotational advance on a branch only for spheres: with clumps the
         // component update reads the quaternions at once
-        const bool rest_branch = (tail & kHeadRest) && !timed && sphere_;
-        if ((tail & kHeadRest) && !rest_branch) launch_advance_rest(O_, dt_, sm_count_, s);
+        const bool head_rot = tail & (kHeadRest | kHeadAdvance);
+        const bool rest_branch = head_rot && !timed && sphere_;
+        auto rotational = [&](cudaStream_t on) {
+            if (tail & kHeadRest) launch_advance_rest(O_, dt_, sm_count_, on);
+            else launch_advance_rot(O_, dt_, sm_count_, on);
+        };
+        if (tail & kHeadAdvance) launch_advance_pos(O_, dt_, s);
+        if (head_rot && !rest_branch) rotational(s);
         auto download = [&](cudaStream_t on) {
             if (!(tail & kTailD2H) || nb_ <= 0) return;
             check(cudaMemcpyAsync(pin_body_result(), BO_.result, sizeof(double) * nb_ * kBodyFieldCount,
@@ -681,7 +689,7 @@ public:
         launch_step_counter(K_, 1, s);
         if (!sphere_) launch_update_components(C_, O_, s);
         link(s, br, 7);
-        if (rest_branch) launch_advance_rest(O_, dt_, sm_count_, br);
+        if (rest_branch) rotational(br);
         if (walls) {
             link(br, bw, 0);  // the wall law reads velocities
             contacts(1, bw);
@@ -971,10 +979,9 @@ public:
     {
         const bool mbd = nb_ > 0;
         ensure_graphs(mbd);
-        launch_advance(O_, dt_, stream_);
         for (int s = 0; s < steps; ++s) {
             const bool last = s == steps - 1;
-            cudaGraphExec_t g = graphs_[graph_index(mbd, s > 0, last)];
+            cudaGraphExec_t g = graphs_[graph_index(mbd, s > 0 ? 1 : 2, last)];
             if (mbd) {
                 body_position_update(dt_);
                 double* p = pin_body_state();
@@ -993,22 +1000,25 @@ public:
                 body_half_update(false, dt_);
             }
         }
-        check(cudaStreamSynchronize(stream_), "run steps");
+        // the callers synchronize (after their own downloads)
     }
 
-    static int graph_index(bool mbd, bool head_rest, bool last) { return (mbd ? 4 : 0) | (head_rest ? 2 : 0) | (last ? 1 : 0); }
+    // head: 1 the previous step's rotational advance, 2 this step's advance
+    static int graph_index(bool mbd, int head, bool last) { return (mbd ? 6 : 0) + head * 2 + (last ? 1 : 0); }
 
     // Captured force evaluation with dt, optionally with the body upload /
-    // load download around it and the previous step's rotational advance at
-    // its head, followed by finish (last) or finish + the position advance.
-    void capture(cudaGraphExec_t& ex, bool mbd, bool head_rest, bool last)
+    // load download around it and an advance at its head (head 1: the rest
+    // of the previous step's, 2: this step's own), followed by finish (last)
+    // or finish + the position advance.
+    void capture(cudaGraphExec_t& ex, bool mbd, int head, bool last)
     {
         if (ex) return;
         cudaGraph_t g = nullptr;
         check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
         try {
             if (mbd) enqueue_body_h2d();
-            forces(dt_, false, (mbd ? kTailTransform | kTailD2H : 0u) | (head_rest ? kHeadRest : 0u) |
+            forces(dt_, false, (mbd ? kTailTransform | kTailD2H : 0u) |
+                                   (head == 1 ? kHeadRest : head == 2 ? kHeadAdvance : 0u) |
                                    (last ? kTailFinish : kTailFinishPos));
         } catch (...) {
             cudaStreamEndCapture(stream_, &g);
@@ -1045,7 +1055,7 @@ public:
     }
     void ensure_graphs(bool mbd)
     {
-        for (int head = 0; head < 2; ++head)
+        for (int head = 1; head <= 2; ++head)
             for (int last = 0; last < 2; ++last)
                 capture(graphs_[graph_index(mbd, head, last)], mbd, head, last);
     }
@@ -1697,7 +1707,7 @@ public:
     std::vector<double> oin_host_;  // owner principal inertia [n][3] (host copy)
     void* pinned_ = nullptr;
     size_t pinned_bytes_ = 0;
-    std::array<cudaGraphExec_t, 8> graphs_{};  // by graph_index(bodies, rotational head, last step)
+    std::array<cudaGraphExec_t, 12> graphs_{};  // by graph_index(bodies, head, last step)
 
     Owners O_{};
     Comps C_{};

@@ -610,6 +610,34 @@ __global__ void k_advance(Owners d, double dt)
     d.wz[i] = d.whz[i] + d.awz[i] * (0.5 * dt);
 }
 
+// k_advance in two parts, for the first step of a graph-launched run: the
+// positions (all the particle grid needs), then the quaternions and the
+// full-step velocities beside the grid (grid-stride, two blocks per SM).
+__global__ void k_advance_pos(Owners d, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n || d.status[i] == -1) return;
+    d.px[i] += d.vhx[i] * dt;
+    d.py[i] += d.vhy[i] * dt;
+    d.pz[i] += d.vhz[i] * dt;
+}
+__global__ void __launch_bounds__(256) k_advance_rot(Owners d, double dt)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+        if (d.status[i] == -1) continue;
+        double qw = d.qw[i] + d.hqw[i] * dt, qx = d.qx[i] + d.hqx[i] * dt;
+        double qy = d.qy[i] + d.hqy[i] * dt, qz = d.qz[i] + d.hqz[i] * dt;
+        normalize_quat(qw, qx, qy, qz);
+        d.qw[i] = qw; d.qx[i] = qx; d.qy[i] = qy; d.qz[i] = qz;
+        d.vx[i] = d.vhx[i] + d.ax[i] * (0.5 * dt);
+        d.vy[i] = d.vhy[i] + d.ay[i] * (0.5 * dt);
+        d.vz[i] = d.vhz[i] + d.az[i] * (0.5 * dt);
+        d.wx[i] = d.whx[i] + d.awx[i] * (0.5 * dt);
+        d.wy[i] = d.why[i] + d.awy[i] * (0.5 * dt);
+        d.wz[i] = d.whz[i] + d.awz[i] * (0.5 * dt);
+    }
+}
+
 // advanceHalfVelocityKernel (:239-265)
 __global__ void k_finish(Owners d, double dt)
 {
@@ -787,6 +815,14 @@ void launch_leapfrog_init(const Owners& o, double h, cudaStream_t s)
 void launch_advance(const Owners& o, double dt, cudaStream_t s)
 {
     if (o.n > 0) k_advance<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_advance_pos(const Owners& o, double dt, cudaStream_t s)
+{
+    if (o.n > 0) k_advance_pos<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_advance_rot(const Owners& o, double dt, int sm_count, cudaStream_t s)
+{
+    if (o.n > 0) k_advance_rot<<<std::min(blocks(o.n, 256), 2 * sm_count), 256, 0, s>>>(o, dt);
 }
 void launch_finish(const Owners& o, double dt, cudaStream_t s)
 {

@@ -322,6 +322,9 @@ void launch_finish(const Owners& o, double dt, cudaStream_t s);
 // the next particle grid needs), then the rest of the advance.
 void launch_finish_advance_pos(const Owners& o, double dt, cudaStream_t s);
 void launch_advance_rest(const Owners& o, double dt, int sm_count, cudaStream_t s);
+// launch_advance in two parts: positions, then quaternions and velocities.
+void launch_advance_pos(const Owners& o, double dt, cudaStream_t s);
+void launch_advance_rot(const Owners& o, double dt, int sm_count, cudaStream_t s);
 // reset != 0: clear the per-step counters; 0: advance the contact step index.
 void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
 
