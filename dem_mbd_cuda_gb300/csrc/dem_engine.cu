@@ -122,6 +122,7 @@ public:
         for (auto* e : adj_ev_) if (e) cudaEventDestroy(e);
         arena_.release();
         if (pinned_) cudaFreeHost(pinned_);
+        if (diag_pin_) cudaFreeHost(diag_pin_);
         for (auto* b : branch_) if (b) cudaStreamDestroy(b);
         if (stream_) cudaStreamDestroy(stream_);
     }
@@ -400,8 +401,15 @@ public:
         G_.total_cells = arena_.alloc<int>(1, "total cells");
         G_.nvalid = arena_.alloc<int>(1, "nvalid");
         G_.scan = alloc_scan(cap + 1, 4096, "cell scan");
-        G_.err = arena_.alloc<unsigned>(1, "err");
-        check(cudaMemsetAsync(G_.err, 0, sizeof(unsigned), s), "clear err");
+        // Diagnostics block, one allocation so that one copy reads it back:
+        // 16 counters, the error word, then the interval sums the reference
+        // resets at every diagnostic read (regime counts, microstate sums,
+        // native steps).
+        diag_bytes_ = kDiagIntervalOff + sizeof(double) * ((size_t)nb_ * (kRegime + kMicro) + 1);
+        diag_dev_ = arena_.alloc<char>(diag_bytes_, "diagnostics");
+        check(cudaMemsetAsync(diag_dev_, 0, diag_bytes_, s), "clear diagnostics");
+        check(cudaMallocHost(&diag_pin_, diag_bytes_), "cudaMallocHost");
+        G_.err = reinterpret_cast<unsigned*>(diag_dev_ + 64);
 
         // ---- records
         R_.pos = arena_.alloc<D4>(nc_, "rec pos");
@@ -479,8 +487,7 @@ public:
         }
 
         // ---- counters
-        int* cnt = arena_.alloc<int>(16, "counters");
-        check(cudaMemsetAsync(cnt, 0, sizeof(int) * 16, s), "clear counters");
+        int* cnt = reinterpret_cast<int*>(diag_dev_);
         K_.pcontacts = cnt; K_.pover = cnt + 1; K_.bover = cnt + 2; K_.phigh = cnt + 3; K_.bhigh = cnt + 4;
         K_.tgover = cnt + 5; K_.ct_total = cnt + 6; K_.step = cnt + 8;
         K_.pt_ctotal = cnt + 9;
@@ -508,12 +515,9 @@ public:
             BO_.partial = arena_.alloc<double>((size_t)nb_ * BO_.groups * kBodyFieldCount, "body partial");
             BO_.result = arena_.alloc<double>((size_t)nb_ * kBodyFieldCount, "body result");
             check(cudaMemsetAsync(BO_.result, 0, sizeof(double) * nb_ * kBodyFieldCount, s), "clear");
-            BO_.reg_int = arena_.alloc<unsigned long long>((size_t)nb_ * kRegime, "regime interval");
-            BO_.micro_int = arena_.alloc<double>((size_t)nb_ * kMicro, "micro interval");
-            BO_.native_steps = arena_.alloc<unsigned long long>(1, "native steps");
-            check(cudaMemsetAsync(BO_.reg_int, 0, sizeof(unsigned long long) * nb_ * kRegime, s), "clear");
-            check(cudaMemsetAsync(BO_.micro_int, 0, sizeof(double) * nb_ * kMicro, s), "clear");
-            check(cudaMemsetAsync(BO_.native_steps, 0, sizeof(unsigned long long), s), "clear");
+            BO_.reg_int = reinterpret_cast<unsigned long long*>(diag_dev_ + kDiagIntervalOff);
+            BO_.micro_int = reinterpret_cast<double*>(BO_.reg_int + (size_t)nb_ * kRegime);
+            BO_.native_steps = reinterpret_cast<unsigned long long*>(BO_.micro_int + (size_t)nb_ * kMicro);
         }
         // pinned staging: body state (13 doubles/body) + body results
         pinned_bytes_ = sizeof(double) * ((size_t)13 * std::max(nb_, 1) + (size_t)kBodyFieldCount * std::max(nb_, 1) + 64);
@@ -597,7 +601,8 @@ public:
     // kHeadAdvance opens the first step of a run with the advance itself,
     // split the same way (positions first, the rest on the branch).
     enum : unsigned {
-        kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kHeadRest = 8, kTailFinishPos = 16, kHeadAdvance = 32
+        kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kHeadRest = 8, kTailFinishPos = 16, kHeadAdvance = 32,
+        kTailDiag = 64
     };
 
     template <typename T, typename TB>
@@ -663,6 +668,7 @@ public:
             n_marks_ = e;
             download(s);
             integrate(s);
+            if (tail & kTailDiag) enqueue_diag_download(s);
             return;
         }
         // Branches (a DAG when captured into the step graph):
@@ -729,6 +735,7 @@ public:
         integrate(s);
         if (pt) link(bt, s, 5);
         launch_step_counter(K_, 0, s);
+        if (tail & kTailDiag) enqueue_diag_download(s);
     }
 
     void forces(double dt_eff, bool timed = false, unsigned tail = 0)
@@ -794,28 +801,26 @@ public:
         return DEM_OK;
     }
 
-    int collect_diagnostics(double* body_forces)
+    // Copy the diagnostics block to its pinned mirror and reset the interval
+    // sums (the reference's read-and-reset, src/cuda_backend_cuda.cu:500-508).
+    void enqueue_diag_download(cudaStream_t s)
+    {
+        check(cudaMemcpyAsync(diag_pin_, diag_dev_, diag_bytes_, cudaMemcpyDeviceToHost, s), "download diagnostics");
+        if (nb_ > 0)
+            check(cudaMemsetAsync(diag_dev_ + kDiagIntervalOff, 0, diag_bytes_ - kDiagIntervalOff, s), "reset intervals");
+    }
+
+    // downloaded: the stream already holds the download (a run's last graph).
+    int collect_diagnostics(double* body_forces, bool downloaded = false)
     {
         cudaStream_t s = stream_;
-        int cnt[16];
-        unsigned err = 0;
-        check(cudaMemcpyAsync(cnt, K_.pcontacts, sizeof(int) * 16, cudaMemcpyDeviceToHost, s), "download counters");
-        check(cudaMemcpyAsync(&err, G_.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "download err");
-        std::vector<unsigned long long> rint(kRegime * std::max(nb_, 1));
-        std::vector<double> mint(kMicro * std::max(nb_, 1));
-        unsigned long long native = 0;
-        if (nb_ > 0) {
-            check(cudaMemcpyAsync(rint.data(), BO_.reg_int, sizeof(unsigned long long) * nb_ * kRegime,
-                                  cudaMemcpyDeviceToHost, s), "download regime interval");
-            check(cudaMemcpyAsync(mint.data(), BO_.micro_int, sizeof(double) * nb_ * kMicro, cudaMemcpyDeviceToHost, s),
-                  "download micro interval");
-            check(cudaMemcpyAsync(&native, BO_.native_steps, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
-                  "download native steps");
-            check(cudaMemsetAsync(BO_.reg_int, 0, sizeof(unsigned long long) * nb_ * kRegime, s), "reset regime interval");
-            check(cudaMemsetAsync(BO_.micro_int, 0, sizeof(double) * nb_ * kMicro, s), "reset micro interval");
-            check(cudaMemsetAsync(BO_.native_steps, 0, sizeof(unsigned long long), s), "reset native steps");
-        }
+        if (!downloaded) enqueue_diag_download(s);
         check(cudaStreamSynchronize(s), "collect diagnostics");
+        const int* cnt = reinterpret_cast<const int*>(diag_pin_);
+        const unsigned err = *reinterpret_cast<const unsigned*>(diag_pin_ + 64);
+        const unsigned long long* rint = reinterpret_cast<const unsigned long long*>(diag_pin_ + kDiagIntervalOff);
+        const double* mint = reinterpret_cast<const double*>(rint + (size_t)nb_ * kRegime);
+        const unsigned long long native = nb_ > 0 ? *reinterpret_cast<const unsigned long long*>(mint + (size_t)nb_ * kMicro) : 0ull;
         dem_step_stats st{};
         st.particle_contacts = cnt[0];
         st.particle_history_overflows = cnt[1];
@@ -828,9 +833,9 @@ public:
         st.body_candidate_items = cnt[9];
         st.wall_candidates = cnt[10];
         reg_inst_.assign((size_t)kRegime * nb_, 0ull);
-        reg_int_.assign(rint.begin(), rint.begin() + (size_t)kRegime * nb_);
+        reg_int_.assign(rint, rint + (size_t)kRegime * nb_);
         micro_inst_.assign((size_t)kMicro * nb_, 0.0);
-        micro_int_.assign(mint.begin(), mint.begin() + (size_t)kMicro * nb_);
+        micro_int_.assign(mint, mint + (size_t)kMicro * nb_);
         if (nb_ > 0) {
             const double* r = pin_body_result();
             double fz = 0.0, md = 0.0;
@@ -966,7 +971,7 @@ public:
         }
         if (steps <= 0) return;
         step_loop(steps);
-        collect_diagnostics(nullptr);
+        collect_diagnostics(nullptr, true);
     }
 
     // `steps` reference steps after the start: advance, then for every step
@@ -1019,7 +1024,7 @@ public:
             if (mbd) enqueue_body_h2d();
             forces(dt_, false, (mbd ? kTailTransform | kTailD2H : 0u) |
                                    (head == 1 ? kHeadRest : head == 2 ? kHeadAdvance : 0u) |
-                                   (last ? kTailFinish : kTailFinishPos));
+                                   (last ? kTailFinish | kTailDiag : kTailFinishPos));
         } catch (...) {
             cudaStreamEndCapture(stream_, &g);
             if (g) cudaGraphDestroy(g);
@@ -1077,6 +1082,7 @@ public:
         float ms = 0;
         check(cudaEventElapsedTime(&ms, a, b), "elapsed");
         cudaEventDestroy(a); cudaEventDestroy(b);
+        collect_diagnostics(nullptr, true);  // the last graph downloaded them
         return ms;
     }
 
@@ -1706,6 +1712,10 @@ public:
     Adjoint adj_;
     std::vector<double> oin_host_;  // owner principal inertia [n][3] (host copy)
     void* pinned_ = nullptr;
+    static constexpr size_t kDiagIntervalOff = 72;  // counters [16] int, error word, then the interval sums
+    char* diag_dev_ = nullptr;
+    char* diag_pin_ = nullptr;
+    size_t diag_bytes_ = 0;
     size_t pinned_bytes_ = 0;
     std::array<cudaGraphExec_t, 12> graphs_{};  // by graph_index(bodies, head, last step)
 
