@@ -431,7 +431,6 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     const int step = *k.step;
     const int nvalid = *g.nvalid;
     int pover = 0, phigh = 0, found = 0;
-    __shared__ int s_base;
     // grid-stride over blocks of sorted positions: the launch may use fewer
     // blocks than positions so that the kernels beside it find free slots
     for (int t0 = blockIdx.x * blockDim.x; t0 < nvalid; t0 += gridDim.x * blockDim.x) {
@@ -532,17 +531,24 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         hp.hw[ci] = phw;
         ct.cnt[ci] = count;
     }
-    int total;
-    const int ex = block_exclusive_scan_c(count, total);
-    if (threadIdx.x == 0) s_base = total ? atomicAdd(k.ct_total, total) : 0;
-    __syncthreads();
-    const int base = s_base + ex;
+    // the warp's contacts take one range of the flat list (no block barrier:
+    // a warp that finishes its candidates early goes on to its next pass)
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int incl = count;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int wtotal = __shfl_sync(FULL, incl, 31);
+    int wbase = 0;
+    if (lane == 31 && wtotal) wbase = atomicAdd(k.ct_total, wtotal);
+    const int base = __shfl_sync(FULL, wbase, 31) + incl - count;
     for (int q = 0; q < count; ++q) {
         ct.ent[base + q] = make_int4(t, stage_t[q], ci * kPSlots + (stage_s[q] & 0xff), q * nc + ci);
         if (ct.tape.pp_new) ct.tape.pp_new[base + q] = (unsigned char)(stage_s[q] >> 8);
     }
     found += count;
-    __syncthreads();  // s_base is reused by the next pass
     }
     block_add(k.pcontacts, found);
     block_add(k.pover, pover);
