@@ -62,3 +62,21 @@ def test_autotune_returns_an_accepted_setting():
         e.set_pt_warp_items(out["pt_warp_items"])
     e.run(3)
     assert e.stepStats()["particle_contacts"] > 0
+
+
+def test_candidate_counts_bound_the_contacts():
+    """The engine-only step stats: the particle-triangle items the FP32
+    probe kept cover every particle with a body contact, and the wall
+    candidates every particle with a wall contact (FP32 tests reject only
+    pairs that are certainly apart)."""
+    sc = G.small_mbd()
+    e = engine_for(sc, precision="mixed")
+    e.run(5)
+    st = e.stepStats()
+    _, l_body, _ = e.history(2)
+    _, l_wall, _ = e.history(1)
+    step = max(int(l_body.max()), int(l_wall.max()))  # the last evaluation
+    with_body = int((l_body == step).any(axis=1).sum())
+    with_wall = int((l_wall == step).any(axis=1).sum())
+    assert st["body_candidate_items"] >= with_body > 0
+    assert st["wall_candidates"] >= with_wall
