@@ -1,11 +1,13 @@
 """Speed settings change no result: the blocks per SM of the sweep, the
 gathers and the particle law (grid-stride) leave the trajectory, the bodies
-and the contact histories bit-identical;
+and the contact histories bit-identical, also where a component holds more
+than a warp's width of contacts;
 the autotuner returns a setting the engine accepts."""
 import numpy as np
 import pytest
 
-from gpu_helpers import engine_for
+from gpu_helpers import compare_evaluation, engine_for
+from oracle.oracle import Oracle
 from dem_mbd_cuda_gb300 import generate as G
 
 pytestmark = pytest.mark.gpu
@@ -27,8 +29,12 @@ def test_sweep_blocks_do_not_change_results(precision, maker):
         e.run(15)
         runs.append(e)
     ref = runs[0]
+    _assert_same_runs(sc, ref, runs[1:])
+
+
+def _assert_same_runs(sc, ref, others):
     st0 = ref.downloadParticleState()
-    for e in runs[1:]:
+    for e in others:
         st = e.downloadParticleState()
         for k in ("pos", "vel", "omega", "quat"):
             np.testing.assert_array_equal(st[k], st0[k], err_msg=k)
@@ -40,6 +46,54 @@ def test_sweep_blocks_do_not_change_results(precision, maker):
             np.testing.assert_array_equal(v1, v2)
         if sc.n_bodies:
             np.testing.assert_array_equal(e.bodies()["loads"], ref.bodies()["loads"])
+
+
+def crowded(counts=(60, 40, 20), big=8e-3, small=1e-3, overlap=2e-6):
+    """Large spheres each covered by small ones that all touch it: a large
+    component holds more than 32 contacts, and more than the 64 history
+    slots where its count is above 64 (the reference's capacity error).
+    The small spheres stand more than 3 mm apart, clear of one another."""
+    pos, rad = [], []
+    for k, m in enumerate(counts):
+        c = np.array([0.03 * k - 0.03, 0.0, 0.02])
+        pos.append(c)
+        rad.append(big)
+        i = np.arange(m) + 0.5
+        th = np.arccos(1 - 2 * i / m)
+        ph = np.pi * (1 + 5 ** 0.5) * i
+        d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=1)
+        pos.extend(c + (big + small - overlap) * d)
+        rad.extend([small] * m)
+    pos, rad = np.array(pos), np.array(rad)
+    kw = G.make_spheres(pos, rad, G.DENSITY)
+    wo, wn = G.box_walls(np.array([-0.06, -0.03, 0.0]), np.array([0.06, 0.03, 0.06]))
+    m = G.mech(kN=1e5, epsN=0.5, epsS=0.6, mu=0.4, muT=0.1, muR=0.05, beta=0.5)
+    return G.Scene(**kw, pp=m, pt=m, pw=m, dt=1e-6, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
+                   wall_normal=wn, name="crowded")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_crowded_components(precision):
+    """Up to 60 contacts on one component: every sweep grid agrees bit for
+    bit, and (FP64) with the oracle; 80 contacts on one component is the
+    capacity error, as in the oracle."""
+    sc = crowded()
+    runs = [engine_for(sc, precision=precision).set_sweep_blocks(b) for b in (0, 1)]
+    for e in runs:
+        e.run(4)
+    st = runs[0].stepStats()
+    assert st["particle_history_overflows"] == 0 and st["particle_history_high_water"] == 60
+    _assert_same_runs(sc, runs[0], runs[1:])
+    if precision == "fp64":
+        o = Oracle(sc)
+        o.run(4)
+        for e in runs:
+            compare_evaluation(e, o, 4)
+    over = crowded(counts=(80,))
+    with pytest.raises(RuntimeError, match="capacity"):
+        Oracle(over).run(1)
+    with pytest.raises(Exception, match="capacity"):
+        engine_for(over, precision=precision).run(1)
 
 
 def test_autotune_returns_an_accepted_setting():
