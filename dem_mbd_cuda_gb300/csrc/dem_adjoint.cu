@@ -201,20 +201,81 @@ __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const 
     st3(T, kTEMW, n, i, z3());
 }
 
+// Material gradients of one block, by scene: a few shared rows tagged with
+// their scene.  A thread adds its running sums to its scene's row when its
+// scene changes and at the end; a scene that finds no row free goes straight
+// to global memory.  `grads` is scene-major, [scene][2][kAdjParams], and
+// `chan` selects the particle (0) or wall (1) parameters.
+constexpr int kGradRows = 4;
+struct GradRows {
+    int tag[kGradRows];
+    double g[kGradRows][kAdjParams];
+};
+__device__ void grad_rows_init(GradRows& r)
+{
+    if (threadIdx.x < kGradRows) r.tag[threadIdx.x] = -1;
+    if (threadIdx.x < kGradRows * kAdjParams) (&r.g[0][0])[threadIdx.x] = 0.0;
+    __syncthreads();
+}
+__device__ void grad_add(GradRows& r, int s, const MatGrad& g, double* grads, int chan)
+{
+    const double gv[kAdjParams] = {g.kN, g.mu, g.logN, g.logS, g.muT, g.muR};
+    int row = -1;
+    for (int j = 0; j < kGradRows && row < 0; ++j) {
+        const int t = atomicCAS(&r.tag[j], -1, s);  // claims a free row, or reads its scene
+        if (t == -1 || t == s) row = j;
+    }
+    for (int f = 0; f < kAdjParams; ++f) {
+        if (row >= 0) atomicAdd(&r.g[row][f], gv[f]);
+        else atomicAdd(grads + ((size_t)s * 2 + chan) * kAdjParams + f, gv[f]);
+    }
+}
+__device__ void grad_rows_flush(GradRows& r, double* grads, int chan)
+{
+    __syncthreads();
+    if (threadIdx.x < kGradRows * kAdjParams) {
+        const int j = threadIdx.x / kAdjParams, f = threadIdx.x % kAdjParams;
+        if (r.tag[j] >= 0) atomicAdd(grads + ((size_t)r.tag[j] * 2 + chan) * kAdjParams + f, r.g[j][f]);
+    }
+}
+
+// The entries [k, end) of a block, visited with stride `step`.  One scene:
+// grid-stride over all entries.  A batch: a contiguous share of the entries
+// per block, so that a thread's scene changes rarely (the entries of one
+// warp's components sit together in the tape).
+struct EntryRange {
+    int k, end, step;
+};
+__device__ EntryRange entry_range(int count, int block, int blocks, int nscenes)
+{
+    if (nscenes == 1) return {block * (int)blockDim.x + (int)threadIdx.x, count, blocks * (int)blockDim.x};
+    const int per = (count + blocks - 1) / blocks;
+    const int k0 = block * per;
+    return {k0 + (int)threadIdx.x, min(count, k0 + per), (int)blockDim.x};
+}
+
 // Particle contact sides of one step (tape entries), reverse.
 __device__ void adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTape tp, int count, const double* P,
-                       double* T, double* lhist, double dt_eff, double* grads, int block, int blocks, double* sg)
+                       double* T, double* lhist, double dt_eff, double* grads, int block, int blocks, int nscenes,
+                       GradRows& rows)
 {
     const int n = o.n;
     tp = tape_at(tp);
     if (count < 0) count = min(*tp.pp_count, tp.pp_cap);
-    if (threadIdx.x < kAdjParams) sg[threadIdx.x] = 0.0;
-    __syncthreads();
+    grad_rows_init(rows);
     MatGrad gsum = {0, 0, 0, 0, 0, 0};
-    const MatC& m = sc[0].pp;   // one scene (checked by the engine)
-    for (int k = block * blockDim.x + threadIdx.x; k < count; k += blocks * blockDim.x) {
+    int cur = -1;  // the scene gsum belongs to
+    const EntryRange er = entry_range(count, block, blocks, nscenes);
+    for (int k = er.k; k < er.end; k += er.step) {
         const int4 e = tp.pp[k];
         const int i = e.x, j = e.y;
+        const int si = nscenes == 1 ? 0 : o.scene[i];
+        if (si != cur) {
+            if (cur >= 0) grad_add(rows, cur, gsum, grads, 0);
+            gsum = MatGrad{0, 0, 0, 0, 0, 0};
+            cur = si;
+        }
+        const MatC& m = sc[si].pp;
         D3 xi = ld3(P, kPX, n, i), xj = ld3(P, kPX, n, j);
         const D3 vi = ld3(P, kPV, n, i), vj = ld3(P, kPV, n, j);
         const D3 mvi = ld3(P, kPMV, n, i), mvj = ld3(P, kPMV, n, j);
@@ -245,10 +306,8 @@ __device__ void adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTap
         add3(T, kTEMW, n, i, ad.mwi);
         add3(T, kTEMW, n, j, ad.mwj);
     }
-    const double gv[kAdjParams] = {gsum.kN, gsum.mu, gsum.logN, gsum.logS, gsum.muT, gsum.muR};
-    for (int f = 0; f < kAdjParams; ++f) atomicAdd(sg + f, gv[f]);
-    __syncthreads();
-    if (threadIdx.x < kAdjParams) atomicAdd(grads + threadIdx.x, sg[threadIdx.x]);
+    if (cur >= 0) grad_add(rows, cur, gsum, grads, 0);
+    grad_rows_flush(rows, grads, 0);
 }
 
 __device__ void pw_one(const Comps& c, const Owners& o, const SceneC& S, const Walls& walls, const StepTape& tp, int k,
@@ -281,22 +340,27 @@ __device__ void pw_one(const Comps& c, const Owners& o, const SceneC& S, const W
 // Wall contacts of one step (tape entries), reverse.
 __device__ void adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls, StepTape tp, int count,
                        const double* P, double* T, double* lhist, double dt_eff, double* grads, int block, int blocks,
-                       double* sg)
+                       int nscenes, GradRows& rows)
 {
     tp = tape_at(tp);
     if (count < 0) count = min(*tp.pw_count, tp.pw_cap);
-    if (threadIdx.x < kAdjParams) sg[threadIdx.x] = 0.0;
-    __syncthreads();
+    grad_rows_init(rows);
     MatGrad g = {0, 0, 0, 0, 0, 0};
-    for (int k = block * blockDim.x + threadIdx.x; k < count; k += blocks * blockDim.x) {
+    int cur = -1;
+    const EntryRange er = entry_range(count, block, blocks, nscenes);
+    for (int k = er.k; k < er.end; k += er.step) {
+        const int si = nscenes == 1 ? 0 : o.scene[tp.pw[k].x];
+        if (si != cur) {
+            if (cur >= 0) grad_add(rows, cur, g, grads, 1);
+            g = MatGrad{0, 0, 0, 0, 0, 0};
+            cur = si;
+        }
         MatGrad gk = {0, 0, 0, 0, 0, 0};
-        pw_one(c, o, sc[0], walls, tp, k, P, T, lhist, dt_eff, gk);
+        pw_one(c, o, sc[si], walls, tp, k, P, T, lhist, dt_eff, gk);
         g.kN += gk.kN; g.mu += gk.mu; g.logN += gk.logN; g.logS += gk.logS; g.muT += gk.muT; g.muR += gk.muR;
     }
-    const double gv[kAdjParams] = {g.kN, g.mu, g.logN, g.logS, g.muT, g.muR};
-    for (int f = 0; f < kAdjParams; ++f) atomicAdd(sg + f, gv[f]);
-    __syncthreads();
-    if (threadIdx.x < kAdjParams) atomicAdd(grads + kAdjParams + threadIdx.x, sg[threadIdx.x]);
+    if (cur >= 0) grad_add(rows, cur, g, grads, 1);
+    grad_rows_flush(rows, grads, 1);
 }
 
 // Particle and wall contacts of one step in one launch: blocks [0, bpp) take
@@ -306,13 +370,14 @@ __device__ void adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls w
 // sets cost their longer chain instead of the sum of both.
 __global__ void __launch_bounds__(128) k_adj_contacts(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
                                                       StepTape tp, int npp, int npw, int bpp, const double* P, double* T,
-                                                      double* lh_pp, double* lh_pw, double dt_eff, double* grads)
+                                                      double* lh_pp, double* lh_pw, double dt_eff, double* grads,
+                                                      int nscenes)
 {
-    __shared__ double sg[kAdjParams];
+    __shared__ GradRows rows;
     if ((int)blockIdx.x < bpp)
-        adj_pp(c, o, sc, tp, npp, P, T, lh_pp, dt_eff, grads, blockIdx.x, bpp, sg);
+        adj_pp(c, o, sc, tp, npp, P, T, lh_pp, dt_eff, grads, blockIdx.x, bpp, nscenes, rows);
     else
-        adj_pw(c, o, sc, walls, tp, npw, P, T, lh_pw, dt_eff, grads, blockIdx.x - bpp, gridDim.x - bpp, sg);
+        adj_pw(c, o, sc, walls, tp, npw, P, T, lh_pw, dt_eff, grads, blockIdx.x - bpp, gridDim.x - bpp, nscenes, rows);
 }
 
 
@@ -389,8 +454,8 @@ void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s)
 }
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
                      int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
-                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int sm_count,
-                     cudaStream_t s)
+                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int nscenes,
+                     int sm_count, cudaStream_t s)
 {
     if (o.n <= 0) return;
     // device counts: S, S1 at the tape's slot, fixed grid-stride grids
@@ -399,7 +464,8 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
     const int bpp = npp < 0 ? sm_count * 8 : min(nblocks(npp, 128), sm_count * 8);
     const int bpw = npw < 0 ? sm_count * 2 : min(nblocks(npw, 128), sm_count * 2);
     if (bpp + bpw > 0)
-        k_adj_contacts<<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff, grads);
+        k_adj_contacts<<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff, grads,
+                                                 nscenes);
     k_adj_advance<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, P, T, Lp, dt, init, slot);
 }
 

@@ -1391,7 +1391,6 @@ public:
             throw DemError(DEM_ERR_INVALID, "the adjoint runs on the FP64 form (precision DEM_PRECISION_FP64)");
         if (nb_ > 0) throw DemError(DEM_ERR_INVALID, "the adjoint does not cover rigid bodies");
         if (!sphere_) throw DemError(DEM_ERR_INVALID, "the adjoint covers spheres (one component per owner)");
-        if (S_ != 1) throw DemError(DEM_ERR_INVALID, "the adjoint covers one scene per engine");
         for (int i = 0; i < n_; ++i)
             if (!(oin_host_[3 * (size_t)i] == oin_host_[3 * (size_t)i + 1] &&
                   oin_host_[3 * (size_t)i + 1] == oin_host_[3 * (size_t)i + 2]))
@@ -1470,7 +1469,7 @@ public:
         A.T = adj_arena_.alloc<double>((size_t)kTFields * n_, "adjoint state");
         A.lh_pp = adj_arena_.alloc<double>((size_t)nc_ * kPSlots * kHV, "adjoint history");
         A.lh_pw = adj_arena_.alloc<double>((size_t)nc_ * kWSlots * kHV, "adjoint history");
-        A.grads = adj_arena_.alloc<double>(2 * kAdjParams, "adjoint parameters");
+        A.grads = adj_arena_.alloc<double>((size_t)S_ * 2 * kAdjParams, "adjoint parameters");
         A.Lb[0] = A.L; A.Lb[1] = A.Lp;
         adj_save(A.ck[0]);
         run_steps(0);
@@ -1564,7 +1563,7 @@ public:
                 cap(t.g_rev[p], [&] {
                     launch_adj_slot_add(t.slot, -1, stream_);
                     launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, t.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T,
-                                    A.lh_pp, A.lh_pw, dt_, dt_, 0, A.grads, sm_count_, stream_);
+                                    A.lh_pp, A.lh_pw, dt_, dt_, 0, A.grads, S_, sm_count_, stream_);
                 });
         }
     }
@@ -1582,7 +1581,7 @@ public:
         check(cudaMemsetAsync(A.L, 0, sizeof(double) * kAdjFields * N, s), "adjoint");
         check(cudaMemsetAsync(A.lh_pp, 0, sizeof(double) * (size_t)nc_ * kPSlots * kHV, s), "adjoint");
         check(cudaMemsetAsync(A.lh_pw, 0, sizeof(double) * (size_t)nc_ * kWSlots * kHV, s), "adjoint");
-        check(cudaMemsetAsync(A.grads, 0, sizeof(double) * 2 * kAdjParams, s), "adjoint");
+        check(cudaMemsetAsync(A.grads, 0, sizeof(double) * S_ * 2 * kAdjParams, s), "adjoint");
         check(cudaMemsetAsync(A.overflow, 0, sizeof(int), s), "adjoint");
         {
             std::vector<double> h(kAdjFields * N, 0.0);
@@ -1654,12 +1653,11 @@ public:
         launch_adj_snapshot(O_, A.tb[0].S, s);
         counts(1);
         launch_adj_step(C_, O_, d_sc_, W_, adj_tape_step(0), npp[0], npw[0], A.tb[0].S, A.tb[0].S, A.L, A.Lp, A.P, A.T,
-                        A.lh_pp, A.lh_pw, 0.5 * dt_, 0.0, 1, A.grads, sm_count_, s);
+                        A.lh_pp, A.lh_pw, 0.5 * dt_, 0.0, 1, A.grads, S_, sm_count_, s);
         check(cudaGetLastError(), "adjoint backward");
-        std::vector<double> h(kAdjFields * N);
-        double g[2 * kAdjParams];
+        std::vector<double> h(kAdjFields * N), g((size_t)S_ * 2 * kAdjParams);
         check(cudaMemcpyAsync(h.data(), A.Lp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s), "adjoint");
-        check(cudaMemcpyAsync(g, A.grads, sizeof g, cudaMemcpyDeviceToHost, s), "adjoint");
+        check(cudaMemcpyAsync(g.data(), A.grads, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s), "adjoint");
         check(cudaStreamSynchronize(s), "adjoint");
         for (size_t i = 0; i < N; ++i)
             for (int a = 0; a < 3; ++a) {
@@ -1667,18 +1665,19 @@ public:
                 if (dl_dvel0) dl_dvel0[3 * i + a] = h[(kAdjV + a) * N + i];
                 if (dl_domega0) dl_domega0[3 * i + a] = h[(kAdjW + a) * N + i];
             }
-        if (dl_dparams) {
-            const MatC* mats[2] = {&scenes_h_[0].pp, &scenes_h_[0].pw};
-            for (int c = 0; c < 2; ++c) {
-                const double* gc = g + c * kAdjParams;
-                double* o = dl_dparams + c * kAdjParams;
-                // kN, mu, epsN (log epsN = logN), epsS, muT, muR
-                o[0] = gc[0]; o[1] = gc[1];
-                o[2] = gc[2] / std::exp(mats[c]->logN);
-                o[3] = gc[3] / std::exp(mats[c]->logS);
-                o[4] = gc[4]; o[5] = gc[5];
+        if (dl_dparams)
+            for (int sc = 0; sc < S_; ++sc) {
+                const MatC* mats[2] = {&scenes_h_[sc].pp, &scenes_h_[sc].pw};
+                for (int c = 0; c < 2; ++c) {
+                    const double* gc = g.data() + ((size_t)sc * 2 + c) * kAdjParams;
+                    double* o = dl_dparams + ((size_t)sc * 2 + c) * kAdjParams;
+                    // kN, mu, epsN (log epsN = logN), epsS, muT, muR
+                    o[0] = gc[0]; o[1] = gc[1];
+                    o[2] = gc[2] / std::exp(mats[c]->logN);
+                    o[3] = gc[3] / std::exp(mats[c]->logS);
+                    o[4] = gc[4]; o[5] = gc[5];
+                }
             }
-        }
         // leave the engine at the end of the forward run
         adj_restore(A.ck[A.nseg + 1]);
         check(cudaStreamSynchronize(s), "adjoint backward");

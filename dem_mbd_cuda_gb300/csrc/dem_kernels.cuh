@@ -333,11 +333,12 @@ void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s, const int* 
 void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s);
 // One reverse step.  npp / npw < 0: the counts are the tape's own
 // (pp_count / pw_count at the device slot) and S, S1 are taken at *tp.slot
-// and *tp.slot + 1 of the snapshot array S.
+// and *tp.slot + 1 of the snapshot array S.  `grads` holds
+// [nscenes][2][kAdjParams] material gradients (particle, then wall).
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
                      int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
-                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int sm_count,
-                     cudaStream_t s);
+                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int nscenes,
+                     int sm_count, cudaStream_t s);
 // Device step index of a taped segment: add `delta`.
 void launch_adj_slot_add(int* slot, int delta, cudaStream_t s);
 // Before a taped step: zero its wall entry count.  After it: record its

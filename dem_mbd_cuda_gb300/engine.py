@@ -103,6 +103,7 @@ class CudaDemSolver:
         self.h = h
         self._keep = []
         self.n = self.nc = self.nb = self.nt = self.nw = 0
+        self.scenes = 1
 
     def _check(self, rc):
         if rc != 0:
@@ -131,7 +132,9 @@ class CudaDemSolver:
                 self._keep.append(keep)
             self._keep.append(cs)
             self._check(self.lib.dem_initialize_batch(self.h, C.cast(cs, C.c_void_p), len(scene), C.byref(o)))
+            self.scenes = len(scene)
         else:
+            self.scenes = 1
             c, keep = scene.to_c()
             self._keep += [c, keep]
             self._check(self.lib.dem_initialize(self.h, C.byref(c), C.byref(o)))
@@ -274,17 +277,19 @@ class CudaDemSolver:
         """Gradient of a scalar loss given its adjoint w.r.t. the final
         positions / velocities ([n, 3]).  Returns a dict with dl_dpos0,
         dl_dvel0, dl_domega0 ([n, 3]) and dl_dparams ({"pp": ..., "pw": ...}
-        each {kN, mu, epsN, epsS, muT, muR})."""
+        each {kN, mu, epsN, epsS, muT, muR}; for a batch, a list of those,
+        one per scene)."""
         n = self.n
         a = None if dl_dpos is None else np.ascontiguousarray(dl_dpos, dtype=np.float64).reshape(n, 3)
         b = None if dl_dvel is None else np.ascontiguousarray(dl_dvel, dtype=np.float64).reshape(n, 3)
         x0, v0, w0 = (np.zeros((n, 3)) for _ in range(3))
-        p = np.zeros(12)
+        p = np.zeros(12 * self.scenes)
         self._check(self.lib.dem_adjoint_backward(self.h, _p(a) if a is not None else None,
                                                   _p(b) if b is not None else None, _p(x0), _p(v0), _p(w0), _p(p)))
         keys = ("kN", "mu", "epsN", "epsS", "muT", "muR")
+        per = [{"pp": dict(zip(keys, q[:6])), "pw": dict(zip(keys, q[6:]))} for q in p.reshape(self.scenes, 12)]
         return {"dl_dpos0": x0, "dl_dvel0": v0, "dl_domega0": w0,
-                "dl_dparams": {"pp": dict(zip(keys, p[:6])), "pw": dict(zip(keys, p[6:]))}}
+                "dl_dparams": per[0] if self.scenes == 1 else per}
 
     def set_pt_warp_items(self, n):
         """Crossover of the two particle-triangle kernels: up to n contact

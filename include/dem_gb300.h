@@ -286,9 +286,10 @@ int dem_cell_sort_static(const double* x, const double* y, const double* z,
  * No counterpart in the reference, which has no gradients.  A hand-written
  * adjoint of each step of the FP64 form: within a step the contact set is
  * the one the forward step found, and at the Coulomb / twisting / rolling
- * caps the derivative is that of the branch taken.  Covers one scene of
- * spheres with walls and particle contacts (no rigid bodies), precision
- * DEM_PRECISION_FP64; other engines return DEM_ERR_INVALID.
+ * caps the derivative is that of the branch taken.  Covers spheres with
+ * walls and particle contacts (no rigid bodies), one scene or a batch
+ * (dem_initialize_batch), precision DEM_PRECISION_FP64; other engines
+ * return DEM_ERR_INVALID.
  *
  * dem_adjoint_forward runs the reference's step sequence from a freshly
  * initialized engine: the first evaluation (dt = 0), the leapfrog start and
@@ -298,8 +299,9 @@ int dem_cell_sort_static(const double* x, const double* y, const double* z,
  * the final positions and velocities ([n][3] each, owner order; either may
  * be NULL for zero) and returns its gradient with respect to the initial
  * positions, velocities and angular velocities ([n][3]; NULL to skip) and
- * to the materials (dl_dparams[2][6]: particle-particle then particle-wall,
- * each d/dkN, d/dmu, d/depsN, d/depsS, d/dmuT, d/dmuR).  It recomputes each
+ * to the materials (dl_dparams[scenes][2][6]: per scene of the engine,
+ * particle-particle then particle-wall, each d/dkN, d/dmu, d/depsN, d/depsS,
+ * d/dmuT, d/dmuR; scenes is 1 for dem_initialize).  It recomputes each
  * segment from its checkpoint and leaves the engine at the end of the
  * forward run. */
 int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every);

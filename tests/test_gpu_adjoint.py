@@ -113,6 +113,73 @@ def test_initial_position_and_spin_gradients_match_central_differences():
     _close(an, (lp - lm) / (2 * eps), "w0 direction", abs(an))
 
 
+def _batch_scenes():
+    """Three walled boxes of spheres (the same box, so their coordinates
+    overlap) with their own materials and particle counts: a batch of the
+    calibration workload's kind."""
+    out = []
+    for k, (n, mu, eps) in enumerate(((300, 0.4, 0.5), (200, 0.7, 0.3), (250, 0.2, 0.8))):
+        sc = G.small_dem(n=n, seed=21 + k, vel_std=0.05)
+        pp = dataclasses.replace(sc.pp, mu=mu, epsN=eps)
+        pw = dataclasses.replace(sc.pp, mu=0.5 * mu, epsN=eps)
+        out.append(dataclasses.replace(sc, pp=pp, pw=pw, pt=dataclasses.replace(pp)))
+    return out
+
+
+def test_batched_adjoint_matches_scene_by_scene():
+    """One batched reverse sweep of the sum of the scenes' losses gives each
+    scene's material and initial-state gradients as its own engine does
+    (the scenes are independent; only the order of the atomic sums differs)."""
+    scenes = _batch_scenes()
+    from dem_mbd_cuda_gb300.engine import CudaDemSolver
+    b = CudaDemSolver().initialize(scenes, precision="fp64").adjoint_forward(STEPS, K)
+    dpos = np.zeros((b.n, 3))
+    dvel = np.zeros((b.n, 3))
+    off = 0
+    for sc in scenes:
+        dpos[off:off + sc.n, 2] = 1.0 / sc.n
+        dvel[off:off + sc.n, 0] = CV / sc.n
+        off += sc.n
+    gb = b.adjoint_backward(dpos, dvel)
+    assert len(gb["dl_dparams"]) == len(scenes)
+    off = 0
+    for k, sc in enumerate(scenes):
+        _, g = _adjoint(sc)
+        for cls in ("pp", "pw"):
+            for key, a in g["dl_dparams"][cls].items():
+                bk = gb["dl_dparams"][k][cls][key]
+                assert abs(bk - a) <= 1e-9 * abs(a) + 1e-15, (k, cls, key, bk, a)
+        for name in ("dl_dpos0", "dl_dvel0", "dl_domega0"):
+            ref = g[name]
+            got = gb[name][off:off + sc.n]
+            assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max() + 1e-18, (k, name)
+        off += sc.n
+
+
+def test_batched_autograd_gradients():
+    """simulate_batch returns per-scene material gradients equal to the
+    engine's batched backward result."""
+    torch = pytest.importorskip("torch")
+    from dem_mbd_cuda_gb300.autograd import materials, simulate_batch
+    scenes = _batch_scenes()
+    pp = torch.stack([materials(s.pp) for s in scenes]).requires_grad_(True)
+    pw = torch.stack([materials(s.pw) for s in scenes])
+    v0 = torch.tensor(np.concatenate([s.vel for s in scenes]))
+    pos, _ = simulate_batch(scenes, STEPS, pp, pw, v0, checkpoint_every=K)
+    off, loss = 0, 0.0
+    for s in scenes:
+        loss = loss + pos[off:off + s.n, 2].mean()
+        off += s.n
+    loss.backward()
+    assert pp.grad.shape == (len(scenes), 6)
+    for k, s in enumerate(scenes):
+        e = engine_for(s, precision="fp64").adjoint_forward(STEPS, K)
+        dpos = np.zeros((s.n, 3)); dpos[:, 2] = 1.0 / s.n
+        g = e.adjoint_backward(dpos, None)["dl_dparams"]["pp"]
+        for f, key in enumerate(("kN", "mu", "epsN", "epsS", "muT", "muR")):
+            assert abs(pp.grad[k, f].item() - g[key]) <= 1e-9 * abs(g[key]) + 1e-15, (k, key)
+
+
 def test_adjoint_scope_errors():
     sc = _scene()
     e = engine_for(sc, precision="mixed")
