@@ -645,6 +645,7 @@ __device__ __noinline__ double circle_triangle_area_fp64(V3<double> n, V3<double
 template <typename T>
 __device__ double tri_area_scale(const double* W, V3<double> p, double r, double& dist)
 {
+    if constexpr (sizeof(T) == sizeof(double)) return tri_area_scale64(W, p, r, dist);
     const V3<double> n = mk(W[12], W[13], W[14]);
     const V3<double> a = mk(W[3], W[4], W[5]);
     dist = dot(n, p - a);

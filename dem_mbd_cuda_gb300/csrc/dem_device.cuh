@@ -374,4 +374,57 @@ template <typename T> DEM_DEV T circle_triangle_area(V3<T> normal, V3<T> ra, V3<
     return fmin(area, T(kPi) * r * r);
 }
 
+// World record of one triangle (transformTrianglesKernel,
+// src/cuda/cuda_body_backend.cu:71-112): W[0..11] the vertices v1..v4 at
+// R(q) L_k + c, W[12..14] the normal R(q) L[12..14], W[15] the circumradius of
+// v2..v4 about their centroid (used only to skip disjoint pairs).  Also
+// returns that centroid (g) for the FP32 prefilter copies.
+DEM_DEV void tri_world(const double* L, double qw, double qx, double qy, double qz, double cx, double cy, double cz,
+                       double* W, double g[3])
+{
+    for (int k = 0; k < 4; ++k) {
+        const V3<double> p = rot_iv(qw, qx, qy, qz, mk(L[3 * k], L[3 * k + 1], L[3 * k + 2]));
+        W[3 * k] = p.x + cx; W[3 * k + 1] = p.y + cy; W[3 * k + 2] = p.z + cz;
+    }
+    const V3<double> nn = rot_iv(qw, qx, qy, qz, mk(L[12], L[13], L[14]));
+    W[12] = nn.x; W[13] = nn.y; W[14] = nn.z;
+    g[0] = (W[3] + W[6] + W[9]) * (1.0 / 3.0);
+    g[1] = (W[4] + W[7] + W[10]) * (1.0 / 3.0);
+    g[2] = (W[5] + W[8] + W[11]) * (1.0 / 3.0);
+    double r2 = 0.0;
+    for (int k = 1; k < 4; ++k) {
+        const double dx = W[3 * k] - g[0], dy = W[3 * k + 1] - g[1], dz = W[3 * k + 2] - g[2];
+        r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
+    }
+    W[15] = sqrt(r2) * (1.0 + 1e-12) + 1e-15;
+}
+
+// bodyTriangleAreaScale (:380-407) in FP64: the share of the contact disk of
+// a sphere (centre p, radius r) that lies on the world triangle W, and the
+// sphere's distance above the triangle's plane (dist, along the normal).
+DEM_DEV double tri_area_scale64(const double* W, V3<double> p, double r, double& dist)
+{
+    const V3<double> n = mk(W[12], W[13], W[14]);
+    const V3<double> a = mk(W[3], W[4], W[5]);
+    dist = dot(n, p - a);
+    if (dist <= 0.0) return 0.0;
+    const double c2 = r * r - dist * dist;
+    if (c2 <= 1.0e-30) return 0.0;
+    const V3<double> ce = p - n * dist;
+    const V3<double> ra = a - ce, rb = mk(W[6], W[7], W[8]) - ce, rc = mk(W[9], W[10], W[11]) - ce;
+    // Disk and triangle disjoint (disk centre farther from the triangle's
+    // centroid than the disk radius plus the triangle's circumradius about
+    // it, W[15]): the reference's edge sum then cancels to rounding noise,
+    // far below its 1e-12 threshold, so the scale is 0 either way.
+    {
+        const V3<double> cen = (ra + rb + rc) * (1.0 / 3.0);
+        const double reach = (sqrt(c2) + W[15]) * (1.0 + 1e-9);
+        if (dot(cen, cen) > reach * reach) return 0.0;
+    }
+    const double area = circle_triangle_area<double>(n, ra, rb, rc, sqrt(c2));
+    if (area <= 0.0) return 0.0;
+    const double sc = fmin(1.0, area / (kPi * c2));
+    return sc > 1.0e-12 ? sc : 0.0;
+}
+
 }  // namespace demgb

@@ -401,31 +401,15 @@ __global__ void k_tri_transform(Tris t, Bodies b, const SceneC* __restrict__ sc)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= t.nt) return;
     const int ib = t.body[i];
-    const double qw = b.q[4 * ib], qx = b.q[4 * ib + 1], qy = b.q[4 * ib + 2], qz = b.q[4 * ib + 3];
     const double* L = t.local + 15 * (size_t)i;
     double* W = t.world + 16 * (size_t)i;
-    const double cx = b.c[3 * ib], cy = b.c[3 * ib + 1], cz = b.c[3 * ib + 2];
-    for (int k = 0; k < 4; ++k) {
-        const V3<double> p = rot_iv(qw, qx, qy, qz, mk(L[3 * k], L[3 * k + 1], L[3 * k + 2]));
-        W[3 * k] = p.x + cx; W[3 * k + 1] = p.y + cy; W[3 * k + 2] = p.z + cz;
-    }
-    const V3<double> nn = rot_iv(qw, qx, qy, qz, mk(L[12], L[13], L[14]));
-    W[12] = nn.x; W[13] = nn.y; W[14] = nn.z;
-    // circumradius of v2, v3, v4 about their centroid (disjointness test)
-    {
-        const double gx = (W[3] + W[6] + W[9]) * (1.0 / 3.0), gy = (W[4] + W[7] + W[10]) * (1.0 / 3.0),
-                     gz = (W[5] + W[8] + W[11]) * (1.0 / 3.0);
-        double r2 = 0.0;
-        for (int k = 1; k < 4; ++k) {
-            const double dx = W[3 * k] - gx, dy = W[3 * k + 1] - gy, dz = W[3 * k + 2] - gz;
-            r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
-        }
-        W[15] = sqrt(r2) * (1.0 + 1e-12) + 1e-15;
-        if (t.tf) {
-            const double na = nn.x * W[3] + nn.y * W[4] + nn.z * W[5];
-            t.tf[2 * (size_t)i] = make_float4((float)nn.x, (float)nn.y, (float)nn.z, (float)na);
-            t.tf[2 * (size_t)i + 1] = make_float4((float)gx, (float)gy, (float)gz, (float)W[15]);
-        }
+    double g[3];
+    tri_world(L, b.q[4 * ib], b.q[4 * ib + 1], b.q[4 * ib + 2], b.q[4 * ib + 3], b.c[3 * ib], b.c[3 * ib + 1],
+              b.c[3 * ib + 2], W, g);
+    if (t.tf) {
+        const double na = W[12] * W[3] + W[13] * W[4] + W[14] * W[5];
+        t.tf[2 * (size_t)i] = make_float4((float)W[12], (float)W[13], (float)W[14], (float)na);
+        t.tf[2 * (size_t)i + 1] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)W[15]);
     }
     // Padded-AABB cell range (countTriangleCellsKernel,
     // src/cuda/cuda_contact_backend.cu:409-452): floor((min - pad) / mesh)
