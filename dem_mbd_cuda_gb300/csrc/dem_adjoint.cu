@@ -204,8 +204,9 @@ __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const 
 // Material gradients of one block, by scene: a few shared rows tagged with
 // their scene.  A thread adds its running sums to its scene's row when its
 // scene changes and at the end; a scene that finds no row free goes straight
-// to global memory.  `grads` is scene-major, [scene][2][kAdjParams], and
-// `chan` selects the particle (0) or wall (1) parameters.
+// to global memory.  `grads` is scene-major, [scene][3][kAdjParams], and
+// `chan` selects the particle (0), wall (1) or particle-triangle (2)
+// parameters.
 constexpr int kGradRows = 4;
 struct GradRows {
     int tag[kGradRows];
@@ -227,7 +228,7 @@ __device__ void grad_add(GradRows& r, int s, const MatGrad& g, double* grads, in
     }
     for (int f = 0; f < kAdjParams; ++f) {
         if (row >= 0) atomicAdd(&r.g[row][f], gv[f]);
-        else atomicAdd(grads + ((size_t)s * 2 + chan) * kAdjParams + f, gv[f]);
+        else atomicAdd(grads + ((size_t)s * 3 + chan) * kAdjParams + f, gv[f]);
     }
 }
 __device__ void grad_rows_flush(GradRows& r, double* grads, int chan)
@@ -235,7 +236,7 @@ __device__ void grad_rows_flush(GradRows& r, double* grads, int chan)
     __syncthreads();
     if (threadIdx.x < kGradRows * kAdjParams) {
         const int j = threadIdx.x / kAdjParams, f = threadIdx.x % kAdjParams;
-        if (r.tag[j] >= 0) atomicAdd(grads + ((size_t)r.tag[j] * 2 + chan) * kAdjParams + f, r.g[j][f]);
+        if (r.tag[j] >= 0) atomicAdd(grads + ((size_t)r.tag[j] * 3 + chan) * kAdjParams + f, r.g[j][f]);
     }
 }
 
@@ -381,6 +382,116 @@ __global__ void __launch_bounds__(128) k_adj_contacts(Comps c, Owners o, const S
 }
 
 
+// Particle-body manifolds of one step (tape entries), reverse: one thread
+// per manifold.  The sphere's adjoints go to T like a wall contact's; the
+// body's pose adjoints (centre, orientation, velocity, spin) to its row of
+// the body adjoints; the adjoint of the body's reaction load comes from
+// the row's kBlF (the half update's reverse, run before this kernel).
+__device__ __forceinline__ int adj_global_step(const int* base, const int* slot)
+{
+    return (base ? *base : 0) + (slot ? *slot : 0);
+}
+__global__ void __launch_bounds__(64) k_adj_pt(Comps c, Owners o, const SceneC* __restrict__ sc, StepTape tp, int count,
+                                               const double* P, double* T, double* lhist, AdjBodies ab, double dt_eff,
+                                               double* grads, int nscenes)
+{
+    __shared__ GradRows rows;
+    const int n = o.n;
+    const int g = adj_global_step(ab.base, tp.slot);
+    tp = tape_at(tp);
+    if (count < 0) count = min(*tp.pb_count, tp.pb_cap);
+    grad_rows_init(rows);
+    MatGrad gs = {0, 0, 0, 0, 0, 0};
+    int cur = -1;
+    const EntryRange er = entry_range(count, blockIdx.x, gridDim.x, nscenes);
+    for (int k = er.k; k < er.end; k += er.step) {
+        const int4 e = tp.pb[k];
+        const int i = e.x, b = e.y;
+        const int si = nscenes == 1 ? 0 : o.scene[i];
+        if (si != cur) {
+            if (cur >= 0) grad_add(rows, cur, gs, grads, 2);
+            gs = MatGrad{0, 0, 0, 0, 0, 0};
+            cur = si;
+        }
+        const double* rec = ab.rec + ((size_t)g * ab.nb + b) * kBR;
+        PTIn in;
+        in.p = ld3(P, kPX, n, i); in.ev = ld3(P, kPV, n, i); in.mv = ld3(P, kPMV, n, i);
+        in.ew = ld3(P, kPEW, n, i); in.mw = ld3(P, kPEMW, n, i);
+        in.rad = c.radius[i]; in.mass = o.mass[i];
+        in.c = ldv3(rec, kBrC); in.V = ldv3(rec, kBrV); in.w = ldv3(rec, kBrW);
+        for (int q = 0; q < 4; ++q) in.q[q] = rec[kBrQ + q];
+        const int* tl = tp.pb_tri + (size_t)k * kPbTri;
+        in.ntri = min(tl[0], kPbTris);
+        for (int t = 0; t < in.ntri; ++t) in.L[t] = ab.local + 15 * (size_t)tl[1 + t];
+        for (int a = 0; a < 9; ++a) in.h[a] = tp.pb_h[(size_t)k * kHV + a];
+        double* lh = lhist + (size_t)e.z * kHV;
+        double lho[9];
+        for (int a = 0; a < 9; ++a) lho[a] = lh[a];
+        PTAdj ad;
+        ad.p = ad.ev = ad.mv = ad.ew = ad.mw = ad.c = ad.V = ad.w = z3();
+        for (int q = 0; q < 4; ++q) ad.q[q] = 0.0;
+        for (int a = 0; a < 9; ++a) ad.h[a] = 0.0;
+        double* Lb = ab.L + (size_t)b * kBL;
+        pt_manifold_vjp(sc[si].pt, dt_eff, in, ld3(T, kTF, n, i), ld3(T, kTTau, n, i), ldv3(Lb, kBlF),
+                        ldv3(Lb, kBlF + 3), lho, ad, gs);
+        for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : ad.h[a];
+        add3(T, kTX, n, i, ad.p);
+        add3(T, kTV, n, i, ad.ev);
+        add3(T, kTMV, n, i, ad.mv);
+        add3(T, kTEW, n, i, ad.ew);
+        add3(T, kTEMW, n, i, ad.mw);
+        const double pose[13] = {ad.c.x, ad.c.y, ad.c.z, ad.q[0], ad.q[1], ad.q[2], ad.q[3],
+                                 ad.V.x, ad.V.y, ad.V.z, ad.w.x, ad.w.y, ad.w.z};
+        for (int f = 0; f < 13; ++f) atomicAdd(Lb + kBlC + f, pose[f]);
+    }
+    if (cur >= 0) grad_add(rows, cur, gs, grads, 2);
+    grad_rows_flush(rows, grads, 2);
+}
+
+// The body leapfrog's reverse, one thread per body (dynamic bodies only:
+// the others follow their prescribed or fixed motion and carry no
+// adjoint).  Part A: the half update of the step (before the contacts'
+// reverse, which reads the loads' adjoint).  Part C: the position update
+// into the step, from the previous step's record.
+__global__ void k_adj_body_a(AdjBodies ab, const int* slot, int first)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= ab.nb) return;
+    double* Lb = ab.L + (size_t)b * kBL;
+    const double* cst = ab.cst + 5 * (size_t)b;
+    if (cst[4] != 0.0) {
+        for (int f = 0; f < kBL; ++f) Lb[f] = 0.0;
+        return;
+    }
+    const int g = adj_global_step(ab.base, slot);
+    body_half_vjp(ab.rec + ((size_t)g * ab.nb + b) * kBR, cst, ab.dt, first != 0, Lb);
+}
+__global__ void k_adj_body_c(AdjBodies ab, const int* slot)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= ab.nb) return;
+    double* Lb = ab.L + (size_t)b * kBL;
+    if (ab.cst[5 * (size_t)b + 4] != 0.0) {
+        for (int f = 0; f < kBL; ++f) Lb[f] = 0.0;
+        return;
+    }
+    const int g = adj_global_step(ab.base, slot);
+    body_pos_vjp(ab.rec + ((size_t)(g - 1) * ab.nb + b) * kBR, ab.dt, Lb);
+}
+__global__ void k_adj_body_pose(Bodies bd, const double* rec, const int* base, const int* slot)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bd.nb) return;
+    const double* r = rec + ((size_t)adj_global_step(base, slot) * bd.nb + b) * kBR;
+    for (int a = 0; a < 3; ++a) {
+        bd.c[3 * b + a] = r[kBrC + a];
+        bd.v[3 * b + a] = r[kBrV + a];
+        bd.w[3 * b + a] = r[kBrW + a];
+    }
+    for (int q = 0; q < 4; ++q) bd.q[4 * b + q] = r[kBrQ + q];
+}
+__global__ void k_set_int(int* p, int v) { *p = v; }
+
 // advance^T: T (complete) and the vh, wh partials of Lp -> Lp = adjoint of
 // S_s.  With init = 1 (the first evaluation, no advance): Lp = adjoint of
 // the initial x, q, v, w.
@@ -453,24 +564,40 @@ void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s)
     if (o.n > 0) k_adj_restore<<<dim3(nblocks(o.n, 256), kAdjFields), 256, 0, s>>>(o, S);
 }
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
-                     int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
-                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int nscenes,
-                     int sm_count, cudaStream_t s)
+                     int npw, int npb, const double* S, const double* S1, const double* L, double* Lp, double* P,
+                     double* T, double* lh_pp, double* lh_pw, double* lh_pb, const AdjBodies& ab, double dt,
+                     double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s)
 {
     if (o.n <= 0) return;
     // device counts: S, S1 at the tape's slot, fixed grid-stride grids
     const int* slot = (npp < 0 || npw < 0) ? tp.slot : nullptr;
+    const bool bodies = ab.nb > 0 && tp.pb;
+    if (bodies) k_adj_body_a<<<nblocks(ab.nb, 32), 32, 0, s>>>(ab, slot, init);
     k_adj_finish<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init, slot);
     const int bpp = npp < 0 ? sm_count * 8 : min(nblocks(npp, 128), sm_count * 8);
     const int bpw = npw < 0 ? sm_count * 2 : min(nblocks(npw, 128), sm_count * 2);
     if (bpp + bpw > 0)
         k_adj_contacts<<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff, grads,
                                                  nscenes);
+    if (bodies) {
+        const int bpb = npb < 0 ? sm_count * 2 : min(nblocks(npb, 64), sm_count * 2);
+        if (bpb > 0) k_adj_pt<<<bpb, 64, 0, s>>>(c, o, sc, tp, npb, P, T, lh_pb, ab, dt_eff, grads, nscenes);
+    }
     k_adj_advance<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, P, T, Lp, dt, init, slot);
+    if (bodies && !init) k_adj_body_c<<<nblocks(ab.nb, 32), 32, 0, s>>>(ab, slot);
 }
+void launch_adj_body_pose(const Bodies& b, const double* rec, const int* base, const int* slot, cudaStream_t s)
+{
+    if (b.nb > 0) k_adj_body_pose<<<nblocks(b.nb, 32), 32, 0, s>>>(b, rec, base, slot);
+}
+void launch_set_int(int* p, int v, cudaStream_t s) { k_set_int<<<1, 1, 0, s>>>(p, v); }
 
 __global__ void k_adj_slot_add(int* slot, int delta) { *slot += delta; }
-__global__ void k_adj_tape_begin(int* pw_count, const int* slot) { pw_count[*slot] = 0; }
+__global__ void k_adj_tape_begin(int* pw_count, int* pb_count, const int* slot)
+{
+    pw_count[*slot] = 0;
+    if (pb_count) pb_count[*slot] = 0;
+}
 __global__ void k_adj_tape_end(int* pp_count, const int* ct_total, int* slot)
 {
     pp_count[*slot] = *ct_total;
@@ -478,7 +605,10 @@ __global__ void k_adj_tape_end(int* pp_count, const int* ct_total, int* slot)
 }
 
 void launch_adj_slot_add(int* slot, int delta, cudaStream_t s) { k_adj_slot_add<<<1, 1, 0, s>>>(slot, delta); }
-void launch_adj_tape_begin(int* pw_count, const int* slot, cudaStream_t s) { k_adj_tape_begin<<<1, 1, 0, s>>>(pw_count, slot); }
+void launch_adj_tape_begin(int* pw_count, int* pb_count, const int* slot, cudaStream_t s)
+{
+    k_adj_tape_begin<<<1, 1, 0, s>>>(pw_count, pb_count, slot);
+}
 void launch_adj_tape_end(int* pp_count, const int* ct_total, int* slot, cudaStream_t s)
 {
     k_adj_tape_end<<<1, 1, 0, s>>>(pp_count, ct_total, slot);

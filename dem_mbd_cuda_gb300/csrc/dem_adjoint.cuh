@@ -496,7 +496,6 @@ DEM_DEV void pw_law_vjp(const MatC& m, double dt, D3 out, double depth, double r
 // advanceBodyManifoldHistory :855-949 and bodyContact :708-853), written
 // once more in FP64 for the reverse sweep: the forward pieces below repeat
 // what the PT kernels compute, and each has its vector-Jacobian product.
-constexpr int kPbTris = 12;  // triangles of one manifold the reverse sweep keeps
 struct PTIn {
     D3 p, ev, mv, ew, mw;  // sphere: centre, endpoint and midpoint velocity, world spins (endpoint, midpoint)
     double rad, mass;

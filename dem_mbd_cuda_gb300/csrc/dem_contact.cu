@@ -952,6 +952,25 @@ __device__ void pt_microstate(const MatC& m, const PtItem& it, const PtBody& bd,
 // item (FP64 throughput bound).  Both kernels are launched; the count on the
 // device picks the one that works.
 
+// Adjoint tape of one particle-body manifold (FP64 form): the component,
+// body, history slot, whether the slot is new, the history before the
+// update and the triangles with an area share, in triangle order.
+template <typename T>
+__device__ void tape_pb(const StepTape& tp, int ci, int b, int slot, bool fresh, const T* h, const int* tri, int ntri,
+                        bool spill)
+{
+    const int k = atomicAdd(tp.pb_count, 1);
+    if (k >= tp.pb_cap || spill || ntri > kPbTris) {
+        atomicOr(tp.overflow, 4);
+        return;
+    }
+    tp.pb[k] = make_int4(ci, b, ci * kBSlots + slot, fresh ? 1 : 0);
+    int* tl = tp.pb_tri + (size_t)k * kPbTri;
+    tl[0] = ntri;
+    for (int q = 0; q < ntri; ++q) tl[1 + q] = tri[q];
+    for (int a = 0; a < 9; ++a) tp.pb_h[(size_t)k * kHV + a] = (double)h[a];
+}
+
 // ---------------------------------------------------- PT, thread per item
 constexpr int kTriCache = 24;
 
@@ -963,6 +982,7 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
     const int step = *k.step;
     const int total = *ct.pt_ctotal_ptr;
     if (total <= k.pt_warp_items) return;
+    const StepTape tape = tape_at(ct.tape);
     int bover = 0, bhigh = 0;
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < total; item += gridDim.x * blockDim.x) {
         const int t = ct.pt_clist[item];
@@ -1009,11 +1029,13 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
             const V3<double> mn = normalized(wn);
             const V3<double> mc = wc * (1.0 / tot);
             const double md = wd / tot;
-            const int slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh);
+            bool fresh = false;
+            const int slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh, &fresh);
             if (slot < 0) { ++bover; continue; }
             T* hv = hb.val + ((size_t)ci * kBSlots + slot) * kHV;
             T h[9];
             hv_load(hv, h);
+            if (tape.pb) tape_pb(tape, ci, b, slot, fresh, h, ctri, ncache, spill);
             const PtBody bd = pt_body(bodies, b);
             const MatC& m = S.pt;
             bool slide = false, twist = false;

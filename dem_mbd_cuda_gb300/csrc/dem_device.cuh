@@ -25,6 +25,7 @@ constexpr double kGravityConstant = 6.67430e-11;
 constexpr int kPSlots = 64;   // particle history slots per component
 constexpr int kWSlots = 16;   // wall history slots per component
 constexpr int kBSlots = 64;   // body history slots per component
+constexpr int kPbTris = 12;   // triangles of one particle-body manifold the reverse mode keeps
 constexpr int kRegime = 7;
 constexpr int kMicro = 22;
 constexpr int kPtRecord = 32;  // doubles per (PT component, body) record

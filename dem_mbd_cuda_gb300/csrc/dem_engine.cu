@@ -7,6 +7,7 @@
 // integration loop of src/cuda_simulation_integrator.cpp:245-446 with the
 // host MBD step of src/dyneq.cpp:97-130.
 #include "../../include/dem_gb300.h"
+#include "dem_adjoint.cuh"
 #include "dem_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -957,6 +958,34 @@ public:
         }
     }
 
+    // The pose a force evaluation uses, per body (centre, orientation,
+    // velocity, spin), and the reverse mode's record of one step: that pose,
+    // the loads and the state after the half update.
+    std::vector<double> body_pose() const
+    {
+        std::vector<double> p(13 * (size_t)nb_);
+        for (int b = 0; b < nb_; ++b) {
+            double* r = p.data() + 13 * (size_t)b;
+            for (int a = 0; a < 3; ++a) { r[a] = hbc_[3 * b + a]; r[7 + a] = hbv_[3 * b + a]; r[10 + a] = hbw_[3 * b + a]; }
+            for (int k = 0; k < 4; ++k) r[3 + k] = hbq_[4 * b + k];
+        }
+        return p;
+    }
+    void adj_record(const std::vector<double>& pose)
+    {
+        for (int b = 0; b < nb_; ++b) {
+            double r[kBR];
+            std::memcpy(r, pose.data() + 13 * (size_t)b, 13 * sizeof(double));
+            for (int k = 0; k < 6; ++k) r[kBrF + k] = hbloads_[6 * b + k];
+            for (int a = 0; a < 3; ++a) {
+                r[kBrHV + a] = hbhv_[3 * b + a]; r[kBrHW + a] = hbhw_[3 * b + a];
+                r[kBrAcc + a] = hbacc_[3 * b + a]; r[kBrDom + a] = hbdom_[3 * b + a];
+            }
+            for (int k = 0; k < 4; ++k) { r[kBrHQ + k] = hbhq_[4 * b + k]; r[kBrHDQ + k] = hbhdq_[4 * b + k]; }
+            adj_rec_->insert(adj_rec_->end(), r, r + kBR);
+        }
+    }
+
     // IntegrateDem / IntegrateDemMultiBody without output frames.
     void run_steps(int steps)
     {
@@ -964,9 +993,11 @@ public:
         const double dt = dt_;
         if (!started_) {
             dem_body_states bs{hbc_.data(), hbq_.data(), hbv_.data(), hbw_.data()};
+            const std::vector<double> pose = adj_rec_ ? body_pose() : std::vector<double>();
             compute_forces(nb_ > 0 ? &bs : nullptr, nb_ > 0 ? hbloads_.data() : nullptr, 1);
             if (!restored_) leapfrog_init(0.5 * dt);
             if (nb_ > 0) body_half_update(true, dt);
+            if (adj_rec_ && nb_ > 0) adj_record(pose);
             started_ = true;
         }
         if (steps <= 0) return;
@@ -987,6 +1018,7 @@ public:
         for (int s = 0; s < steps; ++s) {
             const bool last = s == steps - 1;
             cudaGraphExec_t g = graphs_[graph_index(mbd, s > 0 ? 1 : 2, last)];
+            std::vector<double> pose;
             if (mbd) {
                 body_position_update(dt_);
                 double* p = pin_body_state();
@@ -994,6 +1026,7 @@ public:
                 std::memcpy(p + 3 * nb_, hbq_.data(), sizeof(double) * 4 * nb_);
                 std::memcpy(p + 7 * nb_, hbv_.data(), sizeof(double) * 3 * nb_);
                 std::memcpy(p + 10 * nb_, hbw_.data(), sizeof(double) * 3 * nb_);
+                if (adj_rec_) pose = body_pose();
             }
             check(cudaGraphLaunch(g, stream_), "cudaGraphLaunch");
             ++step_index_;
@@ -1003,6 +1036,7 @@ public:
                 check(cudaEventSynchronize(body_ready_), "mbd step");
                 body_forces_from_pinned(hbloads_.data());
                 body_half_update(false, dt_);
+                if (adj_rec_) adj_record(pose);
             }
         }
         // the callers synchronize (after their own downloads)
@@ -1350,6 +1384,9 @@ public:
         int *pl = nullptr, *wl = nullptr;          // last seen
         double *pv = nullptr, *wv = nullptr;       // values
         int *phw = nullptr, *whw = nullptr;        // high-water marks
+        uint64_t* bk = nullptr;                    // body history (with rigid bodies)
+        int *bl = nullptr, *bhw = nullptr;
+        double* bv = nullptr;
         int* step = nullptr;                       // device step counter
         int step_index = 0;
         bool started = false;
@@ -1364,11 +1401,16 @@ public:
         int4 *pp = nullptr, *pw = nullptr;         // [K + 1][cap]
         double *pp_h = nullptr, *pw_h = nullptr;
         int *pp_cnt = nullptr, *pw_cnt = nullptr, *slot = nullptr;
+        int4* pb = nullptr;                        // particle-body manifolds [K + 1][cap]
+        int* pb_tri = nullptr;
+        double* pb_h = nullptr;
+        int* pb_cnt = nullptr;
+        int* base = nullptr;                       // global step of slot 0 (device)
         cudaGraphExec_t g_fwd = nullptr, g_rev[2] = {nullptr, nullptr};
     };
     struct Adjoint {
         bool ready = false;
-        int steps = 0, K = 0, nseg = 0, cap_pp = 0, cap_pw = 0;
+        int steps = 0, K = 0, nseg = 0, cap_pp = 0, cap_pw = 0, cap_pb = 0;
         std::vector<AdjCkpt> ck;                   // [0] before the first evaluation, [1 + k] after segment k - 1
         AdjTape tb[2];
         unsigned char* pp_new = nullptr;
@@ -1376,6 +1418,10 @@ public:
         double *L = nullptr, *Lp = nullptr, *P = nullptr, *T = nullptr, *lh_pp = nullptr, *lh_pw = nullptr;
         double* grads = nullptr;
         double* Lb[2] = {nullptr, nullptr};        // the two adjoint-state buffers L and Lp alternate between
+        // rigid bodies: the forward run's records ([steps + 1][nb][kBR],
+        // host and device), constants, adjoints, body-history adjoints
+        std::vector<double> brec_host;
+        double *brec = nullptr, *bcst = nullptr, *Lbody = nullptr, *lh_pb = nullptr;
     };
     void adj_release_graphs()
     {
@@ -1389,7 +1435,6 @@ public:
         need_init();
         if (precision_ != DEM_PRECISION_FP64)
             throw DemError(DEM_ERR_INVALID, "the adjoint runs on the FP64 form (precision DEM_PRECISION_FP64)");
-        if (nb_ > 0) throw DemError(DEM_ERR_INVALID, "the adjoint does not cover rigid bodies");
         if (!sphere_) throw DemError(DEM_ERR_INVALID, "the adjoint covers spheres (one component per owner)");
         for (int i = 0; i < n_; ++i)
             if (!(oin_host_[3 * (size_t)i] == oin_host_[3 * (size_t)i + 1] &&
@@ -1405,6 +1450,11 @@ public:
         c.pv = adj_arena_.alloc<double>(ps * kHV, "adjoint checkpoint"); c.phw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
         c.wk = adj_arena_.alloc<uint64_t>(ws, "adjoint checkpoint"); c.wl = adj_arena_.alloc<int>(ws, "adjoint checkpoint");
         c.wv = adj_arena_.alloc<double>(ws * kHV, "adjoint checkpoint"); c.whw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
+        if (nb_ > 0) {
+            const size_t bs = (size_t)nc_ * kBSlots;
+            c.bk = adj_arena_.alloc<uint64_t>(bs, "adjoint checkpoint"); c.bl = adj_arena_.alloc<int>(bs, "adjoint checkpoint");
+            c.bv = adj_arena_.alloc<double>(bs * kHV, "adjoint checkpoint"); c.bhw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
+        }
         c.step = adj_arena_.alloc<int>(1, "adjoint checkpoint");
         return c;
     }
@@ -1417,6 +1467,10 @@ public:
         };
         cp(c.pk, hp64_.key, ps * 8); cp(c.pl, hp64_.last, ps * 4); cp(c.pv, hp64_.val, ps * kHV * 8); cp(c.phw, hp64_.hw, (size_t)nc_ * 4);
         cp(c.wk, hw64_.key, ws * 8); cp(c.wl, hw64_.last, ws * 4); cp(c.wv, hw64_.val, ws * kHV * 8); cp(c.whw, hw64_.hw, (size_t)nc_ * 4);
+        if (c.bk) {
+            const size_t bs = (size_t)nc_ * kBSlots;
+            cp(c.bk, hb64_.key, bs * 8); cp(c.bl, hb64_.last, bs * 4); cp(c.bv, hb64_.val, bs * kHV * 8); cp(c.bhw, hb64_.hw, (size_t)nc_ * 4);
+        }
         cp(c.step, K_.step, 4);
     }
     void adj_save(AdjCkpt& c)
@@ -1449,6 +1503,7 @@ public:
         A.steps = steps; A.K = std::min(K, steps); A.nseg = (steps + A.K - 1) / A.K;
         A.cap_pp = 16 * nc_ + 1024;
         A.cap_pw = 2 * nc_ + 1024;
+        A.cap_pb = nb_ > 0 ? 2 * nc_ + 1024 : 0;
         for (int k = 0; k < A.nseg + 2; ++k) A.ck.push_back(adj_alloc_ckpt());
         const size_t slots = (size_t)A.K + 1;
         for (AdjTape& t : A.tb) {
@@ -1460,6 +1515,13 @@ public:
             t.pp_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
             t.pw_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
             t.slot = adj_arena_.alloc<int>(1, "adjoint slot");
+            t.base = adj_arena_.alloc<int>(1, "adjoint slot");
+            if (nb_ > 0) {
+                t.pb = adj_arena_.alloc<int4>(slots * A.cap_pb, "adjoint tape");
+                t.pb_tri = adj_arena_.alloc<int>(slots * A.cap_pb * kPbTri, "adjoint tape");
+                t.pb_h = adj_arena_.alloc<double>(slots * A.cap_pb * kHV, "adjoint tape");
+                t.pb_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
+            }
         }
         A.pp_new = adj_arena_.alloc<unsigned char>((size_t)nc_ * kPSlots, "adjoint tape");
         A.overflow = adj_arena_.alloc<int>(1, "adjoint tape");
@@ -1469,15 +1531,38 @@ public:
         A.T = adj_arena_.alloc<double>((size_t)kTFields * n_, "adjoint state");
         A.lh_pp = adj_arena_.alloc<double>((size_t)nc_ * kPSlots * kHV, "adjoint history");
         A.lh_pw = adj_arena_.alloc<double>((size_t)nc_ * kWSlots * kHV, "adjoint history");
-        A.grads = adj_arena_.alloc<double>((size_t)S_ * 2 * kAdjParams, "adjoint parameters");
+        A.grads = adj_arena_.alloc<double>((size_t)S_ * 3 * kAdjParams, "adjoint parameters");
         A.Lb[0] = A.L; A.Lb[1] = A.Lp;
-        adj_save(A.ck[0]);
-        run_steps(0);
-        adj_save(A.ck[1]);
-        for (int k = 0; k < A.nseg; ++k) {
-            run_steps(std::min(A.K, A.steps - k * A.K));
-            adj_save(A.ck[k + 2]);
+        if (nb_ > 0) {
+            A.lh_pb = adj_arena_.alloc<double>((size_t)nc_ * kBSlots * kHV, "adjoint history");
+            A.Lbody = adj_arena_.alloc<double>((size_t)nb_ * kBL, "adjoint bodies");
+            std::vector<double> cst(5 * (size_t)nb_);
+            for (int b = 0; b < nb_; ++b) {
+                cst[5 * b] = body_mass_[b];
+                cst[5 * b + 1] = body_inertia_[9 * b];
+                cst[5 * b + 2] = body_inertia_[9 * b + 4];
+                cst[5 * b + 3] = body_inertia_[9 * b + 8];
+                cst[5 * b + 4] = (double)body_state_[b];
+            }
+            A.bcst = adj_arena_.upload(cst.data(), cst.size(), "adjoint bodies", stream_);
+            A.brec_host.clear();
+            A.brec_host.reserve((size_t)(steps + 1) * nb_ * kBR);
+            adj_rec_ = &A.brec_host;
         }
+        try {
+            adj_save(A.ck[0]);
+            run_steps(0);
+            adj_save(A.ck[1]);
+            for (int k = 0; k < A.nseg; ++k) {
+                run_steps(std::min(A.K, A.steps - k * A.K));
+                adj_save(A.ck[k + 2]);
+            }
+        } catch (...) {
+            adj_rec_ = nullptr;
+            throw;
+        }
+        adj_rec_ = nullptr;
+        if (nb_ > 0) A.brec = adj_arena_.upload(A.brec_host.data(), A.brec_host.size(), "adjoint bodies", stream_);
         check(cudaStreamSynchronize(stream_), "adjoint forward");
         A.ready = true;
     }
@@ -1494,6 +1579,10 @@ public:
         tp.pw = t.pw + (size_t)sl * A.cap_pw; tp.pw_h = t.pw_h + (size_t)sl * A.cap_pw * kHV; tp.pw_cap = A.cap_pw;
         tp.pw_count = t.pw_cnt + sl;
         tp.overflow = A.overflow;
+        if (t.pb) {
+            tp.pb = t.pb + (size_t)sl * A.cap_pb; tp.pb_tri = t.pb_tri + (size_t)sl * A.cap_pb * kPbTri;
+            tp.pb_h = t.pb_h + (size_t)sl * A.cap_pb * kHV; tp.pb_cap = A.cap_pb; tp.pb_count = t.pb_cnt + sl;
+        }
         return tp;
     }
     // One recomputed force evaluation with its tape in step `sl` of buffer 0.
@@ -1501,9 +1590,13 @@ public:
     {
         Adjoint& A = adj_;
         check(cudaMemsetAsync(A.tb[0].pw_cnt + sl, 0, sizeof(int), stream_), "adjoint tape");
+        if (A.tb[0].pb_cnt) check(cudaMemsetAsync(A.tb[0].pb_cnt + sl, 0, sizeof(int), stream_), "adjoint tape");
         ct64_.tape = adj_tape_step(sl);
         const double dt_eff = step_index_ == 0 ? 0.0 : dt_;
-        forces(dt_eff);
+        const int warp_items = K_.pt_warp_items;
+        K_.pt_warp_items = -1;  // the thread-per-item PT kernel writes the tape
+        forces(dt_eff, false, nb_ > 0 ? kTailTransform : 0u);
+        K_.pt_warp_items = warp_items;
         ct64_.tape = StepTape{};
         ++step_index_;
         check(cudaMemcpyAsync(A.tb[0].pp_cnt + sl, K_.ct_total, sizeof(int), cudaMemcpyDeviceToDevice, stream_),
@@ -1522,6 +1615,9 @@ public:
         tp.pw_count = t.pw_cnt; tp.pp_count = t.pp_cnt;
         tp.overflow = A.overflow;
         tp.slot = t.slot;
+        if (t.pb) {
+            tp.pb = t.pb; tp.pb_tri = t.pb_tri; tp.pb_h = t.pb_h; tp.pb_cap = A.cap_pb; tp.pb_count = t.pb_cnt;
+        }
         return tp;
     }
     // Per buffer: a recomputed, taped step (snapshot, advance, forces,
@@ -1546,32 +1642,45 @@ public:
             check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
             cudaGraphDestroy(g);
         };
+        const int warp_items = K_.pt_warp_items;
+        K_.pt_warp_items = -1;  // the thread-per-item PT kernel writes the tape
         for (int b = 0; b < 2; ++b) {
             AdjTape& t = A.tb[b];
             const StepTape tp = adj_tape_slotted(b);
             cap(t.g_fwd, [&] {
                 launch_adj_snapshot(O_, t.S, stream_, t.slot);
                 launch_advance(O_, dt_, stream_);
-                launch_adj_tape_begin(t.pw_cnt, t.slot, stream_);
+                launch_adj_tape_begin(t.pw_cnt, t.pb_cnt, t.slot, stream_);
+                if (nb_ > 0) launch_adj_body_pose(B_, A.brec, t.base, t.slot, stream_);
                 ct64_.tape = tp;
-                forces(dt_);
+                forces(dt_, false, nb_ > 0 ? kTailTransform : 0u);
                 ct64_.tape = StepTape{};
                 launch_finish(O_, dt_, stream_);
                 launch_adj_tape_end(t.pp_cnt, K_.ct_total, t.slot, stream_);
             });
+            const AdjBodies ab = adj_bodies(t.base);
             for (int p = 0; p < 2; ++p)
                 cap(t.g_rev[p], [&] {
                     launch_adj_slot_add(t.slot, -1, stream_);
-                    launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, t.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T,
-                                    A.lh_pp, A.lh_pw, dt_, dt_, 0, A.grads, S_, sm_count_, stream_);
+                    launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, -1, t.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T,
+                                    A.lh_pp, A.lh_pw, A.lh_pb, ab, dt_, dt_, 0, A.grads, S_, sm_count_, stream_);
                 });
         }
+        K_.pt_warp_items = warp_items;
+    }
+    AdjBodies adj_bodies(const int* base) const
+    {
+        const Adjoint& A = adj_;
+        AdjBodies ab{};
+        ab.nb = nb_ > 0 ? nb_ : 0;
+        ab.rec = A.brec; ab.cst = A.bcst; ab.L = A.Lbody; ab.base = base; ab.local = T_.local; ab.dt = dt_;
+        return ab;
     }
 
     // dem_adjoint_backward: the adjoint of the final positions and velocities
     // in, those of the initial state and of the materials out.
-    void adjoint_backward(const double* dl_dpos, const double* dl_dvel, double* dl_dpos0, double* dl_dvel0,
-                          double* dl_domega0, double* dl_dparams)
+    void adjoint_backward(const double* dl_dpos, const double* dl_dvel, const double* dl_dbc, const double* dl_dbv,
+                          double* dl_dpos0, double* dl_dvel0, double* dl_domega0, double* dl_dparams)
     {
         adj_require();
         Adjoint& A = adj_;
@@ -1581,8 +1690,22 @@ public:
         check(cudaMemsetAsync(A.L, 0, sizeof(double) * kAdjFields * N, s), "adjoint");
         check(cudaMemsetAsync(A.lh_pp, 0, sizeof(double) * (size_t)nc_ * kPSlots * kHV, s), "adjoint");
         check(cudaMemsetAsync(A.lh_pw, 0, sizeof(double) * (size_t)nc_ * kWSlots * kHV, s), "adjoint");
-        check(cudaMemsetAsync(A.grads, 0, sizeof(double) * S_ * 2 * kAdjParams, s), "adjoint");
+        check(cudaMemsetAsync(A.grads, 0, sizeof(double) * S_ * 3 * kAdjParams, s), "adjoint");
         check(cudaMemsetAsync(A.overflow, 0, sizeof(int), s), "adjoint");
+        std::vector<double> lbody(nb_ > 0 ? (size_t)nb_ * kBL : 0, 0.0);
+        if (nb_ > 0) {
+            // the loss's adjoint of the final body centres and velocities
+            // (the pose of the last evaluation), dynamic bodies only
+            for (int b = 0; b < nb_; ++b)
+                for (int a = 0; a < 3; ++a) {
+                    if (body_state_[b] != 0) continue;
+                    if (dl_dbc) lbody[(size_t)b * kBL + kBlC + a] = dl_dbc[3 * b + a];
+                    if (dl_dbv) lbody[(size_t)b * kBL + kBlV + a] = dl_dbv[3 * b + a];
+                }
+            check(cudaMemsetAsync(A.lh_pb, 0, sizeof(double) * (size_t)nc_ * kBSlots * kHV, s), "adjoint");
+            check(cudaMemcpyAsync(A.Lbody, lbody.data(), sizeof(double) * lbody.size(), cudaMemcpyHostToDevice, s),
+                  "adjoint");
+        }
         {
             std::vector<double> h(kAdjFields * N, 0.0);
             for (size_t i = 0; i < N; ++i)
@@ -1593,15 +1716,20 @@ public:
             check(cudaMemcpyAsync(A.L, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s), "adjoint");
             check(cudaStreamSynchronize(s), "adjoint");
         }
-        std::vector<int> npp(A.K + 1), npw(A.K + 1);
+        std::vector<int> npp(A.K + 1), npw(A.K + 1), npb(A.K + 1, 0);
         auto counts = [&](int k) {
             int of = 0;
             check(cudaMemcpyAsync(npp.data(), A.tb[0].pp_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
             check(cudaMemcpyAsync(npw.data(), A.tb[0].pw_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s), "adjoint counts");
+            if (A.tb[0].pb_cnt)
+                check(cudaMemcpyAsync(npb.data(), A.tb[0].pb_cnt, sizeof(int) * k, cudaMemcpyDeviceToHost, s),
+                      "adjoint counts");
             check(cudaMemcpyAsync(&of, A.overflow, sizeof(int), cudaMemcpyDeviceToHost, s), "adjoint counts");
             check(cudaStreamSynchronize(s), "adjoint counts");
             if (of) throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
-            for (int j = 0; j < k; ++j) { npp[j] = std::min(npp[j], A.cap_pp); npw[j] = std::min(npw[j], A.cap_pw); }
+            for (int j = 0; j < k; ++j) {
+                npp[j] = std::min(npp[j], A.cap_pp); npw[j] = std::min(npw[j], A.cap_pw); npb[j] = std::min(npb[j], A.cap_pb);
+            }
         };
         adj_capture();
         // Segment pipeline: the engine stream recomputes segment k - 1 into
@@ -1615,6 +1743,7 @@ public:
             const int ks = std::min(A.K, A.steps - seg * A.K);
             adj_restore(A.ck[seg + 1]);
             check(cudaMemsetAsync(t.slot, 0, sizeof(int), s), "adjoint slot");
+            launch_set_int(t.base, seg * A.K + 1, s);
             for (int sl = 0; sl < ks; ++sl) {
                 check(cudaGraphLaunch(t.g_fwd, s), "adjoint recompute");
                 ++step_index_;
@@ -1648,14 +1777,16 @@ public:
         A.Lp = A.Lb[1 - par];
         // the first evaluation (dt = 0) and the leapfrog start, on tape 0
         adj_restore(A.ck[0]);
+        if (nb_ > 0) launch_adj_body_pose(B_, A.brec, nullptr, nullptr, s);
         adj_tape_forces(0);
         launch_leapfrog_init(O_, 0.5 * dt_, s);
         launch_adj_snapshot(O_, A.tb[0].S, s);
         counts(1);
-        launch_adj_step(C_, O_, d_sc_, W_, adj_tape_step(0), npp[0], npw[0], A.tb[0].S, A.tb[0].S, A.L, A.Lp, A.P, A.T,
-                        A.lh_pp, A.lh_pw, 0.5 * dt_, 0.0, 1, A.grads, S_, sm_count_, s);
+        launch_adj_step(C_, O_, d_sc_, W_, adj_tape_step(0), npp[0], npw[0], npb[0], A.tb[0].S, A.tb[0].S, A.L, A.Lp,
+                        A.P, A.T, A.lh_pp, A.lh_pw, A.lh_pb, adj_bodies(nullptr), 0.5 * dt_, 0.0, 1, A.grads, S_,
+                        sm_count_, s);
         check(cudaGetLastError(), "adjoint backward");
-        std::vector<double> h(kAdjFields * N), g((size_t)S_ * 2 * kAdjParams);
+        std::vector<double> h(kAdjFields * N), g((size_t)S_ * 3 * kAdjParams);
         check(cudaMemcpyAsync(h.data(), A.Lp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s), "adjoint");
         check(cudaMemcpyAsync(g.data(), A.grads, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s), "adjoint");
         check(cudaStreamSynchronize(s), "adjoint");
@@ -1667,10 +1798,10 @@ public:
             }
         if (dl_dparams)
             for (int sc = 0; sc < S_; ++sc) {
-                const MatC* mats[2] = {&scenes_h_[sc].pp, &scenes_h_[sc].pw};
-                for (int c = 0; c < 2; ++c) {
-                    const double* gc = g.data() + ((size_t)sc * 2 + c) * kAdjParams;
-                    double* o = dl_dparams + ((size_t)sc * 2 + c) * kAdjParams;
+                const MatC* mats[3] = {&scenes_h_[sc].pp, &scenes_h_[sc].pw, &scenes_h_[sc].pt};
+                for (int c = 0; c < 3; ++c) {
+                    const double* gc = g.data() + ((size_t)sc * 3 + c) * kAdjParams;
+                    double* o = dl_dparams + ((size_t)sc * 3 + c) * kAdjParams;
                     // kN, mu, epsN (log epsN = logN), epsS, muT, muR
                     o[0] = gc[0]; o[1] = gc[1];
                     o[2] = gc[2] / std::exp(mats[c]->logN);
@@ -1678,8 +1809,10 @@ public:
                     o[4] = gc[4]; o[5] = gc[5];
                 }
             }
-        // leave the engine at the end of the forward run
+        // leave the engine at the end of the forward run (the host keeps the
+        // bodies' end state; their device pose is put back)
         adj_restore(A.ck[A.nseg + 1]);
+        if (nb_ > 0) upload_body_state_async();
         check(cudaStreamSynchronize(s), "adjoint backward");
     }
 
@@ -1709,6 +1842,7 @@ public:
     int n_marks_ = 0;
     DeviceArena arena_, arena_tmp_, adj_arena_;
     Adjoint adj_;
+    std::vector<double>* adj_rec_ = nullptr;  // body records of the forward run, while dem_adjoint_forward runs
     std::vector<double> oin_host_;  // owner principal inertia [n][3] (host copy)
     void* pinned_ = nullptr;
     static constexpr size_t kDiagIntervalOff = 72;  // counters [16] int, error word, then the interval sums
@@ -1989,7 +2123,21 @@ int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every)
 int dem_adjoint_backward(dem_engine* e, const double* dl_dpos, const double* dl_dvel, double* dl_dpos0,
                          double* dl_dvel0, double* dl_domega0, double* dl_dparams)
 {
-    return guarded([&] { NEED(e); e->e.adjoint_backward(dl_dpos, dl_dvel, dl_dpos0, dl_dvel0, dl_domega0, dl_dparams); });
+    return guarded([&] {
+        NEED(e);
+        e->e.adjoint_backward(dl_dpos, dl_dvel, nullptr, nullptr, dl_dpos0, dl_dvel0, dl_domega0, dl_dparams);
+    });
+}
+
+int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double* dl_dvel, const double* dl_dbody_center,
+                             const double* dl_dbody_vel, double* dl_dpos0, double* dl_dvel0, double* dl_domega0,
+                             double* dl_dparams)
+{
+    return guarded([&] {
+        NEED(e);
+        e->e.adjoint_backward(dl_dpos, dl_dvel, dl_dbody_center, dl_dbody_vel, dl_dpos0, dl_dvel0, dl_domega0,
+                              dl_dparams);
+    });
 }
 
 int dem_x_synchronize(dem_engine* e)

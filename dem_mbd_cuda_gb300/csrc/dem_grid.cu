@@ -518,22 +518,28 @@ __global__ void k_tri_place(Tris t, Grid g)
 __device__ __forceinline__ void quat_derivative(double qw, double qx, double qy, double qz, double wx, double wy,
                                                 double wz, double& dw, double& dx, double& dy, double& dz)
 {
-    dw = 0.5 * (-qx * wx - qy * wy - qz * wz);
-    dx = 0.5 * (qw * wx + qy * wz - qz * wy);
-    dy = 0.5 * (qw * wy - qx * wz + qz * wx);
-    dz = 0.5 * (qw * wz + qx * wy - qy * wx);
+    dw = 0.5 * fma(-qz, wz, fma(-qy, wy, -qx * wx));
+    dx = 0.5 * fma(-qz, wy, fma(qy, wz, qw * wx));
+    dy = 0.5 * fma(qz, wx, fma(-qx, wz, qw * wy));
+    dz = 0.5 * fma(-qy, wx, fma(qx, wy, qw * wz));
 }
 // q + quatDerivative(q, w) * h with the derivative's factor 0.5 moved onto
 // h: (0.5 s) h and s (0.5 h) are the same product, so the fused result has
 // the same bits, without the four multiplications by 0.5.
+//
+// The quaternion arithmetic here is written with explicit fma: the kernels
+// that advance quaternions (a step's finish and advance as two kernels, or
+// fused and split around the particle grid) then round alike whatever the
+// compiler would contract in each, so a run split into several calls gives
+// the bits of one call.
 __device__ __forceinline__ void quat_half_step(double& pw, double& px, double& py, double& pz, double wx, double wy,
                                                double wz, double h)
 {
     const double qw = pw, qx = px, qy = py, qz = pz, hh = 0.5 * h;
-    pw += (-qx * wx - qy * wy - qz * wz) * hh;
-    px += (qw * wx + qy * wz - qz * wy) * hh;
-    py += (qw * wy - qx * wz + qz * wx) * hh;
-    pz += (qw * wz + qx * wy - qy * wx) * hh;
+    pw = fma(fma(-qz, wz, fma(-qy, wy, -qx * wx)), hh, pw);
+    px = fma(fma(-qz, wy, fma(qy, wz, qw * wx)), hh, px);
+    py = fma(fma(qz, wx, fma(-qx, wz, qw * wy)), hh, py);
+    pz = fma(fma(-qy, wx, fma(qx, wy, qw * wz)), hh, pz);
 }
 // 1/sqrt(n2) away from |n2 - 1| < 2^-20, and the reference's degenerate case
 // (:170-174); out of line so its FP64 work is issued only by warps that need it.
@@ -545,7 +551,7 @@ __device__ __noinline__ double inv_norm_general(double n2) { return n2 <= 1.0e-2
 // range test reads the exponent of d with integer operations.
 __device__ __forceinline__ void normalize_quat(double& qw, double& qx, double& qy, double& qz)
 {
-    const double n2 = qw * qw + qx * qx + qy * qy + qz * qz;
+    const double n2 = fma(qz, qz, fma(qy, qy, fma(qx, qx, qw * qw)));
     const double d = n2 - 1.0;
     double inv;
     if (((unsigned)__double2hiint(d) & 0x7fffffffu) < 0x3eb00000u) {  // |d| < 2^-20
@@ -582,8 +588,8 @@ __global__ void k_advance(Owners d, double dt)
     d.px[i] += d.vhx[i] * dt;
     d.py[i] += d.vhy[i] * dt;
     d.pz[i] += d.vhz[i] * dt;
-    double qw = d.qw[i] + d.hqw[i] * dt, qx = d.qx[i] + d.hqx[i] * dt;
-    double qy = d.qy[i] + d.hqy[i] * dt, qz = d.qz[i] + d.hqz[i] * dt;
+    double qw = fma(d.hqw[i], dt, d.qw[i]), qx = fma(d.hqx[i], dt, d.qx[i]);
+    double qy = fma(d.hqy[i], dt, d.qy[i]), qz = fma(d.hqz[i], dt, d.qz[i]);
     normalize_quat(qw, qx, qy, qz);
     d.qw[i] = qw; d.qx[i] = qx; d.qy[i] = qy; d.qz[i] = qz;
     d.vx[i] = d.vhx[i] + d.ax[i] * (0.5 * dt);
@@ -609,8 +615,8 @@ __global__ void __launch_bounds__(256) k_advance_rot(Owners d, double dt)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
         if (d.status[i] == -1) continue;
-        double qw = d.qw[i] + d.hqw[i] * dt, qx = d.qx[i] + d.hqx[i] * dt;
-        double qy = d.qy[i] + d.hqy[i] * dt, qz = d.qz[i] + d.hqz[i] * dt;
+        double qw = fma(d.hqw[i], dt, d.qw[i]), qx = fma(d.hqx[i], dt, d.qx[i]);
+        double qy = fma(d.hqy[i], dt, d.qy[i]), qz = fma(d.hqz[i], dt, d.qz[i]);
         normalize_quat(qw, qx, qy, qz);
         d.qw[i] = qw; d.qx[i] = qx; d.qy[i] = qy; d.qz[i] = qz;
         d.vx[i] = d.vhx[i] + d.ax[i] * (0.5 * dt);
@@ -674,7 +680,7 @@ __device__ __forceinline__ void advance_rest_one(Owners d, int i, double dt)
     quat_derivative(pw, px, py, pz, whx, why, whz, hqw, hqx, hqy, hqz);
     d.hqw[i] = hqw; d.hqx[i] = hqx; d.hqy[i] = hqy; d.hqz[i] = hqz;
     if (d.status[i] == -1) return;
-    qw += hqw * dt; qx += hqx * dt; qy += hqy * dt; qz += hqz * dt;
+    qw = fma(hqw, dt, qw); qx = fma(hqx, dt, qx); qy = fma(hqy, dt, qy); qz = fma(hqz, dt, qz);
     normalize_quat(qw, qx, qy, qz);
     d.qw[i] = qw; d.qx[i] = qx; d.qy[i] = qy; d.qz[i] = qz;
     d.vx[i] = d.vhx[i] + d.ax[i] * (0.5 * dt);

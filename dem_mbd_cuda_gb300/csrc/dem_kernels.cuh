@@ -254,7 +254,13 @@ struct StepTape {
     int* overflow;
     int* pp_count;          // particle entries of the step (read by the reverse kernels)
     const int* slot;        // device step index, or null: the pointers are the step's own
+    int4* pb;               // particle-body manifolds: component, body, history index (c * kBSlots + slot), new
+    int* pb_tri;            // [entry][kPbTri]: triangle count, then the triangles (those with an area share)
+    double* pb_h;           // [entry][kHV] history before the step
+    int pb_cap;
+    int* pb_count;
 };
+constexpr int kPbTri = kPbTris + 1;
 
 #ifdef __CUDACC__
 __device__ __forceinline__ StepTape tape_at(StepTape t)
@@ -267,6 +273,12 @@ __device__ __forceinline__ StepTape tape_at(StepTape t)
         t.pw_h += k * t.pw_cap * kHV;
         t.pw_count += k;
         if (t.pp_count) t.pp_count += k;
+        if (t.pb) {
+            t.pb += k * t.pb_cap;
+            t.pb_tri += k * t.pb_cap * kPbTri;
+            t.pb_h += k * t.pb_cap * kHV;
+            t.pb_count += k;
+        }
         t.slot = nullptr;
     }
     return t;
@@ -335,15 +347,33 @@ void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s);
 // (pp_count / pw_count at the device slot) and S, S1 are taken at *tp.slot
 // and *tp.slot + 1 of the snapshot array S.  `grads` holds
 // [nscenes][2][kAdjParams] material gradients (particle, then wall).
+// The rigid bodies of the reverse mode: the forward run's body records
+// ([step][body][39]: the pose the evaluation used, the loads, the state after
+// the half update), constants ([body][5]: mass, principal inertia, state),
+// the adjoints ([body][35]) and the triangles' body-frame records.  The
+// global step of a tape slot is *base + slot (base null: slot 0 is step 0).
+struct AdjBodies {
+    int nb;
+    const double* rec;
+    const double* cst;
+    double* L;
+    const int* base;
+    const double* local;
+    double dt;
+};
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
-                     int npw, const double* S, const double* S1, const double* L, double* Lp, double* P, double* T,
-                     double* lh_pp, double* lh_pw, double dt, double dt_eff, int init, double* grads, int nscenes,
-                     int sm_count, cudaStream_t s);
+                     int npw, int npb, const double* S, const double* S1, const double* L, double* Lp, double* P,
+                     double* T, double* lh_pp, double* lh_pw, double* lh_pb, const AdjBodies& ab, double dt,
+                     double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s);
+// Recompute: the body pose of the tape's step (record *base + *slot; null
+// pointers: record 0) into the engine's body arrays.
+void launch_adj_body_pose(const Bodies& b, const double* rec, const int* base, const int* slot, cudaStream_t s);
+void launch_set_int(int* p, int v, cudaStream_t s);
 // Device step index of a taped segment: add `delta`.
 void launch_adj_slot_add(int* slot, int delta, cudaStream_t s);
 // Before a taped step: zero its wall entry count.  After it: record its
 // particle entry count (the contact total) and move to the next step.
-void launch_adj_tape_begin(int* pw_count, const int* slot, cudaStream_t s);
+void launch_adj_tape_begin(int* pw_count, int* pb_count, const int* slot, cudaStream_t s);
 void launch_adj_tape_end(int* pp_count, const int* ct_total, int* slot, cudaStream_t s);
 
 // The sorted records: geometry (positions only; all the sweep reads), then

@@ -61,6 +61,7 @@ _SIGS = {
     "dem_x_set_launch": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
     "dem_adjoint_forward": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
     "dem_adjoint_backward": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
+    "dem_adjoint_backward_mbd": ([C.c_void_p] + [C.c_void_p] * 8, C.c_int),
 }
 
 
@@ -269,25 +270,30 @@ class CudaDemSolver:
     def adjoint_forward(self, steps, checkpoint_every=100):
         """The reference's step sequence from a fresh engine (first
         evaluation, leapfrog start, `steps` steps) with checkpoints for the
-        reverse sweep (FP64 form, spheres, no bodies)."""
+        reverse sweep (FP64 form, spheres; rigid bodies included)."""
         self._check(self.lib.dem_adjoint_forward(self.h, int(steps), int(checkpoint_every)))
         return self
 
-    def adjoint_backward(self, dl_dpos=None, dl_dvel=None):
+    def adjoint_backward(self, dl_dpos=None, dl_dvel=None, dl_dbody_center=None, dl_dbody_vel=None):
         """Gradient of a scalar loss given its adjoint w.r.t. the final
-        positions / velocities ([n, 3]).  Returns a dict with dl_dpos0,
-        dl_dvel0, dl_domega0 ([n, 3]) and dl_dparams ({"pp": ..., "pw": ...}
-        each {kN, mu, epsN, epsS, muT, muR}; for a batch, a list of those,
-        one per scene)."""
+        positions / velocities ([n, 3]) and, with rigid bodies, the dynamic
+        bodies' final centres / velocities ([nb, 3]).  Returns a dict with
+        dl_dpos0, dl_dvel0, dl_domega0 ([n, 3]) and dl_dparams ({"pp", "pw",
+        "pt"}: each {kN, mu, epsN, epsS, muT, muR}; for a batch, a list of
+        those, one per scene)."""
         n = self.n
-        a = None if dl_dpos is None else np.ascontiguousarray(dl_dpos, dtype=np.float64).reshape(n, 3)
-        b = None if dl_dvel is None else np.ascontiguousarray(dl_dvel, dtype=np.float64).reshape(n, 3)
+
+        def arr(x, rows):
+            return None if x is None else np.ascontiguousarray(x, dtype=np.float64).reshape(rows, 3)
+        a, b = arr(dl_dpos, n), arr(dl_dvel, n)
+        bc, bv = arr(dl_dbody_center, max(self.nb, 1)), arr(dl_dbody_vel, max(self.nb, 1))
         x0, v0, w0 = (np.zeros((n, 3)) for _ in range(3))
-        p = np.zeros(12 * self.scenes)
-        self._check(self.lib.dem_adjoint_backward(self.h, _p(a) if a is not None else None,
-                                                  _p(b) if b is not None else None, _p(x0), _p(v0), _p(w0), _p(p)))
+        p = np.zeros(18 * self.scenes)
+        opt = [None if x is None else _p(x) for x in (a, b, bc, bv)]
+        self._check(self.lib.dem_adjoint_backward_mbd(self.h, *opt, _p(x0), _p(v0), _p(w0), _p(p)))
         keys = ("kN", "mu", "epsN", "epsS", "muT", "muR")
-        per = [{"pp": dict(zip(keys, q[:6])), "pw": dict(zip(keys, q[6:]))} for q in p.reshape(self.scenes, 12)]
+        per = [{"pp": dict(zip(keys, q[:6])), "pw": dict(zip(keys, q[6:12])), "pt": dict(zip(keys, q[12:]))}
+               for q in p.reshape(self.scenes, 18)]
         return {"dl_dpos0": x0, "dl_dvel0": v0, "dl_domega0": w0,
                 "dl_dparams": per[0] if self.scenes == 1 else per}
 

@@ -491,6 +491,47 @@ def small_mbd(n=400, seed=7, dt=2e-5, caps=True, name="small_mbd"):
                  wall_normal=wn, keep_body_particle=1, keep_body_detail=1, name=name)
 
 
+def plate_on_monolayer(nx=4, ny=4, r=2e-3, gap=0.4e-3, plate_mass=0.01, seed=11, vel_std=1e-3, omega_std=2.0,
+                       dt=1e-5, name="plate_on_monolayer"):
+    """A dynamic plate resting on one layer of equal spheres on the floor of
+    a walled box (tests of the rigid-body reverse mode): every sphere under
+    the plate touches it from the first step, with the small overlap the
+    plate's weight needs.  The particle-triangle material has no Coulomb,
+    twisting or rolling cap (mu = 1e20, mu_T = mu_R = 0), so no contact
+    sits on a cap."""
+    rng = np.random.default_rng(seed)
+    g = 9.81
+    pitch = 2 * r + gap
+    xs = (np.arange(nx) - (nx - 1) / 2) * pitch
+    ys = (np.arange(ny) - (ny - 1) / 2) * pitch
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    m1 = DENSITY * 4.0 / 3.0 * np.pi * r ** 3
+    n = nx * ny
+    load = (m1 + plate_mass / n) * g
+    zc = r - load / 1e5          # the floor overlap that carries sphere and plate share
+    pos = np.stack([X.ravel(), Y.ravel(), np.full(n, zc)], axis=1)
+    rad = np.full(n, r)
+    kw = make_spheres(pos, rad, DENSITY, vel=rng.normal(0, vel_std, size=(n, 3)))
+    kw["omega"] = rng.normal(0, omega_std, size=(n, 3))
+    half = (nx * pitch / 2, ny * pitch / 2, 1e-3)
+    plate_v, plate_f = box_mesh(half, (nx, ny, 1))
+    top = zc + r
+    plate_center = [0.0, 0.0, top + half[2] - (plate_mass / n) * g / 1e5]
+    ix = plate_mass * (half[1] ** 2 + half[2] ** 2) / 3
+    iy = plate_mass * (half[0] ** 2 + half[2] ** 2) / 3
+    iz = plate_mass * (half[0] ** 2 + half[1] ** 2) / 3
+    bodies = [dict(vertices=plate_v, faces=plate_f, mass=plate_mass, center=plate_center,
+                   inertia=[ix, 0, 0, 0, iy, 0, 0, 0, iz], state=0)]
+    _attach(kw, bodies)
+    lo = [-half[0] - 5e-3, -half[1] - 5e-3, 0.0]
+    hi = [half[0] + 5e-3, half[1] + 5e-3, 0.05]
+    wo, wn = box_walls(lo, hi)
+    m = mech(kN=1e5, epsN=0.5, epsS=0.6, mu=0.4, muT=0.1, muR=0.05, beta=0.5)
+    mt = mech(kN=1e5, epsN=0.5, epsS=0.6, mu=1e20, muT=0.0, muR=0.0, beta=0.5)
+    return Scene(**kw, pp=m, pt=mt, pw=m, dt=dt, gravity=(0.0, 0.0, -g), gravity_enabled=1, wall_origin=wo,
+                 wall_normal=wn, name=name)
+
+
 def small_dem(n=500, seed=3, dt=1e-5, rmin=1.8e-3, rmax=2.2e-3, vel_std=0.01, omega_std=5.0, muT=0.1, muR=0.05,
               overlap=5e-6, name="small_dem"):
     """A few hundred spheres in a small box with random velocities and spins,

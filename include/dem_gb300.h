@@ -287,9 +287,10 @@ int dem_cell_sort_static(const double* x, const double* y, const double* z,
  * adjoint of each step of the FP64 form: within a step the contact set is
  * the one the forward step found, and at the Coulomb / twisting / rolling
  * caps the derivative is that of the branch taken.  Covers spheres with
- * walls and particle contacts (no rigid bodies), one scene or a batch
- * (dem_initialize_batch), precision DEM_PRECISION_FP64; other engines
- * return DEM_ERR_INVALID.
+ * walls, particle contacts and rigid bodies (particle-triangle manifolds
+ * and the host MBD step of dynamic bodies; prescribed and fixed bodies carry
+ * no adjoint), one scene or a batch (dem_initialize_batch), precision
+ * DEM_PRECISION_FP64; other engines return DEM_ERR_INVALID.
  *
  * dem_adjoint_forward runs the reference's step sequence from a freshly
  * initialized engine: the first evaluation (dt = 0), the leapfrog start and
@@ -299,15 +300,23 @@ int dem_cell_sort_static(const double* x, const double* y, const double* z,
  * the final positions and velocities ([n][3] each, owner order; either may
  * be NULL for zero) and returns its gradient with respect to the initial
  * positions, velocities and angular velocities ([n][3]; NULL to skip) and
- * to the materials (dl_dparams[scenes][2][6]: per scene of the engine,
- * particle-particle then particle-wall, each d/dkN, d/dmu, d/depsN, d/depsS,
- * d/dmuT, d/dmuR; scenes is 1 for dem_initialize).  It recomputes each
- * segment from its checkpoint and leaves the engine at the end of the
- * forward run. */
+ * to the materials (dl_dparams[scenes][3][6]: per scene of the engine,
+ * particle-particle, particle-wall, then particle-triangle, each d/dkN,
+ * d/dmu, d/depsN, d/depsS, d/dmuT, d/dmuR; scenes is 1 for dem_initialize).
+ * It recomputes each segment from its checkpoint and leaves the engine at
+ * the end of the forward run.
+ *
+ * dem_adjoint_backward_mbd adds the loss's adjoint with respect to the
+ * dynamic bodies' final centres and velocities ([nb][3] each, the pose of
+ * the last force evaluation; either may be NULL). */
 int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every);
 int dem_adjoint_backward(dem_engine* e, const double* dl_dpos, const double* dl_dvel,
                          double* dl_dpos0, double* dl_dvel0, double* dl_domega0,
                          double* dl_dparams);
+int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double* dl_dvel,
+                             const double* dl_dbody_center, const double* dl_dbody_vel,
+                             double* dl_dpos0, double* dl_dvel0, double* dl_domega0,
+                             double* dl_dparams);
 
 #ifdef __cplusplus
 }
