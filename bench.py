@@ -290,10 +290,11 @@ def batch_summary(steps, warmup):
 
 
 def adjoint_summary(steps=2000, checkpoint_every=100):
-    """Config 3 (without its plate): reverse-mode gradients of the mean
-    particle height with respect to the materials and the initial velocities.
-    Wall-clock times of a plain FP64 forward run, the checkpointed forward
-    run and the backward run (recompute + reverse sweep)."""
+    """Config 3: reverse-mode gradients of the mean particle height plus the
+    sum of the dynamic plate's final centre coordinates with respect to the
+    materials and the initial velocities.  Wall-clock times of a plain FP64
+    forward run, the checkpointed forward run and the backward run
+    (recompute + reverse sweep)."""
     from dem_mbd_cuda_gb300 import generate as G
     from dem_mbd_cuda_gb300.engine import CudaDemSolver
     scene = G.adjoint_settle()
@@ -312,9 +313,11 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
     t_fwd = time.perf_counter() - t0
     dpos = np.zeros((n, 3))
     dpos[:, 2] = 1.0 / n
+    dplate = np.ones((scene.n_bodies, 3))
     t0 = time.perf_counter()
-    g = e.adjoint_backward(dpos, None)
+    g = e.adjoint_backward(dpos, None, dl_dbody_center=dplate)
     t_bwd = time.perf_counter() - t0
+    plate_final = e.bodies()["center"][0].tolist()
     # finite-difference check at short horizons (FP64 central differences,
     # relative step 1e-6) on the same generator at 2,000 spheres: with many
     # colliding pairs a perturbed run crosses contact-onset steps (jumps of
@@ -322,37 +325,99 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
     # not contain; a smaller bed keeps the differences in the smooth range
     fd = {}
     import dataclasses
-    scene = G.adjoint_settle(n=2000)
-    dpos = np.zeros((scene.n, 3))
-    dpos[:, 2] = 1.0 / scene.n
-    for hor in (50, 200):
+
+    def fd_rows(scene, hor, dpos, dplate, keys):
         ea = CudaDemSolver().initialize(scene, precision="fp64").adjoint_forward(hor, min(checkpoint_every, hor))
-        ga = ea.adjoint_backward(dpos, None)
+        ga = ea.adjoint_backward(dpos, None, dl_dbody_center=dplate)
         del ea
 
-        def loss(sc):
+        def final(sc):
             ef = CudaDemSolver().initialize(sc, precision="fp64")
             ef.run(hor)
-            return ef.downloadParticleState()["pos"][:, 2].mean()
+            return ef.downloadParticleState()["pos"][:, 2], ef.bodies()["center"]
 
         row = {}
-        for cls, key in (("pp", "mu"), ("pp", "kN"), ("pp", "epsN"), ("pw", "mu"), ("pw", "epsN")):
+        for cls, key in keys:
             m = getattr(scene, cls)
             x0 = getattr(m, key)
             h = 1e-6 * abs(x0)
-            sp = dataclasses.replace(scene, **{cls: dataclasses.replace(m, **{key: x0 + h})})
-            sm = dataclasses.replace(scene, **{cls: dataclasses.replace(m, **{key: x0 - h})})
-            f = (loss(sp) - loss(sm)) / (2 * h)
+            zp, cp = final(dataclasses.replace(scene, **{cls: dataclasses.replace(m, **{key: x0 + h})}))
+            zm, cm = final(dataclasses.replace(scene, **{cls: dataclasses.replace(m, **{key: x0 - h})}))
+            # differences taken per particle before the sums (exact for close
+            # values), so the loss's own magnitude adds no rounding
+            f = (float(np.mean(zp - zm)) + float(np.sum(cp - cm))) / (2 * h)
             a = ga["dl_dparams"][cls][key]
             row[f"{cls}.{key}"] = {"adjoint": a, "fd": f, "rel_err": abs(a - f) / max(abs(f), 1e-300)}
-        fd[f"{hor}_steps"] = row
-    return {"workload": "%d spheres r~U[1.8,2.2] mm settling in a 0.1 m box of 5 walls, v0 ~ N(0, 0.05 m/s), "
-                        "%d steps of dt 1e-5, checkpoints every %d; loss = mean height (the config's plate is not "
-                        "covered)" % (n, steps, checkpoint_every),
+        return row
+
+    # the bed without its plate at 50 and 200 steps: the plate lands on the
+    # highest spheres, where the onset and break of its contacts make the
+    # loss jump under a perturbation
+    scene = G.adjoint_settle(n=2000, plate=False)
+    dpos = np.zeros((scene.n, 3))
+    dpos[:, 2] = 1.0 / scene.n
+    for hor in (50, 200):
+        fd[f"{hor}_steps"] = fd_rows(scene, hor, dpos, None, (("pp", "mu"), ("pp", "kN"), ("pp", "epsN"),
+                                                              ("pw", "mu"), ("pw", "epsN")))
+    # the plate term with the plate in contact from the first step: a 10 g
+    # plate resting on 16 spheres (the particle-triangle material without
+    # caps, so that no contact sits on a cap)
+    mono = G.plate_on_monolayer()
+    dmono = np.zeros((mono.n, 3))
+    dmono[:, 2] = 1.0 / mono.n
+    fd["plate_on_monolayer_60_steps"] = fd_rows(mono, 60, dmono, np.ones((1, 3)),
+                                                (("pt", "kN"), ("pt", "epsN"), ("pt", "epsS"), ("pw", "kN")))
+    return {"workload": "%d spheres r~U[1.8,2.2] mm settling in a 0.1 m box of 5 walls, v0 ~ N(0, 0.05 m/s), the "
+                        "config-1 plate (1 kg, dynamic) resting on the bed, %d steps of dt 1e-5, checkpoints every "
+                        "%d; loss = mean particle height + sum of the plate's final centre coordinates"
+                        % (n, steps, checkpoint_every),
             "forward_plain_s": t_plain, "forward_checkpointed_s": t_fwd, "backward_s": t_bwd,
             "adjoint_over_forward": t_bwd / t_plain, "total_over_forward": (t_fwd + t_bwd) / t_plain,
+            "plate_final_center": plate_final,
             "dl_dparams": g["dl_dparams"], "dl_dvel0_norm": float(np.linalg.norm(g["dl_dvel0"])),
             "fd_check": fd}
+
+
+def batch_adjoint_summary(nscenes=64, steps=50, checkpoint_every=10):
+    """Config 4's batched reverse mode on the first `nscenes` scenes of the
+    256-scene generator, over a bounded window: the gradients of the sum of
+    the scenes' mean bed heights with respect to every scene's own materials
+    and initial velocities, from one backward run over the batch.  The tapes
+    and checkpoints of all 256 scenes over the config's 3,000 steps do not fit
+    the GPU's memory (about 8.9 kB per sphere per checkpoint, 2.2 kB per
+    sphere per taped step), so the window is bounded; the ratio is per step."""
+    from dem_mbd_cuda_gb300.engine import CudaDemSolver
+    scenes = make_scene("c4")[0][:nscenes]
+    n = sum(sc.n for sc in scenes)
+    plain = CudaDemSolver().initialize(scenes, precision="fp64")
+    plain.run(0)
+    plain.synchronize()
+    t0 = time.perf_counter()
+    plain.run(steps)
+    plain.synchronize()
+    t_plain = time.perf_counter() - t0
+    del plain
+    e = CudaDemSolver().initialize(scenes, precision="fp64")
+    t0 = time.perf_counter()
+    e.adjoint_forward(steps, checkpoint_every)
+    t_fwd = time.perf_counter() - t0
+    dpos = np.zeros((n, 3))
+    off = 0
+    for sc in scenes:
+        dpos[off:off + sc.n, 2] = 1.0 / sc.n
+        off += sc.n
+    t0 = time.perf_counter()
+    g = e.adjoint_backward(dpos, None)
+    t_bwd = time.perf_counter() - t0
+    del e
+    per = g["dl_dparams"]
+    return {"workload": "the first %d scenes of the 256-scene batch (%d spheres), %d steps of dt 1e-5, checkpoints "
+                        "every %d; loss = sum over scenes of the mean bed height" % (nscenes, n, steps,
+                                                                                    checkpoint_every),
+            "forward_plain_s": t_plain, "forward_checkpointed_s": t_fwd, "backward_s": t_bwd,
+            "adjoint_over_forward": t_bwd / t_plain, "total_over_forward": (t_fwd + t_bwd) / t_plain,
+            "per_scene_pp_dmu": [p["pp"]["mu"] for p in per[:4]],
+            "per_scene_pp_depsN": [p["pp"]["epsN"] for p in per[:4]]}
 
 
 def autotune_summary(scene, precision):
@@ -473,6 +538,7 @@ def main():
     if args.config != "c4" and not args.no_batch:
         batch = batch_summary(args.steps, args.warmup)
     adjoint = None if args.no_adjoint else adjoint_summary()
+    adjoint_batch = None if args.no_adjoint or args.no_batch else batch_adjoint_summary()
     tuned = None if args.no_autotune else autotune_summary(scene, args.precision)
     nb = scene.n_bodies
     line = {
@@ -514,6 +580,8 @@ def main():
         line["batch_256"] = batch
     if adjoint:
         line["adjoint_c3"] = adjoint
+    if adjoint_batch:
+        line["adjoint_batch"] = adjoint_batch
     if tuned:
         line["autotuned"] = tuned
     print(json.dumps(line))

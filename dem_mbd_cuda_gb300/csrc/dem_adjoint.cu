@@ -566,25 +566,43 @@ void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s)
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
                      int npw, int npb, const double* S, const double* S1, const double* L, double* Lp, double* P,
                      double* T, double* lh_pp, double* lh_pw, double* lh_pb, const AdjBodies& ab, double dt,
-                     double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s)
+                     double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s,
+                     cudaStream_t s2, cudaEvent_t* ev)
 {
     if (o.n <= 0) return;
     // device counts: S, S1 at the tape's slot, fixed grid-stride grids
     const int* slot = (npp < 0 || npw < 0) ? tp.slot : nullptr;
     const bool bodies = ab.nb > 0 && tp.pb;
-    if (bodies) k_adj_body_a<<<nblocks(ab.nb, 32), 32, 0, s>>>(ab, slot, init);
+    // with bodies and a second stream, a DAG: the body leapfrog's reverse
+    // and the manifolds' run beside the owners' finish and the contacts
+    // (each a chain of dependent FP64 work on a few threads)
+    const bool fork = bodies && s2 && ev;
+    cudaStream_t sb = fork ? s2 : s;
+    if (fork) {
+        cudaEventRecord(ev[0], s);
+        cudaStreamWaitEvent(s2, ev[0], 0);
+    }
+    if (bodies) k_adj_body_a<<<nblocks(ab.nb, 32), 32, 0, sb>>>(ab, slot, init);
     k_adj_finish<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init, slot);
+    if (fork) {
+        cudaEventRecord(ev[1], s);
+        cudaStreamWaitEvent(s2, ev[1], 0);
+    }
+    if (bodies) {
+        const int bpb = npb < 0 ? sm_count * 2 : min(nblocks(npb, 64), sm_count * 2);
+        if (bpb > 0) k_adj_pt<<<bpb, 64, 0, sb>>>(c, o, sc, tp, npb, P, T, lh_pb, ab, dt_eff, grads, nscenes);
+        if (!init) k_adj_body_c<<<nblocks(ab.nb, 32), 32, 0, sb>>>(ab, slot);
+    }
     const int bpp = npp < 0 ? sm_count * 8 : min(nblocks(npp, 128), sm_count * 8);
     const int bpw = npw < 0 ? sm_count * 2 : min(nblocks(npw, 128), sm_count * 2);
     if (bpp + bpw > 0)
         k_adj_contacts<<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff, grads,
                                                  nscenes);
-    if (bodies) {
-        const int bpb = npb < 0 ? sm_count * 2 : min(nblocks(npb, 64), sm_count * 2);
-        if (bpb > 0) k_adj_pt<<<bpb, 64, 0, s>>>(c, o, sc, tp, npb, P, T, lh_pb, ab, dt_eff, grads, nscenes);
+    if (fork) {
+        cudaEventRecord(ev[2], s2);
+        cudaStreamWaitEvent(s, ev[2], 0);
     }
     k_adj_advance<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, P, T, Lp, dt, init, slot);
-    if (bodies && !init) k_adj_body_c<<<nblocks(ab.nb, 32), 32, 0, s>>>(ab, slot);
 }
 void launch_adj_body_pose(const Bodies& b, const double* rec, const int* base, const int* slot, cudaStream_t s)
 {

@@ -1129,6 +1129,7 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
     const int step = *k.step;
     const int total = *ct.pt_ctotal_ptr;
     if (total > k.pt_warp_items) return;
+    const StepTape tape = tape_at(ct.tape);
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     int bover = 0, bhigh = 0;
@@ -1182,9 +1183,12 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
                 return tris.body[tri] == b && pt_may_touch(tris.tf, tri, pq);
             };
             const int span = listed ? ncand : te - tb;
-            // pass 1: manifold sums (:1154-1183)
+            // pass 1: manifold sums (:1154-1183); the triangles with a share
+            // are kept in order for the adjoint tape
             double tot = 0.0, wd = 0.0;
             V3<double> wn = mk(0.0, 0.0, 0.0), wc = mk(0.0, 0.0, 0.0);
+            int ttri[kPbTris];
+            int tn = 0;
             for (int k0 = 0; k0 < span; k0 += 32) {
                 double as = 0.0, dist = 0.0;
                 int tri = 0;
@@ -1197,7 +1201,12 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
                     const int src = __ffs(msk) - 1;
                     msk &= msk - 1;
                     const double a_ = __shfl_sync(FULL, as, src), d_ = __shfl_sync(FULL, dist, src);
-                    const double* W = tris.world + 16 * (size_t)__shfl_sync(FULL, tri, src);
+                    const int t_ = __shfl_sync(FULL, tri, src);
+                    if (tape.pb) {
+                        if (tn < kPbTris) ttri[tn] = t_;
+                        ++tn;
+                    }
+                    const double* W = tris.world + 16 * (size_t)t_;
                     const V3<double> out = mk(W[12], W[13], W[14]);
                     const V3<double> ce = it.p - out * d_;
                     tot += a_;
@@ -1211,7 +1220,8 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
             const V3<double> mc = wc * (1.0 / tot);
             const double md = wd / tot;
             int slot = 0;
-            if (lane == 0) slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh);
+            bool fresh = false;
+            if (lane == 0) slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh, &fresh);
             slot = __shfl_sync(FULL, slot, 0);
             bhw = __shfl_sync(FULL, bhw, 0);
             if (slot < 0) {
@@ -1221,6 +1231,7 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
             T* hv = hb.val + ((size_t)ci * kBSlots + slot) * kHV;
             T h[9];
             hv_load(hv, h);
+            if (tape.pb && lane == 0) tape_pb(tape, ci, b, slot, fresh, h, ttri, tn, false);
             const PtBody bd = pt_body(bodies, b);
             const MatC& m = S.pt;
             bool slide = false, twist = false;

@@ -1593,10 +1593,7 @@ public:
         if (A.tb[0].pb_cnt) check(cudaMemsetAsync(A.tb[0].pb_cnt + sl, 0, sizeof(int), stream_), "adjoint tape");
         ct64_.tape = adj_tape_step(sl);
         const double dt_eff = step_index_ == 0 ? 0.0 : dt_;
-        const int warp_items = K_.pt_warp_items;
-        K_.pt_warp_items = -1;  // the thread-per-item PT kernel writes the tape
         forces(dt_eff, false, nb_ > 0 ? kTailTransform : 0u);
-        K_.pt_warp_items = warp_items;
         ct64_.tape = StepTape{};
         ++step_index_;
         check(cudaMemcpyAsync(A.tb[0].pp_cnt + sl, K_.ct_total, sizeof(int), cudaMemcpyDeviceToDevice, stream_),
@@ -1642,8 +1639,6 @@ public:
             check(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
             cudaGraphDestroy(g);
         };
-        const int warp_items = K_.pt_warp_items;
-        K_.pt_warp_items = -1;  // the thread-per-item PT kernel writes the tape
         for (int b = 0; b < 2; ++b) {
             AdjTape& t = A.tb[b];
             const StepTape tp = adj_tape_slotted(b);
@@ -1663,10 +1658,10 @@ public:
                 cap(t.g_rev[p], [&] {
                     launch_adj_slot_add(t.slot, -1, stream_);
                     launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, -1, t.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T,
-                                    A.lh_pp, A.lh_pw, A.lh_pb, ab, dt_, dt_, 0, A.grads, S_, sm_count_, stream_);
+                                    A.lh_pp, A.lh_pw, A.lh_pb, ab, dt_, dt_, 0, A.grads, S_, sm_count_, stream_,
+                                    branch_[0], fork_ev_.data());
                 });
         }
-        K_.pt_warp_items = warp_items;
     }
     AdjBodies adj_bodies(const int* base) const
     {

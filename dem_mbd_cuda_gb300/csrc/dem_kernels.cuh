@@ -343,10 +343,6 @@ void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
 // Owner-state snapshots [29][n]; with `slot`, into S + *slot * 29 n.
 void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s, const int* slot = nullptr);
 void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s);
-// One reverse step.  npp / npw < 0: the counts are the tape's own
-// (pp_count / pw_count at the device slot) and S, S1 are taken at *tp.slot
-// and *tp.slot + 1 of the snapshot array S.  `grads` holds
-// [nscenes][2][kAdjParams] material gradients (particle, then wall).
 // The rigid bodies of the reverse mode: the forward run's body records
 // ([step][body][39]: the pose the evaluation used, the loads, the state after
 // the half update), constants ([body][5]: mass, principal inertia, state),
@@ -361,10 +357,16 @@ struct AdjBodies {
     const double* local;
     double dt;
 };
+// One reverse step.  npp / npw / npb < 0: the counts are the tape's own
+// (at the device slot) and S, S1 are taken at *tp.slot and *tp.slot + 1 of
+// the snapshot array S.  `grads` holds [nscenes][3][kAdjParams] material
+// gradients (particle, wall, triangle).  With rigid bodies, s2 and three
+// events make the step a DAG (the bodies' reverse beside the owners').
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
                      int npw, int npb, const double* S, const double* S1, const double* L, double* Lp, double* P,
                      double* T, double* lh_pp, double* lh_pw, double* lh_pb, const AdjBodies& ab, double dt,
-                     double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s);
+                     double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s,
+                     cudaStream_t s2 = nullptr, cudaEvent_t* ev = nullptr);
 // Recompute: the body pose of the tape's step (record *base + *slot; null
 // pointers: record 0) into the engine's body arrays.
 void launch_adj_body_pose(const Bodies& b, const double* rec, const int* base, const int* slot, cudaStream_t s);

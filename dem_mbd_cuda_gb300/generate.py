@@ -451,14 +451,27 @@ def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5, settled=False)
     return out
 
 
-def adjoint_settle(n=50000, seed=1003, dt=1e-5, vel_std=0.05, name="c3_adjoint"):
-    """Config 3 without its plate: spheres r ~ U[1.8, 2.2] mm on a lattice in
-    a 0.1 m box of 5 walls (open top, walls 0.6 m high), seeded normal
-    initial velocities (std 0.05 m/s); the bed settles during the run."""
+def adjoint_settle(n=50000, seed=1003, dt=1e-5, vel_std=0.05, plate=True, name="c3_adjoint"):
+    """Config 3: spheres r ~ U[1.8, 2.2] mm on a lattice in a 0.1 m box of 5
+    walls (open top, walls 0.6 m high), seeded normal initial velocities (std
+    0.05 m/s); the bed settles during the run.  With ``plate`` the config-1
+    plate (1 kg, 100 x 100 x 4 mm, 192 triangles, inertia 1e-3 I, dynamic)
+    rests on the highest sphere, centred over the box."""
     sc = pure_dem(n=n, seed=seed, box=(0.1, 0.1, 0.6), dt=dt, name=name, fill_width=True)
     rng = np.random.default_rng(seed + 1)
     sc.vel = rng.normal(0.0, vel_std, size=sc.vel.shape)
-    return sc
+    if not plate:
+        return sc
+    kw = {f: getattr(sc, f) for f in ("owner_id", "owner_status", "owner_mass", "owner_radius", "owner_inertia", "pos",
+                                      "vel", "omega", "quat")}
+    half = (0.05, 0.05, 0.002)
+    plate_v, plate_f = box_mesh(half, (6, 6, 1))
+    top = float((sc.pos[:, 2] + sc.owner_radius).max())
+    bodies = [dict(vertices=plate_v, faces=plate_f, mass=1.0, center=[0.0, 0.0, top + half[2] - 2e-7],
+                   inertia=[1e-3, 0, 0, 0, 1e-3, 0, 0, 0, 1e-3], state=0)]
+    _attach(kw, bodies)
+    return Scene(**kw, pp=sc.pp, pt=sc.pw, pw=sc.pw, dt=sc.dt, gravity=sc.gravity, gravity_enabled=sc.gravity_enabled,
+                 wall_origin=sc.wall_origin, wall_normal=sc.wall_normal, name=name)
 
 
 def small_mbd(n=400, seed=7, dt=2e-5, caps=True, name="small_mbd"):
