@@ -326,7 +326,7 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
     fd = {}
     import dataclasses
 
-    def fd_rows(scene, hor, dpos, dplate, keys):
+    def fd_rows(scene, hor, dpos, dplate, keys, rel=1e-6):
         ea = CudaDemSolver().initialize(scene, precision="fp64").adjoint_forward(hor, min(checkpoint_every, hor))
         ga = ea.adjoint_backward(dpos, None, dl_dbody_center=dplate)
         del ea
@@ -340,7 +340,7 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
         for cls, key in keys:
             m = getattr(scene, cls)
             x0 = getattr(m, key)
-            h = 1e-6 * abs(x0)
+            h = rel * abs(x0)
             zp, cp = final(dataclasses.replace(scene, **{cls: dataclasses.replace(m, **{key: x0 + h})}))
             zm, cm = final(dataclasses.replace(scene, **{cls: dataclasses.replace(m, **{key: x0 - h})}))
             # differences taken per particle before the sums (exact for close
@@ -361,12 +361,13 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
                                                               ("pw", "mu"), ("pw", "epsN")))
     # the plate term with the plate in contact from the first step: a 10 g
     # plate resting on 16 spheres (the particle-triangle material without
-    # caps, so that no contact sits on a cap)
+    # caps, so that no contact sits on a cap); its gradients are small, so a
+    # relative step of 1e-5 keeps the differences above FP64's resolution
     mono = G.plate_on_monolayer()
     dmono = np.zeros((mono.n, 3))
     dmono[:, 2] = 1.0 / mono.n
     fd["plate_on_monolayer_60_steps"] = fd_rows(mono, 60, dmono, np.ones((1, 3)),
-                                                (("pt", "kN"), ("pt", "epsN"), ("pt", "epsS"), ("pw", "kN")))
+                                                (("pt", "kN"), ("pt", "epsN"), ("pt", "epsS"), ("pw", "kN")), rel=1e-5)
     return {"workload": "%d spheres r~U[1.8,2.2] mm settling in a 0.1 m box of 5 walls, v0 ~ N(0, 0.05 m/s), the "
                         "config-1 plate (1 kg, dynamic) resting on the bed, %d steps of dt 1e-5, checkpoints every "
                         "%d; loss = mean particle height + sum of the plate's final centre coordinates"
@@ -441,6 +442,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the embedded config-3 adjoint summary")
     ap.add_argument("--no-autotune", action="store_true", help="skip the embedded autotuner summary")
     ap.add_argument("--adjoint-only", action="store_true", help="print the config-3 adjoint summary alone")
+    ap.add_argument("--adjoint-batch", type=int, default=None, metavar="SCENES",
+                    help="print the batched adjoint summary alone, on the first SCENES scenes, over --steps steps")
     ap.add_argument("--particles", type=int, default=None,
                     help="particle count of the generated scene (profiling captures of a smaller case)")
     ap.add_argument("--single", action="store_true",
@@ -455,10 +458,13 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    if args.adjoint_only:
+    if args.adjoint_only or args.adjoint_batch:
         from dem_mbd_cuda_gb300 import build as _b
         _b.build()
-        print(json.dumps(adjoint_summary()))
+        if args.adjoint_batch:
+            print(json.dumps(batch_adjoint_summary(args.adjoint_batch, args.steps, min(10, args.steps))))
+        else:
+            print(json.dumps(adjoint_summary()))
         return
     scene, desc = make_scene(args.config, args.particles)
     if isinstance(scene, list) and not args.single:
