@@ -197,9 +197,10 @@ __device__ __forceinline__ V3<float> rot_ivf(float qw, float qx, float qy, float
 // The records in sorted order, in two parts: the geometry (positions,
 // cells, indices: all the sweep reads, available once the positions are)
 // and the velocities (after the rotational advance).
-__global__ void k_gather_geom(Comps c, Owners o, Grid g, Recs r)
+__global__ void k_gather_geom(Comps c, Owners o, Grid g, Recs r, Counters k)
 {
     const int nvalid = *g.nvalid;
+    bool moved = false;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
         const int ci = g.sorted_id[t];
         const int w = c.owner[ci];
@@ -214,7 +215,14 @@ __global__ void k_gather_geom(Comps c, Owners o, Grid g, Recs r)
         const double mesh = g.sc[s].mesh;
         r.relf[t] = make_float4(f32_rn(__fma_rn(-(double)cx, mesh, x)), f32_rn(__fma_rn(-(double)cy, mesh, y)),
                                 f32_rn(__fma_rn(-(double)cz, mesh, z)), f32_rn(rad));
+        if (k.nl_on) {
+            // moved more than half the skin since the lists' build
+            const double* xr = k.nl_xref + 3 * (size_t)ci;
+            const double dx = x - xr[0], dy = y - xr[1], dz = z - xr[2];
+            moved |= dx * dx + dy * dy + dz * dz > g.sc[s].nl_half2;
+        }
     }
+    if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) k.nl_flag[0] = 1;
 }
 
 template <typename T> __global__ void k_gather_vel(Comps c, Owners o, Grid g, Recs r, double dt_eff)
@@ -415,6 +423,79 @@ __device__ __noinline__ bool exact_contact(const D4* __restrict__ pos, const int
     return true;
 }
 
+// The sweep of one component from its neighbour list (the pairs within
+// r_i + r_j + skin at the list's build, no component having moved half the
+// skin since): each listed partner's cell is adjacent, and the same FP32
+// test and exact FP64 test as the cell sweep decide the contact.  The
+// contacts are then taken in the cell sweep's order (column (dx, dy), then
+// sorted position), so the slots, the list and every sum come out as the
+// cell sweep's.  Returns the contact count; stage_t / stage_s as k_sweep.
+template <typename T>
+__device__ int sweep_list_one(const Grid& g, const Recs& r, const SceneC* __restrict__ sc, Hist<T> hp, Counters k,
+                              int t, int nvalid, int step, int* stage_t, int* stage_s, int& pover, int& phigh)
+{
+    const int4 meta = r.meta[t];
+    const int ci = meta.x, owner = meta.y, s = meta.w;
+    const int4 cell = r.cell[t];
+    const D4 pi = r.pos[t];
+    const float4 fi = r.relf[t];
+    const float mesh_f = sc[s].mesh_f, margin_f = sc[s].margin_f;
+    const float offx[3] = {-mesh_f - fi.x, -fi.x, mesh_f - fi.x};
+    const float offy[3] = {-mesh_f - fi.y, -fi.y, mesh_f - fi.y};
+    const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
+    expire(hp, kPSlots, ci, step);
+    int phw = hp.hw[ci];
+    const int nn = min(k.nl_cnt[ci], kNL);
+    const int* L = k.nl_idx + (size_t)ci * kNL;
+    int fkey[kNL], fcid[kNL];
+    int found = 0;
+    for (int q = 0; q < nn; ++q) {
+        const int j = L[q];
+        const int u = g.pos_of[j];
+        if (u < 0 || u >= nvalid) continue;
+        const int4 mj = r.meta[u];
+        if (mj.x != j) continue;  // not in this step's grid
+        const int4 cj = r.cell[u];
+        const int dx = cj.x - cell.x, dy = cj.y - cell.y, dz = cj.z - cell.z;
+        if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;
+        const float4 fj = r.relf[u];
+        const float ddx = fj.x + offx[dx + 1], ddy = fj.y + offy[dy + 1], ddz = fj.z + offz[dz + 1];
+        const float rsf = fj.w + fi.w + margin_f;
+        const float dd2 = ddx * ddx + ddy * ddy + ddz * ddz;
+        if (dd2 >= rsf * rsf) continue;
+        const float rin = rsf - 2.f * margin_f;
+        int cid;
+        if (dd2 < rin * rin && dd2 > 4.f * margin_f * margin_f) {
+            if (mj.y == owner) continue;
+            cid = mj.z;
+        } else if (!exact_contact(r.pos, r.meta, u, owner, pi.x, pi.y, pi.z, pi.w, cid)) {
+            continue;
+        }
+        // insert in the cell sweep's order: column, then sorted position
+        const int key = ((dx + 1) * 3 + (dy + 1)) * (1 << 27) + u;
+        int at = found++;
+        while (at > 0 && fkey[at - 1] > key) {
+            fkey[at] = fkey[at - 1];
+            fcid[at] = fcid[at - 1];
+            --at;
+        }
+        fkey[at] = key;
+        fcid[at] = cid;
+    }
+    int count = 0;
+    for (int q = 0; q < found; ++q) {
+        if (count >= kMaxContacts) { ++pover; continue; }
+        bool fresh;
+        const int slot = acquire(hp, kPSlots, ci, (uint64_t)(uint32_t)fcid[q] + 1ull, step, phw, phigh, &fresh);
+        if (slot < 0) { ++pover; continue; }
+        stage_t[count] = fkey[q] & ((1 << 27) - 1);
+        stage_s[count] = slot | (fresh ? 0x100 : 0);
+        ++count;
+    }
+    hp.hw[ci] = phw;
+    return count;
+}
+
 // One thread per component in cell order: the reference's 27-cell sweep
 // (:1124-1146) over the cell start table, in the reference's order (dx, dy,
 // dz ascending; members of a cell in ascending component order).  For each
@@ -430,6 +511,10 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
 {
     const int step = *k.step;
     const int nvalid = *g.nvalid;
+    // neighbour lists: this step sweeps the lists, or sweeps the cells and
+    // rebuilds them (kNL partners within r_i + r_j + skin per component)
+    const bool from_lists = k.nl_on && *k.nl_flag == 0;
+    const bool build = k.nl_on && !from_lists;
     int pover = 0, phigh = 0, found = 0;
     // grid-stride over blocks of sorted positions: the launch may use fewer
     // blocks than positions so that the kernels beside it find free slots
@@ -439,7 +524,11 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     int stage_t[kCandidates];
     int stage_s[kMaxContacts];
     int ci = -1;
-    if (t < nvalid) {
+    if (t < nvalid && from_lists) {
+        ci = r.meta[t].x;
+        count = sweep_list_one(g, r, sc, hp, k, t, nvalid, step, stage_t, stage_s, pover, phigh);
+        ct.cnt[ci] = count;
+    } else if (t < nvalid) {
         const int4 meta = r.meta[t];
         ci = meta.x;
         const int owner = meta.y, s = meta.w;
@@ -452,6 +541,9 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         const float offy[3] = {-mesh_f - fi.y, -fi.y, mesh_f - fi.y};
         const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
         const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
+        const float skin_f = sc[s].skin_f;
+        int* nl = build ? k.nl_idx + (size_t)ci * kNL : nullptr;
+        int nlist = 0;
         // expireHistory (:1109-1117) for the component's particle slots,
         // before any slot of this step is acquired (the wall and body slots
         // expire in their own probes)
@@ -517,6 +609,13 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
                         const float ddx = fj[q].x + ox, ddy = fj[q].y + oy, ddz = fj[q].z + oz;
                         const float rsf = fj[q].w + fi.w + margin_f;
                         const float dd2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        if (build && u != t) {
+                            const float rsb = rsf + skin_f;
+                            if (dd2 < rsb * rsb) {
+                                if (nlist < kNL) nl[nlist] = r.meta[u].x;
+                                ++nlist;
+                            }
+                        }
                         if (dd2 >= rsf * rsf) continue;
                         const float rin = rsf - 2.f * margin_f;
                         const bool certain = dd2 < rin * rin && dd2 > 4.f * margin_f * margin_f;
@@ -530,6 +629,12 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         exact_pass();
         hp.hw[ci] = phw;
         ct.cnt[ci] = count;
+        if (build) {
+            k.nl_cnt[ci] = min(nlist, kNL);
+            if (nlist > kNL) k.nl_flag[1] = 1;
+            double* xr = k.nl_xref + 3 * (size_t)ci;
+            xr[0] = pi.x; xr[1] = pi.y; xr[2] = pi.z;
+        }
     }
     // the warp's contacts take one range of the flat list (no block barrier:
     // a warp that finishes its candidates early goes on to its next pass)
@@ -1622,9 +1727,9 @@ void launch_gather_vel(const Comps& c, const Owners& o, const Grid& g, const Rec
 }
 
 void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, int bps,
-                        cudaStream_t s)
+                        const Counters& k, cudaStream_t s)
 {
-    k_gather_geom<<<sm_count * bps, 256, 0, s>>>(c, o, g, r);
+    k_gather_geom<<<sm_count * bps, 256, 0, s>>>(c, o, g, r, k);
 }
 
 template <typename T, typename TB>

@@ -85,7 +85,7 @@ constexpr int kDefaultPtWarpItems = 3072;
 // register-limited residency: that grid leaves nothing beside it and was
 // the slowest setting on the 2M drum.
 constexpr int kSmallScene = 500000;
-constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 8;
+constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 16;
 // The gathers and the particle law, likewise (blocks of 256 per SM).
 constexpr int kGatherBlocksSmall = 2, kGatherBlocksLarge = 8;
 constexpr int kDefaultPpBlocksPerSm = 16;
@@ -247,6 +247,7 @@ public:
             S.mesh_f = (float)S.mesh;
             S.margin_f = (float)(1.0e-5 * S.mesh);
             S.inv_mesh_f = (float)S.inv_mesh;
+            set_skin(S);
             for (int a = 0; a < 3; ++a) S.g[a] = x.gravity[a];
             S.grav = x.gravity_enabled ? 1 : 0;
             S.wall_begin = (int)wo.size() / 3;
@@ -498,6 +499,16 @@ public:
         K_.sweep_bps = nt_ == 0 ? 0 : (nc_ <= kSmallScene ? kSweepBlocksSmall : kSweepBlocksLarge);
         K_.gather_bps = nc_ <= kSmallScene ? kGatherBlocksSmall : kGatherBlocksLarge;
         K_.pp_bps = kDefaultPpBlocksPerSm;
+        // neighbour lists (set_launch 3 turns them off)
+        K_.nl_on = 1;
+        K_.nl_flag = arena_.alloc<int>(2, "neighbour lists");
+        K_.nl_cnt = arena_.alloc<int>(nc_, "neighbour lists");
+        K_.nl_idx = arena_.alloc<int>((size_t)nc_ * kNL, "neighbour lists");
+        K_.nl_xref = arena_.alloc<double>(3 * (size_t)nc_, "neighbour lists");
+        // no list yet: counts 0, build positions far away (about 1.4e306 m)
+        check(cudaMemsetAsync(K_.nl_cnt, 0, sizeof(int) * nc_, s), "neighbour lists");
+        check(cudaMemsetAsync(K_.nl_xref, 0x7f, sizeof(double) * 3 * (size_t)nc_, s), "neighbour lists");
+        nl_request_rebuild();
 
         // ---- scene constants
         scenes_h_ = sc;
@@ -654,7 +665,7 @@ public:
             mark();
             if (pt) launch_tri_build(T_, B_, G_, K_.tgover, sm_count_, s);
             if (O_.ugx) launch_universal_gravity(O_, s);
-            launch_gather_geom(C_, O_, G_, R_, sm_count_, K_.gather_bps, s);
+            launch_gather_geom(C_, O_, G_, R_, sm_count_, K_.gather_bps, K_, s);
             launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, K_.gather_bps, s);
             mark();
             for (int stage : {2, 1, 4, 8}) {
@@ -708,7 +719,7 @@ public:
         }
         launch_grid_sort(C_, O_, G_, sm_count_, s);
         if (O_.ugx) launch_universal_gravity(O_, s);
-        launch_gather_geom(C_, O_, G_, R_, sm_count_, K_.gather_bps, s);
+        launch_gather_geom(C_, O_, G_, R_, sm_count_, K_.gather_bps, K_, s);
         if (pt) {
             // PT reads the geometry records and the owner state itself
             link(s, bt, 2);
@@ -748,6 +759,22 @@ public:
             enqueue_forces<double, double>(dt_eff, hp64_, hw64_, hb64_, ct64_, timed, tail);
         }
         check(cudaGetLastError(), "force pipeline launch");
+    }
+
+    // The neighbour lists' skin of a scene: a share of the room the cell edge
+    // leaves beyond the largest pair (r_i + r_j + skin stays within the edge,
+    // so the 27 cells of the build sweep hold every pair to list).
+    void set_skin(SceneC& S) const
+    {
+        const double room = std::max(0.0, S.mesh - 2.0 * S.pad);
+        const double skin = nl_skin_frac_ * room * (1.0 - 1e-6);
+        S.skin_f = (float)skin;
+        S.nl_half2 = 0.25 * skin * skin;
+    }
+    void nl_request_rebuild()
+    {
+        check(cudaMemsetAsync(K_.nl_flag, 0x01, sizeof(int), stream_), "neighbour lists");
+        check(cudaMemsetAsync(K_.nl_flag + 1, 0, sizeof(int), stream_), "neighbour lists");
     }
 
     double* pin_body_state() { return static_cast<double*>(pinned_); }
@@ -1087,7 +1114,17 @@ public:
         if (what == 0) K_.sweep_bps = std::max(0, n);
         else if (what == 1) K_.gather_bps = std::max(1, n);
         else if (what == 2) K_.pp_bps = std::max(0, n);
-        else throw DemError(DEM_ERR_INVALID, "unknown launch setting");
+        else if (what == 3) {
+            K_.nl_on = n ? 1 : 0;
+            nl_request_rebuild();
+        } else if (what == 4) {
+            // the skin as a share (per mille) of the room the cells leave
+            nl_skin_frac_ = std::min(1000, std::max(0, n)) * 1e-3;
+            for (SceneC& S : scenes_h_) set_skin(S);
+            check(cudaMemcpy(d_sc_, scenes_h_.data(), sizeof(SceneC) * scenes_h_.size(), cudaMemcpyHostToDevice),
+                  "scene constants");
+            nl_request_rebuild();
+        } else throw DemError(DEM_ERR_INVALID, "unknown launch setting");
         for (cudaGraphExec_t& g : graphs_)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         adj_release_graphs();
@@ -1823,6 +1860,7 @@ public:
     int precision_ = 0, block_ = 128, sm_count_ = 0;
     bool pt_fp32_ = false;
     double cell_factor_ = 2.5, mesh_ = 0.0, max_radius_ = 0.0, dt_ = 0.0;
+    double nl_skin_frac_ = 0.5;
     int step_index_ = 0;
     size_t free_before_ = 0;
     cudaStream_t stream_ = nullptr;

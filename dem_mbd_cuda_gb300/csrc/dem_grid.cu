@@ -735,8 +735,14 @@ __global__ void k_step_counter(Counters k, int reset)
     if (threadIdx.x != 0) return;
     if (reset) {
         *k.pcontacts = 0; *k.phigh = 0; *k.bhigh = 0; *k.ct_total = 0; *k.tgover = 0; *k.wl_total = 0;
+        if (k.nl_flag) {
+            // an overflowed list is rebuilt by this step's cell sweep
+            if (k.nl_flag[1]) k.nl_flag[0] = 1;
+            k.nl_flag[1] = 0;
+        }
     } else {
         *k.step += 1;
+        if (k.nl_flag) k.nl_flag[0] = 0;
     }
 }
 

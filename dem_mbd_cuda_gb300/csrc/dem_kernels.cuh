@@ -127,6 +127,12 @@ struct SceneC {
     // of a batch is gridded exactly as it would be alone.
     double mesh, inv_mesh, pad;
     float mesh_f, margin_f, inv_mesh_f;
+    // Neighbour lists: the skin (FP32, m) and (skin / 2)^2 (FP64, m^2), the
+    // displacement since the lists' build that calls for a rebuild.  The
+    // skin keeps r_i + r_j + skin within the cell edge, so the build sweep's
+    // 27 cells hold every pair it must list.
+    float skin_f;
+    double nl_half2;
     int grav;
     int wall_begin, wall_count;
     int body_begin, body_count;
@@ -169,6 +175,7 @@ struct Recs {
 // stride of 12 so a slot starts on a 16-byte boundary and moves as three
 // float4 (FP32) or five double2 (FP64) accesses.
 constexpr int kHV = 12;
+constexpr int kNL = 32;  // neighbour-list capacity per component
 
 template <typename T> struct Hist {
     uint64_t* key;
@@ -216,6 +223,16 @@ struct Counters {
     int pt_warp_items;  // PT: warp-per-item kernel up to this many contact items
     int sweep_bps;      // sweep blocks per SM (grid-stride), 0 = one thread per component
     int gather_bps;     // gather blocks of 256 per SM (grid-stride)
+    // Neighbour lists (nl_on): per component up to kNL partner components
+    // within r_i + r_j + skin at the last build, and the build positions.
+    // nl_flag[0] nonzero: this step sweeps the cells and rebuilds the lists
+    // (set by the host, by a displacement past skin/2, or by an overflow);
+    // nl_flag[1]: the last build overflowed a list.
+    int nl_on;
+    int* nl_flag;
+    int* nl_cnt;
+    int* nl_idx;
+    double* nl_xref;
     int pp_bps;         // particle-law blocks of 256 per SM (grid-stride), 0 = 16
 };
 
@@ -382,7 +399,7 @@ void launch_adj_tape_end(int* pp_count, const int* ct_total, int* slot, cudaStre
 // velocities (after the rotational advance).
 // bps: blocks of 256 per SM (grid-stride), so the kernels beside them keep slots.
 void launch_gather_geom(const Comps& c, const Owners& o, const Grid& g, const Recs& r, int sm_count, int bps,
-                        cudaStream_t s);
+                        const Counters& k, cudaStream_t s);
 template <typename T>
 void launch_gather_vel(const Comps& c, const Owners& o, const Grid& g, const Recs& r, double dt_eff, int sm_count,
                        int bps, cudaStream_t s);

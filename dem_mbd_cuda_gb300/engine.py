@@ -315,6 +315,17 @@ class CudaDemSolver:
         self._check(self.lib.dem_x_set_launch(self.h, 1, int(blocks_per_sm)))
         return self
 
+    def set_neighbor_lists(self, on, skin_permille=None):
+        """Sweep particle pairs from per-component neighbour lists (rebuilt by
+        the cell sweep when a component has moved half the skin) instead of
+        the 27 cells every step.  skin_permille: the skin as a share of the
+        room the cell edge leaves beyond the largest pair (default 500).
+        Changes only the speed."""
+        if skin_permille is not None:
+            self._check(self.lib.dem_x_set_launch(self.h, 4, int(skin_permille)))
+        self._check(self.lib.dem_x_set_launch(self.h, 3, 1 if on else 0))
+        return self
+
     def set_pp_blocks(self, blocks_per_sm):
         """Blocks of 256 per SM of the particle law (0: 16).  Changes only the speed."""
         self._check(self.lib.dem_x_set_launch(self.h, 2, int(blocks_per_sm)))

@@ -99,15 +99,18 @@ def test_crowded_components(precision):
 def test_autotune_returns_an_accepted_setting():
     from dem_mbd_cuda_gb300.autotune import autotune
     sc = G.small_mbd()
-    out = autotune(sc, factors=(2.5, 3.0), sweep_blocks=(2, 4), gather_blocks=(1, 8), warp_items=(512,), steps=3,
-                   warmup=2)
+    out = autotune(sc, factors=(2.5, 3.0), sweep_blocks=(2, 4), gather_blocks=(1, 8), warp_items=(512,),
+                   skins=(0, 500), steps=3, warmup=2)
     assert out["cell_factor"] in (2.5, 3.0)
+    assert out["nl_skin"] in (None, 0, 500)
     assert out["sweep_blocks"] in (None, 2, 4)
     assert out["gather_blocks"] in (None, 1, 8)
     assert out["pt_warp_items"] in (None, 512)
     assert out["ms_per_step"] > 0 and out["default_ms_per_step"] > 0
-    assert len(out["table"]) == 2 + 2 + 2 + 1
+    assert len(out["table"]) == 2 + 2 + 2 + 2 + 1
     e = engine_for(sc, precision="mixed", cell_factor=out["cell_factor"])
+    if out["nl_skin"] is not None:
+        e.set_neighbor_lists(out["nl_skin"] > 0, out["nl_skin"] or None)
     if out["sweep_blocks"] is not None:
         e.set_sweep_blocks(out["sweep_blocks"])
     if out["gather_blocks"] is not None:
@@ -155,3 +158,31 @@ def test_run_split_into_calls_gives_the_same_bits(maker):
             np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
         np.testing.assert_array_equal(e.bodies()["center"], runs[0].bodies()["center"])
         np.testing.assert_array_equal(e.bodies()["quat"], runs[0].bodies()["quat"])
+
+
+@pytest.mark.parametrize("maker", ["small_dem", "small_mbd", "plate_on_monolayer"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_neighbor_lists_give_the_cell_sweep_bits(maker, precision):
+    """The sweep from neighbour lists takes the contacts in the cell sweep's
+    order: trajectories, bodies and histories are bit-identical, with the
+    default skin (few rebuilds) and with a skin so thin that the lists are
+    rebuilt every few steps."""
+    sc = getattr(G, maker)()
+    runs = [engine_for(sc, precision=precision).set_neighbor_lists(False)]
+    for permille in (500, 2):
+        e = engine_for(sc, precision=precision).set_neighbor_lists(True, permille)
+        runs.append(e)
+    for e in runs:
+        e.run(40)
+    _assert_same_runs(sc, runs[0], runs[1:])
+
+
+def test_neighbor_lists_with_crowded_components():
+    """Up to 60 contacts on one component (lists of up to 32 partners
+    overflow: those steps sweep the cells)."""
+    sc = crowded()
+    ref = engine_for(sc, precision="fp64").set_neighbor_lists(False)
+    e = engine_for(sc, precision="fp64").set_neighbor_lists(True)
+    for x in (ref, e):
+        x.run(6)
+    _assert_same_runs(sc, ref, [e])
