@@ -123,10 +123,12 @@ def algorithmic_bytes(n, nc, contacts, wall_contacts, body_manifolds, triangles,
 # data each must move once (records, cell rows, history, contact list), for
 # n particles with s contact sides; hv = bytes of one history slot.
 KERNEL_BYTES = {
-    # own record (relf, pos, meta, cell) 80 + 9 cell-row boundaries 144 +
-    # counters 12 + three high-water marks 12 + history key and age 12/slot;
-    # contact list entry 16 + key and age 12 per side
-    "sweep": ("k_sweep", lambda n, s, hv: n * 260 + s * 28),
+    # own record (relf, pos, meta, cell) 80 + counters 12 + three high-water
+    # marks 12 + history key and age 12/slot; contact list entry 16 + key and
+    # age 12 per side; the cells: 9 cell-row boundaries 144, or (neighbour
+    # lists, mean length L) the list count 4 and per entry its index and the
+    # partner's sorted position 8
+    "sweep": ("k_sweep", lambda n, s, hv, L=None: n * (116 + (144 if L is None else 4 + 8 * L)) + s * 28),
     # per side: list entry 16, history slot read + write, result row 24;
     # per particle: its FP64 position 32 and four FP32 rows 64
     "pp_law": ("k_pp_law", lambda n, s, hv: s * (16 + 2 * hv + 24) + n * 96),
@@ -136,12 +138,13 @@ KERNEL_BYTES = {
 }
 
 
-def dominant_kernel(phases, n, sides, hv):
+def dominant_kernel(phases, n, sides, hv, list_length=None):
     """The single-kernel phase that takes longest and its roofline inputs."""
     times = dict(zip(PHASES, phases))
     name = max(KERNEL_BYTES, key=lambda k: times.get(k, 0.0))
     kernel, fn = KERNEL_BYTES[name]
-    return name, kernel, times[name], fn(n, sides, hv)
+    nbytes = fn(n, sides, hv, list_length) if name == "sweep" else fn(n, sides, hv)
+    return name, kernel, times[name], nbytes
 
 
 def measured_traffic(kernel, n):
@@ -185,9 +188,12 @@ def run_engine(scene, precision, steps, warmup):
     stats = e.stepStats()
     # per-kernel times: CUDA events on the engine stream around each phase
     # of five force evaluations after the timed region, averaged
+    nl = e.neighbor_stats()
+    nl["steps"] = max(1, warmup) + steps
     runs = [e.compute_forces_timed(diag=(k == 4)) for k in range(5)]
     phases = [sum(r[k] for r in runs) / len(runs) for k in range(len(runs[0]))]
     stats_after = e.stepStats()
+    stats_after["neighbor_lists"] = nl
     return e, ms, clk.summary(), stats, phases, stats_after
 
 
@@ -263,11 +269,11 @@ def drum_summary(steps, warmup):
     scene, desc = make_scene("c2")
     out = {"workload": desc, "particles": scene.n}
     for prec in ("mixed", "fp64"):
-        e, ms, clocks, stats, phases, _ = run_engine(scene, prec, steps, warmup)
+        e, ms, clocks, stats, phases, after = run_engine(scene, prec, steps, warmup)
         out[prec] = {"value": scene.n * steps / (ms / 1000.0), "ms_per_step": ms / steps,
                      "contact_sides_per_step": stats["particle_contacts"],
                      "body_manifolds": stats["body_contacts"], "phase_ms": dict(zip(PHASES, phases)),
-                     "clocks": clocks}
+                     "neighbor_lists": after["neighbor_lists"], "clocks": clocks}
         del e
     out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["load_error_vs_fp64"] = load_error(scene)
@@ -500,7 +506,8 @@ def main():
     build.build()
     if dist:
         dist.barrier()
-    e, ms, clocks, stats, phases, _ = run_engine(scene, args.precision, args.steps, args.warmup)
+    e, ms, clocks, stats, phases, after = run_engine(scene, args.precision, args.steps, args.warmup)
+    nlists = after["neighbor_lists"]
     if args.single:
         n_total = sum(sc.n for sc in scene) if isinstance(scene, list) else scene.n
         print(json.dumps({"metric": "particle-steps/s", "value": n_total * args.steps / (ms / 1000.0),
@@ -527,7 +534,7 @@ def main():
     hv = 3 * h * 4            # one history slot: 9 values padded to 12
     contacts = stats["particle_contacts"]
     peak, peak_kind = hbm_peak()
-    pname, kernel, kms, kbytes = dominant_kernel(phases, scene.n, contacts, hv)
+    pname, kernel, kms, kbytes = dominant_kernel(phases, scene.n, contacts, hv, nlists["mean_length"])
     achieved = kbytes / (kms / 1000.0) / 1e9
     traffic, traffic_src = measured_traffic(kernel, scene.n)
     step_bytes = algorithmic_bytes(scene.n, scene.n_components, contacts, 0, stats["body_contacts"],
@@ -568,6 +575,7 @@ def main():
         "contact_sides_per_step": contacts,
         "load_error_vs_fp64": errs,
         "phase_ms": dict(zip(PHASES, phases)),
+        "neighbor_lists": nlists,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": kernel, "phase": pname, "kernel_ms": kms,
                      "algorithmic_bytes": kbytes, "traffic_source": traffic_src,

@@ -501,7 +501,8 @@ public:
         K_.pp_bps = kDefaultPpBlocksPerSm;
         // neighbour lists (set_launch 3 turns them off)
         K_.nl_on = 1;
-        K_.nl_flag = arena_.alloc<int>(2, "neighbour lists");
+        K_.nl_flag = arena_.alloc<int>(3, "neighbour lists");
+        check(cudaMemsetAsync(K_.nl_flag, 0, 3 * sizeof(int), s), "neighbour lists");
         K_.nl_cnt = arena_.alloc<int>(nc_, "neighbour lists");
         K_.nl_idx = arena_.alloc<int>((size_t)nc_ * kNL, "neighbour lists");
         K_.nl_xref = arena_.alloc<double>(3 * (size_t)nc_, "neighbour lists");
@@ -770,6 +771,20 @@ public:
         const double skin = nl_skin_frac_ * room * (1.0 - 1e-6);
         S.skin_f = (float)skin;
         S.nl_half2 = 0.25 * skin * skin;
+    }
+    // Builds so far and the mean list length (host copies; synchronizes).
+    void neighbor_stats(int* builds, double* mean_len, int* max_len = nullptr, int* overflowed = nullptr)
+    {
+        need_init();
+        std::vector<int> cnt(nc_);
+        int f[3] = {0, 0, 0};
+        check(cudaMemcpyAsync(cnt.data(), K_.nl_cnt, sizeof(int) * nc_, cudaMemcpyDeviceToHost, stream_), "stats");
+        check(cudaMemcpyAsync(f, K_.nl_flag, sizeof f, cudaMemcpyDeviceToHost, stream_), "stats");
+        check(cudaStreamSynchronize(stream_), "stats");
+        if (builds) *builds = f[2];
+        if (mean_len) *mean_len = nc_ > 0 ? std::accumulate(cnt.begin(), cnt.end(), 0.0) / nc_ : 0.0;
+        if (max_len) *max_len = nc_ > 0 ? *std::max_element(cnt.begin(), cnt.end()) : 0;
+        if (overflowed) *overflowed = f[1];
     }
     void nl_request_rebuild()
     {
@@ -2171,6 +2186,11 @@ int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double*
         e->e.adjoint_backward(dl_dpos, dl_dvel, dl_dbody_center, dl_dbody_vel, dl_dpos0, dl_dvel0, dl_domega0,
                               dl_dparams);
     });
+}
+
+int dem_x_neighbor_stats(dem_engine* e, int* builds, double* mean_length, int* max_length, int* overflowed)
+{
+    return guarded([&] { NEED(e); e->e.neighbor_stats(builds, mean_length, max_length, overflowed); });
 }
 
 int dem_x_synchronize(dem_engine* e)

@@ -742,7 +742,10 @@ __global__ void k_step_counter(Counters k, int reset)
         }
     } else {
         *k.step += 1;
-        if (k.nl_flag) k.nl_flag[0] = 0;
+        if (k.nl_flag) {
+            if (k.nl_on && k.nl_flag[0]) k.nl_flag[2] += 1;
+            k.nl_flag[0] = 0;
+        }
     }
 }
 

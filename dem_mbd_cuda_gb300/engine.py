@@ -62,6 +62,7 @@ _SIGS = {
     "dem_adjoint_forward": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
     "dem_adjoint_backward": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
     "dem_adjoint_backward_mbd": ([C.c_void_p] + [C.c_void_p] * 8, C.c_int),
+    "dem_x_neighbor_stats": ([C.c_void_p] + [C.c_void_p] * 4, C.c_int),
 }
 
 
@@ -325,6 +326,14 @@ class CudaDemSolver:
             self._check(self.lib.dem_x_set_launch(self.h, 4, int(skin_permille)))
         self._check(self.lib.dem_x_set_launch(self.h, 3, 1 if on else 0))
         return self
+
+    def neighbor_stats(self):
+        """Neighbour-list builds so far, the mean and longest list, and
+        whether the last build overflowed a list (those steps sweep the
+        cells)."""
+        b, m, x, o = C.c_int(), C.c_double(), C.c_int(), C.c_int()
+        self._check(self.lib.dem_x_neighbor_stats(self.h, C.byref(b), C.byref(m), C.byref(x), C.byref(o)))
+        return {"builds": b.value, "mean_length": m.value, "max_length": x.value, "overflowed": bool(o.value)}
 
     def set_pp_blocks(self, blocks_per_sm):
         """Blocks of 256 per SM of the particle law (0: 16).  Changes only the speed."""
