@@ -8,7 +8,7 @@ Built here:
   * libref_geometry.so -- the reference's CPU sphere/triangle overlap area
     (src/contact_geometry.cpp) behind oracle/ref_geometry_harness.cpp.
 The reference's CUDA step engine itself needs a GPU and its CMake build; it
-is not built here (see DESIGN.md).
+is not built here.
 """
 import os
 import subprocess
