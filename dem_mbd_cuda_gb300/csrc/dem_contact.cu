@@ -200,7 +200,8 @@ __device__ __forceinline__ V3<float> rot_ivf(float qw, float qx, float qy, float
 __global__ void k_gather_geom(Comps c, Owners o, Grid g, Recs r, Counters k)
 {
     const int nvalid = *g.nvalid;
-    bool moved = false;
+    const int step = k.nl_on ? *k.step : 0;
+    int movers = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nvalid; t += gridDim.x * blockDim.x) {
         const int ci = g.sorted_id[t];
         const int w = c.owner[ci];
@@ -216,13 +217,22 @@ __global__ void k_gather_geom(Comps c, Owners o, Grid g, Recs r, Counters k)
         r.relf[t] = make_float4(f32_rn(__fma_rn(-(double)cx, mesh, x)), f32_rn(__fma_rn(-(double)cy, mesh, y)),
                                 f32_rn(__fma_rn(-(double)cz, mesh, z)), f32_rn(rad));
         if (k.nl_on) {
-            // moved more than half the skin since the lists' build
+            // a mover (more than half the skin since the lists' build) marks
+            // its cell for this step
             const double* xr = k.nl_xref + 3 * (size_t)ci;
             const double dx = x - xr[0], dy = y - xr[1], dz = z - xr[2];
-            moved |= dx * dx + dy * dy + dz * dz > g.sc[s].nl_half2;
+            if (dx * dx + dy * dy + dz * dz > g.sc[s].nl_half2) {
+                k.nl_hot[g.clin[ci]] = step;
+                ++movers;
+            }
         }
     }
-    if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) k.nl_flag[0] = 1;
+    // beyond the limit every list is rebuilt this step
+    for (int o2 = 16; o2 > 0; o2 >>= 1) movers += __shfl_xor_sync(0xffffffffu, movers, o2);
+    if (movers && (threadIdx.x & 31) == 0) {
+        const int before = atomicAdd(k.nl_flag + 3, movers);
+        if (before + movers > k.nl_limit) k.nl_flag[0] = 1;
+    }
 }
 
 template <typename T> __global__ void k_gather_vel(Comps c, Owners o, Grid g, Recs r, double dt_eff)
@@ -496,6 +506,31 @@ __device__ int sweep_list_one(const Grid& g, const Recs& r, const SceneC* __rest
     return count;
 }
 
+// Whether one of the 27 cells around sorted position t held a mover this
+// step (a component past half the skin since the lists' build): such a
+// component sweeps the cells instead of its list.  Every list and build
+// position is from the same build, so a component with no mover in its
+// cells and any partner it touches have each moved at most half the skin
+// since: the pair is listed.
+__device__ __forceinline__ bool mover_near(const Grid& g, const Recs& r, const Counters& k, int t, int step)
+{
+    const int4 cell = r.cell[t];
+    const int* lay = g.scene_layout + 8 * r.meta[t].w;
+    const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
+    bool hot = false;
+    for (int dx = -1; dx <= 1; ++dx) {
+        const int nx = cell.x + dx;
+        if (nx < lay[0] || nx >= lay[0] + lay[3]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int ny = cell.y + dy;
+            if (ny < lay[1] || ny >= lay[1] + lay[4]) continue;
+            const int row = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] - lay[2];
+            for (int z = z0; z <= z1; ++z) hot |= k.nl_hot[row + z] == step;
+        }
+    }
+    return hot;
+}
+
 // One thread per component in cell order: the reference's 27-cell sweep
 // (:1124-1146) over the cell start table, in the reference's order (dx, dy,
 // dz ascending; members of a cell in ascending component order).  For each
@@ -524,7 +559,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     int stage_t[kCandidates];
     int stage_s[kMaxContacts];
     int ci = -1;
-    if (t < nvalid && from_lists) {
+    if (t < nvalid && from_lists && !mover_near(g, r, k, t, step)) {
         ci = r.meta[t].x;
         count = sweep_list_one(g, r, sc, hp, k, t, nvalid, step, stage_t, stage_s, pover, phigh);
         ct.cnt[ci] = count;

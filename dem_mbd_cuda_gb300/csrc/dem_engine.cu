@@ -501,8 +501,11 @@ public:
         K_.pp_bps = kDefaultPpBlocksPerSm;
         // neighbour lists (set_launch 3 turns them off)
         K_.nl_on = 1;
-        K_.nl_flag = arena_.alloc<int>(3, "neighbour lists");
-        check(cudaMemsetAsync(K_.nl_flag, 0, 3 * sizeof(int), s), "neighbour lists");
+        K_.nl_flag = arena_.alloc<int>(4, "neighbour lists");
+        check(cudaMemsetAsync(K_.nl_flag, 0, 4 * sizeof(int), s), "neighbour lists");
+        K_.nl_hot = arena_.alloc<int>((size_t)G_.capacity, "neighbour lists");
+        check(cudaMemsetAsync(K_.nl_hot, 0xff, sizeof(int) * (size_t)G_.capacity, s), "neighbour lists");
+        K_.nl_limit = std::max(64, nc_ / 64);
         K_.nl_cnt = arena_.alloc<int>(nc_, "neighbour lists");
         K_.nl_idx = arena_.alloc<int>((size_t)nc_ * kNL, "neighbour lists");
         K_.nl_xref = arena_.alloc<double>(3 * (size_t)nc_, "neighbour lists");

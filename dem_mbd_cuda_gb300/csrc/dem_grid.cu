@@ -739,6 +739,7 @@ __global__ void k_step_counter(Counters k, int reset)
             // an overflowed list is rebuilt by this step's cell sweep
             if (k.nl_flag[1]) k.nl_flag[0] = 1;
             k.nl_flag[1] = 0;
+            k.nl_flag[3] = 0;
         }
     } else {
         *k.step += 1;

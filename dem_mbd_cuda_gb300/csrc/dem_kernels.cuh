@@ -229,7 +229,9 @@ struct Counters {
     // (set by the host, by a displacement past skin/2, or by an overflow);
     // nl_flag[1]: the last build overflowed a list.
     int nl_on;
-    int* nl_flag;       // [0] rebuild this step, [1] overflow at the last build, [2] builds so far
+    int* nl_flag;       // [0] rebuild this step, [1] overflow at the last build, [2] builds so far, [3] movers this step
+    int* nl_hot;        // per cell of the dense table: the step at which it held a mover
+    int nl_limit;       // movers beyond which every list is rebuilt
     int* nl_cnt;
     int* nl_idx;
     double* nl_xref;
