@@ -550,6 +550,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     // rebuilds them (kNL partners within r_i + r_j + skin per component)
     const bool from_lists = k.nl_on && *k.nl_flag == 0;
     const bool build = k.nl_on && !from_lists;
+    const bool movers = from_lists && k.nl_flag[3] > 0;  // any cell stamped this step
     int pover = 0, phigh = 0, found = 0;
     // grid-stride over blocks of sorted positions: the launch may use fewer
     // blocks than positions so that the kernels beside it find free slots
@@ -559,7 +560,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     int stage_t[kCandidates];
     int stage_s[kMaxContacts];
     int ci = -1;
-    if (t < nvalid && from_lists && !mover_near(g, r, k, t, step)) {
+    if (t < nvalid && from_lists && !(movers && mover_near(g, r, k, t, step))) {
         ci = r.meta[t].x;
         count = sweep_list_one(g, r, sc, hp, k, t, nvalid, step, stage_t, stage_s, pover, phigh);
         ct.cnt[ci] = count;
