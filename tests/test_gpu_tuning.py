@@ -3,6 +3,8 @@ gathers and the particle law (grid-stride) leave the trajectory, the bodies
 and the contact histories bit-identical, also where a component holds more
 than a warp's width of contacts;
 the autotuner returns a setting the engine accepts."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -185,4 +187,23 @@ def test_neighbor_lists_with_crowded_components():
     e = engine_for(sc, precision="fp64").set_neighbor_lists(True)
     for x in (ref, e):
         x.run(6)
+    _assert_same_runs(sc, ref, [e])
+
+
+def test_neighbor_lists_with_a_fast_mover():
+    """One sphere thrown through a resting bed: it passes half the skin within
+    a few steps, its neighbourhoods sweep the cells while every other
+    component keeps its list (no global rebuild), and the run equals the
+    cell sweep bit for bit."""
+    sc = G.small_dem(n=400, seed=12, vel_std=0.0, omega_std=0.0)
+    vel = np.zeros_like(sc.pos)
+    k = int(np.argmax(sc.pos[:, 2]))
+    vel[k] = [3.0, 0.0, -3.0]
+    sc = dataclasses.replace(sc, vel=vel)
+    ref = engine_for(sc, precision="fp64").set_neighbor_lists(False)
+    e = engine_for(sc, precision="fp64").set_neighbor_lists(True)
+    for x in (ref, e):
+        x.run(60)
+    st = e.neighbor_stats()
+    assert st["builds"] == 1, st
     _assert_same_runs(sc, ref, [e])
