@@ -775,6 +775,32 @@ public:
         S.skin_f = (float)skin;
         S.nl_half2 = 0.25 * skin * skin;
     }
+    // The single-pass scans' bounded wait, made to run out (a predecessor
+    // tile that never publishes): returns the error word it sets.
+    unsigned scan_wait_probe()
+    {
+        unsigned long long* status = nullptr;
+        unsigned* err = nullptr;
+        check(cudaMalloc(&status, sizeof(unsigned long long)), "probe");
+        check(cudaMalloc(&err, sizeof(unsigned)), "probe");
+        unsigned out = 0;
+        try {
+            check(cudaMemsetAsync(status, 0, sizeof(unsigned long long), stream_), "probe");
+            check(cudaMemsetAsync(err, 0, sizeof(unsigned), stream_), "probe");
+            launch_scan_wait_probe(status, err, stream_);
+            check(cudaGetLastError(), "probe");
+            check(cudaMemcpyAsync(&out, err, sizeof out, cudaMemcpyDeviceToHost, stream_), "probe");
+            check(cudaStreamSynchronize(stream_), "probe");
+        } catch (...) {
+            cudaFree(status);
+            cudaFree(err);
+            throw;
+        }
+        cudaFree(status);
+        cudaFree(err);
+        return out;
+    }
+
     // Builds so far and the mean list length (host copies; synchronizes).
     void neighbor_stats(int* builds, double* mean_len, int* max_len = nullptr, int* overflowed = nullptr)
     {
@@ -2194,6 +2220,11 @@ int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double*
 int dem_x_neighbor_stats(dem_engine* e, int* builds, double* mean_length, int* max_length, int* overflowed)
 {
     return guarded([&] { NEED(e); e->e.neighbor_stats(builds, mean_length, max_length, overflowed); });
+}
+
+int dem_x_scan_wait_probe(dem_engine* e, unsigned* err)
+{
+    return guarded([&] { NEED(e); NEED(err); *err = e->e.scan_wait_probe(); });
 }
 
 int dem_x_synchronize(dem_engine* e)

@@ -767,6 +767,18 @@ void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int 
     k_scan_apply<<<g, kScanBlock, 0, s>>>(in, out, n_dev, tile_sums);
 }
 
+__global__ void k_scan_wait_probe(ScanState st, unsigned* err)
+{
+    // epoch 1: the zero word of tile 0 is never current, so the look-back
+    // waits on it until its bound
+    (void)scan_lookback(st, 1, 1u, err);
+}
+void launch_scan_wait_probe(unsigned long long* status, unsigned* err, cudaStream_t s)
+{
+    ScanState st{status, nullptr, 1};
+    k_scan_wait_probe<<<1, 32, 0, s>>>(st, err);
+}
+
 void launch_scan1(const int* in, int* out, const int* n_dev, const ScanState& st, unsigned* err, int sm_count,
                   cudaStream_t s)
 {

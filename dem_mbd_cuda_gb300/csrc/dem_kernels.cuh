@@ -340,6 +340,10 @@ void launch_grid_layout(const Comps& c, const Owners& o, const Grid& g, cudaStre
 void launch_grid_sort(const Comps& c, const Owners& o, const Grid& g, int sm_count, cudaStream_t s);
 void launch_scan(const int* in, int* out, const int* n_dev, int* tile_sums, int sm_count, cudaStream_t s);
 // Single-pass exclusive scan of in[0, n) into out[0, n] (out[n] = total).
+// Failure detection of the single-pass scans without a fault: one warp looks
+// back from tile 1 at a tile 0 that never publishes; the bounded wait gives
+// up and sets kErrScanWait in *err.  `status` holds one zero word.
+void launch_scan_wait_probe(unsigned long long* status, unsigned* err, cudaStream_t s);
 void launch_scan1(const int* in, int* out, const int* n_dev, const ScanState& st, unsigned* err, int sm_count,
                   cudaStream_t s);
 void launch_tri_transform(const Tris& t, const Bodies& b, const SceneC* sc, cudaStream_t s);

@@ -63,6 +63,7 @@ _SIGS = {
     "dem_adjoint_backward": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
     "dem_adjoint_backward_mbd": ([C.c_void_p] + [C.c_void_p] * 8, C.c_int),
     "dem_x_neighbor_stats": ([C.c_void_p] + [C.c_void_p] * 4, C.c_int),
+    "dem_x_scan_wait_probe": ([C.c_void_p, C.c_void_p], C.c_int),
 }
 
 
@@ -326,6 +327,13 @@ class CudaDemSolver:
             self._check(self.lib.dem_x_set_launch(self.h, 4, int(skin_permille)))
         self._check(self.lib.dem_x_set_launch(self.h, 3, 1 if on else 0))
         return self
+
+    def scan_wait_probe(self):
+        """Run out the single-pass scans' bounded wait on purpose (a tile
+        that never publishes) and return the error word it sets."""
+        v = C.c_uint()
+        self._check(self.lib.dem_x_scan_wait_probe(self.h, C.byref(v)))
+        return v.value
 
     def neighbor_stats(self):
         """Neighbour-list builds so far, the mean and longest list, and

@@ -127,3 +127,16 @@ def test_empty_scene_is_rejected():
     sc = _scene(np.zeros((0, 3)), np.zeros(0))
     with pytest.raises(RuntimeError, match="requires particles"):
         CudaDemSolver().initialize(sc)
+
+
+def test_scan_wait_runs_out_without_a_fault():
+    """Failure detection of the single-pass scans: a look-back whose
+    predecessor tile never publishes gives up at its bound, reports
+    kErrScanWait (16) through its error word, and the context stays usable
+    (the engine steps on)."""
+    e = engine_for(G.small_dem(n=200, seed=2), precision="fp64")
+    assert e.scan_wait_probe() & 16
+    ref = engine_for(G.small_dem(n=200, seed=2), precision="fp64")
+    e.run(5)
+    ref.run(5)
+    np.testing.assert_array_equal(e.downloadParticleState()["pos"], ref.downloadParticleState()["pos"])
