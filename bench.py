@@ -475,6 +475,13 @@ def main():
     scene, desc = make_scene(args.config, args.particles)
     if isinstance(scene, list) and not args.single:
         ap.error("--config c4 runs with --single; the default line carries it as batch_256")
+    n_all = sum(sc.n for sc in scene) if isinstance(scene, list) else scene.n
+    sharded = isinstance(scene, list) and world > 1 and args.impl != "reference"
+    if sharded:
+        # a batch shards by scene: each rank runs its share as one engine
+        from dem_mbd_cuda_gb300.shard import partition
+        parts = partition([sc.n for sc in scene], world)
+        scene = [scene[i] for i in parts[rank]]
 
     if args.impl == "reference":
         # The reference's own hot path is CUDA-only; its CPU implementation of
@@ -509,10 +516,20 @@ def main():
     e, ms, clocks, stats, phases, after = run_engine(scene, args.precision, args.steps, args.warmup)
     nlists = after["neighbor_lists"]
     if args.single:
-        n_total = sum(sc.n for sc in scene) if isinstance(scene, list) else scene.n
-        print(json.dumps({"metric": "particle-steps/s", "value": n_total * args.steps / (ms / 1000.0),
-                          "ms_per_step": ms / args.steps, "precision": args.precision,
-                          "phase_ms": dict(zip(PHASES, phases)),
+        if sharded:
+            # the whole batch's particles over the slowest rank's time
+            from dem_mbd_cuda_gb300.shard import max_over_ranks
+            ms = max_over_ranks(ms)
+            value = n_all * args.steps / (ms / 1000.0)
+        else:
+            value = world * n_all * args.steps / (ms / 1000.0)
+        if rank != 0:
+            return
+        print(json.dumps({"metric": "particle-steps/s", "value": value, "ms_per_step": ms / args.steps,
+                          "n_gpus": world, "scaling": "strong" if sharded else "weak",
+                          "parallelism": ("scenes sharded over %d ranks" % world) if sharded
+                          else ("replicas" if world > 1 else "single"),
+                          "precision": args.precision, "phase_ms": dict(zip(PHASES, phases)),
                           "contact_sides_per_step": stats["particle_contacts"], "clocks": clocks}))
         return
     other = "fp64" if args.precision == "mixed" else "mixed"
