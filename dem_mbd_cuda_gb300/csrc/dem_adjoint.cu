@@ -11,13 +11,16 @@
 //   finish   vh1 = vh + a1 dt, wh1 = wh + aw1 dt,
 //            hq1 = G(N(q1 + dt/2 G(q1, w1)), wh1)  (advanceHalfVelocityKernel,
 //            :239-265)
-// The reverse sweep runs, per step: k_adj_finish (finish^T and the owner
-// part of forces^T), k_adj_pp and k_adj_pw (the contact laws, scattering
-// into the owners with FP64 atomics), k_adj_advance (advance^T).  The
-// history adjoints live in the reference's slot layout, so a contact that
-// persists keeps its slot and its adjoint; a slot acquired new in the step
-// gets a zero adjoint before it.  Spheres only (one component per owner,
-// isotropic inertia), no rigid bodies.
+// The reverse sweep runs, per step: the body leapfrog's half-update
+// reverse (k_adj_body_a), k_adj_finish (finish^T and the owner part of
+// forces^T, Euler's equations with their gyroscopic terms), k_adj_contacts
+// (particle and wall contacts, scattering into the owners with FP64
+// atomics), k_adj_pt (particle-body manifolds) and the body position
+// update's reverse (k_adj_body_c) beside them, then k_adj_advance
+// (advance^T).  The history adjoints live in the reference's slot layout, so
+// a contact that persists keeps its slot and its adjoint; a slot acquired
+// new in the step gets a zero adjoint before it.  Spheres (one component per
+// owner) with any principal inertia; dynamic rigid bodies.
 #include "dem_adjoint.cuh"
 #include "dem_kernels.cuh"
 
@@ -182,13 +185,24 @@ __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const 
         st3(Lp, kAdjVH, n, i, lvh1);
         st3(Lp, kAdjWH, n, i, lwh1);
     }
-    // forces^T, owner part: a1 = F / m, aw1 = R(q1)^T tau / I (isotropic)
-    const double m = o.mass[i], I = o.ix[i];
+    // forces^T, owner part: a1 = F / m; Euler's equations in the body frame,
+    // aw1 = (R(q1)^T tau - gyro(w1)) / I with gyro = ((Iz - Iy) wz wy,
+    // (Ix - Iz) wx wz, (Iy - Ix) wy wx) (zero for isotropic inertia)
+    const double m = o.mass[i], Ix = o.ix[i], Iy = o.iy[i], Iz = o.iz[i];
+    const bool iso = o.iso[i] != 0;
     const D3 lF = la1 * (1.0 / m);
     const D3 aw1 = ld3(S1, kAdjAW, n, i);
-    const D3 tau = rotq(q1, aw1) * I;
+    D3 tb = mk(Ix * aw1.x, Iy * aw1.y, Iz * aw1.z);
+    if (!iso) tb = tb + mk((Iz - Iy) * w1.z * w1.y, (Ix - Iz) * w1.x * w1.z, (Iy - Ix) * w1.y * w1.x);
+    const D3 tau = rotq(q1, tb);
+    const D3 lt = mk(law1.x / Ix, law1.y / Iy, law1.z / Iz);
     D3 ltau = z3();
-    rotq_t_vjp(q1, tau, law1 * (1.0 / I), lq1, ltau);
+    rotq_t_vjp(q1, tau, lt, lq1, ltau);
+    if (!iso) {
+        lw1.z -= lt.x * (Iz - Iy) * w1.y; lw1.y -= lt.x * (Iz - Iy) * w1.z;
+        lw1.x -= lt.y * (Ix - Iz) * w1.z; lw1.z -= lt.y * (Ix - Iz) * w1.x;
+        lw1.y -= lt.z * (Iy - Ix) * w1.x; lw1.x -= lt.z * (Iy - Ix) * w1.y;
+    }
     st3(T, kTX, n, i, ld3(L, kAdjX, n, i));
     st4(T, kTQ, n, i, lq1);
     st3(T, kTV, n, i, lv1);

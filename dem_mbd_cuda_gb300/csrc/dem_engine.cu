@@ -1517,10 +1517,6 @@ public:
         if (precision_ != DEM_PRECISION_FP64)
             throw DemError(DEM_ERR_INVALID, "the adjoint runs on the FP64 form (precision DEM_PRECISION_FP64)");
         if (!sphere_) throw DemError(DEM_ERR_INVALID, "the adjoint covers spheres (one component per owner)");
-        for (int i = 0; i < n_; ++i)
-            if (!(oin_host_[3 * (size_t)i] == oin_host_[3 * (size_t)i + 1] &&
-                  oin_host_[3 * (size_t)i + 1] == oin_host_[3 * (size_t)i + 2]))
-                throw DemError(DEM_ERR_INVALID, "the adjoint covers isotropic inertia");
     }
     AdjCkpt adj_alloc_ckpt()
     {

@@ -286,8 +286,8 @@ int dem_cell_sort_static(const double* x, const double* y, const double* z,
  * No counterpart in the reference, which has no gradients.  A hand-written
  * adjoint of each step of the FP64 form: within a step the contact set is
  * the one the forward step found, and at the Coulomb / twisting / rolling
- * caps the derivative is that of the branch taken.  Covers spheres with
- * walls, particle contacts and rigid bodies (particle-triangle manifolds
+ * caps the derivative is that of the branch taken.  Covers spheres (any
+ * principal inertia) with walls, particle contacts and rigid bodies (particle-triangle manifolds
  * and the host MBD step of dynamic bodies; prescribed and fixed bodies carry
  * no adjoint), one scene or a batch (dem_initialize_batch), precision
  * DEM_PRECISION_FP64; other engines return DEM_ERR_INVALID.
