@@ -281,8 +281,11 @@ public:
             gvec_.push_back({x.gravity[0], x.gravity[1], x.gravity[2]});
         }
         n_ = (int)oid.size();
-        if (cown.size() >= (size_t)1 << 30)
-            throw DemError(DEM_ERR_CAPACITY, "more than 2^30 components: sorted positions carry a flag in bit 30");
+        // the contact list and the history slots hold kPSlots entries per
+        // component and are indexed by int
+        if (cown.size() > (size_t)INT_MAX / kPSlots)
+            throw DemError(DEM_ERR_CAPACITY, "more than " + std::to_string(INT_MAX / kPSlots) +
+                                                 " components: per-component contact slots exceed the int index range");
         nc_ = (int)cown.size();
         nw_ = (int)wo.size() / 3;
         nb_ = (int)bmass.size();

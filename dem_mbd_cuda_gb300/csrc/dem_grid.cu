@@ -201,11 +201,12 @@ __global__ void k_layout(Grid g)
                 nx = (long long)box[3] - box[0] + 1;
                 ny = (long long)box[4] - box[1] + 1;
                 nz = (long long)box[5] - box[2] + 1;
-                cells = nx * ny * nz;
-                if (off + cells > (long long)g.capacity) {
+                // each extent is at most 2^21, so nx * ny * nz can reach 2^63
+                // and wrap; the product is only formed once nx * ny fits
+                if (nx * ny > (long long)g.capacity || off + nx * ny * nz > (long long)g.capacity)
                     atomicOr(g.err, kErrCellCapacity);
-                    cells = 0;
-                }
+                else
+                    cells = nx * ny * nz;
             }
             lay[0] = box[0]; lay[1] = box[1]; lay[2] = box[2];
             lay[3] = cells ? (int)nx : 0; lay[4] = cells ? (int)ny : 0; lay[5] = cells ? (int)nz : 0;

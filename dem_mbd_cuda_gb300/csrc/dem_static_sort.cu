@@ -110,8 +110,11 @@ __global__ void k_s_layout(Scratch s)
     if (threadIdx.x != 0) return;
     long long cells = 0;
     if (s.box[0] <= s.box[3]) {
-        cells = ((long long)s.box[3] - s.box[0] + 1) * ((long long)s.box[4] - s.box[1] + 1) *
-                ((long long)s.box[5] - s.box[2] + 1);
+        // each extent is at most 2^21, so the full product can reach 2^63
+        // and wrap; it is only formed once the first two extents fit
+        const long long nx = (long long)s.box[3] - s.box[0] + 1, ny = (long long)s.box[4] - s.box[1] + 1,
+                        nz = (long long)s.box[5] - s.box[2] + 1;
+        cells = nx * ny > kMaxCells ? (long long)kMaxCells + 1 : nx * ny * nz;
         if (cells > kMaxCells) {
             s.box[7] |= 2;
             cells = 0;

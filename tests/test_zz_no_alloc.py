@@ -56,3 +56,21 @@ def test_static_sort_rejects_oversize(engine_lib):
     rc = engine_lib.dem_cell_sort_static(None, None, None, n, 1e-3, None, None, None)
     assert rc != 0
     assert b"262144" in engine_lib.dem_last_error()
+
+
+def test_static_sort_rejects_a_cell_box_spanning_the_hash_range(engine_lib):
+    """Components at both ends of the signed 21-bit cell range on every axis:
+    the cell box is 2^21 cells on each side (2^63 in all), which must come
+    back as a capacity error, not wrap to an empty box and a silent success."""
+    torch = pytest.importorskip("torch")
+    lo, hi = -float(1 << 20), float(1 << 20) - 0.5
+    pos = np.array([[lo, lo, lo], [hi, hi, hi], [0.25, 0.25, 0.25]])
+    dev = torch.device("cuda:0")
+    x, y, z = (torch.tensor(pos[:, k].copy(), dtype=torch.float64, device=dev) for k in range(3))
+    keys = torch.zeros(3, dtype=torch.int64, device=dev)
+    ids = torch.zeros(3, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    rc = engine_lib.dem_cell_sort_static(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), C.c_void_p(z.data_ptr()),
+                                         3, 1.0, C.c_void_p(keys.data_ptr()), C.c_void_p(ids.data_ptr()), None)
+    assert rc == 4, engine_lib.dem_last_error()
+    assert b"cell box exceeds" in engine_lib.dem_last_error()
