@@ -140,3 +140,28 @@ def test_scan_wait_runs_out_without_a_fault():
     e.run(5)
     ref.run(5)
     np.testing.assert_array_equal(e.downloadParticleState()["pos"], ref.downloadParticleState()["pos"])
+
+
+@pytest.mark.parametrize("max_cells", [8, 40])
+def test_cell_table_capacity_is_reported(max_cells):
+    """A particle cell box larger than dem_options.max_cells is the
+    reference's capacity error at a diagnostic evaluation.  The scene spans
+    4 x 4 x 5 cells: 8 cells fail on the first two extents already, 40 on
+    the full product."""
+    sc = G.small_dem(n=200, seed=3)
+    with pytest.raises(RuntimeError, match="dense cell-table capacity"):
+        e = CudaDemSolver().initialize(sc, max_cells=max_cells)
+        e.computeForces(0.0, None, False, True)
+
+
+def test_key_range_is_reported():
+    """A sphere beyond the signed 21-bit cell range (2^20 cells of 2.5 r_max,
+    about 5.8 km here) is the reference's key-range error at a diagnostic
+    evaluation; the other spheres still sort."""
+    sc = G.small_dem(n=200, seed=3)
+    mesh = 2.5 * float(sc.owner_radius.max())
+    assert 1.0e4 / mesh > (1 << 20)
+    sc.pos[7] = (1.0e4, 0.0, 0.0)
+    with pytest.raises(RuntimeError, match="21-bit hash range"):
+        e = CudaDemSolver().initialize(sc)
+        e.computeForces(0.0, None, False, True)
