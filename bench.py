@@ -60,7 +60,11 @@ def make_scene(config, particles=None):
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
-    def __init__(self, index=0):
+    def __init__(self, index=None):
+        # nvidia-smi counts physical GPUs: the process's GPU is the first
+        # visible one (an index or a UUID, both accepted by -i)
+        if index is None:
+            index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].strip() or "0")
         self.index = index
         self.samples = []
         self._stop = threading.Event()
@@ -508,7 +512,13 @@ def main():
         print(json.dumps(line))
         return
 
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    if world > 1:
+        # one GPU per rank, fixed before the first CUDA call (the engine runs
+        # on the current device): this rank's entry of the visible list, or
+        # its local rank; a list of one was already narrowed by the launcher
+        ids = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+        if len(ids) != 1:
+            os.environ["CUDA_VISIBLE_DEVICES"] = ids[local] if local < len(ids) else str(local)
     from dem_mbd_cuda_gb300 import build
     build.build()
     if dist:
