@@ -163,7 +163,9 @@ int dem_destroy(dem_engine* engine);
 void dem_default_options(dem_options* options);
 
 /* CudaDemSolver::initialize (src/cuda_backend_cuda.cu:302-381).  `options`
- * may be NULL. */
+ * may be NULL.  An engine (one scene or a whole batch) takes at most
+ * 33,554,431 components, because the contact slots are indexed by int;
+ * beyond that it returns DEM_ERR_CAPACITY. */
 int dem_initialize(dem_engine* engine, const dem_scene* scene,
                    const dem_options* options);
 
