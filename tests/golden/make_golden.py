@@ -42,4 +42,9 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle.reference_build import reference_root
+    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if root is None:
+        sys.exit("pass the reference checkout or set DEM_REFERENCE_ROOT")
+    main(root)

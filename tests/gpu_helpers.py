@@ -26,8 +26,23 @@ def active_contacts(keys, last, step):
     return set(zip(c.tolist(), keys[c, s].tolist()))
 
 
-def compare_evaluation(e, o, step, tol=1e-9):
-    """Bit-exact grid and history slots, tolerance on forces and values."""
+def forces_of(x):
+    """Force output of the engine, the oracle or the reference's CUDA engine."""
+    return x.downloadForceOutput() if isinstance(x, CudaDemSolver) else x.forces()
+
+
+def stats_of(x):
+    return x.stepStats() if isinstance(x, CudaDemSolver) else x.stats()
+
+
+def state_of(x):
+    return x.downloadParticleState() if isinstance(x, CudaDemSolver) else x.state()
+
+
+def compare_evaluation(e, o, step=None, tol=1e-9):
+    """Bit-exact grid and history slots, tolerance on forces and values.
+    `o` is the checker (oracle or the reference's CUDA engine); `e` is the
+    run under test (engine, oracle or reference)."""
     ke, ie = e.grid()
     ko, io = o.grid()
     np.testing.assert_array_equal(ie, io)
@@ -39,11 +54,11 @@ def compare_evaluation(e, o, step, tol=1e-9):
         np.testing.assert_array_equal(l1, l2, err_msg=f"history last-seen kind {kind}")
         scale = max(np.abs(v2).max(), 1e-30)
         assert np.abs(v1 - v2).max() <= tol * scale + 1e-15, f"history values kind {kind}"
-    fe, fo = e.downloadForceOutput(), o.forces()
+    fe, fo = forces_of(e), forces_of(o)
     for name in ("contact", "field", "wall", "total"):
         scale = max(np.abs(fo[name]).max(), 1e-30)
         assert np.abs(fe[name] - fo[name]).max() <= tol * scale + 1e-14, name
-    se, so = e.stepStats(), o.stats()
+    se, so = stats_of(e), stats_of(o)
     for key in ("particle_contacts", "body_contacts", "particle_history_high_water", "body_history_high_water",
                 "particle_history_overflows", "body_history_overflows"):
         assert se[key] == so[key], (key, se[key], so[key])

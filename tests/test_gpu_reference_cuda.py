@@ -1,0 +1,125 @@
+"""The oracle and the engine against the reference's own CUDA engine.
+
+The reference's kernels are compiled from its src/cuda/*.cu (the way its
+CMakeLists.txt builds them) into oracle/_ref/ref_engine.cubin and run
+through oracle/ref_cuda_host.cu, a restatement of its host glue
+(src/cuda_backend_cuda.cu:302-524).  These tests pin the CPU oracle to the
+reference's own FP64 results -- the tangential, twisting and rolling history
+channels, the particle-triangle manifold and the integrator included -- and
+check the engine against the reference directly.
+
+Bars: sorted cell keys and ids, history keys and last-seen steps (the
+contact lists) and the contact counters bit for bit; forces and history
+values within 1e-9 of the largest value for one evaluation; states and body
+loads over several steps within the reference's own bar 1e-8 + 1e-9 |ref|
+(docs/CUDA_MIGRATION_VALIDATION.md:73).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from gpu_helpers import close, compare_evaluation, engine_for, state_of
+from oracle import ref_cuda
+from oracle.oracle import Oracle
+from dem_mbd_cuda_gb300 import generate as G
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not ref_cuda.available(), reason="reference device code not built")]
+
+
+@pytest.fixture(autouse=True)
+def _lib(engine_lib):
+    return engine_lib
+
+
+def scene(name):
+    if name in ("wall_contact", "two_particle", "triangle_contact", "free_fall", "body_states",
+                "data1_pure_dem", "data1_mbd"):
+        return load_golden(name)[0]
+    if name == "small_mbd_nocap":
+        return G.small_mbd(caps=False)
+    return getattr(G, name)()
+
+
+def first_evaluation(x, sc):
+    return x.compute_forces(sc.body_states() if sc.n_bodies else None) if not hasattr(x, "computeForces") else \
+        x.computeForces(0.0, sc.body_states() if sc.n_bodies else None, True, True)
+
+
+@pytest.mark.parametrize("name", ["wall_contact", "two_particle", "triangle_contact", "free_fall"])
+def test_reference_kernels_give_the_reference_known_answers(name):
+    """The launcher reproduces the reference's own analytic checks
+    (tests/scenario_validator.cpp:80-113) with the reference's kernels."""
+    sc = scene(name)
+    r = ref_cuda.RefCuda(sc)
+    loads = first_evaluation(r, sc)
+    f = r.forces()
+    if name == "wall_contact":
+        assert abs(f["wall"][0, 2] - 100.0) <= 1e-9 and abs(f["total"][0, 2] - 100.0) <= 1e-9
+    elif name == "two_particle":
+        assert abs(f["contact"][0, 0] + 100) <= 1e-9 and abs(f["contact"][1, 0] - 100) <= 1e-9
+        assert abs(f["contact"][0, 0] + f["contact"][1, 0]) <= 1e-12
+    elif name == "triangle_contact":
+        assert abs(f["total"][0, 2] - 100.0) <= 1e-8 and abs(loads[0, 2] + 100.0) <= 1e-8
+    else:
+        assert abs(f["total"][0, 2] + 9.8) <= 2e-12
+
+
+@pytest.mark.parametrize("name", ["small_dem", "small_mbd", "data1_pure_dem", "data1_mbd", "triangle_contact"])
+def test_oracle_single_evaluation_matches_reference_kernels(name):
+    sc = scene(name)
+    r = ref_cuda.RefCuda(sc)
+    o = Oracle(sc)
+    lr = first_evaluation(r, sc)
+    lo = first_evaluation(o, sc)
+    compare_evaluation(o, r)
+    if sc.n_bodies:
+        assert np.abs(lo - lr).max() <= 1e-9 * np.abs(lr).max() + 1e-12
+
+
+@pytest.mark.parametrize("name", ["small_dem", "small_mbd", "data1_pure_dem", "data1_mbd"])
+def test_engine_single_evaluation_matches_reference_kernels(name):
+    sc = scene(name)
+    r = ref_cuda.RefCuda(sc)
+    e = engine_for(sc)
+    lr = first_evaluation(r, sc)
+    le = first_evaluation(e, sc)
+    compare_evaluation(e, r)
+    if sc.n_bodies:
+        assert np.abs(le - lr).max() <= 1e-9 * np.abs(lr).max() + 1e-12
+
+
+@pytest.mark.parametrize("name", ["small_dem", "small_mbd_nocap", "data1_pure_dem"])
+def test_oracle_and_engine_trajectories_match_reference_kernels(name):
+    """25 steps of the reference's loop: random velocities and spins load
+    the tangential, twisting and rolling channels (small_dem), and the
+    particle-triangle manifold history (small_mbd_nocap)."""
+    sc = scene(name)
+    steps = 25
+    r = ref_cuda.RefCuda(sc)
+    o = Oracle(sc)
+    e = engine_for(sc)
+    for x in (r, o, e):
+        x.run(steps)
+    sr = r.state()
+    for other in (o, e):
+        so = state_of(other)
+        for k in ("pos", "vel", "quat"):
+            close(so[k], sr[k], what=k)
+        close(so["omega"], sr["omega"], atol=1e-6, what="omega")
+        k1, l1, v1 = other.history(0)
+        k2, l2, v2 = r.history(0)
+        np.testing.assert_array_equal(k1, k2)
+        np.testing.assert_array_equal(l1, l2)
+        # history values integrate the state's rounding differences over the
+        # steps through the contact stiffness
+        assert np.abs(v1 - v2).max() <= 1e-6 * np.abs(v2).max() + 1e-15
+        if sc.n_bodies:
+            bo, br = other.bodies(), r.bodies()
+            for k in ("center", "quat", "vel", "omega"):
+                close(bo[k], br[k], what="body " + k)
+            close(bo["loads"], br["loads"], atol=1e-8 + 1e-6 * np.abs(br["loads"]).max(), what="body loads")
+            k1, l1, v1 = other.history(2)
+            k2, l2, v2 = r.history(2)
+            np.testing.assert_array_equal(k1, k2)
+            assert np.abs(v1 - v2).max() <= 1e-6 * np.abs(v2).max() + 1e-15

@@ -9,11 +9,12 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle.reference_build import reference_root
 
-REF = os.environ.get("DEM_REFERENCE_ROOT", "/root/reference")
+REF = reference_root()
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree not available")
+@pytest.mark.skipif(REF is None, reason="reference tree not available")
 def test_reference_host_program_links_against_engine(engine_lib):
     shim = os.path.join(ROOT, "dem_mbd_cuda_gb300", "shim")
     r = subprocess.run(["make", "-C", shim, f"REF={REF}", "-j8"], capture_output=True, text=True)
