@@ -2,17 +2,20 @@
 
 One "step" is one pass of the reference's step loop (advance, force
 evaluation, finish, host MBD) over the whole scene.  Default workload: the
-DEM-MBD scene of 200,000 spheres (r ~ U[1.5, 2.5] mm) in a 0.4 m box with a
-2,216-triangle rotating blade (prescribed, omega_z = 3 rad/s) and a
-192-triangle 1 kg dynamic plate, dt = 5e-6 s, seeded synthetic bed.
+rotating drum of 2,000,000 lognormal spheres (median 1 mm, sigma 0.25,
+clipped to [0.5, 2] mm) in a 19,520-triangle cylinder of radius 0.3 m and
+length 0.5 m turning at 2 rad/s, dt = 2e-6 s, seeded synthetic bed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--config c1|c0|c2] [--precision mixed|fp64]
+                  [--config c2|c1|c0|c4] [--precision mixed|fp64]
 
 Prints one JSON line.  ``value`` is particle-steps/s of the headline
 precision with the state resident in HBM (CUDA events on the engine stream);
 ``e2e`` is the same metric through the C ABI per step (body states uploaded
-and body loads read back every step, as the reference's host loop does).
+and body loads read back every step, as the reference's host loop does);
+``reference_fp64_cuda`` times the reference's own FP64 CUDA kernels on the
+same GPU and scenes.  With --gpus N > 1 outside torchrun, the script starts
+N ranks itself.
 """
 from __future__ import annotations
 
@@ -48,8 +51,10 @@ def make_scene(config, particles=None):
     if config == "c2":
         n = particles or 2000000
         sc, _ = G.drum(n=n, seed=1002)
-        return sc, ("rotating drum, %d lognormal spheres (median 1 mm) settled in columns and co-rotating, "
-                    "%d-triangle cylinder, dt 2e-6" % (n, sc.n_triangles))
+        return sc, ("rotating drum (R 0.3 m, L 0.5 m, 2 rad/s), %d lognormal spheres (median 1 mm, sigma 0.25, "
+                    "clipped to [0.5, 2] mm) settled in hexagonal columns and co-rotating, filling 45%% of the drum "
+                    "(config: 40%%, a solid fraction of 0.2 for 2M spheres), %d-triangle cylinder, friction 0.5, "
+                    "restitution 0.3, kN 1e5, dt 2e-6" % (n, sc.n_triangles))
     n = particles or 200000
     sc, _ = G.mbd_blade_plate(n=n, seed=1001)
     return sc, ("DEM-MBD, %d spheres r~U[1.5,2.5] mm settled in columns in a 0.4 m box, %d-triangle blade "
@@ -142,10 +147,24 @@ KERNEL_BYTES = {
 }
 
 
-def dominant_kernel(phases, n, sides, hv, list_length=None):
-    """The single-kernel phase that takes longest and its roofline inputs."""
+def pt_bytes(items, manifolds, hv_body):
+    """Algorithmic bytes of the particle-triangle law phase (probe, items and
+    law kernels): per contact item its cell, record and owner state 208 B;
+    per manifold the body history slot read and written and its load record
+    (32 doubles).  Triangle rows are shared by the items of a cell and not
+    counted."""
+    return items * 208 + manifolds * (2 * hv_body + 32 * 8)
+
+
+def dominant_kernel(phases, n, sides, hv, list_length=None, items=0, manifolds=0):
+    """The single-kernel phase that takes longest (sweep, particle law,
+    particle-triangle law or owner sum) and its roofline inputs."""
     times = dict(zip(PHASES, phases))
-    name = max(KERNEL_BYTES, key=lambda k: times.get(k, 0.0))
+    cands = list(KERNEL_BYTES) + (["pt"] if items else [])
+    name = max(cands, key=lambda k: times.get(k, 0.0))
+    if name == "pt":
+        kernel = "k_pt_thread" if items > 3072 else "k_pt_warp"
+        return name, kernel, times[name], pt_bytes(items, manifolds, 108)
     kernel, fn = KERNEL_BYTES[name]
     nbytes = fn(n, sides, hv, list_length) if name == "sweep" else fn(n, sides, hv)
     return name, kernel, times[name], nbytes
@@ -267,20 +286,88 @@ def load_error(scene, evaluations=3):
     return out
 
 
-def drum_summary(steps, warmup):
-    """The 2,000,000-sphere drum in both precisions and the mixed form's
-    error against FP64: the scene the engine's headline target is set on."""
-    scene, desc = make_scene("c2")
-    out = {"workload": desc, "particles": scene.n}
+def wall_contacts(e, scene):
+    """Particle-wall contacts of the engine's last evaluation (wall history
+    slots seen in the latest step)."""
+    if not scene.n_walls:
+        return 0
+    keys, last, _ = e.history(1)
+    used = keys != 0
+    return int((used & (last == last[used].max())).sum()) if used.any() else 0
+
+
+def roofline(phases, scene, stats, nlists, precision, e, per_step_ms):
+    """Roofline of the dominant kernel (CUDA-event time of its phase) and the
+    step-level algorithmic bytes (section (d) of the design notes)."""
+    h = 4 if precision == "mixed" else 8
+    hv = 3 * h * 4            # one history slot: 9 values padded to 12
+    contacts = stats["particle_contacts"]
+    peak, peak_kind = hbm_peak()
+    pname, kernel, kms, kbytes = dominant_kernel(phases, scene.n, contacts, hv, nlists["mean_length"],
+                                                 stats.get("body_candidate_items", 0), stats["body_contacts"])
+    achieved = kbytes / (kms / 1000.0) / 1e9
+    traffic, traffic_src = measured_traffic(kernel, scene.n)
+    step_bytes = algorithmic_bytes(scene.n, scene.n_components, contacts, wall_contacts(e, scene),
+                                   stats["body_contacts"], scene.n_triangles, h)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": kernel, "phase": pname, "kernel_ms": kms,
+            "algorithmic_bytes": kbytes, "traffic_source": traffic_src, "peak_kind": peak_kind + " (hbm_gbs)",
+            "step": {"algorithmic_bytes": step_bytes, "achieved": step_bytes / (per_step_ms / 1000.0) / 1e9}}
+
+
+def scene_summary(config, steps, warmup):
+    """A workload in both precisions, its phases, the dominant kernel's
+    roofline and the mixed form's error against FP64."""
+    scene, desc = make_scene(config)
+    out = {"workload": desc, "particles": scene.n, "triangles": scene.n_triangles}
     for prec in ("mixed", "fp64"):
         e, ms, clocks, stats, phases, after = run_engine(scene, prec, steps, warmup)
         out[prec] = {"value": scene.n * steps / (ms / 1000.0), "ms_per_step": ms / steps,
                      "contact_sides_per_step": stats["particle_contacts"],
                      "body_manifolds": stats["body_contacts"], "phase_ms": dict(zip(PHASES, phases)),
-                     "neighbor_lists": after["neighbor_lists"], "clocks": clocks}
+                     "neighbor_lists": after["neighbor_lists"], "clocks": clocks,
+                     "roofline": roofline(phases, scene, stats, after["neighbor_lists"], prec, e, ms / steps)}
         del e
     out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["load_error_vs_fp64"] = load_error(scene)
+    return out
+
+
+def host_cpu():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def reference_cuda_summary(configs, steps, warmup):
+    """The reference's own FP64 CUDA path on this GPU: its kernels, built
+    from its src/cuda/*.cu for sm_103a (oracle/_ref/ref_engine.cubin), driven
+    by oracle/ref_cuda_host.cu, a restatement of its host loop with the same
+    launches, Thrust calls, synchronous copies and host MBD step on one host
+    thread.  Wall-clock time of `steps` steps after `warmup` steps, device
+    synchronised on both sides."""
+    from oracle import ref_cuda
+    if not ref_cuda.available():
+        return {"unavailable": "the reference's device code was not built (oracle/reference_build.py needs the "
+                               "reference tree where the repository is built)"}
+    ref_cuda.build()
+    out = {"kind": "reference FP64 CUDA kernels (src/cuda/*.cu, sm_103a) with its host loop restated",
+           "host": {"cpu": host_cpu(), "cores": os.cpu_count(), "host_threads_used": 1}}
+    for config in configs:
+        scene, desc = make_scene(config)
+        r = ref_cuda.RefCuda(scene)
+        r.run(max(1, warmup))
+        k = max(1, min(steps, 20))
+        sec = r.time_run(k)
+        out[config] = {"workload": desc, "ms_per_step": 1e3 * sec / k, "value": scene.n * k / sec,
+                       "unit": "particle-steps/s", "steps": k, "warmup": max(1, warmup)}
+        del r
     return out
 
 
@@ -444,10 +531,13 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c4"])
+    ap.add_argument("--config", default="c2", choices=["c0", "c1", "c2", "c4"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-drum", action="store_true", help="skip the embedded 2M-sphere drum summary")
+    ap.add_argument("--no-c1", action="store_true", help="skip the embedded config-1 (200k DEM-MBD) summary")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip the timing of the reference's FP64 CUDA kernels")
     ap.add_argument("--no-batch", action="store_true", help="skip the embedded 256-scene batch summary")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the embedded config-3 adjoint summary")
     ap.add_argument("--no-autotune", action="store_true", help="skip the embedded autotuner summary")
@@ -462,6 +552,18 @@ def main():
     args.warmup = max(3, args.warmup)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: start the ranks here, as the multi-GPU
+        # launcher would (rank 0 prints the line)
+        import socket
+        with socket.socket() as sock:
+            sock.bind(("127.0.0.1", 0))
+            port = sock.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *sys.argv[1:]]
+        sys.exit(subprocess.call(cmd))
+    if world != args.gpus and args.impl != "reference":
+        ap.error(f"--gpus {args.gpus} but WORLD_SIZE={world}")
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
@@ -476,6 +578,8 @@ def main():
         else:
             print(json.dumps(adjoint_summary()))
         return
+    if args.impl == "reference" and rank != 0:
+        return
     scene, desc = make_scene(args.config, args.particles)
     if isinstance(scene, list) and not args.single:
         ap.error("--config c4 runs with --single; the default line carries it as batch_256")
@@ -488,26 +592,37 @@ def main():
         scene = [scene[i] for i in parts[rank]]
 
     if args.impl == "reference":
-        # The reference's own hot path is CUDA-only; its CPU implementation of
-        # the path here is the oracle port on the host cores.
-        if rank != 0:
-            return
+        # The reference's hot path is CUDA-only; its CPU implementation of the
+        # path here is the oracle port on all host cores.  A CPU step of the
+        # 2M-sphere drum takes about half a second, so the timed steps are
+        # bounded to about a minute of work (the line states how many ran).
         from oracle import oracle as orc
         orc.build()
         from oracle.oracle import Oracle
         threads = os.cpu_count() or 1
         o = Oracle(scene, threads=threads)
-        o.run(args.warmup)
+        o.run(1)
         t0 = time.perf_counter()
-        o.run(args.steps)
+        warm = 1
+        while warm < args.warmup and time.perf_counter() - t0 < 10.0:
+            o.run(1)
+            warm += 1
+        done = 0
+        t0 = time.perf_counter()
+        while done < args.steps:
+            o.run(1)
+            done += 1
+            if time.perf_counter() - t0 >= 60.0:
+                break
         dt = time.perf_counter() - t0
-        v = scene.n * args.steps / dt
+        v = scene.n * done / dt
         line = {"impl": "reference", "metric": "particle-steps/s", "value": v, "unit": "particle-steps/s",
-                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
+                "n_gpus": 0, "steps": done, "warmup": warm, "ms_per_step": dt * 1000 / done,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": desc, "particles": scene.n, "triangles": scene.n_triangles},
                 "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                                 "sample": f"{args.steps} steps of the workload after {args.warmup} warm-up steps"},
+                                 "sample": f"{done} of the {args.steps} requested steps of the workload (at most "
+                                           f"60 s of work) after {warm} warm-up steps"},
                 "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -515,10 +630,15 @@ def main():
     if world > 1:
         # one GPU per rank, fixed before the first CUDA call (the engine runs
         # on the current device): this rank's entry of the visible list, or
-        # its local rank; a list of one was already narrowed by the launcher
+        # its local rank when no list is set; a list of one was already
+        # narrowed by the launcher
         ids = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
-        if len(ids) != 1:
-            os.environ["CUDA_VISIBLE_DEVICES"] = ids[local] if local < len(ids) else str(local)
+        if len(ids) > 1:
+            if local >= len(ids):
+                raise SystemExit(f"local rank {local} has no GPU in CUDA_VISIBLE_DEVICES={','.join(ids)}")
+            os.environ["CUDA_VISIBLE_DEVICES"] = ids[local]
+        elif not ids:
+            os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     from dem_mbd_cuda_gb300 import build
     build.build()
     if dist:
@@ -526,13 +646,12 @@ def main():
     e, ms, clocks, stats, phases, after = run_engine(scene, args.precision, args.steps, args.warmup)
     nlists = after["neighbor_lists"]
     if args.single:
-        if sharded:
-            # the whole batch's particles over the slowest rank's time
+        if dist:
             from dem_mbd_cuda_gb300.shard import max_over_ranks
             ms = max_over_ranks(ms)
-            value = n_all * args.steps / (ms / 1000.0)
-        else:
-            value = world * n_all * args.steps / (ms / 1000.0)
+        # sharded: the whole batch's particles over the slowest rank's time;
+        # replicas: every rank's particles over the slowest rank's time
+        value = (n_all if sharded else world * n_all) * args.steps / (ms / 1000.0)
         if rank != 0:
             return
         print(json.dumps({"metric": "particle-steps/s", "value": value, "ms_per_step": ms / args.steps,
@@ -542,6 +661,9 @@ def main():
                           "precision": args.precision, "phase_ms": dict(zip(PHASES, phases)),
                           "contact_sides_per_step": stats["particle_contacts"], "clocks": clocks}))
         return
+    per_step_ms = ms / args.steps
+    roof = roofline(phases, scene, stats, nlists, args.precision, e, per_step_ms)
+    del e
     other = "fp64" if args.precision == "mixed" else "mixed"
     e_o, ms_o, _, _, phases_o, _ = run_engine(scene, other, args.steps, args.warmup)
     del e_o
@@ -553,33 +675,43 @@ def main():
     value = world * scene.n * args.steps / (ms / 1000.0)
     value_other = world * scene.n * args.steps / (ms_o / 1000.0)
     e2e_ms = e2e_run(scene, args.precision, args.steps, args.warmup)
+    if dist:
+        from dem_mbd_cuda_gb300.shard import max_over_ranks
+        e2e_ms = max_over_ranks(e2e_ms)
     e2e_value = world * scene.n * args.steps / (e2e_ms / 1000.0)
     if rank != 0:
         return
     errs = load_error(scene)
-    h = 4 if args.precision == "mixed" else 8
-    hv = 3 * h * 4            # one history slot: 9 values padded to 12
     contacts = stats["particle_contacts"]
-    peak, peak_kind = hbm_peak()
-    pname, kernel, kms, kbytes = dominant_kernel(phases, scene.n, contacts, hv, nlists["mean_length"])
-    achieved = kbytes / (kms / 1000.0) / 1e9
-    traffic, traffic_src = measured_traffic(kernel, scene.n)
-    step_bytes = algorithmic_bytes(scene.n, scene.n_components, contacts, 0, stats["body_contacts"],
-                                   scene.n_triangles, h)
     cpu = None
     if not args.no_cpu_baseline:
         v, cores, done, dt = cpu_baseline(scene)
         cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                "sample": f"{done} steps of the same workload on {cores} threads ({dt:.1f} s)"}
-    drum = None
+    subs = {}
     if args.config != "c2" and not args.no_drum:
-        drum = drum_summary(args.steps, args.warmup)
-    batch = None
+        subs["drum_2m"] = scene_summary("c2", args.steps, args.warmup)
+    if args.config != "c1" and not args.no_c1:
+        subs["c1_200k"] = scene_summary("c1", args.steps, args.warmup)
     if args.config != "c4" and not args.no_batch:
-        batch = batch_summary(args.steps, args.warmup)
-    adjoint = None if args.no_adjoint else adjoint_summary()
-    adjoint_batch = None if args.no_adjoint or args.no_batch else batch_adjoint_summary()
-    tuned = None if args.no_autotune else autotune_summary(scene, args.precision)
+        subs["batch_256"] = batch_summary(args.steps, args.warmup)
+    if not args.no_reference_cuda:
+        ref = reference_cuda_summary([args.config] + (["c1"] if args.config != "c1" and not args.no_c1 else []),
+                                     args.steps, args.warmup)
+        if args.config in ref:
+            ref[args.config]["engine_over_reference"] = {
+                args.precision: value / world / ref[args.config]["value"],
+                other: value_other / world / ref[args.config]["value"]}
+        if "c1" in ref and "c1_200k" in subs:
+            ref["c1"]["engine_over_reference"] = {p: subs["c1_200k"][p]["value"] / ref["c1"]["value"]
+                                                  for p in ("mixed", "fp64")}
+        subs["reference_fp64_cuda"] = ref
+    if not args.no_adjoint:
+        subs["adjoint_c3"] = adjoint_summary()
+        if not args.no_batch:
+            subs["adjoint_batch"] = batch_adjoint_summary()
+    if not args.no_autotune:
+        subs["autotuned"] = autotune_summary(scene, args.precision)
     nb = scene.n_bodies
     line = {
         "metric": "particle-steps/s",
@@ -600,31 +732,19 @@ def main():
         "fp64_value" if args.precision == "mixed" else "mixed_value": value_other,
         "contacts_per_s": contacts * args.steps / (ms / 1000.0) / 2,
         "contact_sides_per_step": contacts,
+        "body_manifolds_per_step": stats["body_contacts"],
         "load_error_vs_fp64": errs,
         "phase_ms": dict(zip(PHASES, phases)),
+        "phase_ms_" + other: dict(zip(PHASES, phases_o)),
         "neighbor_lists": nlists,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": kernel, "phase": pname, "kernel_ms": kms,
-                     "algorithmic_bytes": kbytes, "traffic_source": traffic_src,
-                     "peak_kind": peak_kind + " (hbm_gbs)",
-                     "step": {"algorithmic_bytes": step_bytes,
-                              "achieved": step_bytes / (per_step_ms / 1000.0) / 1e9}},
+        "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 13 * 8 * nb,
                 "d2h_bytes_per_step": 38 * 8 * nb + 16 * 4},
         "gpu_launches": launches_per_step(scene) * args.steps,
         "clocks": clocks,
     }
-    if drum:
-        line["drum_2m"] = drum
-    if batch:
-        line["batch_256"] = batch
-    if adjoint:
-        line["adjoint_c3"] = adjoint
-    if adjoint_batch:
-        line["adjoint_batch"] = adjoint_batch
-    if tuned:
-        line["autotuned"] = tuned
+    line.update(subs)
     print(json.dumps(line))
 
 

@@ -299,8 +299,23 @@ def column_bed(n, col_xy, base_z, radius_fn, rng, cap, g, kN, kN_base, density=D
     return pos, r.ravel()[sel], cols
 
 
-def column_grid(lo, hi, pitch, jitter, rng):
-    """Column axes on a square lattice covering [lo, hi] (2-D), jittered."""
+def column_grid(lo, hi, pitch, jitter, rng, hexagonal=False):
+    """Column axes on a square lattice covering [lo, hi] (2-D), jittered;
+    or (``hexagonal``) on staggered rows ``pitch * sqrt(3) / 2`` apart, every
+    other row shifted by half a pitch, which keeps the nearest axes
+    ``pitch`` apart with 15% more columns per area."""
+    if hexagonal:
+        dy = pitch * np.sqrt(3.0) / 2.0
+        ny = int(np.floor((hi[1] - lo[1]) / dy)) + 1
+        oy = lo[1] + 0.5 * ((hi[1] - lo[1]) - (ny - 1) * dy)
+        rows = []
+        for j in range(ny):
+            shift = 0.5 * pitch * (j % 2)
+            nx = int(np.floor((hi[0] - lo[0] - shift) / pitch)) + 1
+            ox = lo[0] + shift + 0.5 * ((hi[0] - lo[0] - shift) - (nx - 1) * pitch)
+            rows.append(np.column_stack([ox + pitch * np.arange(nx), np.full(nx, oy + j * dy)]))
+        xy = np.concatenate(rows)
+        return xy + rng.uniform(-jitter, jitter, size=xy.shape)
     nx = int(np.floor((hi[0] - lo[0]) / pitch)) + 1
     ny = int(np.floor((hi[1] - lo[1]) / pitch)) + 1
     ox = lo[0] + 0.5 * ((hi[0] - lo[0]) - (nx - 1) * pitch)
@@ -360,7 +375,7 @@ def mbd_blade_plate(n=200000, seed=1001, rmin=1.5e-3, rmax=2.5e-3, box=0.4, dt=5
 
 
 def drum(n=2000000, seed=1002, radius=0.3, length=0.5, omega=2.0, dt=2e-6, name="c2_drum", ntheta=160, nx=50,
-         nrings=6, pitch=3.1e-3):
+         nrings=6, pitch=4.11e-3):
     """Config 2: lognormal radii (median 1 mm, sigma 0.25, clipped to
     [0.5, 2] mm) in a rotating closed cylinder (axis x, inward normals,
     prescribed omega_x), friction 0.5, restitution 0.3, kN 1e5.
@@ -368,9 +383,12 @@ def drum(n=2000000, seed=1002, radius=0.3, length=0.5, omega=2.0, dt=2e-6, name=
     The bed is settled and turning with the drum: vertical columns in force
     balance (``column_bed``) standing on the cylinder's facets, every
     sphere moving with the drum's rigid rotation (v = omega x p, spin =
-    omega), so the wall does not slip under the bed at the start.  The
-    column pitch caps the radii at 1.5 mm (about 5% of the lognormal draws
-    lie above it)."""
+    omega), so the wall does not slip under the bed at the start.  Columns
+    stand on a hexagonal lattice 4.11 mm apart, which admits every radius up
+    to the 2 mm clip; 2,000,000 spheres then fill 45% of the drum (solid
+    fraction 0.17 below the bed surface).  A 40% fill with 2M spheres would
+    need a solid fraction of 0.2, denser than columns that admit 2 mm
+    spheres pack."""
     rng = np.random.default_rng(seed)
     g = 9.81
 
@@ -382,7 +400,7 @@ def drum(n=2000000, seed=1002, radius=0.3, length=0.5, omega=2.0, dt=2e-6, name=
     half_len = length / 2 - cap - 0.5e-3
     inner = radius * np.cos(np.pi / ntheta)          # facet plane distance from the axis
     reach = np.sqrt((inner - cap) ** 2 - (0.5 * inner) ** 2)
-    xy = column_grid(np.array([-half_len, -reach]), np.array([half_len, reach]), pitch, jitter, rng)
+    xy = column_grid(np.array([-half_len, -reach]), np.array([half_len, reach]), pitch, jitter, rng, hexagonal=True)
     # facets of the lower half: plane (cos a, sin a) . (y, z) = inner at the
     # facet's mid angle a (sin a < 0); a sphere of radius r inside has
     # (cos a, sin a) . (y, z) <= inner - r for every facet, so on the
@@ -565,3 +583,92 @@ def small_dem(n=500, seed=3, dt=1e-5, rmin=1.8e-3, rmax=2.2e-3, vel_std=0.01, om
     m = mech(kN=1e5, epsN=0.5, epsS=0.6, mu=0.4, muT=muT, muR=muR, beta=0.5)
     return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
                  wall_normal=wn, name=name)
+
+
+def clumps(n_owners=216, seed=5, dt=1e-5, rc=1.0e-3, vel_std=1e-5, omega_std=0.01, overlap=5e-9, name="clumps"):
+    """A pile of rigid multi-sphere owners (clumps) of 1 to 8 components in a
+    walled box, for tests of the clump path (src/cuda_backend_cuda.cu:121-190,
+    src/particle.cpp:170-278).  Each owner's components sit on random
+    directions at 0 to 1.2 component radii from the owner's mass centre
+    (body frame), so they overlap one another; component ids are unique and
+    the components are listed in shuffled order.  Owners are dropped one by
+    one (unrotated) at random (x, y) onto the floor or the owners below and
+    stop where a component first touches, overlapping by ``overlap``, so
+    every owner rests on something from the first step; small random
+    velocities and spins and anisotropic principal inertia exercise every
+    history channel and the offset torques."""
+    rng = np.random.default_rng(seed)
+    width = 2.6 * rc * np.sqrt(n_owners / 6.0)
+    comp_owner, comp_radius, comp_offset = [], [], []
+    mass, inertia, radius, pos = [], [], [], []
+    placed_p = np.zeros((0, 3))
+    placed_r = np.zeros(0)
+    for i in range(n_owners):
+        k = int(rng.integers(1, 9))
+        d = rng.normal(size=(k, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        off = d * rng.uniform(0.0, 1.2 * rc, size=(k, 1))
+        rr = rng.uniform(0.8 * rc, 1.2 * rc, size=k)
+        mk = DENSITY * 4.0 / 3.0 * np.pi * rr ** 3
+        m = float(mk.sum())
+        off = off - (mk[:, None] * off).sum(0) / m        # offsets about the owner's mass centre
+        I = np.zeros(3)
+        for a in range(3):
+            b, cc = (a + 1) % 3, (a + 2) % 3
+            I[a] = float((mk * (0.4 * rr ** 2 + off[:, b] ** 2 + off[:, cc] ** 2)).sum())
+        xy = rng.uniform(-width / 2, width / 2, size=2)
+        cxy = xy[None, :] + off[:, :2]
+        z = float((rr - off[:, 2]).max())                 # resting on the floor
+        if len(placed_r):
+            h2 = ((cxy[:, None, :] - placed_p[None, :, :2]) ** 2).sum(-1)
+            s2 = (rr[:, None] + placed_r[None, :]) ** 2
+            touch = h2 < s2
+            if touch.any():
+                zc = placed_p[None, :, 2] + np.sqrt(np.where(touch, s2 - h2, 0.0)) - off[:, 2:3]
+                z = max(z, float(zc[touch].max()))
+        z -= overlap
+        centre = np.array([xy[0], xy[1], z])
+        placed_p = np.concatenate([placed_p, centre + off])
+        placed_r = np.concatenate([placed_r, rr])
+        comp_owner += [i] * k
+        comp_radius += rr.tolist()
+        comp_offset += off.tolist()
+        mass.append(m)
+        inertia.append(I)
+        radius.append(float((np.linalg.norm(off, axis=1) + rr).max()))
+        pos.append(centre)
+    own = np.array(comp_owner)
+    nc = len(own)
+    kw = dict(owner_id=np.arange(n_owners, dtype=np.int32) * 3 + 1,
+              owner_status=np.zeros(n_owners, np.int32), owner_mass=np.array(mass),
+              owner_radius=np.array(radius), owner_inertia=np.array(inertia), pos=np.array(pos),
+              vel=rng.normal(0, vel_std, size=(n_owners, 3)), omega=rng.normal(0, omega_std, size=(n_owners, 3)),
+              quat=np.tile([1.0, 0.0, 0.0, 0.0], (n_owners, 1)))
+    perm = rng.permutation(nc)                            # input order need not be owner order
+    ids = rng.permutation(nc).astype(np.int32) + 100
+    span = width / 2 + 3 * rc
+    wo, wn = box_walls([-span, -span, 0.0], [span, span, 0.2])
+    m = mech(kN=1e5, epsN=0.5, epsS=0.6, mu=0.4, muT=0.1, muR=0.05, beta=0.5)
+    return Scene(**kw, comp_owner=own.astype(np.int32)[perm], comp_id=ids,
+                 comp_radius=np.array(comp_radius)[perm], comp_offset=np.array(comp_offset)[perm],
+                 pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, -9.81), gravity_enabled=1, wall_origin=wo,
+                 wall_normal=wn, name=name)
+
+
+def universal_gravity(n=2000, seed=9, dt=1e-5, name="universal_gravity"):
+    """Spheres in a loose cloud with mutual gravitation on
+    (CONTROL universal gravitation, src/cuda/cuda_contact_backend.cu:1095-1106)
+    and a few contacts, no walls.  The density is 1e9 kg/m^3 so the pairwise
+    attraction (constant 6.674e-11) is about 1% of the contact forces, well
+    above their rounding."""
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(n ** (1 / 3)))
+    pitch = 4.1e-3
+    idx = np.stack(np.meshgrid(np.arange(side), np.arange(side), np.arange(side), indexing="ij"), -1).reshape(-1, 3)[:n]
+    pos = idx * pitch + rng.uniform(-0.1e-3, 0.1e-3, size=(n, 3))
+    rad = rng.uniform(1.8e-3, 2.1e-3, size=n)
+    kw = make_spheres(pos, rad, 1e9, vel=rng.normal(0, 0.01, size=(n, 3)))
+    kw["omega"] = rng.normal(0, 5.0, size=(n, 3))
+    m = mech(kN=1e5, epsN=0.5, epsS=0.6, mu=0.4, muT=0.1, muR=0.05, beta=0.5)
+    return Scene(**kw, pp=m, pt=m, pw=m, dt=dt, gravity=(0.0, 0.0, 0.0), gravity_enabled=0,
+                 universal_gravity_enabled=1, name=name)

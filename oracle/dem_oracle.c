@@ -159,6 +159,9 @@ typedef struct orc {
     unsigned long long *reg_inst, *reg_int;
     double *micro_state, *micro_inst, *micro_int;
     unsigned long long reg_native_steps;
+    /* the copies the last diagnostic evaluation downloaded */
+    unsigned long long *diag_reg_inst, *diag_reg_int;
+    double *diag_micro_inst, *diag_micro_int;
     mech_t pp, pt, pw;
     double g[3];
     int grav, ugrav;
@@ -314,6 +317,10 @@ orc* orc_create(const dem_scene* s, int nthreads)
         o->micro_state = zalloc((size_t)nb * nc * NMICRO * sizeof(double));
         o->micro_inst = zalloc((size_t)nb * NMICRO * sizeof(double));
         o->micro_int = zalloc((size_t)nb * NMICRO * sizeof(double));
+        o->diag_reg_inst = zalloc((size_t)nb * NREG * sizeof(unsigned long long));
+        o->diag_reg_int = zalloc((size_t)nb * NREG * sizeof(unsigned long long));
+        o->diag_micro_inst = zalloc((size_t)nb * NMICRO * sizeof(double));
+        o->diag_micro_int = zalloc((size_t)nb * NMICRO * sizeof(double));
         o->bhalf_v = zalloc(3 * nb * sizeof(double)); o->bhalf_w = zalloc(3 * nb * sizeof(double));
         o->bhalf_q = zalloc(4 * nb * sizeof(double)); o->bhalf_dq = zalloc(4 * nb * sizeof(double));
         o->bacc = zalloc(3 * nb * sizeof(double)); o->bdomg = zalloc(3 * nb * sizeof(double));
@@ -343,7 +350,8 @@ void orc_destroy(orc* o)
                     o->bstate, o->tbody, o->tloc, o->tw, o->taabb, o->skey, o->sid, o->tkey, o->tid, o->fcontact,
                     o->ffield, o->fwall, o->ftotal, o->fbodyp, o->fbodyd, o->bres, o->regime_state, o->reg_inst,
                     o->reg_int, o->micro_state, o->micro_inst, o->micro_int, o->bhalf_v, o->bhalf_w, o->bhalf_q,
-                    o->bhalf_dq, o->bacc, o->bdomg, o->bloads};
+                    o->bhalf_dq, o->bacc, o->bdomg, o->bloads, o->diag_reg_inst, o->diag_reg_int,
+                    o->diag_micro_inst, o->diag_micro_int};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; ++k) free(ptrs[k]);
     hist_free(&o->hp); hist_free(&o->hw); hist_free(&o->hb);
     free(o);
@@ -1175,6 +1183,17 @@ int orc_compute_forces(orc* o, const double* bc, const double* bq, const double*
         s->particle_history_high_water = o->phigh; s->body_history_high_water = o->bhigh;
         s->triangle_grid_overflows = o->tgover;
         s->body_regime_interval_native_steps = o->reg_native_steps;
+        /* download the counters and sums, then reset the interval ones
+         * (src/cuda_backend_cuda.cu:431-482) */
+        if (nb > 0) {
+            memcpy(o->diag_reg_inst, o->reg_inst, nb * NREG * sizeof(unsigned long long));
+            memcpy(o->diag_reg_int, o->reg_int, nb * NREG * sizeof(unsigned long long));
+            memcpy(o->diag_micro_inst, o->micro_inst, nb * NMICRO * sizeof(double));
+            memcpy(o->diag_micro_int, o->micro_int, nb * NMICRO * sizeof(double));
+            memset(o->reg_int, 0, nb * NREG * sizeof(unsigned long long));
+            memset(o->micro_int, 0, nb * NMICRO * sizeof(double));
+            o->reg_native_steps = 0;
+        }
         if (o->pover) { set_error("particle contact-history capacity exceeded"); return DEM_ERR_CAPACITY; }
         if (o->bover) { set_error("wall/body contact-history capacity exceeded"); return DEM_ERR_CAPACITY; }
     }
@@ -1191,19 +1210,16 @@ int orc_compute_forces(orc* o, const double* bc, const double* bq, const double*
     return DEM_OK;
 }
 
-/* Copies of the interval counters, then reset, as the diagnostic download
- * does (src/cuda_backend_cuda.cu:431-482). */
+/* The regime counters and microstate sums of the last diagnostic
+ * evaluation, as CudaStepStats carries them (src/cuda_backend_cuda.cu:431-482). */
 void orc_body_diagnostics(orc* o, unsigned long long* ri, unsigned long long* rv, double* mi, double* mv)
 {
     int nb = o->nb;
     if (nb <= 0) return;
-    if (ri) memcpy(ri, o->reg_inst, nb * NREG * sizeof(unsigned long long));
-    if (rv) memcpy(rv, o->reg_int, nb * NREG * sizeof(unsigned long long));
-    if (mi) memcpy(mi, o->micro_inst, nb * NMICRO * sizeof(double));
-    if (mv) memcpy(mv, o->micro_int, nb * NMICRO * sizeof(double));
-    memset(o->reg_int, 0, nb * NREG * sizeof(unsigned long long));
-    memset(o->micro_int, 0, nb * NMICRO * sizeof(double));
-    o->reg_native_steps = 0;
+    if (ri) memcpy(ri, o->diag_reg_inst, nb * NREG * sizeof(unsigned long long));
+    if (rv) memcpy(rv, o->diag_reg_int, nb * NREG * sizeof(unsigned long long));
+    if (mi) memcpy(mi, o->diag_micro_inst, nb * NMICRO * sizeof(double));
+    if (mv) memcpy(mv, o->diag_micro_int, nb * NMICRO * sizeof(double));
 }
 
 /* ---------------------------------------------------------------- leapfrog */
