@@ -50,3 +50,34 @@ def max_over_ranks(x, group=None):
     t = torch.tensor([float(x)], dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
     return float(t[0])
+
+
+def split_by_scene(array, counts):
+    """Rows of a batch array ([sum(counts), ...], scenes one after the other)
+    as one block per scene."""
+    import numpy as np
+    edges = np.cumsum([0] + list(counts))
+    return [array[edges[k]:edges[k + 1]] for k in range(len(counts))]
+
+
+def gather_batch_gradients(local, parts, counts, group=None):
+    """The reverse-mode result of this rank's batch engine
+    (CudaDemSolver.adjoint_backward over the scenes parts[rank], in that
+    order) gathered into the whole batch's result on every rank: dl_dpos0,
+    dl_dvel0 and dl_domega0 as [sum(counts), 3] arrays in scene order and
+    dl_dparams as one entry per scene.  `counts` are the particles of every
+    scene of the batch."""
+    import numpy as np
+    import torch.distributed as dist
+    rank = dist.get_rank(group)
+    mine = [counts[i] for i in parts[rank]]
+    per = local["dl_dparams"]
+    per = per if isinstance(per, list) else [per]
+    if len(per) != len(mine):
+        raise ValueError("one parameter gradient per scene of this rank's share")
+    blocks = {k: split_by_scene(np.asarray(local[k]), mine) for k in ("dl_dpos0", "dl_dvel0", "dl_domega0")}
+    rows = [{"dl_dparams": per[j], **{k: blocks[k][j] for k in blocks}} for j in range(len(mine))]
+    allrows = gather_per_scene(rows, parts, group=group)
+    out = {k: np.concatenate([r[k] for r in allrows]).reshape(-1, 3) for k in blocks}
+    out["dl_dparams"] = [r["dl_dparams"] for r in allrows]
+    return out

@@ -271,8 +271,11 @@ int dem_last_phase_times(dem_engine* engine, float* ms, int capacity,
  * grid build and the reference's sortedCellKey / sortedEntityId: cell keys
  * packCell(floor(p / mesh_size)) of the n positions, sorted stably over the
  * input order.  x, y, z, sorted_key[n] and sorted_id[n] are DEVICE buffers
- * owned by the caller; stream is a cudaStream_t (NULL = default stream) and
- * the call returns after that stream has finished the work.
+ * owned by the caller; stream is a cudaStream_t (NULL = default stream).
+ * The call waits for that stream to finish the work and reads its error
+ * word back before it returns.  Inside a cell the members are ranked by
+ * counting the members with a smaller index, so a cell of m members costs
+ * O(m^2) work (every component in one cell: n^2 compares).
  * Working memory is one built-in device array of about 14 MB that every GPU
  * loading this library keeps until the process exits; n is limited to
  * DEM_STATIC_SORT_MAX_COMPONENTS and the occupied cell box to

@@ -199,3 +199,49 @@ def test_batch_matches_reference_kernels_scene_by_scene():
             np.testing.assert_array_equal(hb[kind][0][off:off + s.n], kr, err_msg=f"{s.name} keys {kind}")
             np.testing.assert_array_equal(hb[kind][1][off:off + s.n], lr, err_msg=f"{s.name} last-seen {kind}")
         off += s.n
+
+
+def _loads_per_step(x, steps):
+    out = []
+    for _ in range(steps):
+        x.run(1)
+        out.append(x.bodies()["loads"].copy())
+    return out
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("name,steps", [("small_mbd", 25), ("c1", 6)])
+def test_cap_knife_edge_is_the_reference_model_s_own(name, steps):
+    """Where particle-triangle manifolds slide at their Coulomb cap, the
+    reference's body loads jump with the last bit of its inputs: the
+    per-triangle pass re-tests the capped history against a limit equal to
+    it up to rounding (src/cuda/cuda_contact_backend.cu:783-807 after
+    :922-947), and the body loads it sums with atomicAdd change in their last
+    bits with the order the atomics land in.  The reference's own spread --
+    the reference run again, and the reference with one input moved by one
+    ulp (the plate's initial height on the small scene, the blade's spin on
+    config 1) -- reaches 1e-3 of the loads within the window, and the FP64
+    engine's departure from the reference stays within three times that
+    spread."""
+    if name == "small_mbd":
+        sc = G.small_mbd()
+        ulp = sc.copy()
+        ulp.body_center[0, 2] = np.nextafter(ulp.body_center[0, 2], np.inf)
+    else:
+        sc = _config_scene("c1")
+        ulp = sc.copy()
+        ulp.body_omega[0, 2] = np.nextafter(ulp.body_omega[0, 2], np.inf)
+    ref = _loads_per_step(ref_cuda.RefCuda(sc), steps)
+    again = _loads_per_step(ref_cuda.RefCuda(sc), steps)
+    moved = _loads_per_step(ref_cuda.RefCuda(ulp), steps)
+    eng = _loads_per_step(engine_for(sc), steps)
+    rerun = max(_rel(a, r) for a, r in zip(again, ref))
+    one_ulp = max(_rel(m, r) for m, r in zip(moved, ref))
+    departure = max(_rel(x, r) for x, r in zip(eng, ref))
+    print(f"{name}: reference rerun {rerun:.3g}, reference one ulp {one_ulp:.3g}, engine {departure:.3g}")
+    envelope = max(rerun, one_ulp)
+    assert envelope >= 1e-3, envelope
+    assert departure <= 3 * envelope, (departure, envelope)
