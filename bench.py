@@ -414,6 +414,7 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
     t0 = time.perf_counter()
     g = e.adjoint_backward(dpos, None, dl_dbody_center=dplate)
     t_bwd = time.perf_counter() - t0
+    mem = e.adjoint_memory()
     plate_final = e.bodies()["center"][0].tolist()
     # finite-difference check at short horizons (FP64 central differences,
     # relative step 1e-6) on the same generator at 2,000 spheres: with many
@@ -471,7 +472,7 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
                         % (n, steps, checkpoint_every),
             "forward_plain_s": t_plain, "forward_checkpointed_s": t_fwd, "backward_s": t_bwd,
             "adjoint_over_forward": t_bwd / t_plain, "total_over_forward": (t_fwd + t_bwd) / t_plain,
-            "plate_final_center": plate_final,
+            "memory": mem, "plate_final_center": plate_final,
             "dl_dparams": g["dl_dparams"], "dl_dvel0_norm": float(np.linalg.norm(g["dl_dvel0"])),
             "fd_check": fd}
 
@@ -507,6 +508,7 @@ def batch_adjoint_summary(nscenes=64, steps=50, checkpoint_every=10):
     t0 = time.perf_counter()
     g = e.adjoint_backward(dpos, None)
     t_bwd = time.perf_counter() - t0
+    mem = e.adjoint_memory()
     del e
     per = g["dl_dparams"]
     return {"workload": "the first %d scenes of the 256-scene batch (%d spheres), %d steps of dt 1e-5, checkpoints "
@@ -514,7 +516,7 @@ def batch_adjoint_summary(nscenes=64, steps=50, checkpoint_every=10):
                                                                                     checkpoint_every),
             "forward_plain_s": t_plain, "forward_checkpointed_s": t_fwd, "backward_s": t_bwd,
             "adjoint_over_forward": t_bwd / t_plain, "total_over_forward": (t_fwd + t_bwd) / t_plain,
-            "per_scene_pp_dmu": [p["pp"]["mu"] for p in per[:4]],
+            "memory": mem, "per_scene_pp_dmu": [p["pp"]["mu"] for p in per[:4]],
             "per_scene_pp_depsN": [p["pp"]["epsN"] for p in per[:4]]}
 
 

@@ -21,6 +21,8 @@
 // a contact that persists keeps its slot and its adjoint; a slot acquired
 // new in the step gets a zero adjoint before it.  Spheres (one component per
 // owner) with any principal inertia; dynamic rigid bodies.
+#include <algorithm>
+
 #include "dem_adjoint.cuh"
 #include "dem_kernels.cuh"
 
@@ -120,6 +122,42 @@ __global__ void k_adj_restore(Owners o, const double* S)
     const int n = o.n;
     if (i >= n) return;
     owner_field(o, f)[i] = S[(size_t)f * n + i];
+}
+
+// Compact checkpoints of one history kind: each component keeps only its
+// occupied prefix [0, hw) of slots.  Every slot at or beyond hw is empty
+// (key 0, last seen -1, values 0): acquire takes the first empty slot at or
+// below hw, and expire clears a slot before it lowers hw past it.  So the
+// prefixes at their offsets (an exclusive scan of hw) restore the history
+// exactly: the unpack writes the prefix back and clears the slots between
+// the stored and the live mark.
+__global__ void k_ckpt_pack(Hist<double> h, int slots, int nc, const int* off, uint64_t* key, int* last,
+                            double* val)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int m = h.hw[c];
+        const size_t src = (size_t)c * slots, dst = (size_t)off[c];
+        for (int q = 0; q < m; ++q) {
+            key[dst + q] = h.key[src + q];
+            last[dst + q] = h.last[src + q];
+            for (int a = 0; a < kHV; ++a) val[(dst + q) * kHV + a] = h.val[(src + q) * kHV + a];
+        }
+    }
+}
+__global__ void k_ckpt_unpack(Hist<double> h, int slots, int nc, const int* hw, const int* off, const uint64_t* key,
+                              const int* last, const double* val)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int m = hw[c], live = h.hw[c];
+        const size_t dst = (size_t)c * slots, src = (size_t)off[c];
+        for (int q = 0; q < max(m, live); ++q) {
+            const bool kept = q < m;
+            h.key[dst + q] = kept ? key[src + q] : 0ull;
+            h.last[dst + q] = kept ? last[src + q] : -1;
+            for (int a = 0; a < kHV; ++a) h.val[(dst + q) * kHV + a] = kept ? val[(src + q) * kHV + a] : 0.0;
+        }
+        h.hw[c] = m;
+    }
 }
 
 // finish^T and the owner part of forces^T for step s: S = S_s, S1 = S_{s+1},
@@ -576,6 +614,19 @@ void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s, const int* 
 void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s)
 {
     if (o.n > 0) k_adj_restore<<<dim3(nblocks(o.n, 256), kAdjFields), 256, 0, s>>>(o, S);
+}
+void launch_ckpt_pack(const Hist<double>& h, int slots, int nc, const int* off, uint64_t* key, int* last, double* val,
+                      int sm_count, cudaStream_t s)
+{
+    if (nc > 0) k_ckpt_pack<<<std::max(1, std::min(nblocks(nc, 256), sm_count * 8)), 256, 0, s>>>(h, slots, nc, off, key,
+                                                                                                   last, val);
+}
+void launch_ckpt_unpack(const Hist<double>& h, int slots, int nc, const int* hw, const int* off, const uint64_t* key,
+                        const int* last, const double* val, int sm_count, cudaStream_t s)
+{
+    if (nc > 0)
+        k_ckpt_unpack<<<std::max(1, std::min(nblocks(nc, 256), sm_count * 8)), 256, 0, s>>>(h, slots, nc, hw, off, key,
+                                                                                             last, val);
 }
 void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Walls& w, const StepTape& tp, int npp,
                      int npw, int npb, const double* S, const double* S1, const double* L, double* Lp, double* P,

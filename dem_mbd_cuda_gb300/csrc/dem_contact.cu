@@ -1101,7 +1101,11 @@ __device__ void tape_pb(const StepTape& tp, int ci, int b, int slot, bool fresh,
                         bool spill)
 {
     const int k = atomicAdd(tp.pb_count, 1);
-    if (k >= tp.pb_cap || spill || ntri > kPbTris) {
+    if (spill || ntri > kPbTris) {
+        atomicOr(tp.overflow, 8);  // more triangles with an area share than a manifold keeps
+        return;
+    }
+    if (k >= tp.pb_cap) {
         atomicOr(tp.overflow, 4);
         return;
     }

@@ -1462,15 +1462,19 @@ public:
     // recomputes each segment from its checkpoint with a per-step tape and
     // sweeps it in reverse.  Spheres, walls and particle contacts in one
     // scene; no rigid bodies.
+    // One history kind of a checkpoint, compact: every component's occupied
+    // prefix [0, hw) of slots at offset off (an exclusive scan of hw).
+    struct AdjHist {
+        int* hw = nullptr;                         // [nc]
+        int* off = nullptr;                        // [nc + 1]
+        uint64_t* key = nullptr;                   // [count]
+        int* last = nullptr;                       // [count]
+        double* val = nullptr;                     // [count][kHV]
+        size_t count = 0;
+    };
     struct AdjCkpt {
         double* S = nullptr;                       // owner state [29][n]
-        uint64_t *pk = nullptr, *wk = nullptr;     // history keys
-        int *pl = nullptr, *wl = nullptr;          // last seen
-        double *pv = nullptr, *wv = nullptr;       // values
-        int *phw = nullptr, *whw = nullptr;        // high-water marks
-        uint64_t* bk = nullptr;                    // body history (with rigid bodies)
-        int *bl = nullptr, *bhw = nullptr;
-        double* bv = nullptr;
+        AdjHist h[3];                              // particle, wall, body history
         int* step = nullptr;                       // device step counter
         int step_index = 0;
         bool started = false;
@@ -1506,6 +1510,13 @@ public:
         // host and device), constants, adjoints, body-history adjoints
         std::vector<double> brec_host;
         double *brec = nullptr, *bcst = nullptr, *Lbody = nullptr, *lh_pb = nullptr;
+        // single-pass scan scratch of the compact checkpoints; their bytes
+        int* scan_n = nullptr;
+        int* scan_tiles = nullptr;
+        size_t ckpt_bytes = 0, tape_bytes = 0;
+        // the largest counts the forward run saw at its checkpoints: contact
+        // sides, particle-wall candidates, body manifolds and items
+        int seen_pp = 0, seen_pw = 0, seen_pb = 0;
     };
     void adj_release_graphs()
     {
@@ -1524,46 +1535,58 @@ public:
     AdjCkpt adj_alloc_ckpt()
     {
         AdjCkpt c;
-        const size_t ps = (size_t)nc_ * kPSlots, ws = (size_t)nc_ * kWSlots;
         c.S = adj_arena_.alloc<double>((size_t)kAdjFields * n_, "adjoint checkpoint");
-        c.pk = adj_arena_.alloc<uint64_t>(ps, "adjoint checkpoint"); c.pl = adj_arena_.alloc<int>(ps, "adjoint checkpoint");
-        c.pv = adj_arena_.alloc<double>(ps * kHV, "adjoint checkpoint"); c.phw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
-        c.wk = adj_arena_.alloc<uint64_t>(ws, "adjoint checkpoint"); c.wl = adj_arena_.alloc<int>(ws, "adjoint checkpoint");
-        c.wv = adj_arena_.alloc<double>(ws * kHV, "adjoint checkpoint"); c.whw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
-        if (nb_ > 0) {
-            const size_t bs = (size_t)nc_ * kBSlots;
-            c.bk = adj_arena_.alloc<uint64_t>(bs, "adjoint checkpoint"); c.bl = adj_arena_.alloc<int>(bs, "adjoint checkpoint");
-            c.bv = adj_arena_.alloc<double>(bs * kHV, "adjoint checkpoint"); c.bhw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
+        for (int k = 0; k < (nb_ > 0 ? 3 : 2); ++k) {
+            c.h[k].hw = adj_arena_.alloc<int>(nc_, "adjoint checkpoint");
+            c.h[k].off = adj_arena_.alloc<int>((size_t)nc_ + 1, "adjoint checkpoint");
         }
         c.step = adj_arena_.alloc<int>(1, "adjoint checkpoint");
         return c;
     }
-    void adj_copy_hist(AdjCkpt& c, bool save)
-    {
-        cudaStream_t s = stream_;
-        const size_t ps = (size_t)nc_ * kPSlots, ws = (size_t)nc_ * kWSlots;
-        auto cp = [&](void* ck, void* live, size_t bytes) {
-            check(cudaMemcpyAsync(save ? ck : live, save ? live : ck, bytes, cudaMemcpyDeviceToDevice, s), "adjoint checkpoint");
-        };
-        cp(c.pk, hp64_.key, ps * 8); cp(c.pl, hp64_.last, ps * 4); cp(c.pv, hp64_.val, ps * kHV * 8); cp(c.phw, hp64_.hw, (size_t)nc_ * 4);
-        cp(c.wk, hw64_.key, ws * 8); cp(c.wl, hw64_.last, ws * 4); cp(c.wv, hw64_.val, ws * kHV * 8); cp(c.whw, hw64_.hw, (size_t)nc_ * 4);
-        if (c.bk) {
-            const size_t bs = (size_t)nc_ * kBSlots;
-            cp(c.bk, hb64_.key, bs * 8); cp(c.bl, hb64_.last, bs * 4); cp(c.bv, hb64_.val, bs * kHV * 8); cp(c.bhw, hb64_.hw, (size_t)nc_ * 4);
-        }
-        cp(c.step, K_.step, 4);
-    }
+    Hist<double>& adj_live_hist(int k) { return k == 0 ? hp64_ : k == 1 ? hw64_ : hb64_; }
+    static int adj_slots(int k) { return k == 0 ? kPSlots : k == 1 ? kWSlots : kBSlots; }
+    // The checkpoint keeps each component's occupied history prefix only
+    // (about 0.7 kB per settled sphere against 8.6 kB for every slot).
     void adj_save(AdjCkpt& c)
     {
-        launch_adj_snapshot(O_, c.S, stream_);
-        adj_copy_hist(c, true);
+        Adjoint& A = adj_;
+        cudaStream_t s = stream_;
+        launch_adj_snapshot(O_, c.S, s);
+        const int kinds = nb_ > 0 ? 3 : 2;
+        int totals[3] = {0, 0, 0};
+        for (int k = 0; k < kinds; ++k) {
+            AdjHist& h = c.h[k];
+            check(cudaMemcpyAsync(h.hw, adj_live_hist(k).hw, sizeof(int) * nc_, cudaMemcpyDeviceToDevice, s),
+                  "adjoint checkpoint");
+            launch_scan(h.hw, h.off, A.scan_n, A.scan_tiles, sm_count_, s);
+            check(cudaMemcpyAsync(totals + k, h.off + nc_, sizeof(int), cudaMemcpyDeviceToHost, s), "adjoint checkpoint");
+        }
+        check(cudaStreamSynchronize(s), "adjoint checkpoint");
+        for (int k = 0; k < kinds; ++k) {
+            AdjHist& h = c.h[k];
+            h.count = (size_t)totals[k];
+            h.key = adj_arena_.alloc<uint64_t>(h.count, "adjoint checkpoint");
+            h.last = adj_arena_.alloc<int>(h.count, "adjoint checkpoint");
+            h.val = adj_arena_.alloc<double>(h.count * kHV, "adjoint checkpoint");
+            launch_ckpt_pack(adj_live_hist(k), adj_slots(k), nc_, h.off, h.key, h.last, h.val, sm_count_, s);
+        }
+        check(cudaMemcpyAsync(c.step, K_.step, sizeof(int), cudaMemcpyDeviceToDevice, s), "adjoint checkpoint");
+        check(cudaGetLastError(), "adjoint checkpoint");
+        A.ckpt_bytes += (size_t)kAdjFields * n_ * 8 + (size_t)kinds * (2 * nc_ + 1) * 4;
+        for (int k = 0; k < kinds; ++k) A.ckpt_bytes += c.h[k].count * (12 + 8 * kHV);
         c.step_index = step_index_;
         c.started = started_;
     }
     void adj_restore(AdjCkpt& c)
     {
-        launch_adj_restore(O_, c.S, stream_);
-        adj_copy_hist(c, false);
+        cudaStream_t s = stream_;
+        launch_adj_restore(O_, c.S, s);
+        for (int k = 0; k < (nb_ > 0 ? 3 : 2); ++k) {
+            const AdjHist& h = c.h[k];
+            launch_ckpt_unpack(adj_live_hist(k), adj_slots(k), nc_, h.hw, h.off, h.key, h.last, h.val, sm_count_, s);
+        }
+        check(cudaMemcpyAsync(K_.step, c.step, sizeof(int), cudaMemcpyDeviceToDevice, s), "adjoint checkpoint");
+        check(cudaGetLastError(), "adjoint restore");
         step_index_ = c.step_index;
         started_ = c.started;
     }
@@ -1577,32 +1600,14 @@ public:
         if (started_ || step_index_ != 0)
             throw DemError(DEM_ERR_STATE, "adjoint forward starts from a freshly initialized engine");
         adj_release_graphs();
+        adj_tape_arena_.release();
         adj_arena_.release();
         adj_ = Adjoint{};
         Adjoint& A = adj_;
         A.steps = steps; A.K = std::min(K, steps); A.nseg = (steps + A.K - 1) / A.K;
-        A.cap_pp = 16 * nc_ + 1024;
-        A.cap_pw = 2 * nc_ + 1024;
-        A.cap_pb = nb_ > 0 ? 2 * nc_ + 1024 : 0;
+        A.scan_n = adj_arena_.upload(&nc_, 1, "adjoint checkpoint", stream_);
+        A.scan_tiles = adj_arena_.alloc<int>((size_t)nc_ / 1024 + 64, "adjoint checkpoint");
         for (int k = 0; k < A.nseg + 2; ++k) A.ck.push_back(adj_alloc_ckpt());
-        const size_t slots = (size_t)A.K + 1;
-        for (AdjTape& t : A.tb) {
-            t.S = adj_arena_.alloc<double>(slots * kAdjFields * n_, "adjoint tape");
-            t.pp = adj_arena_.alloc<int4>(slots * A.cap_pp, "adjoint tape");
-            t.pp_h = adj_arena_.alloc<double>(slots * A.cap_pp * kHV, "adjoint tape");
-            t.pw = adj_arena_.alloc<int4>(slots * A.cap_pw, "adjoint tape");
-            t.pw_h = adj_arena_.alloc<double>(slots * A.cap_pw * kHV, "adjoint tape");
-            t.pp_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
-            t.pw_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
-            t.slot = adj_arena_.alloc<int>(1, "adjoint slot");
-            t.base = adj_arena_.alloc<int>(1, "adjoint slot");
-            if (nb_ > 0) {
-                t.pb = adj_arena_.alloc<int4>(slots * A.cap_pb, "adjoint tape");
-                t.pb_tri = adj_arena_.alloc<int>(slots * A.cap_pb * kPbTri, "adjoint tape");
-                t.pb_h = adj_arena_.alloc<double>(slots * A.cap_pb * kHV, "adjoint tape");
-                t.pb_cnt = adj_arena_.alloc<int>(slots, "adjoint tape");
-            }
-        }
         A.pp_new = adj_arena_.alloc<unsigned char>((size_t)nc_ * kPSlots, "adjoint tape");
         A.overflow = adj_arena_.alloc<int>(1, "adjoint tape");
         A.L = adj_arena_.alloc<double>((size_t)kAdjFields * n_, "adjoint state");
@@ -1629,12 +1634,19 @@ public:
             A.brec_host.reserve((size_t)(steps + 1) * nb_ * kBR);
             adj_rec_ = &A.brec_host;
         }
+        auto seen = [&] {
+            A.seen_pp = std::max(A.seen_pp, stats_.particle_contacts);
+            A.seen_pw = std::max(A.seen_pw, stats_.wall_candidates);
+            A.seen_pb = std::max(A.seen_pb, std::max(stats_.body_contacts, stats_.body_candidate_items));
+        };
         try {
             adj_save(A.ck[0]);
             run_steps(0);
+            seen();
             adj_save(A.ck[1]);
             for (int k = 0; k < A.nseg; ++k) {
                 run_steps(std::min(A.K, A.steps - k * A.K));
+                seen();
                 adj_save(A.ck[k + 2]);
             }
         } catch (...) {
@@ -1645,6 +1657,41 @@ public:
         if (nb_ > 0) A.brec = adj_arena_.upload(A.brec_host.data(), A.brec_host.size(), "adjoint bodies", stream_);
         check(cudaStreamSynchronize(stream_), "adjoint forward");
         A.ready = true;
+    }
+
+    // The two segment tapes, with room for cap_pp particle contact sides,
+    // cap_pw wall contacts and cap_pb body manifolds per step.  The backward
+    // run sizes them from the largest counts its forward run saw and grows a
+    // capacity that a recompute overflows.
+    void adj_alloc_tapes(int cap_pp, int cap_pw, int cap_pb)
+    {
+        Adjoint& A = adj_;
+        adj_release_graphs();
+        adj_tape_arena_.release();
+        A.cap_pp = cap_pp;
+        A.cap_pw = cap_pw;
+        A.cap_pb = nb_ > 0 ? cap_pb : 0;
+        const size_t slots = (size_t)A.K + 1;
+        DeviceArena& a = adj_tape_arena_;
+        for (AdjTape& t : A.tb) {
+            t = AdjTape{};
+            t.S = a.alloc<double>(slots * kAdjFields * n_, "adjoint tape");
+            t.pp = a.alloc<int4>(slots * A.cap_pp, "adjoint tape");
+            t.pp_h = a.alloc<double>(slots * A.cap_pp * kHV, "adjoint tape");
+            t.pw = a.alloc<int4>(slots * A.cap_pw, "adjoint tape");
+            t.pw_h = a.alloc<double>(slots * A.cap_pw * kHV, "adjoint tape");
+            t.pp_cnt = a.alloc<int>(slots, "adjoint tape");
+            t.pw_cnt = a.alloc<int>(slots, "adjoint tape");
+            t.slot = a.alloc<int>(1, "adjoint slot");
+            t.base = a.alloc<int>(1, "adjoint slot");
+            if (nb_ > 0) {
+                t.pb = a.alloc<int4>(slots * A.cap_pb, "adjoint tape");
+                t.pb_tri = a.alloc<int>(slots * A.cap_pb * kPbTri, "adjoint tape");
+                t.pb_h = a.alloc<double>(slots * A.cap_pb * kHV, "adjoint tape");
+                t.pb_cnt = a.alloc<int>(slots, "adjoint tape");
+            }
+        }
+        A.tape_bytes = a.bytes();
     }
 
     // The tape of step `sl` of buffer 0 (the first evaluation), pointers of
@@ -1754,8 +1801,39 @@ public:
 
     // dem_adjoint_backward: the adjoint of the final positions and velocities
     // in, those of the initial state and of the materials out.
+    // A recompute wrote more tape entries than the tapes hold (bits: 1
+    // particle contacts, 2 wall contacts, 4 body manifolds).
+    struct TapeFull {
+        int bits;
+    };
     void adjoint_backward(const double* dl_dpos, const double* dl_dvel, const double* dl_dbc, const double* dl_dbv,
                           double* dl_dpos0, double* dl_dvel0, double* dl_domega0, double* dl_dparams)
+    {
+        adj_require();
+        Adjoint& A = adj_;
+        if (!A.ready) throw DemError(DEM_ERR_STATE, "adjoint backward needs dem_adjoint_forward first");
+        const int worst_pp = 16 * nc_ + 1024, worst_pw = 2 * nc_ + 1024, worst_pb = 2 * nc_ + 1024;
+        if (!A.tb[0].S)
+            adj_alloc_tapes(std::min(worst_pp, A.seen_pp + A.seen_pp / 2 + nc_ / 8 + 1024),
+                            std::min(worst_pw, A.seen_pw + A.seen_pw / 2 + 1024),
+                            std::min(worst_pb, 2 * A.seen_pb + 1024));
+        for (;;) {
+            try {
+                adjoint_backward_pass(dl_dpos, dl_dvel, dl_dbc, dl_dbv, dl_dpos0, dl_dvel0, dl_domega0, dl_dparams);
+                return;
+            } catch (const TapeFull& f) {
+                check(cudaDeviceSynchronize(), "adjoint tapes");
+                const int pp = (f.bits & 1) ? std::min(worst_pp, 2 * A.cap_pp) : A.cap_pp;
+                const int pw = (f.bits & 2) ? std::min(worst_pw, 2 * A.cap_pw) : A.cap_pw;
+                const int pb = (f.bits & 4) ? std::min(worst_pb, 2 * A.cap_pb) : A.cap_pb;
+                if (pp == A.cap_pp && pw == A.cap_pw && pb == A.cap_pb)
+                    throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
+                adj_alloc_tapes(pp, pw, pb);
+            }
+        }
+    }
+    void adjoint_backward_pass(const double* dl_dpos, const double* dl_dvel, const double* dl_dbc, const double* dl_dbv,
+                               double* dl_dpos0, double* dl_dvel0, double* dl_domega0, double* dl_dparams)
     {
         adj_require();
         Adjoint& A = adj_;
@@ -1801,7 +1879,10 @@ public:
                       "adjoint counts");
             check(cudaMemcpyAsync(&of, A.overflow, sizeof(int), cudaMemcpyDeviceToHost, s), "adjoint counts");
             check(cudaStreamSynchronize(s), "adjoint counts");
-            if (of) throw DemError(DEM_ERR_CAPACITY, "adjoint tape capacity exceeded");
+            if (of & 8)
+                throw DemError(DEM_ERR_CAPACITY, "adjoint tape: a particle-body manifold with more than 12 triangles "
+                                                 "with an area share");
+            if (of) throw TapeFull{of};
             for (int j = 0; j < k; ++j) {
                 npp[j] = std::min(npp[j], A.cap_pp); npw[j] = std::min(npw[j], A.cap_pw); npb[j] = std::min(npb[j], A.cap_pb);
             }
@@ -1916,7 +1997,7 @@ public:
     std::array<cudaEvent_t, 6> adj_ev_{};  // reverse-mode pipeline: tapes recomputed [2], setup, tapes swept [2], end
     std::array<cudaEvent_t, 12> ev_{};
     int n_marks_ = 0;
-    DeviceArena arena_, arena_tmp_, adj_arena_;
+    DeviceArena arena_, arena_tmp_, adj_arena_, adj_tape_arena_;
     Adjoint adj_;
     std::vector<double>* adj_rec_ = nullptr;  // body records of the forward run, while dem_adjoint_forward runs
     std::vector<double> oin_host_;  // owner principal inertia [n][3] (host copy)
@@ -2219,6 +2300,15 @@ int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double*
 int dem_x_neighbor_stats(dem_engine* e, int* builds, double* mean_length, int* max_length, int* overflowed)
 {
     return guarded([&] { NEED(e); e->e.neighbor_stats(builds, mean_length, max_length, overflowed); });
+}
+
+int dem_x_adjoint_bytes(dem_engine* e, size_t* checkpoints, size_t* tapes)
+{
+    return guarded([&] {
+        NEED(e);
+        *checkpoints = e->e.adj_.ckpt_bytes;
+        *tapes = e->e.adj_.tape_bytes;
+    });
 }
 
 int dem_x_scan_wait_probe(dem_engine* e, unsigned* err)

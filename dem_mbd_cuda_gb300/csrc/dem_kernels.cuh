@@ -366,6 +366,13 @@ void launch_step_counter(const Counters& k, int reset, cudaStream_t s);
 // Owner-state snapshots [29][n]; with `slot`, into S + *slot * 29 n.
 void launch_adj_snapshot(const Owners& o, double* S, cudaStream_t s, const int* slot = nullptr);
 void launch_adj_restore(const Owners& o, const double* S, cudaStream_t s);
+// Compact checkpoint of one history kind: the occupied prefix [0, hw[c]) of
+// every component c at offset off[c] (an exclusive scan of hw), and back
+// (slots between the stored and the live mark are cleared).
+void launch_ckpt_pack(const Hist<double>& h, int slots, int nc, const int* off, uint64_t* key, int* last, double* val,
+                      int sm_count, cudaStream_t s);
+void launch_ckpt_unpack(const Hist<double>& h, int slots, int nc, const int* hw, const int* off, const uint64_t* key,
+                        const int* last, const double* val, int sm_count, cudaStream_t s);
 // The rigid bodies of the reverse mode: the forward run's body records
 // ([step][body][39]: the pose the evaluation used, the loads, the state after
 // the half update), constants ([body][5]: mass, principal inertia, state),

@@ -63,6 +63,7 @@ _SIGS = {
     "dem_adjoint_backward": ([C.c_void_p] + [C.c_void_p] * 6, C.c_int),
     "dem_adjoint_backward_mbd": ([C.c_void_p] + [C.c_void_p] * 8, C.c_int),
     "dem_x_neighbor_stats": ([C.c_void_p] + [C.c_void_p] * 4, C.c_int),
+    "dem_x_adjoint_bytes": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "dem_x_scan_wait_probe": ([C.c_void_p, C.c_void_p], C.c_int),
 }
 
@@ -342,6 +343,13 @@ class CudaDemSolver:
         b, m, x, o = C.c_int(), C.c_double(), C.c_int(), C.c_int()
         self._check(self.lib.dem_x_neighbor_stats(self.h, C.byref(b), C.byref(m), C.byref(x), C.byref(o)))
         return {"builds": b.value, "mean_length": m.value, "max_length": x.value, "overflowed": bool(o.value)}
+
+    def adjoint_memory(self):
+        """Device bytes of the reverse mode's checkpoints (occupied history
+        prefixes only) and of its two segment tapes."""
+        a, b = C.c_size_t(), C.c_size_t()
+        self._check(self.lib.dem_x_adjoint_bytes(self.h, C.byref(a), C.byref(b)))
+        return {"checkpoint_bytes": a.value, "tape_bytes": b.value}
 
     def set_pp_blocks(self, blocks_per_sm):
         """Blocks of 256 per SM of the particle law (0: 16).  Changes only the speed."""

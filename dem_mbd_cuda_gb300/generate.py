@@ -235,7 +235,7 @@ def _attach(kw, bodies):
 
 
 def pure_dem(n=20000, seed=1000, rmin=1.8e-3, rmax=2.2e-3, box=(0.2, 0.2, 0.4), dt=1e-5, kN=1e5, epsN=0.5, mu=0.3,
-             pitch=None, name="c0_pure_dem", fill_width=False):
+             pitch=None, name="c0_pure_dem", fill_width=False, jitter=0.2e-3):
     """Config 0: spheres r ~ U[rmin, rmax] on a jittered lattice in a box of 5
     walls (floor + 4 sides), kN 1e5, restitution 0.5, friction 0.3."""
     pitch = pitch if pitch is not None else 2.0 * rmin + 0.1e-3
@@ -245,7 +245,8 @@ def pure_dem(n=20000, seed=1000, rmin=1.8e-3, rmax=2.2e-3, box=(0.2, 0.2, 0.4), 
     per = int(width // pitch)
     origin = lo + np.array([rmax, rmax, rmax]) + (width - (per - 1) * pitch) / 2 * np.array([1, 1, 0])
     origin[2] = rmax + 0.3e-3
-    pos, rad, _ = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed, nxy=per if fill_width else None)
+    pos, rad, _ = bed(n, rmin, rmax, pitch, origin, aspect=(1, 1, None), seed=seed, nxy=per if fill_width else None,
+                      jitter=jitter)
     assert pos[:, 0].max() + rad.max() < hi[0] and pos[:, 1].max() + rad.max() < hi[1], "bed exceeds the box"
     kw = make_spheres(pos, rad, DENSITY)
     wo, wn = box_walls(lo, hi)
@@ -453,8 +454,9 @@ def box_columns(n, seed, rmin=1.8e-3, rmax=2.2e-3, box=(0.1, 0.1, 0.4), dt=1e-5,
 def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5, settled=False):
     """Config 4: independent box scenes with N_s ~ U[2k, 40k], per-scene
     friction ~ U[0.1, 0.7] and restitution ~ U[0.2, 0.8], in 0.1 x 0.1 x
-    0.4 m boxes: lattice beds at rest (``settled=False``, they settle during
-    the run) or settled column beds."""
+    0.4 m boxes of 5 walls: jittered lattices at rest (``settled=False``;
+    4.5 mm apart, so every radius of U[1.8, 2.2] mm fits and the layers fall
+    onto each other and settle during the run) or settled column beds."""
     rng = np.random.default_rng(seed)
     out = []
     for s in range(nscenes):
@@ -464,7 +466,8 @@ def batch(nscenes=256, seed=1004, nmin=2000, nmax=40000, dt=1e-5, settled=False)
         if settled:
             sc = box_columns(ns, seed * 1000 + s, dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}")
         else:
-            sc = pure_dem(n=ns, seed=seed * 1000 + s, box=(0.1, 0.1, 0.4), dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}")
+            sc = pure_dem(n=ns, seed=seed * 1000 + s, box=(0.1, 0.1, 0.4), dt=dt, epsN=e, mu=mu, name=f"c4_scene{s}",
+                          fill_width=True, pitch=4.5e-3, jitter=0.05e-3)
         out.append(sc)
     return out
 
