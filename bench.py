@@ -477,14 +477,25 @@ def adjoint_summary(steps=2000, checkpoint_every=100):
             "fd_check": fd}
 
 
+def _scene_heights(pos, counts):
+    """Mean particle height of each scene of a batch (the bed height's
+    measure used as the calibration's loss)."""
+    out, off = [], 0
+    for c in counts:
+        out.append(pos[off:off + c, 2].mean())
+        off += c
+    return out
+
+
 def batch_adjoint_summary(nscenes=64, steps=50, checkpoint_every=10):
-    """Config 4's batched reverse mode on the first `nscenes` scenes of the
-    256-scene generator, over a bounded window: the gradients of the sum of
-    the scenes' mean bed heights with respect to every scene's own materials
-    and initial velocities, from one backward run over the batch.  The tapes
-    and checkpoints of all 256 scenes over the config's 3,000 steps do not fit
-    the GPU's memory (about 8.9 kB per sphere per checkpoint, 2.2 kB per
-    sphere per taped step), so the window is bounded; the ratio is per step."""
+    """Config 4's batched reverse mode on the first `nscenes` settled scenes
+    of the 256-scene generator (contact-dense beds, the reverse mode's most
+    expensive regime): the gradients of the sum of the scenes' mean bed
+    heights with respect to every scene's own materials and initial
+    velocities, from one backward run over the batch, with the reverse law
+    of the particle and wall contacts in FP64 and in FP32 (the forward run,
+    its recompute and the rest of the reverse stay FP64), and the FP32 form's
+    departure from the FP64 gradients."""
     from dem_mbd_cuda_gb300.engine import CudaDemSolver
     scenes = make_scene("c4")[0][:nscenes]
     n = sum(sc.n for sc in scenes)
@@ -496,28 +507,144 @@ def batch_adjoint_summary(nscenes=64, steps=50, checkpoint_every=10):
     plain.synchronize()
     t_plain = time.perf_counter() - t0
     del plain
-    e = CudaDemSolver().initialize(scenes, precision="fp64")
-    t0 = time.perf_counter()
-    e.adjoint_forward(steps, checkpoint_every)
-    t_fwd = time.perf_counter() - t0
     dpos = np.zeros((n, 3))
     off = 0
     for sc in scenes:
         dpos[off:off + sc.n, 2] = 1.0 / sc.n
         off += sc.n
+    out = {"workload": "the first %d settled scenes of the 256-scene batch (%d spheres), %d steps of dt 1e-5, "
+                       "checkpoints every %d; loss = sum over scenes of the mean bed height"
+                       % (nscenes, n, steps, checkpoint_every), "forward_plain_s": t_plain}
+    grads = {}
+    for form in ("fp64", "fp32"):
+        e = CudaDemSolver().initialize(scenes, precision="fp64").set_adjoint_fp32(form == "fp32")
+        t0 = time.perf_counter()
+        e.adjoint_forward(steps, checkpoint_every)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g = e.adjoint_backward(dpos, None)
+        t_bwd = time.perf_counter() - t0
+        out["reverse_" + form] = {"forward_checkpointed_s": t_fwd, "backward_s": t_bwd,
+                                  "adjoint_over_forward": t_bwd / t_plain,
+                                  "total_over_forward": (t_fwd + t_bwd) / t_plain, "memory": e.adjoint_memory()}
+        grads[form] = g
+        del e
+    a, b = grads["fp64"], grads["fp32"]
+    rel = [abs(b["dl_dparams"][k][c][f] - a["dl_dparams"][k][c][f]) / abs(a["dl_dparams"][k][c][f])
+           for k in range(nscenes) for c in ("pp", "pw") for f in ("kN", "epsN", "epsS")
+           if abs(a["dl_dparams"][k][c][f]) > 1e-12]
+    out["fp32_vs_fp64"] = {"material_rel_err_median": float(np.median(rel)) if rel else 0.0,
+                           "material_rel_err_p99": float(np.percentile(rel, 99)) if rel else 0.0,
+                           "dl_dvel0_rel_err": float(np.abs(b["dl_dvel0"] - a["dl_dvel0"]).max()
+                                                     / max(np.abs(a["dl_dvel0"]).max(), 1e-300))}
+    out["per_scene_pp_depsN"] = [p["pp"]["epsN"] for p in a["dl_dparams"][:4]]
+    return out
+
+
+def calibration_summary(nscenes=16, steps=1000, iterations=4, checkpoint_every=100):
+    """Config 4's calibration on its own scenes (jittered lattices that fall
+    and settle): each scene's restitution is recovered from its bed height
+    by Newton steps on the batched reverse mode's gradients
+    (autograd.simulate_batch, one backward run for all scenes per
+    iteration).  The horizon is the one where the reverse mode's gradients
+    of this loss match central differences (measured: 1,000 steps); later,
+    the bed's collisions make the height a non-smooth function of the
+    restitution."""
+    import dataclasses
+
+    import torch
+    from dem_mbd_cuda_gb300 import generate as G
+    from dem_mbd_cuda_gb300.autograd import materials, simulate_batch
+    from dem_mbd_cuda_gb300.engine import CudaDemSolver
+    scenes = G.batch(nscenes=nscenes)
+    counts = [s.n for s in scenes]
+    true_e = np.array([s.pp.epsN for s in scenes])
+    ref = CudaDemSolver().initialize(scenes, precision="fp64")
+    ref.run(steps)
+    target = np.array(_scene_heights(ref.downloadParticleState()["pos"], counts))
+    del ref
+    e = np.clip(true_e + np.where(np.arange(nscenes) % 2 == 0, 0.15, -0.15), 0.1, 0.9)
+    vel0 = torch.tensor(np.concatenate([s.vel for s in scenes]))
+    log = []
     t0 = time.perf_counter()
-    g = e.adjoint_backward(dpos, None)
-    t_bwd = time.perf_counter() - t0
-    mem = e.adjoint_memory()
-    del e
-    per = g["dl_dparams"]
-    return {"workload": "the first %d scenes of the 256-scene batch (%d spheres), %d steps of dt 1e-5, checkpoints "
-                        "every %d; loss = sum over scenes of the mean bed height" % (nscenes, n, steps,
-                                                                                    checkpoint_every),
+    for it in range(iterations + 1):
+        pp = torch.stack([materials(dataclasses.replace(s.pp, epsN=float(x))) for s, x in zip(scenes, e)])
+        pw = torch.stack([materials(dataclasses.replace(s.pw, epsN=float(x))) for s, x in zip(scenes, e)])
+        pp.requires_grad_(True)
+        pw.requires_grad_(True)
+        pos, _ = simulate_batch(scenes, steps, pp, pw, vel0, checkpoint_every)
+        h = torch.stack(_scene_heights(pos, counts))
+        resid = h.detach().numpy() - target
+        log.append({"iteration": it, "height_residual_max_m": float(np.abs(resid).max()),
+                    "restitution_error_max": float(np.abs(e - true_e).max())})
+        if it == iterations:
+            break
+        h.sum().backward()
+        dh = (pp.grad[:, 2] + pw.grad[:, 2]).numpy()
+        step = np.where(np.abs(dh) > 1e-30, resid / np.where(np.abs(dh) > 1e-30, dh, 1.0), 0.0)
+        e = np.clip(e - step, 0.05, 0.95)
+    return {"workload": "%d config-4 scenes (%d spheres, jittered lattices settling in 0.1 m boxes), %d steps of "
+                        "dt 1e-5; unknown: each scene's restitution (particle and wall), from its mean bed height"
+                        % (nscenes, sum(counts), steps),
+            "iterations": log, "seconds": time.perf_counter() - t0}
+
+
+def c4_adjoint_summary(chunk_particles=1_400_000, steps=3000, checkpoint_every=100):
+    """The whole of config 4 in reverse mode: 256 scenes (5.46M spheres,
+    jittered lattices settling) over 3,000 steps, the gradients of every
+    scene's mean bed height with respect to its materials and initial
+    velocities.  Scenes are independent, so the batch runs in chunks of up
+    to `chunk_particles` spheres, one after the other on the GPU (the
+    checkpoints and two segment tapes of the whole batch would not fit
+    beside each other); times are summed over the chunks.  FP32 reverse law
+    for the particle and wall contacts."""
+    from dem_mbd_cuda_gb300 import generate as G
+    from dem_mbd_cuda_gb300.engine import CudaDemSolver
+    scenes = G.batch()
+    chunks, cur, size = [], [], 0
+    for s in scenes:
+        if cur and size + s.n > chunk_particles:
+            chunks.append(cur)
+            cur, size = [], 0
+        cur.append(s)
+        size += s.n
+    chunks.append(cur)
+    t_plain = t_fwd = t_bwd = 0.0
+    peak = {"checkpoint_bytes": 0, "tape_bytes": 0}
+    nonzero = 0
+    for ch in chunks:
+        n = sum(s.n for s in ch)
+        p = CudaDemSolver().initialize(ch, precision="fp64")
+        p.run(0)
+        p.synchronize()
+        t0 = time.perf_counter()
+        p.run(steps)
+        p.synchronize()
+        t_plain += time.perf_counter() - t0
+        del p
+        e = CudaDemSolver().initialize(ch, precision="fp64").set_adjoint_fp32(True)
+        t0 = time.perf_counter()
+        e.adjoint_forward(steps, checkpoint_every)
+        t_fwd += time.perf_counter() - t0
+        dpos = np.zeros((n, 3))
+        off = 0
+        for s in ch:
+            dpos[off:off + s.n, 2] = 1.0 / s.n
+            off += s.n
+        t0 = time.perf_counter()
+        g = e.adjoint_backward(dpos, None)
+        t_bwd += time.perf_counter() - t0
+        mem = e.adjoint_memory()
+        peak = {k: max(peak[k], mem[k]) for k in peak}
+        per = g["dl_dparams"] if isinstance(g["dl_dparams"], list) else [g["dl_dparams"]]
+        nonzero += sum(1 for r in per if r["pp"]["epsN"] != 0.0 or r["pw"]["epsN"] != 0.0)
+        del e
+    return {"workload": "all 256 config-4 scenes (%d spheres, jittered lattices settling), %d steps of dt 1e-5, "
+                        "checkpoints every %d, in %d chunks of up to %d spheres"
+                        % (sum(s.n for s in scenes), steps, checkpoint_every, len(chunks), chunk_particles),
             "forward_plain_s": t_plain, "forward_checkpointed_s": t_fwd, "backward_s": t_bwd,
             "adjoint_over_forward": t_bwd / t_plain, "total_over_forward": (t_fwd + t_bwd) / t_plain,
-            "memory": mem, "per_scene_pp_dmu": [p["pp"]["mu"] for p in per[:4]],
-            "per_scene_pp_depsN": [p["pp"]["epsN"] for p in per[:4]]}
+            "peak_chunk_memory": peak, "scenes_with_restitution_gradient": nonzero}
 
 
 def autotune_summary(scene, precision):
@@ -544,6 +671,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the embedded config-3 adjoint summary")
     ap.add_argument("--no-autotune", action="store_true", help="skip the embedded autotuner summary")
     ap.add_argument("--adjoint-only", action="store_true", help="print the config-3 adjoint summary alone")
+    ap.add_argument("--adjoint-c4", action="store_true",
+                    help="print the reverse mode over all 256 config-4 scenes and 3,000 steps alone")
     ap.add_argument("--adjoint-batch", type=int, default=None, metavar="SCENES",
                     help="print the batched adjoint summary alone, on the first SCENES scenes, over --steps steps")
     ap.add_argument("--particles", type=int, default=None,
@@ -572,10 +701,12 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    if args.adjoint_only or args.adjoint_batch:
+    if args.adjoint_only or args.adjoint_batch or args.adjoint_c4:
         from dem_mbd_cuda_gb300 import build as _b
         _b.build()
-        if args.adjoint_batch:
+        if args.adjoint_c4:
+            print(json.dumps(c4_adjoint_summary()))
+        elif args.adjoint_batch:
             print(json.dumps(batch_adjoint_summary(args.adjoint_batch, args.steps, min(10, args.steps))))
         else:
             print(json.dumps(adjoint_summary()))
@@ -712,6 +843,8 @@ def main():
         subs["adjoint_c3"] = adjoint_summary()
         if not args.no_batch:
             subs["adjoint_batch"] = batch_adjoint_summary()
+            subs["calibration_c4"] = calibration_summary()
+            subs["adjoint_c4"] = c4_adjoint_summary()
     if not args.no_autotune:
         subs["autotuned"] = autotune_summary(scene, args.precision)
     nb = scene.n_bodies

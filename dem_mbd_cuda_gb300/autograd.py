@@ -43,10 +43,11 @@ def _batch_with_materials(scenes, pp, pw, vel0):
 
 class DemRun(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, pp, pw, vel0, scene, steps, checkpoint_every):
+    def forward(ctx, pp, pw, vel0, scene, steps, checkpoint_every, reverse_fp32=False):
         args = (pp.detach().cpu().numpy(), pw.detach().cpu().numpy(), vel0.detach().cpu().numpy().reshape(-1, 3))
         sc = _batch_with_materials(scene, *args) if isinstance(scene, (list, tuple)) else _with_materials(scene, *args)
-        e = CudaDemSolver().initialize(sc, precision="fp64").adjoint_forward(steps, checkpoint_every)
+        e = CudaDemSolver().initialize(sc, precision="fp64").set_adjoint_fp32(reverse_fp32)
+        e.adjoint_forward(steps, checkpoint_every)
         st = e.downloadParticleState()
         ctx.engine = e
         ctx.dtype = pp.dtype
@@ -63,7 +64,7 @@ class DemRun(torch.autograd.Function):
         if not isinstance(per, list):
             pp, pw = pp[0], pw[0]
         dv = torch.as_tensor(g["dl_dvel0"], dtype=gpos.dtype if gpos is not None else gvel.dtype)
-        return pp, pw, dv, None, None, None
+        return pp, pw, dv, None, None, None, None
 
 
 def materials(m):
@@ -71,14 +72,15 @@ def materials(m):
     return torch.tensor([getattr(m, f) for f in FIELDS], dtype=torch.float64)
 
 
-def simulate(scene, steps, pp, pw, vel0, checkpoint_every=100):
+def simulate(scene, steps, pp, pw, vel0, checkpoint_every=100, reverse_fp32=False):
     """Final (positions, velocities) of `steps` steps, differentiable with
-    respect to pp, pw and vel0."""
-    return DemRun.apply(pp, pw, vel0, scene, int(steps), int(checkpoint_every))
+    respect to pp, pw and vel0.  reverse_fp32 runs the reverse law of the
+    particle and wall contacts in FP32 (CudaDemSolver.set_adjoint_fp32)."""
+    return DemRun.apply(pp, pw, vel0, scene, int(steps), int(checkpoint_every), bool(reverse_fp32))
 
 
-def simulate_batch(scenes, steps, pp, pw, vel0, checkpoint_every=100):
+def simulate_batch(scenes, steps, pp, pw, vel0, checkpoint_every=100, reverse_fp32=False):
     """Final (positions, velocities) of `steps` steps of a batch of scenes,
     differentiable with respect to the per-scene materials pp, pw
     ([scenes, 6]) and vel0 (the scenes' owners one after the other)."""
-    return DemRun.apply(pp, pw, vel0, list(scenes), int(steps), int(checkpoint_every))
+    return DemRun.apply(pp, pw, vel0, list(scenes), int(steps), int(checkpoint_every), bool(reverse_fp32))

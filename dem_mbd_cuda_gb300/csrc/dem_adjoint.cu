@@ -307,7 +307,22 @@ __device__ EntryRange entry_range(int count, int block, int blocks, int nscenes)
     return {k0 + (int)threadIdx.x, min(count, k0 + per), (int)blockDim.x};
 }
 
-// Particle contact sides of one step (tape entries), reverse.
+template <typename R> __device__ MatGrad grad64(const MatGradT<R>& g)
+{
+    return MatGrad{cv<double>(g.kN), cv<double>(g.mu), cv<double>(g.logN), cv<double>(g.logS), cv<double>(g.muT),
+                   cv<double>(g.muR)};
+}
+template <typename R> __device__ const auto& mat_of(const MatC& m, const MatF& f)
+{
+    if constexpr (std::is_same<R, double>::value) return m;
+    else return f;
+}
+
+// Particle contact sides of one step (tape entries), reverse.  R = double:
+// the FP64 map; R = float: the law's map in FP32 from FP64 differences of
+// the positions and velocities (the overlap from the FP64 difference of
+// squares), the adjoints scattered into the owners in FP64.
+template <typename R>
 __device__ void adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTape tp, int count, const double* P,
                        double* T, double* lhist, double dt_eff, double* grads, int block, int blocks, int nscenes,
                        GradRows& rows)
@@ -316,7 +331,7 @@ __device__ void adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTap
     tp = tape_at(tp);
     if (count < 0) count = min(*tp.pp_count, tp.pp_cap);
     grad_rows_init(rows);
-    MatGrad gsum = {0, 0, 0, 0, 0, 0};
+    MatGradT<R> gsum = {0, 0, 0, 0, 0, 0};
     int cur = -1;  // the scene gsum belongs to
     const EntryRange er = entry_range(count, block, blocks, nscenes);
     for (int k = er.k; k < er.end; k += er.step) {
@@ -324,47 +339,55 @@ __device__ void adj_pp(Comps c, Owners o, const SceneC* __restrict__ sc, StepTap
         const int i = e.x, j = e.y;
         const int si = nscenes == 1 ? 0 : o.scene[i];
         if (si != cur) {
-            if (cur >= 0) grad_add(rows, cur, gsum, grads, 0);
-            gsum = MatGrad{0, 0, 0, 0, 0, 0};
+            if (cur >= 0) grad_add(rows, cur, grad64(gsum), grads, 0);
+            gsum = MatGradT<R>{0, 0, 0, 0, 0, 0};
             cur = si;
         }
-        const MatC& m = sc[si].pp;
+        const auto& m = mat_of<R>(sc[si].pp, sc[si].ppf);
         D3 xi = ld3(P, kPX, n, i), xj = ld3(P, kPX, n, j);
         const D3 vi = ld3(P, kPV, n, i), vj = ld3(P, kPV, n, j);
         const D3 mvi = ld3(P, kPMV, n, i), mvj = ld3(P, kPMV, n, j);
-        PPIn in;
-        in.delta = xj - xi;
-        in.ri = c.radius[i]; in.rj = c.radius[j]; in.mi = o.mass[i]; in.mj = o.mass[j];
-        in.erv = vj - vi;
-        in.mrv = mvj - mvi;
-        in.ewi = ld3(P, kPEW, n, i); in.ewj = ld3(P, kPEW, n, j);
-        in.mwi = ld3(P, kPEMW, n, i); in.mwj = ld3(P, kPEMW, n, j);
-        for (int a = 0; a < 9; ++a) in.h[a] = tp.pp_h[(size_t)k * kHV + a];
+        const D3 delta = xj - xi;
+        const double ri = c.radius[i], rj = c.radius[j];
+        PPInT<R> in;
+        in.delta = cvt<R>(delta);
+        if constexpr (!std::is_same<R, double>::value) {
+            const double rs = ri + rj, d2 = dot(delta, delta);
+            in.depth = cv<R>(rs * rs - d2) / (cv<R>(rs) + sqrt(dot(in.delta, in.delta)));
+        }
+        in.ri = cv<R>(ri); in.rj = cv<R>(rj); in.mi = cv<R>(o.mass[i]); in.mj = cv<R>(o.mass[j]);
+        in.erv = cvt<R>(vj - vi);
+        in.mrv = cvt<R>(mvj - mvi);
+        in.ewi = cvt<R>(ld3(P, kPEW, n, i)); in.ewj = cvt<R>(ld3(P, kPEW, n, j));
+        in.mwi = cvt<R>(ld3(P, kPEMW, n, i)); in.mwj = cvt<R>(ld3(P, kPEMW, n, j));
+        for (int a = 0; a < 9; ++a) in.h[a] = cv<R>(tp.pp_h[(size_t)k * kHV + a]);
         double* lh = lhist + (size_t)e.z * kHV;
-        double lho[9];
-        for (int a = 0; a < 9; ++a) lho[a] = lh[a];
-        PPAdj ad;
-        ad.delta = ad.erv = ad.mrv = ad.ewi = ad.ewj = ad.mwi = ad.mwj = z3();
-        for (int a = 0; a < 9; ++a) ad.h[a] = 0.0;
-        pp_law_vjp(m, dt_eff, in, ld3(T, kTF, n, i), ld3(T, kTTau, n, i), lho, ad, gsum);
-        for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : ad.h[a];
-        add3(T, kTX, n, j, ad.delta);
-        add3(T, kTX, n, i, ad.delta * -1.0);
-        add3(T, kTV, n, j, ad.erv);
-        add3(T, kTV, n, i, ad.erv * -1.0);
-        add3(T, kTMV, n, j, ad.mrv);
-        add3(T, kTMV, n, i, ad.mrv * -1.0);
-        add3(T, kTEW, n, i, ad.ewi);
-        add3(T, kTEW, n, j, ad.ewj);
-        add3(T, kTEMW, n, i, ad.mwi);
-        add3(T, kTEMW, n, j, ad.mwj);
+        R lho[9];
+        for (int a = 0; a < 9; ++a) lho[a] = cv<R>(lh[a]);
+        PPAdjT<R> ad;
+        ad.delta = ad.erv = ad.mrv = ad.ewi = ad.ewj = ad.mwi = ad.mwj = zr<R>();
+        for (int a = 0; a < 9; ++a) ad.h[a] = R(0);
+        pp_law_vjp(m, cv<R>(dt_eff), in, cvt<R>(ld3(T, kTF, n, i)), cvt<R>(ld3(T, kTTau, n, i)), lho, ad, gsum);
+        for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : cv<double>(ad.h[a]);
+        const D3 adelta = cvt<double>(ad.delta), aerv = cvt<double>(ad.erv), amrv = cvt<double>(ad.mrv);
+        add3(T, kTX, n, j, adelta);
+        add3(T, kTX, n, i, adelta * -1.0);
+        add3(T, kTV, n, j, aerv);
+        add3(T, kTV, n, i, aerv * -1.0);
+        add3(T, kTMV, n, j, amrv);
+        add3(T, kTMV, n, i, amrv * -1.0);
+        add3(T, kTEW, n, i, cvt<double>(ad.ewi));
+        add3(T, kTEW, n, j, cvt<double>(ad.ewj));
+        add3(T, kTEMW, n, i, cvt<double>(ad.mwi));
+        add3(T, kTEMW, n, j, cvt<double>(ad.mwj));
     }
-    if (cur >= 0) grad_add(rows, cur, gsum, grads, 0);
+    if (cur >= 0) grad_add(rows, cur, grad64(gsum), grads, 0);
     grad_rows_flush(rows, grads, 0);
 }
 
+template <typename R>
 __device__ void pw_one(const Comps& c, const Owners& o, const SceneC& S, const Walls& walls, const StepTape& tp, int k,
-                       const double* P, double* T, double* lhist, double dt_eff, MatGrad& g)
+                       const double* P, double* T, double* lhist, double dt_eff, MatGradT<R>& g)
 {
     const int n = o.n;
     const int4 e = tp.pw[k];
@@ -376,21 +399,23 @@ __device__ void pw_one(const Comps& c, const Owners& o, const SceneC& S, const W
     const double r = c.radius[i];
     const double depth = r - dot(x1 - org, out);
     const D3 om = ld3(P, kPEW, n, i);
-    double hin[9], lho[9];
-    for (int a = 0; a < 9; ++a) hin[a] = tp.pw_h[(size_t)k * kHV + a];
+    R hin[9], lho[9];
+    for (int a = 0; a < 9; ++a) hin[a] = cv<R>(tp.pw_h[(size_t)k * kHV + a]);
     double* lh = lhist + (size_t)e.z * kHV;
-    for (int a = 0; a < 9; ++a) lho[a] = lh[a];
-    PWAdj ad;
-    ad.p = ad.vel = ad.om = z3();
-    for (int a = 0; a < 9; ++a) ad.h[a] = 0.0;
-    pw_law_vjp(S.pw, dt_eff, out, depth, r, o.mass[i], v1, om, hin, ld3(T, kTF, n, i), ld3(T, kTTau, n, i), lho, ad, g);
-    for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : ad.h[a];
-    add3(T, kTX, n, i, ad.p);
-    add3(T, kTV, n, i, ad.vel);
-    add3(T, kTEW, n, i, ad.om);
+    for (int a = 0; a < 9; ++a) lho[a] = cv<R>(lh[a]);
+    PWAdjT<R> ad;
+    ad.p = ad.vel = ad.om = zr<R>();
+    for (int a = 0; a < 9; ++a) ad.h[a] = R(0);
+    pw_law_vjp(mat_of<R>(S.pw, S.pwf), cv<R>(dt_eff), cvt<R>(out), cv<R>(depth), cv<R>(r), cv<R>(o.mass[i]),
+               cvt<R>(v1), cvt<R>(om), hin, cvt<R>(ld3(T, kTF, n, i)), cvt<R>(ld3(T, kTTau, n, i)), lho, ad, g);
+    for (int a = 0; a < 9; ++a) lh[a] = e.w ? 0.0 : cv<double>(ad.h[a]);
+    add3(T, kTX, n, i, cvt<double>(ad.p));
+    add3(T, kTV, n, i, cvt<double>(ad.vel));
+    add3(T, kTEW, n, i, cvt<double>(ad.om));
 }
 
 // Wall contacts of one step (tape entries), reverse.
+template <typename R>
 __device__ void adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls, StepTape tp, int count,
                        const double* P, double* T, double* lhist, double dt_eff, double* grads, int block, int blocks,
                        int nscenes, GradRows& rows)
@@ -398,21 +423,21 @@ __device__ void adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls w
     tp = tape_at(tp);
     if (count < 0) count = min(*tp.pw_count, tp.pw_cap);
     grad_rows_init(rows);
-    MatGrad g = {0, 0, 0, 0, 0, 0};
+    MatGradT<R> g = {0, 0, 0, 0, 0, 0};
     int cur = -1;
     const EntryRange er = entry_range(count, block, blocks, nscenes);
     for (int k = er.k; k < er.end; k += er.step) {
         const int si = nscenes == 1 ? 0 : o.scene[tp.pw[k].x];
         if (si != cur) {
-            if (cur >= 0) grad_add(rows, cur, g, grads, 1);
-            g = MatGrad{0, 0, 0, 0, 0, 0};
+            if (cur >= 0) grad_add(rows, cur, grad64(g), grads, 1);
+            g = MatGradT<R>{0, 0, 0, 0, 0, 0};
             cur = si;
         }
-        MatGrad gk = {0, 0, 0, 0, 0, 0};
-        pw_one(c, o, sc[si], walls, tp, k, P, T, lhist, dt_eff, gk);
+        MatGradT<R> gk = {0, 0, 0, 0, 0, 0};
+        pw_one<R>(c, o, sc[si], walls, tp, k, P, T, lhist, dt_eff, gk);
         g.kN += gk.kN; g.mu += gk.mu; g.logN += gk.logN; g.logS += gk.logS; g.muT += gk.muT; g.muR += gk.muR;
     }
-    if (cur >= 0) grad_add(rows, cur, g, grads, 1);
+    if (cur >= 0) grad_add(rows, cur, grad64(g), grads, 1);
     grad_rows_flush(rows, grads, 1);
 }
 
@@ -421,6 +446,7 @@ __device__ void adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls w
 // is a long serial FP64 chain, and a warp issues one FP64 instruction per
 // about 68 cycles whatever its neighbours do, so with few contacts the two
 // sets cost their longer chain instead of the sum of both.
+template <typename R>
 __global__ void __launch_bounds__(128) k_adj_contacts(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
                                                       StepTape tp, int npp, int npw, int bpp, const double* P, double* T,
                                                       double* lh_pp, double* lh_pw, double dt_eff, double* grads,
@@ -428,9 +454,10 @@ __global__ void __launch_bounds__(128) k_adj_contacts(Comps c, Owners o, const S
 {
     __shared__ GradRows rows;
     if ((int)blockIdx.x < bpp)
-        adj_pp(c, o, sc, tp, npp, P, T, lh_pp, dt_eff, grads, blockIdx.x, bpp, nscenes, rows);
+        adj_pp<R>(c, o, sc, tp, npp, P, T, lh_pp, dt_eff, grads, blockIdx.x, bpp, nscenes, rows);
     else
-        adj_pw(c, o, sc, walls, tp, npw, P, T, lh_pw, dt_eff, grads, blockIdx.x - bpp, gridDim.x - bpp, nscenes, rows);
+        adj_pw<R>(c, o, sc, walls, tp, npw, P, T, lh_pw, dt_eff, grads, blockIdx.x - bpp, gridDim.x - bpp, nscenes,
+                  rows);
 }
 
 
@@ -632,7 +659,7 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
                      int npw, int npb, const double* S, const double* S1, const double* L, double* Lp, double* P,
                      double* T, double* lh_pp, double* lh_pw, double* lh_pb, const AdjBodies& ab, double dt,
                      double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s,
-                     cudaStream_t s2, cudaEvent_t* ev)
+                     cudaStream_t s2, cudaEvent_t* ev, bool fp32)
 {
     if (o.n <= 0) return;
     // device counts: S, S1 at the tape's slot, fixed grid-stride grids
@@ -660,9 +687,14 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
     }
     const int bpp = npp < 0 ? sm_count * 8 : min(nblocks(npp, 128), sm_count * 8);
     const int bpw = npw < 0 ? sm_count * 2 : min(nblocks(npw, 128), sm_count * 2);
-    if (bpp + bpw > 0)
-        k_adj_contacts<<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff, grads,
-                                                 nscenes);
+    if (bpp + bpw > 0) {
+        if (fp32)
+            k_adj_contacts<float><<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff,
+                                                            grads, nscenes);
+        else
+            k_adj_contacts<double><<<bpp + bpw, 128, 0, s>>>(c, o, sc, w, tp, npp, npw, bpp, P, T, lh_pp, lh_pw, dt_eff,
+                                                             grads, nscenes);
+    }
     if (fork) {
         cudaEventRecord(ev[2], s2);
         cudaStreamWaitEvent(s, ev[2], 0);

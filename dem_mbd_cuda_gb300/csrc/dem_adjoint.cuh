@@ -12,6 +12,8 @@
 // so tests check them against central differences on the CPU.
 #pragma once
 
+#include <type_traits>
+
 #include "dem_device.cuh"
 
 namespace demgb {
@@ -21,24 +23,26 @@ using D3 = V3<double>;
 // Adjoints of the material constants of one contact class: kN (kS = 2 kN / 7
 // is folded in), mu, log(epsN) and log(epsS) (the denominators pi^2 + log^2
 // are folded in), muT, muR.
-struct MatGrad {
-    double kN, mu, logN, logS, muT, muR;
+template <typename R> struct MatGradT {
+    R kN, mu, logN, logS, muT, muR;
 };
+using MatGrad = MatGradT<double>;
 
 DEM_DEV D3 z3() { return mk(0.0, 0.0, 0.0); }
+template <typename R> DEM_DEV V3<R> zr() { return mk<R>(R(0), R(0), R(0)); }
 
 // ------------------------------------------------------------- primitives
 // a x b: adjoint la += b x lo, lb += lo x a
-DEM_DEV void cross_vjp(D3 a, D3 b, D3 lo, D3& la, D3& lb)
+template <typename R> DEM_DEV void cross_vjp(V3<R> a, V3<R> b, V3<R> lo, V3<R>& la, V3<R>& lb)
 {
     la = la + cross(b, lo);
     lb = lb + cross(lo, a);
 }
 // |a|
-DEM_DEV void norm_vjp(D3 a, double lo, D3& la)
+template <typename R> DEM_DEV void norm_vjp(V3<R> a, R lo, V3<R>& la)
 {
-    const double n = norm(a);
-    if (n > 0.0) la = la + a * (lo / n);
+    const R n = norm(a);
+    if (n > R(0)) la = la + a * (lo / n);
 }
 // q / |q| (normalize_quat; the degenerate reset to identity has no adjoint)
 DEM_DEV void normq_vjp(const double q[4], const double lo[4], double lq[4])
@@ -104,63 +108,64 @@ DEM_DEV void rotq_t_vjp(const double q[4], D3 t, D3 lo, double lq[4], D3& lt)
 }
 
 // --------------------------------------------------------- history maps
-DEM_DEV void transport_tangent_vjp(D3 h, D3 n, D3 lo, D3& lh, D3& ln)
+template <typename R> DEM_DEV void transport_tangent_vjp(V3<R> h, V3<R> n, V3<R> lo, V3<R>& lh, V3<R>& ln)
 {
-    const double pn = norm(h);
-    const double hn = dot(h, n);
-    const D3 proj = h - n * hn;
-    const double qn = norm(proj);
-    if (pn <= 1.0e-30 || qn <= 1.0e-30) return;
-    const double s = pn / qn;
-    D3 lproj = lo * s;
-    const double ls = dot(proj, lo);
-    const double lpn = ls / qn, lqn = -ls * pn / (qn * qn);
+    const R pn = norm(h);
+    const R hn = dot(h, n);
+    const V3<R> proj = h - n * hn;
+    const R qn = norm(proj);
+    if (pn <= R(1.0e-30) || qn <= R(1.0e-30)) return;
+    const R s = pn / qn;
+    V3<R> lproj = lo * s;
+    const R ls = dot(proj, lo);
+    const R lpn = ls / qn, lqn = -ls * pn / (qn * qn);
     lproj = lproj + proj * (lqn / qn);
     lh = lh + h * (lpn / pn);
-    const double nl = dot(n, lproj);
+    const R nl = dot(n, lproj);
     lh = lh + (lproj - n * nl);
     ln = ln + lproj * (-hn) - h * nl;
 }
-DEM_DEV void transport_axial_vjp(D3 h, D3 n, D3 lo, D3& lh, D3& ln)
+template <typename R> DEM_DEV void transport_axial_vjp(V3<R> h, V3<R> n, V3<R> lo, V3<R>& lh, V3<R>& ln)
 {
-    const double pn = norm(h);
-    if (pn <= 1.0e-30) return;
-    const double al = dot(h, n);
-    if (fabs(al) <= 1.0e-30) return;
-    const double sg = al < 0.0 ? -1.0 : 1.0;
+    const R pn = norm(h);
+    if (pn <= R(1.0e-30)) return;
+    const R al = dot(h, n);
+    if (fabs(al) <= R(1.0e-30)) return;
+    const R sg = al < R(0) ? R(-1) : R(1);
     ln = ln + lo * (sg * pn);
     lh = lh + h * (sg * dot(n, lo) / pn);
 }
 
 // limitedHistoryResponseRates (:267-299): (resp, stored) from (hrate,
 // rrate, k, c, prev, limit); lr = adjoint of resp, ls = of stored.
-DEM_DEV void limited_rates_vjp(D3 hrate, D3 rrate, double k, double c, double dt, D3 prev, double limit, D3 lr, D3 ls,
-                               D3& lhrate, D3& lrrate, double& lk, double& lc, D3& lprev, double& llimit)
+template <typename R>
+DEM_DEV void limited_rates_vjp(V3<R> hrate, V3<R> rrate, R k, R c, R dt, V3<R> prev, R limit, V3<R> lr, V3<R> ls,
+                               V3<R>& lhrate, V3<R>& lrrate, R& lk, R& lc, V3<R>& lprev, R& llimit)
 {
-    const D3 delta = hrate * dt;
-    const D3 inc = delta * k;
-    const D3 et = inc + prev;
-    const double tn = norm(et);
-    D3 linc = z3();
+    const V3<R> delta = hrate * dt;
+    const V3<R> inc = delta * k;
+    const V3<R> et = inc + prev;
+    const R tn = norm(et);
+    V3<R> linc = zr<R>();
     if (tn > limit) {
-        const D3 lR = lr + ls;
-        if (norm(delta) > 1.0e-14) {
-            const double g = limit / tn;
-            D3 let = lR * g;
-            const double lg = dot(et, lR);
+        const V3<R> lR = lr + ls;
+        if (norm(delta) > R(1.0e-14)) {
+            const R g = limit / tn;
+            V3<R> let = lR * g;
+            const R lg = dot(et, lR);
             llimit += lg / tn;
-            const double ltn = -lg * limit / (tn * tn);
+            const R ltn = -lg * limit / (tn * tn);
             let = let + et * (ltn / tn);
             linc = let;
             lprev = lprev + let;
         } else {
-            const double pn = norm(prev);
-            if (pn > 1.0e-14) {
-                const double g = limit / pn;
+            const R pn = norm(prev);
+            if (pn > R(1.0e-14)) {
+                const R g = limit / pn;
                 lprev = lprev + lR * g;
-                const double lg = dot(prev, lR);
+                const R lg = dot(prev, lR);
                 llimit += lg / pn;
-                const double lpn = -lg * limit / (pn * pn);
+                const R lpn = -lg * limit / (pn * pn);
                 lprev = lprev + prev * (lpn / pn);
             }
         }
@@ -175,25 +180,25 @@ DEM_DEV void limited_rates_vjp(D3 hrate, D3 rrate, double k, double c, double dt
 }
 
 // wallHistoryResponse (:951-973)
-DEM_DEV void wall_response_vjp(D3 rate, double k, double c, double dt, D3 prev, double limit, bool check_damped,
-                               bool zero_at_zero, D3 lr, D3 ls, D3& lrate, double& lk, double& lc, D3& lprev,
-                               double& llimit)
+template <typename R>
+DEM_DEV void wall_response_vjp(V3<R> rate, R k, R c, R dt, V3<R> prev, R limit, bool check_damped, bool zero_at_zero,
+                               V3<R> lr, V3<R> ls, V3<R>& lrate, R& lk, R& lc, V3<R>& lprev, R& llimit)
 {
-    const D3 delta = rate * dt;
-    const D3 et = prev + delta * k;
-    const D3 st = et + rate * c;
-    const double tn = norm(check_damped ? st : et);
-    D3 let = z3();
+    const V3<R> delta = rate * dt;
+    const V3<R> et = prev + delta * k;
+    const V3<R> st = et + rate * c;
+    const R tn = norm(check_damped ? st : et);
+    V3<R> let = zr<R>();
     if (tn > limit) {
-        const D3 lR = lr + ls;
-        const double dn = norm(delta);
-        if (dn > 1.0e-14 && tn > 1.0e-14) {
-            const D3 lt = check_damped ? st : et;
-            const double g = limit / tn;
-            D3 llt = lR * g;
-            const double lg = dot(lt, lR);
+        const V3<R> lR = lr + ls;
+        const R dn = norm(delta);
+        if (dn > R(1.0e-14) && tn > R(1.0e-14)) {
+            const V3<R> lt = check_damped ? st : et;
+            const R g = limit / tn;
+            V3<R> llt = lR * g;
+            const R lg = dot(lt, lR);
             llimit += lg / tn;
-            const double ltn = -lg * limit / (tn * tn);
+            const R ltn = -lg * limit / (tn * tn);
             llt = llt + lt * (ltn / tn);
             if (check_damped) {
                 let = llt;
@@ -217,35 +222,39 @@ DEM_DEV void wall_response_vjp(D3 rate, double k, double c, double dt, D3 prev, 
 
 // Adjoints of the per-contact constants (law_constants) -> material
 // adjoints.  mred and the radius term are fixed per pair.
-struct LawL {
-    double kN, kS, cN, cS, kT, cT, kR, cR;
+template <typename R> struct LawLT {
+    R kN, kS, cN, cS, kT, cT, kR, cR;
 };
-DEM_DEV void law_constants_vjp(const MatC& m, double mred, double rterm, const LawL& l, MatGrad& g)
+using LawL = LawLT<double>;
+template <typename R, typename M>
+DEM_DEV void law_constants_vjp(const M& m, R mred, R rterm, const LawLT<R>& l, MatGradT<R>& g)
 {
-    const double brs = m.beta * rterm * m.beta * rterm;
-    double lkS = l.kS + 2.0 * brs * l.kT;
-    const double lcS = l.cS + 2.0 * brs * l.cT;
-    double lkN = l.kN + brs * l.kR;
-    const double lcN = l.cN + brs * l.cR;
+    const R beta = R(m.beta), kN = R(m.kN), kS = R(m.kS), denN = R(m.denN), denS = R(m.denS);
+    const R logN = R(m.logN), logS = R(m.logS);
+    const R brs = beta * rterm * beta * rterm;
+    R lkS = l.kS + R(2.0) * brs * l.kT;
+    const R lcS = l.cS + R(2.0) * brs * l.cT;
+    R lkN = l.kN + brs * l.kR;
+    const R lcN = l.cN + brs * l.cR;
     // cN = -2 logN sqrt(kN mred / denN), denN = pi^2 + logN^2
     {
-        const double A = m.kN * mred / m.denN, sA = sqrt(A);
-        const double lA = -m.logN * lcN / sA;
-        g.logN += -2.0 * sA * lcN;
-        lkN += lA * mred / m.denN;
-        const double lden = -lA * m.kN * mred / (m.denN * m.denN);
-        g.logN += 2.0 * m.logN * lden;
+        const R A = kN * mred / denN, sA = sqrt(A);
+        const R lA = -logN * lcN / sA;
+        g.logN += R(-2.0) * sA * lcN;
+        lkN += lA * mred / denN;
+        const R lden = -lA * kN * mred / (denN * denN);
+        g.logN += R(2.0) * logN * lden;
     }
     // cS = -2 logS sqrt(kS mred / denS)
     {
-        const double A = m.kS * mred / m.denS, sA = sqrt(A);
-        const double lA = -m.logS * lcS / sA;
-        g.logS += -2.0 * sA * lcS;
-        lkS += lA * mred / m.denS;
-        const double lden = -lA * m.kS * mred / (m.denS * m.denS);
-        g.logS += 2.0 * m.logS * lden;
+        const R A = kS * mred / denS, sA = sqrt(A);
+        const R lA = -logS * lcS / sA;
+        g.logS += R(-2.0) * sA * lcS;
+        lkS += lA * mred / denS;
+        const R lden = -lA * kS * mred / (denS * denS);
+        g.logS += R(2.0) * logS * lden;
     }
-    g.kN += lkN + lkS * (2.0 / 7.0);
+    g.kN += lkN + lkS * R(2.0 / 7.0);
 }
 
 // --------------------------------------------------------- particle law
@@ -253,106 +262,116 @@ DEM_DEV void law_constants_vjp(const MatC& m, double mred, double rterm, const L
 // masses, endpoint and midpoint relative velocities (erv, mrv), world
 // angular velocities (endpoint ew, midpoint mw), history h[9] before the
 // step.  Output adjoints: force lF, couple lC (on i), stored history lh[9].
-struct PPIn {
-    D3 delta;
-    double ri, rj, mi, mj;
-    D3 erv, mrv, ewi, ewj, mwi, mwj;
-    double h[9];
+template <typename R> struct PPInT {
+    V3<R> delta;
+    R ri, rj, mi, mj;
+    V3<R> erv, mrv, ewi, ewj, mwi, mwj;
+    R h[9];
+    R depth;  // the overlap, given by the caller of the FP32 form (from FP64 positions)
 };
-struct PPAdj {
-    D3 delta, erv, mrv, ewi, ewj, mwi, mwj;
-    double h[9];
+template <typename R> struct PPAdjT {
+    V3<R> delta, erv, mrv, ewi, ewj, mwi, mwj;
+    R h[9];
 };
+using PPIn = PPInT<double>;
+using PPAdj = PPAdjT<double>;
 
-DEM_DEV void pp_law_vjp(const MatC& m, double dt, const PPIn& in, D3 lF, D3 lC, const double lh_out[9], PPAdj& a,
-                        MatGrad& g)
+// R = double: the FP64 form.  R = float: the same map in FP32 (material
+// constants M = MatF); the overlap in.depth comes from the caller, who forms
+// it from the FP64 positions (r_i + r_j - d cancels in FP32).
+template <typename R, typename M>
+DEM_DEV void pp_law_vjp(const M& m, R dt, const PPInT<R>& in, V3<R> lF, V3<R> lC, const R lh_out[9], PPAdjT<R>& a,
+                        MatGradT<R>& g)
 {
+    const R mu = R(m.mu), muT = R(m.muT), muR = R(m.muR), beta = R(m.beta), coh = R(m.coh);
     // forward
-    const double d2 = dot(in.delta, in.delta);
-    const double d = sqrt(d2);
-    const D3 n = in.delta * (1.0 / d);
-    const double rs = in.ri + in.rj;
-    const double depth = rs - d;
-    const double mred = in.mi * in.mj / (in.mi + in.mj);
-    const double reff = in.ri * in.rj / rs;
-    const LawC<double> c = law_constants<double, MatC>(m, mred, reff);
-    const double ervn = dot(in.erv, n);
-    const double phi = -c.kN * depth + c.cN * ervn + m.coh * 4.0 * c.brs;
-    const D3 fn = n * phi;
-    const double A = in.ri * in.ri - in.rj * in.rj;
-    const double li = (A + d2) / (2.0 * d);
-    const double lj = d - li;
-    const D3 X1 = cross(n, in.ewi), X2 = cross(n, in.ewj), Y1 = cross(n, in.mwi), Y2 = cross(n, in.mwj);
-    const double mrvn = dot(in.mrv, n);
-    const D3 etv = in.erv - n * ervn + X1 * li + X2 * lj;
-    const D3 mtv = in.mrv - n * mrvn + Y1 * li + Y2 * lj;
-    const D3 h0 = mk(in.h[0], in.h[1], in.h[2]), h1 = mk(in.h[3], in.h[4], in.h[5]), h2 = mk(in.h[6], in.h[7], in.h[8]);
-    const D3 prev_t = transport_tangent(h1, n);
-    const double fnn = norm(fn);
-    const double Lt = m.mu * fnn;
-    D3 st;
+    const R d2 = dot(in.delta, in.delta);
+    const R d = sqrt(d2);
+    const V3<R> n = in.delta * (R(1.0) / d);
+    const R rs = in.ri + in.rj;
+    R depth;
+    if constexpr (std::is_same<R, double>::value) depth = rs - d;
+    else depth = in.depth;
+    const R mred = in.mi * in.mj / (in.mi + in.mj);
+    const R reff = in.ri * in.rj / rs;
+    const LawC<R> c = law_constants<R, M>(m, mred, reff);
+    const R ervn = dot(in.erv, n);
+    const R phi = -c.kN * depth + c.cN * ervn + coh * R(4.0) * c.brs;
+    const V3<R> fn = n * phi;
+    const R A = in.ri * in.ri - in.rj * in.rj;
+    const R li = (A + d2) / (R(2.0) * d);
+    const R lj = d - li;
+    const V3<R> X1 = cross(n, in.ewi), X2 = cross(n, in.ewj), Y1 = cross(n, in.mwi), Y2 = cross(n, in.mwj);
+    const R mrvn = dot(in.mrv, n);
+    const V3<R> etv = in.erv - n * ervn + X1 * li + X2 * lj;
+    const V3<R> mtv = in.mrv - n * mrvn + Y1 * li + Y2 * lj;
+    const V3<R> h0 = mk(in.h[0], in.h[1], in.h[2]), h1 = mk(in.h[3], in.h[4], in.h[5]), h2 = mk(in.h[6], in.h[7], in.h[8]);
+    const V3<R> prev_t = transport_tangent(h1, n);
+    const R fnn = norm(fn);
+    const R Lt = mu * fnn;
+    V3<R> st;
     bool y;
-    const D3 fr = limited_rates<double>(mtv, etv, c.kS, c.cS, dt, prev_t, Lt, st, y);
-    const D3 erw = in.ewj - in.ewi, mrw = in.mwj - in.mwi;
-    const double erwn = dot(erw, n), mrwn = dot(mrw, n);
-    const D3 etw = n * erwn, mtw = n * mrwn;
-    const D3 erl = erw - etw, mrl = mrw - mtw;
-    const double ms = m.beta * reff * fnn;
-    const D3 prev_w = transport_axial(h2, n);
-    const double Lw = m.mu * m.muT * ms;
-    const D3 prev_r = transport_tangent(h0, n);
-    const double Lr = m.muR * ms;
+    const V3<R> fr = limited_rates<R>(mtv, etv, c.kS, c.cS, dt, prev_t, Lt, st, y);
+    const V3<R> erw = in.ewj - in.ewi, mrw = in.mwj - in.mwi;
+    const R erwn = dot(erw, n), mrwn = dot(mrw, n);
+    const V3<R> etw = n * erwn, mtw = n * mrwn;
+    const V3<R> erl = erw - etw, mrl = mrw - mtw;
+    const R ms = beta * reff * fnn;
+    const V3<R> prev_w = transport_axial(h2, n);
+    const R Lw = mu * muT * ms;
+    const V3<R> prev_r = transport_tangent(h0, n);
+    const R Lr = muR * ms;
 
     // reverse
-    D3 ln = z3(), lfn = lF, lfr = lF;
-    double lli = 0.0, llj = 0.0, ld = 0.0, ld2 = 0.0, ldepth = 0.0;
-    LawL ll = {0, 0, 0, 0, 0, 0, 0, 0};
+    V3<R> ln = zr<R>(), lfn = lF, lfr = lF;
+    R lli = 0, llj = 0, ld = 0, ld2 = 0, ldepth = 0;
+    LawLT<R> ll = {0, 0, 0, 0, 0, 0, 0, 0};
     // couple = (tw + rl) + cross(n, fr) li
-    const D3 lX = lC * li;
+    const V3<R> lX = lC * li;
     lli += dot(cross(n, fr), lC);
     cross_vjp(n, fr, lX, ln, lfr);
     // roll channel
-    D3 lmrl = z3(), lerl = z3(), lpr = z3();
-    double lLr = 0.0;
+    V3<R> lmrl = zr<R>(), lerl = zr<R>(), lpr = zr<R>();
+    R lLr = 0;
     limited_rates_vjp(mrl, erl, c.kR, c.cR, dt, prev_r, Lr, lC, mk(lh_out[0], lh_out[1], lh_out[2]), lmrl, lerl, ll.kR,
                       ll.cR, lpr, lLr);
     // twist channel
-    D3 lmtw = z3(), letw = z3(), lpw = z3();
-    double lLw = 0.0;
+    V3<R> lmtw = zr<R>(), letw = zr<R>(), lpw = zr<R>();
+    R lLw = 0;
     limited_rates_vjp(mtw, etw, c.kT, c.cT, dt, prev_w, Lw, lC, mk(lh_out[6], lh_out[7], lh_out[8]), lmtw, letw, ll.kT,
                       ll.cT, lpw, lLw);
     // tangential channel
-    D3 lmtv = z3(), letv = z3(), lpt = z3();
-    double lLt = 0.0;
+    V3<R> lmtv = zr<R>(), letv = zr<R>(), lpt = zr<R>();
+    R lLt = 0;
     limited_rates_vjp(mtv, etv, c.kS, c.cS, dt, prev_t, Lt, lfr, mk(lh_out[3], lh_out[4], lh_out[5]), lmtv, letv, ll.kS,
                       ll.cS, lpt, lLt);
     // limits
-    double lms = m.muR * lLr + m.mu * m.muT * lLw;
+    R lms = muR * lLr + mu * muT * lLw;
     g.muR += ms * lLr;
-    g.mu += m.muT * ms * lLw + fnn * lLt;
-    g.muT += m.mu * ms * lLw;
-    const double lfnn = m.beta * reff * lms + m.mu * lLt;
+    g.mu += muT * ms * lLw + fnn * lLt;
+    g.muT += mu * ms * lLw;
+    const R lfnn = beta * reff * lms + mu * lLt;
     norm_vjp(fn, lfnn, lfn);
     // transports
-    D3 lh0 = z3(), lh1 = z3(), lh2 = z3();
+    V3<R> lh0 = zr<R>(), lh1 = zr<R>(), lh2 = zr<R>();
     transport_tangent_vjp(h0, n, lpr, lh0, ln);
     transport_axial_vjp(h2, n, lpw, lh2, ln);
     transport_tangent_vjp(h1, n, lpt, lh1, ln);
     // rolling and twisting rates: erl = erw - n (erw.n), etw = n (erw.n)
-    D3 lerw = z3(), lmrw = z3();
+    V3<R> lerw = zr<R>(), lmrw = zr<R>();
     {
-        const double nl = dot(n, lerl);
+        const R nl = dot(n, lerl);
         lerw = lerw + lerl - n * nl;
         ln = ln + lerl * (-erwn) - erw * nl;
-        const double nt = dot(n, letw);
+        const R nt = dot(n, letw);
         ln = ln + letw * erwn + erw * nt;
         lerw = lerw + n * nt;
     }
     {
-        const double nl = dot(n, lmrl);
+        const R nl = dot(n, lmrl);
         lmrw = lmrw + lmrl - n * nl;
         ln = ln + lmrl * (-mrwn) - mrw * nl;
-        const double nt = dot(n, lmtw);
+        const R nt = dot(n, lmtw);
         ln = ln + lmtw * mrwn + mrw * nt;
         lmrw = lmrw + n * nt;
     }
@@ -360,7 +379,7 @@ DEM_DEV void pp_law_vjp(const MatC& m, double dt, const PPIn& in, D3 lF, D3 lC, 
     a.mwj = a.mwj + lmrw; a.mwi = a.mwi - lmrw;
     // etv = erv - n (erv.n) + X1 li + X2 lj
     {
-        const double nl = dot(n, letv);
+        const R nl = dot(n, letv);
         a.erv = a.erv + letv - n * nl;
         ln = ln + letv * (-ervn) - in.erv * nl;
         lli += dot(X1, letv);
@@ -369,7 +388,7 @@ DEM_DEV void pp_law_vjp(const MatC& m, double dt, const PPIn& in, D3 lF, D3 lC, 
         cross_vjp(n, in.ewj, letv * lj, ln, a.ewj);
     }
     {
-        const double nl = dot(n, lmtv);
+        const R nl = dot(n, lmtv);
         a.mrv = a.mrv + lmtv - n * nl;
         ln = ln + lmtv * (-mrvn) - in.mrv * nl;
         lli += dot(Y1, lmtv);
@@ -380,11 +399,11 @@ DEM_DEV void pp_law_vjp(const MatC& m, double dt, const PPIn& in, D3 lF, D3 lC, 
     // lj = d - li, li = (A + d2) / (2 d)
     ld += llj;
     lli -= llj;
-    ld2 += lli / (2.0 * d);
-    ld -= lli * (A + d2) / (2.0 * d * d);
+    ld2 += lli / (R(2.0) * d);
+    ld -= lli * (A + d2) / (R(2.0) * d * d);
     // fn = n phi
     ln = ln + lfn * phi;
-    const double lphi = dot(n, lfn);
+    const R lphi = dot(n, lfn);
     ll.kN += -depth * lphi;
     ldepth += -c.kN * lphi;
     ll.cN += ervn * lphi;
@@ -393,9 +412,9 @@ DEM_DEV void pp_law_vjp(const MatC& m, double dt, const PPIn& in, D3 lF, D3 lC, 
     law_constants_vjp(m, mred, reff, ll, g);
     // geometry: depth = rs - d, n = delta / d, d = sqrt(d2), d2 = delta.delta
     ld -= ldepth;
-    a.delta = a.delta + ln * (1.0 / d);
+    a.delta = a.delta + ln * (R(1.0) / d);
     ld -= dot(in.delta, ln) / (d * d);
-    a.delta = a.delta + n * ld + in.delta * (2.0 * ld2);
+    a.delta = a.delta + n * ld + in.delta * (R(2.0) * ld2);
     a.h[0] += lh0.x; a.h[1] += lh0.y; a.h[2] += lh0.z;
     a.h[3] += lh1.x; a.h[4] += lh1.y; a.h[5] += lh1.z;
     a.h[6] += lh2.x; a.h[7] += lh2.y; a.h[8] += lh2.z;
@@ -404,78 +423,81 @@ DEM_DEV void pp_law_vjp(const MatC& m, double dt, const PPIn& in, D3 lF, D3 lC, 
 // ------------------------------------------------------------- wall law
 // One particle and one planar wall: out = wall normal, depth = r - (p - o).out,
 // endpoint velocity vel and world angular velocity om.
-struct PWAdj {
-    D3 p, vel, om;
-    double h[9];
+template <typename R> struct PWAdjT {
+    V3<R> p, vel, om;
+    R h[9];
 };
-DEM_DEV void pw_law_vjp(const MatC& m, double dt, D3 out, double depth, double r, double mass, D3 vel, D3 om,
-                        const double hin[9], D3 lF, D3 lC, const double lh_out[9], PWAdj& a, MatGrad& g)
+using PWAdj = PWAdjT<double>;
+template <typename R, typename M>
+DEM_DEV void pw_law_vjp(const M& m, R dt, V3<R> out, R depth, R r, R mass, V3<R> vel, V3<R> om, const R hin[9],
+                        V3<R> lF, V3<R> lC, const R lh_out[9], PWAdjT<R>& a, MatGradT<R>& g)
 {
-    const D3 n = out * -1.0;
-    const double lever = r - depth;
-    const D3 rv = vel * -1.0;
-    const double rvn = dot(rv, n);
-    const D3 Z = cross(n, om);
-    const D3 tv = rv - n * rvn + Z * lever;
-    const D3 rw = om * -1.0;
-    const double rwn = dot(rw, n);
-    const D3 twr = n * rwn;
-    const bool lev = fabs(lever) > 1.0e-30;
-    const D3 Q = cross(n, tv);
-    const D3 rlr = lev ? (rw - twr) + Q * (0.5 / lever) : rw - twr;
-    const LawC<double> c = law_constants<double, MatC>(m, mass, r);
-    const D3 fn = n * (-c.kN * depth) + n * (c.cN * rvn);
-    const double fnn = norm(fn);
-    const double flim = m.mu * fnn;
-    const double ms = m.beta * r * fnn;
-    const D3 h0 = mk(hin[0], hin[1], hin[2]), h1 = mk(hin[3], hin[4], hin[5]), h2 = mk(hin[6], hin[7], hin[8]);
-    const D3 prev_t = transport_tangent(h1, n), prev_w = transport_axial(h2, n), prev_r = transport_tangent(h0, n);
-    D3 st;
-    const D3 fr = wall_response<double>(tv, c.kS, c.cS, dt, prev_t, flim, false, false, st);
-    const double Lw = m.mu * m.muT * ms, Lr = m.muR * ms;
+    const R mu = R(m.mu), muT = R(m.muT), muR = R(m.muR), beta = R(m.beta);
+    const V3<R> n = out * R(-1.0);
+    const R lever = r - depth;
+    const V3<R> rv = vel * R(-1.0);
+    const R rvn = dot(rv, n);
+    const V3<R> Z = cross(n, om);
+    const V3<R> tv = rv - n * rvn + Z * lever;
+    const V3<R> rw = om * R(-1.0);
+    const R rwn = dot(rw, n);
+    const V3<R> twr = n * rwn;
+    const bool lev = fabs(lever) > R(1.0e-30);
+    const V3<R> Q = cross(n, tv);
+    const V3<R> rlr = lev ? (rw - twr) + Q * (R(0.5) / lever) : rw - twr;
+    const LawC<R> c = law_constants<R, M>(m, mass, r);
+    const V3<R> fn = n * (-c.kN * depth) + n * (c.cN * rvn);
+    const R fnn = norm(fn);
+    const R flim = mu * fnn;
+    const R ms = beta * r * fnn;
+    const V3<R> h0 = mk(hin[0], hin[1], hin[2]), h1 = mk(hin[3], hin[4], hin[5]), h2 = mk(hin[6], hin[7], hin[8]);
+    const V3<R> prev_t = transport_tangent(h1, n), prev_w = transport_axial(h2, n), prev_r = transport_tangent(h0, n);
+    V3<R> st;
+    const V3<R> fr = wall_response<R>(tv, c.kS, c.cS, dt, prev_t, flim, false, false, st);
+    const R Lw = mu * muT * ms, Lr = muR * ms;
 
-    D3 lfn = lF, lfr = lF, ln_unused = z3();
-    double llever = 0.0, ldepth = 0.0;
-    LawL ll = {0, 0, 0, 0, 0, 0, 0, 0};
+    V3<R> lfn = lF, lfr = lF, ln_unused = zr<R>();
+    R llever = 0, ldepth = 0;
+    LawLT<R> ll = {0, 0, 0, 0, 0, 0, 0, 0};
     // couple = (tw + rl) + cross(n, fr) lever
     llever += dot(cross(n, fr), lC);
     cross_vjp(n, fr, lC * lever, ln_unused, lfr);
-    D3 lrlr = z3(), lpr = z3();
-    double lLr = 0.0;
+    V3<R> lrlr = zr<R>(), lpr = zr<R>();
+    R lLr = 0;
     wall_response_vjp(rlr, c.kR, c.cR, dt, prev_r, Lr, true, true, lC, mk(lh_out[0], lh_out[1], lh_out[2]), lrlr, ll.kR,
                       ll.cR, lpr, lLr);
-    D3 ltwr = z3(), lpw = z3();
-    double lLw = 0.0;
+    V3<R> ltwr = zr<R>(), lpw = zr<R>();
+    R lLw = 0;
     wall_response_vjp(twr, c.kT, c.cT, dt, prev_w, Lw, false, true, lC, mk(lh_out[6], lh_out[7], lh_out[8]), ltwr, ll.kT,
                       ll.cT, lpw, lLw);
-    D3 ltv = z3(), lpt = z3();
-    double lflim = 0.0;
+    V3<R> ltv = zr<R>(), lpt = zr<R>();
+    R lflim = 0;
     wall_response_vjp(tv, c.kS, c.cS, dt, prev_t, flim, false, false, lfr, mk(lh_out[3], lh_out[4], lh_out[5]), ltv,
                       ll.kS, ll.cS, lpt, lflim);
-    const double lms = m.muR * lLr + m.mu * m.muT * lLw;
+    const R lms = muR * lLr + mu * muT * lLw;
     g.muR += ms * lLr;
-    g.mu += m.muT * ms * lLw + fnn * lflim;
-    g.muT += m.mu * ms * lLw;
-    norm_vjp(fn, m.beta * r * lms + m.mu * lflim, lfn);
-    D3 lh0 = z3(), lh1 = z3(), lh2 = z3();
+    g.mu += muT * ms * lLw + fnn * lflim;
+    g.muT += mu * ms * lLw;
+    norm_vjp(fn, beta * r * lms + mu * lflim, lfn);
+    V3<R> lh0 = zr<R>(), lh1 = zr<R>(), lh2 = zr<R>();
     transport_tangent_vjp(h0, n, lpr, lh0, ln_unused);
     transport_axial_vjp(h2, n, lpw, lh2, ln_unused);
     transport_tangent_vjp(h1, n, lpt, lh1, ln_unused);
     // rlr = rw - n (rw.n) [+ Q (0.5 / lever)], Q = n x tv
-    D3 lrw = lrlr - n * dot(n, lrlr);
+    V3<R> lrw = lrlr - n * dot(n, lrlr);
     if (lev) {
-        const D3 lQ = lrlr * (0.5 / lever);
-        llever += -dot(Q, lrlr) * 0.5 / (lever * lever);
+        const V3<R> lQ = lrlr * (R(0.5) / lever);
+        llever += -dot(Q, lrlr) * R(0.5) / (lever * lever);
         cross_vjp(n, tv, lQ, ln_unused, ltv);
     }
     lrw = lrw + n * dot(n, ltwr);
     a.om = a.om - lrw;
     // tv = rv - n (rv.n) + Z lever, Z = n x om
-    D3 lrv = ltv - n * dot(n, ltv);
+    V3<R> lrv = ltv - n * dot(n, ltv);
     llever += dot(Z, ltv);
     cross_vjp(n, om, ltv * lever, ln_unused, a.om);
     // fn = n (-kN depth) + n (cN rv.n)
-    const double lphi = dot(n, lfn);
+    const R lphi = dot(n, lfn);
     ll.kN += -depth * lphi;
     ldepth += -c.kN * lphi;
     ll.cN += rvn * lphi;

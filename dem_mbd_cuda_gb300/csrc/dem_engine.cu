@@ -1517,6 +1517,9 @@ public:
         // the largest counts the forward run saw at its checkpoints: contact
         // sides, particle-wall candidates, body manifolds and items
         int seen_pp = 0, seen_pw = 0, seen_pb = 0;
+        // the last backward run's adjoints of the bodies' initial state
+        // ([nb][kBL] rows; dynamic bodies only)
+        std::vector<double> body_grads;
     };
     void adj_release_graphs()
     {
@@ -1786,7 +1789,7 @@ public:
                     launch_adj_slot_add(t.slot, -1, stream_);
                     launch_adj_step(C_, O_, d_sc_, W_, tp, -1, -1, -1, t.S, nullptr, A.Lb[p], A.Lb[1 - p], A.P, A.T,
                                     A.lh_pp, A.lh_pw, A.lh_pb, ab, dt_, dt_, 0, A.grads, S_, sm_count_, stream_,
-                                    branch_[0], fork_ev_.data());
+                                    branch_[0], fork_ev_.data(), adj_fp32_);
                 });
         }
     }
@@ -1940,11 +1943,16 @@ public:
         counts(1);
         launch_adj_step(C_, O_, d_sc_, W_, adj_tape_step(0), npp[0], npw[0], npb[0], A.tb[0].S, A.tb[0].S, A.L, A.Lp,
                         A.P, A.T, A.lh_pp, A.lh_pw, A.lh_pb, adj_bodies(nullptr), 0.5 * dt_, 0.0, 1, A.grads, S_,
-                        sm_count_, s);
+                        sm_count_, s, nullptr, nullptr, adj_fp32_);
         check(cudaGetLastError(), "adjoint backward");
         std::vector<double> h(kAdjFields * N), g((size_t)S_ * 3 * kAdjParams);
         check(cudaMemcpyAsync(h.data(), A.Lp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s), "adjoint");
         check(cudaMemcpyAsync(g.data(), A.grads, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s), "adjoint");
+        A.body_grads.assign(nb_ > 0 ? (size_t)nb_ * kBL : 0, 0.0);
+        if (nb_ > 0)
+            check(cudaMemcpyAsync(A.body_grads.data(), A.Lbody, sizeof(double) * A.body_grads.size(),
+                                  cudaMemcpyDeviceToHost, s),
+                  "adjoint");
         check(cudaStreamSynchronize(s), "adjoint");
         for (size_t i = 0; i < N; ++i)
             for (int a = 0; a < 3; ++a) {
@@ -1999,6 +2007,34 @@ public:
     int n_marks_ = 0;
     DeviceArena arena_, arena_tmp_, adj_arena_, adj_tape_arena_;
     Adjoint adj_;
+    // The reverse law of the particle and wall contacts in FP32 (the forward
+    // run, the recompute and everything else stay FP64).
+    bool adj_fp32_ = false;
+    // dem_adjoint_body_gradients: the last backward run's gradients with
+    // respect to the bodies' initial centre, orientation, velocity and
+    // body-frame spin (zero for prescribed and fixed bodies).
+    void adjoint_body_gradients(double* c, double* q, double* v, double* w) const
+    {
+        const Adjoint& A = adj_;
+        if (A.body_grads.size() != (size_t)nb_ * kBL)
+            throw DemError(DEM_ERR_STATE, "adjoint body gradients need dem_adjoint_backward first");
+        for (int b = 0; b < nb_; ++b) {
+            const double* r = A.body_grads.data() + (size_t)b * kBL;
+            const bool dyn = body_state_[b] == 0;
+            for (int a = 0; a < 3; ++a) {
+                if (c) c[3 * b + a] = dyn ? r[kBlC + a] : 0.0;
+                if (v) v[3 * b + a] = dyn ? r[kBlV + a] : 0.0;
+                if (w) w[3 * b + a] = dyn ? r[kBlW + a] : 0.0;
+            }
+            for (int a = 0; a < 4; ++a)
+                if (q) q[4 * b + a] = dyn ? r[kBlQ + a] : 0.0;
+        }
+    }
+    void set_adjoint_fp32(bool on)
+    {
+        if (on != adj_fp32_) adj_release_graphs();
+        adj_fp32_ = on;
+    }
     std::vector<double>* adj_rec_ = nullptr;  // body records of the forward run, while dem_adjoint_forward runs
     std::vector<double> oin_host_;  // owner principal inertia [n][3] (host copy)
     void* pinned_ = nullptr;
@@ -2300,6 +2336,20 @@ int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double*
 int dem_x_neighbor_stats(dem_engine* e, int* builds, double* mean_length, int* max_length, int* overflowed)
 {
     return guarded([&] { NEED(e); e->e.neighbor_stats(builds, mean_length, max_length, overflowed); });
+}
+
+int dem_adjoint_body_gradients(dem_engine* e, double* dl_dbody_center0, double* dl_dbody_quat0,
+                               double* dl_dbody_vel0, double* dl_dbody_omega0)
+{
+    return guarded([&] {
+        NEED(e);
+        e->e.adjoint_body_gradients(dl_dbody_center0, dl_dbody_quat0, dl_dbody_vel0, dl_dbody_omega0);
+    });
+}
+
+int dem_x_set_adjoint_fp32(dem_engine* e, int on)
+{
+    return guarded([&] { NEED(e); e->e.set_adjoint_fp32(on != 0); });
 }
 
 int dem_x_adjoint_bytes(dem_engine* e, size_t* checkpoints, size_t* tapes)

@@ -396,7 +396,7 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
                      int npw, int npb, const double* S, const double* S1, const double* L, double* Lp, double* P,
                      double* T, double* lh_pp, double* lh_pw, double* lh_pb, const AdjBodies& ab, double dt,
                      double dt_eff, int init, double* grads, int nscenes, int sm_count, cudaStream_t s,
-                     cudaStream_t s2 = nullptr, cudaEvent_t* ev = nullptr);
+                     cudaStream_t s2 = nullptr, cudaEvent_t* ev = nullptr, bool fp32 = false);
 // Recompute: the body pose of the tape's step (record *base + *slot; null
 // pointers: record 0) into the engine's body arrays.
 void launch_adj_body_pose(const Bodies& b, const double* rec, const int* base, const int* slot, cudaStream_t s);

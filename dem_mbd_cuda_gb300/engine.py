@@ -64,6 +64,8 @@ _SIGS = {
     "dem_adjoint_backward_mbd": ([C.c_void_p] + [C.c_void_p] * 8, C.c_int),
     "dem_x_neighbor_stats": ([C.c_void_p] + [C.c_void_p] * 4, C.c_int),
     "dem_x_adjoint_bytes": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "dem_x_set_adjoint_fp32": ([C.c_void_p, C.c_int], C.c_int),
+    "dem_adjoint_body_gradients": ([C.c_void_p] * 5, C.c_int),
     "dem_x_scan_wait_probe": ([C.c_void_p, C.c_void_p], C.c_int),
 }
 
@@ -297,8 +299,14 @@ class CudaDemSolver:
         keys = ("kN", "mu", "epsN", "epsS", "muT", "muR")
         per = [{"pp": dict(zip(keys, q[:6])), "pw": dict(zip(keys, q[6:12])), "pt": dict(zip(keys, q[12:]))}
                for q in p.reshape(self.scenes, 18)]
-        return {"dl_dpos0": x0, "dl_dvel0": v0, "dl_domega0": w0,
-                "dl_dparams": per[0] if self.scenes == 1 else per}
+        out = {"dl_dpos0": x0, "dl_dvel0": v0, "dl_domega0": w0,
+               "dl_dparams": per[0] if self.scenes == 1 else per}
+        if self.nb > 0:
+            nb = self.nb
+            bc, bq, bv, bw = np.zeros((nb, 3)), np.zeros((nb, 4)), np.zeros((nb, 3)), np.zeros((nb, 3))
+            self._check(self.lib.dem_adjoint_body_gradients(self.h, _p(bc), _p(bq), _p(bv), _p(bw)))
+            out.update(dl_dbody_center0=bc, dl_dbody_quat0=bq, dl_dbody_vel0=bv, dl_dbody_omega0=bw)
+        return out
 
     def set_pt_warp_items(self, n):
         """Crossover of the two particle-triangle kernels: up to n contact
@@ -343,6 +351,14 @@ class CudaDemSolver:
         b, m, x, o = C.c_int(), C.c_double(), C.c_int(), C.c_int()
         self._check(self.lib.dem_x_neighbor_stats(self.h, C.byref(b), C.byref(m), C.byref(x), C.byref(o)))
         return {"builds": b.value, "mean_length": m.value, "max_length": x.value, "overflowed": bool(o.value)}
+
+    def set_adjoint_fp32(self, on=True):
+        """Run the reverse law of the particle and wall contacts in FP32 (the
+        forward run, its recompute and the rest of the reverse sweep stay
+        FP64); its gradients carry FP32 rounding, stated against the FP64
+        reverse by the tests and the bench."""
+        self._check(self.lib.dem_x_set_adjoint_fp32(self.h, 1 if on else 0))
+        return self
 
     def adjoint_memory(self):
         """Device bytes of the reverse mode's checkpoints (occupied history

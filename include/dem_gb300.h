@@ -322,6 +322,14 @@ int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double*
                              const double* dl_dbody_center, const double* dl_dbody_vel,
                              double* dl_dpos0, double* dl_dvel0, double* dl_domega0,
                              double* dl_dparams);
+/* The last backward run's gradient with respect to the rigid bodies'
+ * initial state: centres and velocities [nb][3], orientations [nb][4]
+ * (w, x, y, z; the component along q is the normalisation's null direction)
+ * and body-frame spins [nb][3].  Dynamic bodies only; prescribed and fixed
+ * bodies read zero.  Any pointer may be NULL.  DEM_ERR_STATE before a
+ * backward run.  No counterpart in the reference. */
+int dem_adjoint_body_gradients(dem_engine* e, double* dl_dbody_center0, double* dl_dbody_quat0,
+                               double* dl_dbody_vel0, double* dl_dbody_omega0);
 
 #ifdef __cplusplus
 }

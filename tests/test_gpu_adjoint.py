@@ -41,8 +41,8 @@ def _loss(sc):
     return st["pos"][:, 2].mean() + CV * st["vel"][:, 0].mean()
 
 
-def _adjoint(sc):
-    e = engine_for(sc, precision="fp64").adjoint_forward(STEPS, K)
+def _adjoint(sc, fp32=False):
+    e = engine_for(sc, precision="fp64").set_adjoint_fp32(fp32).adjoint_forward(STEPS, K)
     n = e.n
     dpos = np.zeros((n, 3)); dpos[:, 2] = 1.0 / n
     dvel = np.zeros((n, 3)); dvel[:, 0] = CV / n
@@ -64,10 +64,13 @@ def test_adjoint_forward_matches_plain_run():
         np.testing.assert_array_equal(st[k], rs[k], err_msg=k)
 
 
+@pytest.mark.parametrize("fp32", [False, True])
 @pytest.mark.parametrize("cls", ["pp", "pw"])
-def test_material_gradients_match_central_differences(cls):
+def test_material_gradients_match_central_differences(cls, fp32):
+    """Both forms of the reverse law (FP64, and FP32 for the particle and
+    wall contacts) against central differences of the FP64 forward run."""
     sc = _scene()
-    _, g = _adjoint(sc)
+    _, g = _adjoint(sc, fp32)
     grads = g["dl_dparams"][cls]
     scale = max(abs(v) * abs(getattr(getattr(sc, cls), k)) for k, v in grads.items() if k != "epsS")
     for key, field in (("kN", "kN"), ("mu", "mu"), ("epsN", "epsN"), ("epsS", "epsS"), ("muT", "muT"), ("muR", "muR")):
@@ -80,9 +83,10 @@ def test_material_gradients_match_central_differences(cls):
         _close(grads[key] * x0, fd * x0, f"{cls}.{key}", scale)
 
 
-def test_initial_velocity_gradient_matches_central_differences():
+@pytest.mark.parametrize("fp32", [False, True])
+def test_initial_velocity_gradient_matches_central_differences(fp32):
     sc = _scene()
-    _, g = _adjoint(sc)
+    _, g = _adjoint(sc, fp32)
     rng = np.random.default_rng(5)
     for trial in range(3):
         d = rng.normal(size=sc.vel.shape)
@@ -111,6 +115,23 @@ def test_initial_position_and_spin_gradients_match_central_differences():
     lp = _loss(dataclasses.replace(sc, omega=sc.omega + eps * d))
     lm = _loss(dataclasses.replace(sc, omega=sc.omega - eps * d))
     _close(an, (lp - lm) / (2 * eps), "w0 direction", abs(an))
+
+
+def test_fp32_reverse_stays_close_to_the_fp64_reverse():
+    """The FP32 reverse law of the particle and wall contacts changes every
+    gradient by less than 1e-5 of its size (material gradients, and the
+    initial positions', velocities' and spins' gradients measured on their
+    largest entry)."""
+    sc = _scene()
+    _, g64 = _adjoint(sc)
+    _, g32 = _adjoint(sc, True)
+    for cls in ("pp", "pw"):
+        for key, a in g64["dl_dparams"][cls].items():
+            b = g32["dl_dparams"][cls][key]
+            assert abs(b - a) <= 1e-5 * abs(a) + 1e-12, (cls, key, a, b)
+    for name in ("dl_dpos0", "dl_dvel0", "dl_domega0"):
+        ref = g64[name]
+        assert np.abs(g32[name] - ref).max() <= 1e-5 * np.abs(ref).max(), name
 
 
 def _batch_scenes():
@@ -299,6 +320,23 @@ def test_rigid_body_material_gradients_match_central_differences(cls, keys):
         lp = _mbd_loss(dataclasses.replace(sc, **{cls: dataclasses.replace(m, **{key: x0 + h})}))
         lm = _mbd_loss(dataclasses.replace(sc, **{cls: dataclasses.replace(m, **{key: x0 - h})}))
         _close(grads[key] * x0, (lp - lm) / (2 * h) * x0, f"{cls}.{key}", scale)
+
+
+def test_rigid_body_initial_state_gradients_match_central_differences():
+    """dem_adjoint_body_gradients: the loss's gradient with respect to the
+    dynamic plate's initial centre, velocity and body-frame spin (random
+    directions) against central differences of the FP64 forward run."""
+    sc = _mbd_scene()
+    _, g = _mbd_adjoint(sc)
+    assert g["dl_dbody_quat0"].shape == (1, 4)
+    rng = np.random.default_rng(9)
+    for name, field, eps in (("dl_dbody_center0", "body_center", 1e-10), ("dl_dbody_vel0", "body_vel", 1e-7),
+                             ("dl_dbody_omega0", "body_omega", 1e-6)):
+        d = rng.normal(size=getattr(sc, field).shape)
+        an = float((g[name] * d).sum())
+        lp = _mbd_loss(dataclasses.replace(sc, **{field: getattr(sc, field) + eps * d}))
+        lm = _mbd_loss(dataclasses.replace(sc, **{field: getattr(sc, field) - eps * d}))
+        _close(an, (lp - lm) / (2 * eps), name, abs(an))
 
 
 def test_rigid_body_initial_velocity_gradient_matches_central_differences():
