@@ -170,16 +170,23 @@ def dominant_kernel(phases, n, sides, hv, list_length=None, items=0, manifolds=0
     return name, kernel, times[name], nbytes
 
 
-def measured_traffic(kernel, n):
-    """DRAM bytes of one launch, from the committed ncu capture of the kernel
-    (profiles/traffic.json: read + write bytes per particle at a stated
-    scene size), scaled to n particles; None when there is no capture."""
+def traffic_record(kernel, config):
+    """The committed ncu capture of a kernel on a workload
+    (profiles/traffic.json: read + write DRAM bytes per particle at a stated
+    scene size, FP64 pipe activity), or None."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            rec = json.load(f)[kernel]
-        return rec["bytes_per_particle"] * n, rec["source"]
+            return json.load(f)[config][kernel]
     except Exception:
-        return None, None
+        return None
+
+
+def measured_traffic(kernel, n, config):
+    """DRAM bytes of one launch from the kernel's capture, scaled to n
+    particles (per-particle traffic measured on a smaller scene of the same
+    generator); None when there is no capture."""
+    rec = traffic_record(kernel, config)
+    return (rec["bytes_per_particle"] * n, rec["source"]) if rec else (None, None)
 
 
 def launches_per_step(scene):
@@ -296,7 +303,7 @@ def wall_contacts(e, scene):
     return int((used & (last == last[used].max())).sum()) if used.any() else 0
 
 
-def roofline(phases, scene, stats, nlists, precision, e, per_step_ms):
+def roofline(phases, scene, stats, nlists, precision, e, per_step_ms, config):
     """Roofline of the dominant kernel (CUDA-event time of its phase) and the
     step-level algorithmic bytes (section (d) of the design notes)."""
     h = 4 if precision == "mixed" else 8
@@ -306,13 +313,27 @@ def roofline(phases, scene, stats, nlists, precision, e, per_step_ms):
     pname, kernel, kms, kbytes = dominant_kernel(phases, scene.n, contacts, hv, nlists["mean_length"],
                                                  stats.get("body_candidate_items", 0), stats["body_contacts"])
     achieved = kbytes / (kms / 1000.0) / 1e9
-    traffic, traffic_src = measured_traffic(kernel, scene.n)
+    traffic, traffic_src = measured_traffic(kernel, scene.n, config)
     step_bytes = algorithmic_bytes(scene.n, scene.n_components, contacts, wall_contacts(e, scene),
                                    stats["body_contacts"], scene.n_triangles, h)
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": kernel, "phase": pname, "kernel_ms": kms,
             "algorithmic_bytes": kbytes, "traffic_source": traffic_src, "peak_kind": peak_kind + " (hbm_gbs)",
             "step": {"algorithmic_bytes": step_bytes, "achieved": step_bytes / (per_step_ms / 1000.0) / 1e9}}
+
+
+def fp64_roofline(phases, config, precision):
+    """FP64-bound kernels (the FP64 form's particle law, the particle-triangle
+    law): their phase time and the FP64 pipe's activity in their ncu
+    capture (sm__pipe_fp64_cycles_active, % of peak)."""
+    times = dict(zip(PHASES, phases))
+    out = {}
+    for phase, kernel in (("pp_law", "k_pp_law<double>" if precision == "fp64" else None), ("pt", "k_pt_thread")):
+        rec = traffic_record(kernel, config) if kernel else None
+        if rec and rec.get("fp64_pipe_pct") is not None:
+            out[kernel] = {"phase_ms": times.get(phase), "fp64_pipe_active_frac": rec["fp64_pipe_pct"] / 100.0,
+                           "source": rec["source"]}
+    return out
 
 
 def scene_summary(config, steps, warmup):
@@ -326,7 +347,8 @@ def scene_summary(config, steps, warmup):
                      "contact_sides_per_step": stats["particle_contacts"],
                      "body_manifolds": stats["body_contacts"], "phase_ms": dict(zip(PHASES, phases)),
                      "neighbor_lists": after["neighbor_lists"], "clocks": clocks,
-                     "roofline": roofline(phases, scene, stats, after["neighbor_lists"], prec, e, ms / steps)}
+                     "roofline": roofline(phases, scene, stats, after["neighbor_lists"], prec, e, ms / steps, config),
+                     "fp64_roofline": fp64_roofline(phases, config, prec)}
         del e
     out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["load_error_vs_fp64"] = load_error(scene)
@@ -795,11 +817,13 @@ def main():
                           "contact_sides_per_step": stats["particle_contacts"], "clocks": clocks}))
         return
     per_step_ms = ms / args.steps
-    roof = roofline(phases, scene, stats, nlists, args.precision, e, per_step_ms)
+    roof = roofline(phases, scene, stats, nlists, args.precision, e, per_step_ms, args.config)
     del e
     other = "fp64" if args.precision == "mixed" else "mixed"
     e_o, ms_o, _, _, phases_o, _ = run_engine(scene, other, args.steps, args.warmup)
     del e_o
+    fp64_roof = fp64_roofline(phases_o if other == "fp64" else phases, args.config, "fp64")
+    fp64_roof.update(fp64_roofline(phases, args.config, args.precision))
     if dist:
         t = __import__("torch").tensor([ms, ms_o], dtype=__import__("torch").float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -873,6 +897,7 @@ def main():
         "phase_ms_" + other: dict(zip(PHASES, phases_o)),
         "neighbor_lists": nlists,
         "roofline": roof,
+        "fp64_roofline": fp64_roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 13 * 8 * nb,
                 "d2h_bytes_per_step": 38 * 8 * nb + 16 * 4},
