@@ -135,11 +135,24 @@ __device__ __forceinline__ D4 ldg_d4(const D4* p)
 template <typename T> __device__ void expire(Hist<T> h, int slots, int c, int step)
 {
     const size_t base = (size_t)c * slots;
+    // the first two keys and four last-seen steps load beside the high-water
+    // mark, not after it (rows of 64 slots from an allocation's base are
+    // 16-byte aligned)
+    ulonglong2 k01 = make_ulonglong2(0, 0);
+    int4 l03 = make_int4(0, 0, 0, 0);
+    const bool head = slots == kPSlots;
+    if (head) {
+        k01 = *reinterpret_cast<const ulonglong2*>(h.key + base);
+        l03 = *reinterpret_cast<const int4*>(h.last + base);
+    }
     const int hw = h.hw[c];
     int nhw = 0;
     for (int s = 0; s < hw; ++s) {
-        if (h.key[base + s] != 0) {
-            if (h.last[base + s] < step - 1) {
+        const uint64_t key = head && s < 2 ? (s == 0 ? k01.x : k01.y) : h.key[base + s];
+        if (key != 0) {
+            const int last = head && s < 4 ? (s == 0 ? l03.x : s == 1 ? l03.y : s == 2 ? l03.z : l03.w)
+                                           : h.last[base + s];
+            if (last < step - 1) {
                 h.key[base + s] = 0;
                 h.last[base + s] = -1;
                 zero_hv(h.val + (base + s) * kHV);
@@ -217,12 +230,18 @@ __global__ void k_gather_geom(Comps c, Owners o, Grid g, Recs r, Counters k)
         r.relf[t] = make_float4(f32_rn(__fma_rn(-(double)cx, mesh, x)), f32_rn(__fma_rn(-(double)cy, mesh, y)),
                                 f32_rn(__fma_rn(-(double)cz, mesh, z)), f32_rn(rad));
         if (k.nl_on) {
-            // a mover (more than half the skin since the lists' build) marks
-            // its cell for this step
             const double* xr = k.nl_xref + 3 * (size_t)ci;
             const double dx = x - xr[0], dy = y - xr[1], dz = z - xr[2];
             if (dx * dx + dy * dy + dz * dz > g.sc[s].nl_half2) {
-                k.nl_hot[g.clin[ci]] = step;
+                // a mover (more than half the skin since the lists' build)
+                // marks the up to 27 cells around its own for this step
+                const int* lay = g.scene_layout + 8 * s;
+                const int z0 = max(cz - 1, lay[2]), z1 = min(cz + 1, lay[2] + lay[5] - 1);
+                for (int nx = max(cx - 1, lay[0]); nx <= min(cx + 1, lay[0] + lay[3] - 1); ++nx)
+                    for (int ny = max(cy - 1, lay[1]); ny <= min(cy + 1, lay[1] + lay[4] - 1); ++ny) {
+                        const int row = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] - lay[2];
+                        for (int nz = z0; nz <= z1; ++nz) k.nl_hot[row + nz] = step;
+                    }
                 ++movers;
             }
         }
@@ -453,14 +472,17 @@ __device__ int sweep_list_one(const Grid& g, const Recs& r, const SceneC* __rest
     const float offx[3] = {-mesh_f - fi.x, -fi.x, mesh_f - fi.x};
     const float offy[3] = {-mesh_f - fi.y, -fi.y, mesh_f - fi.y};
     const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
+    const int* L = k.nl_idx + (size_t)ci * kNL;
+    // the list's first four entries load with its length (a row is 128
+    // bytes, aligned)
+    const int4 head = *reinterpret_cast<const int4*>(L);
+    const int nn = min(k.nl_cnt[ci], kNL);
     expire(hp, kPSlots, ci, step);
     int phw = hp.hw[ci];
-    const int nn = min(k.nl_cnt[ci], kNL);
-    const int* L = k.nl_idx + (size_t)ci * kNL;
     int fkey[kNL], fcid[kNL];
     int found = 0;
     for (int q = 0; q < nn; ++q) {
-        const int j = L[q];
+        const int j = q == 0 ? head.x : q == 1 ? head.y : q == 2 ? head.z : q == 3 ? head.w : L[q];
         const int u = g.pos_of[j];
         if (u < 0 || u >= nvalid) continue;
         const int4 mj = r.meta[u];
@@ -511,24 +533,12 @@ __device__ int sweep_list_one(const Grid& g, const Recs& r, const SceneC* __rest
 // component sweeps the cells instead of its list.  Every list and build
 // position is from the same build, so a component with no mover in its
 // cells and any partner it touches have each moved at most half the skin
-// since: the pair is listed.
-__device__ __forceinline__ bool mover_near(const Grid& g, const Recs& r, const Counters& k, int t, int step)
+// since: the pair is listed.  Cell adjacency is symmetric, so the movers
+// mark the cells around theirs (k_gather_geom) and the component reads its
+// own cell's mark.
+__device__ __forceinline__ bool mover_near(const Recs& r, const Counters& k, int t, int step)
 {
-    const int4 cell = r.cell[t];
-    const int* lay = g.scene_layout + 8 * r.meta[t].w;
-    const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
-    bool hot = false;
-    for (int dx = -1; dx <= 1; ++dx) {
-        const int nx = cell.x + dx;
-        if (nx < lay[0] || nx >= lay[0] + lay[3]) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int ny = cell.y + dy;
-            if (ny < lay[1] || ny >= lay[1] + lay[4]) continue;
-            const int row = lay[6] + ((nx - lay[0]) * lay[4] + (ny - lay[1])) * lay[5] - lay[2];
-            for (int z = z0; z <= z1; ++z) hot |= k.nl_hot[row + z] == step;
-        }
-    }
-    return hot;
+    return k.nl_hot[r.cell[t].w] == step;
 }
 
 // One thread per component in cell order: the reference's 27-cell sweep
@@ -560,7 +570,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     int stage_t[kCandidates];
     int stage_s[kMaxContacts];
     int ci = -1;
-    if (t < nvalid && from_lists && !(movers && mover_near(g, r, k, t, step))) {
+    if (t < nvalid && from_lists && !(movers && mover_near(r, k, t, step))) {
         ci = r.meta[t].x;
         count = sweep_list_one(g, r, sc, hp, k, t, nvalid, step, stage_t, stage_s, pover, phigh);
         ct.cnt[ci] = count;
