@@ -58,11 +58,13 @@ __device__ __forceinline__ void add4(double* A, int f, int n, int i, const doubl
 {
     for (int k = 0; k < 4; ++k) atomicAdd(A + (size_t)(f + k) * n + i, q[k]);
 }
-__device__ __forceinline__ void normq(double q[4])
+template <typename R> __device__ __forceinline__ void normq(R q[4])
 {
-    const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
-    if (n2 <= 1.0e-24) { q[0] = 1.0; q[1] = q[2] = q[3] = 0.0; return; }
-    const double inv = rsqrt(n2);
+    const R n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (n2 <= R(1.0e-24)) { q[0] = R(1.0); q[1] = q[2] = q[3] = R(0.0); return; }
+    R inv;
+    if constexpr (std::is_same<R, double>::value) inv = rsqrt(n2);
+    else inv = rsqrtf(n2);
     for (int k = 0; k < 4; ++k) q[k] *= inv;
 }
 
@@ -166,7 +168,12 @@ __global__ void k_ckpt_unpack(Hist<double> h, int slots, int nc, const int* hw, 
 // midpoint velocities (zeroed, filled by the contact kernels), and of the
 // total force and torque.  With init = 1 the step is the first evaluation
 // (dt = 0, no advance, no midpoint) followed by initializeLeapfrogKernel
-// (:185-210) with half step h: L is then the adjoint of S_0.
+// (:185-210) with half step h: L is then the adjoint of S_0.  R = double:
+// the FP64 map; R = float: the post-advance state and every adjoint that
+// carries from step to step stay FP64, the quaternion and rotation maps'
+// increments (and the world-frame spins the FP32 contact laws read) are
+// FP32.
+template <typename R>
 __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const double* L, double* Lp, double* P,
                              double* T, double dt, int init, const int* slot)
 {
@@ -184,30 +191,35 @@ __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const 
     post_advance(S, n, i, dt, moves, mid, x1, q1, v1, w1, mv, mw);
     st3(P, kPX, n, i, x1); st4(P, kPQ, n, i, q1); st3(P, kPV, n, i, v1); st3(P, kPW, n, i, w1);
     st3(P, kPMV, n, i, mv); st3(P, kPMW, n, i, mw);
+    R qr[4];
+    for (int k = 0; k < 4; ++k) qr[k] = cv<R>(q1[k]);
+    const V3<R> w1r = cvt<R>(w1);
     // the world-frame spins every contact of the owner uses
-    st3(P, kPEW, n, i, rotq(q1, w1)); st3(P, kPEMW, n, i, rotq(q1, mw));
+    st3(P, kPEW, n, i, cvt<double>(rotq(qr, w1r))); st3(P, kPEMW, n, i, cvt<double>(rotq(qr, cvt<R>(mw))));
     // S1's finish half: the half step h = dt/2 of the finish, or the
     // leapfrog start's half step (dt holds it when init)
-    const double h = init ? dt : 0.5 * dt;
+    const R h = cv<R>(init ? dt : 0.5 * dt);
     const double dtv = dt;  // velocity increment: the step, or the start's half step when init
-    const D3 wh1 = ld3(S1, kAdjWH, n, i);
-    double lhq[4], lp[4] = {0, 0, 0, 0}, ls[4] = {0, 0, 0, 0}, lq1[4];
-    ld4(L, kAdjHQ, n, i, lhq);
+    const V3<R> wh1 = cvt<R>(ld3(S1, kAdjWH, n, i));
+    double lhq_d[4], lq1[4];
+    R lhq[4], lp[4] = {0, 0, 0, 0}, ls[4] = {0, 0, 0, 0};
+    ld4(L, kAdjHQ, n, i, lhq_d);
+    for (int k = 0; k < 4; ++k) lhq[k] = cv<R>(lhq_d[k]);
     // hq1 = G(p, wh1), p = N(s), s = q1 + h G(q1, w1)
-    double s[4], g[4];
-    quatd(q1, w1, g);
-    for (int k = 0; k < 4; ++k) s[k] = q1[k] + g[k] * h;
-    double p[4] = {s[0], s[1], s[2], s[3]};
+    R s[4], g[4];
+    quatd(qr, w1r, g);
+    for (int k = 0; k < 4; ++k) s[k] = qr[k] + g[k] * h;
+    R p[4] = {s[0], s[1], s[2], s[3]};
     normq(p);
     D3 lwh1 = ld3(L, kAdjWH, n, i);
     quatd_vjp(p, wh1, lhq, lp, lwh1);
     normq_vjp(s, lp, ls);
     ld4(L, kAdjQ, n, i, lq1);
     D3 lw1 = ld3(L, kAdjW, n, i);
-    for (int k = 0; k < 4; ++k) lq1[k] += ls[k];
-    double lsh[4];
+    for (int k = 0; k < 4; ++k) lq1[k] += cv<double>(ls[k]);
+    R lsh[4];
     for (int k = 0; k < 4; ++k) lsh[k] = ls[k] * h;
-    quatd_vjp(q1, w1, lsh, lq1, lw1);
+    quatd_vjp(qr, w1r, lsh, lq1, lw1);
     // vh1 = vh + a1 dt (or v0 + a0 h), wh1 likewise
     const D3 lvh1 = ld3(L, kAdjVH, n, i);
     const D3 la1 = ld3(L, kAdjA, n, i) + lvh1 * dtv;
@@ -232,10 +244,11 @@ __global__ void k_adj_finish(Owners o, const double* S, const double* S1, const 
     const D3 aw1 = ld3(S1, kAdjAW, n, i);
     D3 tb = mk(Ix * aw1.x, Iy * aw1.y, Iz * aw1.z);
     if (!iso) tb = tb + mk((Iz - Iy) * w1.z * w1.y, (Ix - Iz) * w1.x * w1.z, (Iy - Ix) * w1.y * w1.x);
-    const D3 tau = rotq(q1, tb);
-    const D3 lt = mk(law1.x / Ix, law1.y / Iy, law1.z / Iz);
+    const V3<R> tau = rotq(qr, cvt<R>(tb));
+    const V3<R> ltr = mk(cv<R>(law1.x) / cv<R>(Ix), cv<R>(law1.y) / cv<R>(Iy), cv<R>(law1.z) / cv<R>(Iz));
+    const D3 lt = cvt<double>(ltr);
     D3 ltau = z3();
-    rotq_t_vjp(q1, tau, lt, lq1, ltau);
+    rotq_t_vjp(qr, tau, ltr, lq1, ltau);
     if (!iso) {
         lw1.z -= lt.x * (Iz - Iy) * w1.y; lw1.y -= lt.x * (Iz - Iy) * w1.z;
         lw1.x -= lt.y * (Ix - Iz) * w1.z; lw1.z -= lt.y * (Ix - Iz) * w1.x;
@@ -573,7 +586,9 @@ __global__ void k_set_int(int* p, int v) { *p = v; }
 
 // advance^T: T (complete) and the vh, wh partials of Lp -> Lp = adjoint of
 // S_s.  With init = 1 (the first evaluation, no advance): Lp = adjoint of
-// the initial x, q, v, w.
+// the initial x, q, v, w.  R as k_adj_finish: the rotations' increments in
+// R, the normalisation's map of the carried quaternion adjoint in FP64.
+template <typename R>
 __global__ void k_adj_advance(Owners o, const double* S, const double* P, const double* T, double* Lp, double dt,
                               int init, const int* slot)
 {
@@ -592,8 +607,10 @@ __global__ void k_adj_advance(Owners o, const double* S, const double* P, const 
         // R(q1) w_mid, to the quaternion and the body-frame spins
         double q1[4];
         ld4(P, kPQ, n, i, q1);
-        rotq_vjp(q1, ld3(P, kPW, n, i), ld3(T, kTEW, n, i), lq1, lw1);
-        rotq_vjp(q1, ld3(P, kPMW, n, i), ld3(T, kTEMW, n, i), lq1, lmw);
+        R qr[4];
+        for (int k = 0; k < 4; ++k) qr[k] = cv<R>(q1[k]);
+        rotq_vjp(qr, cvt<R>(ld3(P, kPW, n, i)), cvt<R>(ld3(T, kTEW, n, i)), lq1, lw1);
+        rotq_vjp(qr, cvt<R>(ld3(P, kPMW, n, i)), cvt<R>(ld3(T, kTEMW, n, i)), lq1, lmw);
     }
     const bool moves = !init && o.status[i] != -1;
     double zero4[4] = {0, 0, 0, 0};
@@ -675,7 +692,10 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
         cudaStreamWaitEvent(s2, ev[0], 0);
     }
     if (bodies) k_adj_body_a<<<nblocks(ab.nb, 32), 32, 0, sb>>>(ab, slot, init);
-    k_adj_finish<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init, slot);
+    if (fp32)
+        k_adj_finish<float><<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init, slot);
+    else
+        k_adj_finish<double><<<nblocks(o.n, 256), 256, 0, s>>>(o, S, S1, L, Lp, P, T, dt, init, slot);
     if (fork) {
         cudaEventRecord(ev[1], s);
         cudaStreamWaitEvent(s2, ev[1], 0);
@@ -699,7 +719,10 @@ void launch_adj_step(const Comps& c, const Owners& o, const SceneC* sc, const Wa
         cudaEventRecord(ev[2], s2);
         cudaStreamWaitEvent(s, ev[2], 0);
     }
-    k_adj_advance<<<nblocks(o.n, 256), 256, 0, s>>>(o, S, P, T, Lp, dt, init, slot);
+    if (fp32)
+        k_adj_advance<float><<<nblocks(o.n, 256), 256, 0, s>>>(o, S, P, T, Lp, dt, init, slot);
+    else
+        k_adj_advance<double><<<nblocks(o.n, 256), 256, 0, s>>>(o, S, P, T, Lp, dt, init, slot);
 }
 void launch_adj_body_pose(const Bodies& b, const double* rec, const int* base, const int* slot, cudaStream_t s)
 {

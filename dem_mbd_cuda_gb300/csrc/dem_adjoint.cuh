@@ -44,65 +44,89 @@ template <typename R> DEM_DEV void norm_vjp(V3<R> a, R lo, V3<R>& la)
     const R n = norm(a);
     if (n > R(0)) la = la + a * (lo / n);
 }
+// The quaternion maps below take their inputs in R and add their adjoints
+// into accumulators of type A: R = A = double is the FP64 reverse; R =
+// float, A = double computes each increment in FP32 and adds it to the FP64
+// adjoint that carries it from step to step (B: the accumulator of a
+// second output, where it may differ).
+
 // q / |q| (normalize_quat; the degenerate reset to identity has no adjoint)
-DEM_DEV void normq_vjp(const double q[4], const double lo[4], double lq[4])
+template <typename R, typename A> DEM_DEV void normq_vjp(const R q[4], const R lo[4], A lq[4])
 {
-    const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
-    if (n2 <= 1.0e-24) return;
-    const double inv = 1.0 / sqrt(n2);
-    double o[4], d = 0.0;
+    const R n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (n2 <= R(1.0e-24)) return;
+    const R inv = R(1.0) / sqrt(n2);
+    R o[4], d = R(0.0);
     for (int k = 0; k < 4; ++k) { o[k] = q[k] * inv; d += o[k] * lo[k]; }
-    for (int k = 0; k < 4; ++k) lq[k] += (lo[k] - o[k] * d) * inv;
+    for (int k = 0; k < 4; ++k) lq[k] += A((lo[k] - o[k] * d) * inv);
 }
 // quat_derivative G(q, w) = 0.5 q (x) (0, w)
-DEM_DEV void quatd(const double q[4], D3 w, double o[4])
+template <typename R> DEM_DEV void quatd(const R q[4], V3<R> w, R o[4])
 {
-    o[0] = 0.5 * (-q[1] * w.x - q[2] * w.y - q[3] * w.z);
-    o[1] = 0.5 * (q[0] * w.x + q[2] * w.z - q[3] * w.y);
-    o[2] = 0.5 * (q[0] * w.y - q[1] * w.z + q[3] * w.x);
-    o[3] = 0.5 * (q[0] * w.z + q[1] * w.y - q[2] * w.x);
+    o[0] = R(0.5) * (-q[1] * w.x - q[2] * w.y - q[3] * w.z);
+    o[1] = R(0.5) * (q[0] * w.x + q[2] * w.z - q[3] * w.y);
+    o[2] = R(0.5) * (q[0] * w.y - q[1] * w.z + q[3] * w.x);
+    o[3] = R(0.5) * (q[0] * w.z + q[1] * w.y - q[2] * w.x);
 }
-DEM_DEV void quatd_vjp(const double q[4], D3 w, const double lo[4], double lq[4], D3& lw)
+template <typename R, typename A, typename B>
+DEM_DEV void quatd_vjp(const R q[4], V3<R> w, const R lo[4], A lq[4], V3<B>& lw)
 {
-    lq[0] += 0.5 * (lo[1] * w.x + lo[2] * w.y + lo[3] * w.z);
-    lq[1] += 0.5 * (-lo[0] * w.x - lo[2] * w.z + lo[3] * w.y);
-    lq[2] += 0.5 * (-lo[0] * w.y + lo[1] * w.z - lo[3] * w.x);
-    lq[3] += 0.5 * (-lo[0] * w.z - lo[1] * w.y + lo[2] * w.x);
-    lw.x += 0.5 * (-lo[0] * q[1] + lo[1] * q[0] + lo[2] * q[3] - lo[3] * q[2]);
-    lw.y += 0.5 * (-lo[0] * q[2] - lo[1] * q[3] + lo[2] * q[0] + lo[3] * q[1]);
-    lw.z += 0.5 * (-lo[0] * q[3] + lo[1] * q[2] - lo[2] * q[1] + lo[3] * q[0]);
+    lq[0] += A(R(0.5) * (lo[1] * w.x + lo[2] * w.y + lo[3] * w.z));
+    lq[1] += A(R(0.5) * (-lo[0] * w.x - lo[2] * w.z + lo[3] * w.y));
+    lq[2] += A(R(0.5) * (-lo[0] * w.y + lo[1] * w.z - lo[3] * w.x));
+    lq[3] += A(R(0.5) * (-lo[0] * w.z - lo[1] * w.y + lo[2] * w.x));
+    lw.x += B(R(0.5) * (-lo[0] * q[1] + lo[1] * q[0] + lo[2] * q[3] - lo[3] * q[2]));
+    lw.y += B(R(0.5) * (-lo[0] * q[2] - lo[1] * q[3] + lo[2] * q[0] + lo[3] * q[1]));
+    lw.z += B(R(0.5) * (-lo[0] * q[3] + lo[1] * q[2] - lo[2] * q[1] + lo[3] * q[0]));
 }
 // rot_iv(q, v) = R(q) v (body -> world)
-DEM_DEV D3 rotq(const double q[4], D3 v) { return rot_iv(q[0], q[1], q[2], q[3], v); }
-DEM_DEV void rotq_vjp(const double q[4], D3 v, D3 lo, double lq[4], D3& lv)
+template <typename R> DEM_DEV V3<R> rotq(const R q[4], V3<R> v)
 {
-    const double qw = q[0], qx = q[1], qy = q[2], qz = q[3];
+    if constexpr (std::is_same<R, double>::value) {
+        return rot_iv(q[0], q[1], q[2], q[3], v);
+    } else {
+        const R qw = q[0], qx = q[1], qy = q[2], qz = q[3];
+        return {(R(1) - R(2) * (qy * qy + qz * qz)) * v.x + R(2) * (qx * qy - qw * qz) * v.y +
+                    R(2) * (qx * qz + qw * qy) * v.z,
+                R(2) * (qx * qy + qw * qz) * v.x + (R(1) - R(2) * (qx * qx + qz * qz)) * v.y +
+                    R(2) * (qy * qz - qw * qx) * v.z,
+                R(2) * (qx * qz - qw * qy) * v.x + R(2) * (qy * qz + qw * qx) * v.y +
+                    (R(1) - R(2) * (qx * qx + qy * qy)) * v.z};
+    }
+}
+template <typename R, typename A> DEM_DEV void rotq_vjp(const R q[4], V3<R> v, V3<R> lo, A lq[4], V3<A>& lv)
+{
+    const R qw = q[0], qx = q[1], qy = q[2], qz = q[3];
+    const R one = R(1.0), two = R(2.0), four = R(4.0);
     // lv += R^T lo
-    lv.x += (1.0 - 2.0 * (qy * qy + qz * qz)) * lo.x + 2.0 * (qx * qy + qw * qz) * lo.y + 2.0 * (qx * qz - qw * qy) * lo.z;
-    lv.y += 2.0 * (qx * qy - qw * qz) * lo.x + (1.0 - 2.0 * (qx * qx + qz * qz)) * lo.y + 2.0 * (qy * qz + qw * qx) * lo.z;
-    lv.z += 2.0 * (qx * qz + qw * qy) * lo.x + 2.0 * (qy * qz - qw * qx) * lo.y + (1.0 - 2.0 * (qx * qx + qy * qy)) * lo.z;
+    lv.x += A((one - two * (qy * qy + qz * qz)) * lo.x + two * (qx * qy + qw * qz) * lo.y +
+              two * (qx * qz - qw * qy) * lo.z);
+    lv.y += A(two * (qx * qy - qw * qz) * lo.x + (one - two * (qx * qx + qz * qz)) * lo.y +
+              two * (qy * qz + qw * qx) * lo.z);
+    lv.z += A(two * (qx * qz + qw * qy) * lo.x + two * (qy * qz - qw * qx) * lo.y +
+              (one - two * (qx * qx + qy * qy)) * lo.z);
     // lq += (d(R v)/dq)^T lo
-    const double vx = v.x, vy = v.y, vz = v.z;
-    lq[0] += lo.x * (-2.0 * qz * vy + 2.0 * qy * vz) + lo.y * (2.0 * qz * vx - 2.0 * qx * vz) +
-             lo.z * (-2.0 * qy * vx + 2.0 * qx * vy);
-    lq[1] += lo.x * (2.0 * qy * vy + 2.0 * qz * vz) + lo.y * (2.0 * qy * vx - 4.0 * qx * vy - 2.0 * qw * vz) +
-             lo.z * (2.0 * qz * vx + 2.0 * qw * vy - 4.0 * qx * vz);
-    lq[2] += lo.x * (-4.0 * qy * vx + 2.0 * qx * vy + 2.0 * qw * vz) + lo.y * (2.0 * qx * vx + 2.0 * qz * vz) +
-             lo.z * (-2.0 * qw * vx + 2.0 * qz * vy - 4.0 * qy * vz);
-    lq[3] += lo.x * (-4.0 * qz * vx - 2.0 * qw * vy + 2.0 * qx * vz) + lo.y * (2.0 * qw * vx - 4.0 * qz * vy + 2.0 * qy * vz) +
-             lo.z * (2.0 * qx * vx + 2.0 * qy * vy);
+    const R vx = v.x, vy = v.y, vz = v.z;
+    lq[0] += A(lo.x * (-two * qz * vy + two * qy * vz) + lo.y * (two * qz * vx - two * qx * vz) +
+               lo.z * (-two * qy * vx + two * qx * vy));
+    lq[1] += A(lo.x * (two * qy * vy + two * qz * vz) + lo.y * (two * qy * vx - four * qx * vy - two * qw * vz) +
+               lo.z * (two * qz * vx + two * qw * vy - four * qx * vz));
+    lq[2] += A(lo.x * (-four * qy * vx + two * qx * vy + two * qw * vz) + lo.y * (two * qx * vx + two * qz * vz) +
+               lo.z * (-two * qw * vx + two * qz * vy - four * qy * vz));
+    lq[3] += A(lo.x * (-four * qz * vx - two * qw * vy + two * qx * vz) +
+               lo.y * (two * qw * vx - four * qz * vy + two * qy * vz) + lo.z * (two * qx * vx + two * qy * vy));
 }
 // R(q)^T t (world -> body, the Euler-equation transform of the owner sum) is
 // R(conj q) t
-DEM_DEV D3 rotq_t(const double q[4], D3 t)
+template <typename R> DEM_DEV V3<R> rotq_t(const R q[4], V3<R> t)
 {
-    const double c[4] = {q[0], -q[1], -q[2], -q[3]};
+    const R c[4] = {q[0], -q[1], -q[2], -q[3]};
     return rotq(c, t);
 }
-DEM_DEV void rotq_t_vjp(const double q[4], D3 t, D3 lo, double lq[4], D3& lt)
+template <typename R, typename A> DEM_DEV void rotq_t_vjp(const R q[4], V3<R> t, V3<R> lo, A lq[4], V3<A>& lt)
 {
-    const double c[4] = {q[0], -q[1], -q[2], -q[3]};
-    double lc[4] = {0.0, 0.0, 0.0, 0.0};
+    const R c[4] = {q[0], -q[1], -q[2], -q[3]};
+    A lc[4] = {A(0), A(0), A(0), A(0)};
     rotq_vjp(c, t, lo, lc, lt);
     lq[0] += lc[0]; lq[1] -= lc[1]; lq[2] -= lc[2]; lq[3] -= lc[3];
 }
