@@ -140,8 +140,8 @@ __global__ void k_ckpt_pack(Hist<double> h, int slots, int nc, const int* off, u
         const int m = h.hw[c];
         const size_t src = (size_t)c * slots, dst = (size_t)off[c];
         for (int q = 0; q < m; ++q) {
-            key[dst + q] = h.key[src + q];
-            last[dst + q] = h.last[src + q];
+            key[dst + q] = h.key[hslot(h, c, q)];
+            last[dst + q] = h.last[hslot(h, c, q)];
             for (int a = 0; a < kHV; ++a) val[(dst + q) * kHV + a] = h.val[(src + q) * kHV + a];
         }
     }
@@ -154,8 +154,8 @@ __global__ void k_ckpt_unpack(Hist<double> h, int slots, int nc, const int* hw, 
         const size_t dst = (size_t)c * slots, src = (size_t)off[c];
         for (int q = 0; q < max(m, live); ++q) {
             const bool kept = q < m;
-            h.key[dst + q] = kept ? key[src + q] : 0ull;
-            h.last[dst + q] = kept ? last[src + q] : -1;
+            h.key[hslot(h, c, q)] = kept ? key[src + q] : 0ull;
+            h.last[hslot(h, c, q)] = kept ? last[src + q] : -1;
             for (int a = 0; a < kHV; ++a) h.val[(dst + q) * kHV + a] = kept ? val[(src + q) * kHV + a] : 0.0;
         }
         h.hw[c] = m;

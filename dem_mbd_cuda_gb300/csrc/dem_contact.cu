@@ -135,26 +135,19 @@ __device__ __forceinline__ D4 ldg_d4(const D4* p)
 template <typename T> __device__ void expire(Hist<T> h, int slots, int c, int step)
 {
     const size_t base = (size_t)c * slots;
-    // the first two keys and four last-seen steps load beside the high-water
-    // mark, not after it (rows of 64 slots from an allocation's base are
-    // 16-byte aligned)
-    ulonglong2 k01 = make_ulonglong2(0, 0);
-    int4 l03 = make_int4(0, 0, 0, 0);
-    const bool head = slots == kPSlots;
-    if (head) {
-        k01 = *reinterpret_cast<const ulonglong2*>(h.key + base);
-        l03 = *reinterpret_cast<const int4*>(h.last + base);
-    }
+    // the first two keys and last-seen steps load beside the high-water mark,
+    // not after it (every kind has at least two slots)
+    const uint64_t k0 = h.key[hslot(h, c, 0)], k1 = h.key[hslot(h, c, 1)];
+    const int l0 = h.last[hslot(h, c, 0)], l1 = h.last[hslot(h, c, 1)];
     const int hw = h.hw[c];
     int nhw = 0;
     for (int s = 0; s < hw; ++s) {
-        const uint64_t key = head && s < 2 ? (s == 0 ? k01.x : k01.y) : h.key[base + s];
+        const uint64_t key = s == 0 ? k0 : s == 1 ? k1 : h.key[hslot(h, c, s)];
         if (key != 0) {
-            const int last = head && s < 4 ? (s == 0 ? l03.x : s == 1 ? l03.y : s == 2 ? l03.z : l03.w)
-                                           : h.last[base + s];
+            const int last = s == 0 ? l0 : s == 1 ? l1 : h.last[hslot(h, c, s)];
             if (last < step - 1) {
-                h.key[base + s] = 0;
-                h.last[base + s] = -1;
+                h.key[hslot(h, c, s)] = 0;
+                h.last[hslot(h, c, s)] = -1;
                 zero_hv(h.val + (base + s) * kHV);
             } else {
                 nhw = s + 1;
@@ -173,9 +166,9 @@ __device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int&
     const size_t base = (size_t)c * slots;
     int empty = -1;
     for (int s = 0; s < hw; ++s) {
-        const uint64_t k = h.key[base + s];
+        const uint64_t k = h.key[hslot(h, c, s)];
         if (k == key) {
-            h.last[base + s] = step;
+            h.last[hslot(h, c, s)] = step;
             high = max(high, s + 1);
             return s;
         }
@@ -185,8 +178,8 @@ __device__ int acquire(Hist<T> h, int slots, int c, uint64_t key, int step, int&
         if (hw >= slots) return -1;
         empty = hw;
     }
-    h.key[base + empty] = key;
-    h.last[base + empty] = step;
+    h.key[hslot(h, c, empty)] = key;
+    h.last[hslot(h, c, empty)] = step;
     zero_hv(h.val + (base + empty) * kHV);
     if (fresh) *fresh = true;
     if (empty + 1 > hw) hw = empty + 1;
@@ -461,7 +454,7 @@ __device__ __noinline__ bool exact_contact(const D4* __restrict__ pos, const int
 // cell sweep's.  Returns the contact count; stage_t / stage_s as k_sweep.
 template <typename T>
 __device__ int sweep_list_one(const Grid& g, const Recs& r, const SceneC* __restrict__ sc, Hist<T> hp, Counters k,
-                              int t, int nvalid, int step, int* stage_t, int* stage_s, int& pover, int& phigh)
+                              int t, int nvalid, int nc, int step, int* stage_t, int* stage_s, int& pover, int& phigh)
 {
     const int4 meta = r.meta[t];
     const int ci = meta.x, owner = meta.y, s = meta.w;
@@ -472,17 +465,17 @@ __device__ int sweep_list_one(const Grid& g, const Recs& r, const SceneC* __rest
     const float offx[3] = {-mesh_f - fi.x, -fi.x, mesh_f - fi.x};
     const float offy[3] = {-mesh_f - fi.y, -fi.y, mesh_f - fi.y};
     const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
-    const int* L = k.nl_idx + (size_t)ci * kNL;
-    // the list's first four entries load with its length (a row is 128
-    // bytes, aligned)
-    const int4 head = *reinterpret_cast<const int4*>(L);
+    // the list is entry-major (entry q of component ci at q * nc + ci); its
+    // first four entries load with its length
+    const int* L = k.nl_idx + ci;
+    const int l0 = L[0], l1 = L[nc], l2 = L[2 * (size_t)nc], l3 = L[3 * (size_t)nc];
     const int nn = min(k.nl_cnt[ci], kNL);
     expire(hp, kPSlots, ci, step);
     int phw = hp.hw[ci];
     int fkey[kNL], fcid[kNL];
     int found = 0;
     for (int q = 0; q < nn; ++q) {
-        const int j = q == 0 ? head.x : q == 1 ? head.y : q == 2 ? head.z : q == 3 ? head.w : L[q];
+        const int j = q == 0 ? l0 : q == 1 ? l1 : q == 2 ? l2 : q == 3 ? l3 : L[(size_t)q * nc];
         const int u = g.pos_of[j];
         if (u < 0 || u >= nvalid) continue;
         const int4 mj = r.meta[u];
@@ -572,7 +565,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
     int ci = -1;
     if (t < nvalid && from_lists && !(movers && mover_near(r, k, t, step))) {
         ci = r.meta[t].x;
-        count = sweep_list_one(g, r, sc, hp, k, t, nvalid, step, stage_t, stage_s, pover, phigh);
+        count = sweep_list_one(g, r, sc, hp, k, t, nvalid, nc, step, stage_t, stage_s, pover, phigh);
         ct.cnt[ci] = count;
     } else if (t < nvalid) {
         const int4 meta = r.meta[t];
@@ -588,7 +581,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         const float offz[3] = {-mesh_f - fi.z, -fi.z, mesh_f - fi.z};
         const int z0 = max(cell.z - 1, lay[2]), z1 = min(cell.z + 1, lay[2] + lay[5] - 1);
         const float skin_f = sc[s].skin_f;
-        int* nl = build ? k.nl_idx + (size_t)ci * kNL : nullptr;
+        int* nl = build ? k.nl_idx + ci : nullptr;  // entry-major: entry q at nl[q * nc]
         int nlist = 0;
         // expireHistory (:1109-1117) for the component's particle slots,
         // before any slot of this step is acquired (the wall and body slots
@@ -658,7 +651,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
                         if (build && u != t) {
                             const float rsb = rsf + skin_f;
                             if (dd2 < rsb * rsb) {
-                                if (nlist < kNL) nl[nlist] = r.meta[u].x;
+                                if (nlist < kNL) nl[(size_t)nlist * nc] = r.meta[u].x;
                                 ++nlist;
                             }
                         }

@@ -558,6 +558,7 @@ public:
         h.last = arena_.alloc<int>(n, "history last seen");
         h.val = arena_.alloc<H>(n * kHV, "history values");
         h.hw = arena_.alloc<int>(nc_, "history hw");
+        h.nc = nc_;
         check(cudaMemsetAsync(h.key, 0, n * sizeof(uint64_t), s), "clear history keys");
         check(cudaMemsetAsync(h.last, 0xff, n * sizeof(int), s), "clear history age");
         check(cudaMemsetAsync(h.val, 0, n * kHV * sizeof(H), s), "clear history values");
@@ -1288,8 +1289,20 @@ public:
     template <typename T> void download_hist(const Hist<T>& h, int slots, uint64_t* keys, int* last, double* val)
     {
         const size_t n = (size_t)nc_ * slots;
-        if (keys) check(cudaMemcpy(keys, h.key, n * sizeof(uint64_t), cudaMemcpyDeviceToHost), "download keys");
-        if (last) check(cudaMemcpy(last, h.last, n * sizeof(int), cudaMemcpyDeviceToHost), "download last");
+        // keys and last-seen steps are slot-major on the device, the
+        // reference's component-major order here
+        if (keys) {
+            std::vector<uint64_t> k(n);
+            check(cudaMemcpy(k.data(), h.key, n * sizeof(uint64_t), cudaMemcpyDeviceToHost), "download keys");
+            for (int c = 0; c < nc_; ++c)
+                for (int s = 0; s < slots; ++s) keys[(size_t)c * slots + s] = k[(size_t)s * nc_ + c];
+        }
+        if (last) {
+            std::vector<int> l(n);
+            check(cudaMemcpy(l.data(), h.last, n * sizeof(int), cudaMemcpyDeviceToHost), "download last");
+            for (int c = 0; c < nc_; ++c)
+                for (int s = 0; s < slots; ++s) last[(size_t)c * slots + s] = l[(size_t)s * nc_ + c];
+        }
         if (val) {
             std::vector<T> v(n * kHV);
             check(cudaMemcpy(v.data(), h.val, n * kHV * sizeof(T), cudaMemcpyDeviceToHost), "download values");
@@ -1316,7 +1329,10 @@ public:
     template <typename T> void upload_hist(Hist<T>& h, int slots, const uint64_t* keys, const double* val)
     {
         const size_t n = (size_t)nc_ * slots;
-        check(cudaMemcpy(h.key, keys, n * sizeof(uint64_t), cudaMemcpyHostToDevice), "upload keys");
+        std::vector<uint64_t> kt(n);
+        for (int c = 0; c < nc_; ++c)
+            for (int s = 0; s < slots; ++s) kt[(size_t)s * nc_ + c] = keys[(size_t)c * slots + s];
+        check(cudaMemcpy(h.key, kt.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice), "upload keys");
         std::vector<T> v(n * kHV, T(0));
         for (size_t k = 0; k < n; ++k)
             for (int a = 0; a < 9; ++a) v[kHV * k + a] = (T)val[9 * k + a];

@@ -177,12 +177,22 @@ struct Recs {
 constexpr int kHV = 12;
 constexpr int kNL = 32;  // neighbour-list capacity per component
 
+// One history kind.  Keys and last-seen steps are slot-major, slot s of
+// component c at s * nc + c, so a warp of neighbouring components reads one
+// slot in a few lines; the values are component-major, slot s of component
+// c at (c * slots + s) * kHV, so one contact side reads its 9 values from one
+// row.  The "slot index" that contact lists and tapes carry is c * slots + s.
 template <typename T> struct Hist {
     uint64_t* key;
     int* last;
     T* val;
     int* hw;  // per component: 1 + highest occupied slot
+    int nc;   // components (the key and last-seen stride)
 };
+template <typename T> __host__ __device__ inline size_t hslot(const Hist<T>& h, int c, int s)
+{
+    return (size_t)s * h.nc + c;
+}
 
 struct Walls {
     int count;      // walls of all scenes
