@@ -1257,9 +1257,17 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
 // triangles.  A list longer than the per-warp cache takes the uncompacted
 // loops (same sums, recomputed areas).
 constexpr int kPtTriCache = 128;  // per-warp candidate list: triangle, (area scale, distance)
-// One warp per block: a block of this kernel (255 registers a thread) then
-// fits beside the particle law and the sweep that run at the same time.
-constexpr int kPtWarpBlock = 32;
+// Two warps per block.  With few items (at most `pair_items`, the blocks that
+// are resident at once) the block takes one item: warp 0 runs the law and
+// hands each manifold's normal, centre, distance, area and updated history
+// to warp 1 through shared memory, and warp 1 computes the microstate while
+// warp 0 runs the per-triangle loads -- two FP64 chains on two of the SM's
+// sub-partitions instead of one after the other.  With more items each warp
+// takes items of its own and computes its microstates itself.
+constexpr int kPtWarpBlock = 64;
+// Blocks of k_pt_warp resident on one SM (255 registers a thread): the
+// paired mode's item limit per SM.
+constexpr int kPtPairBlocksPerSm = 4;
 
 __device__ __forceinline__ V3<double> shfl3(V3<double> v, int src)
 {
@@ -1267,25 +1275,65 @@ __device__ __forceinline__ V3<double> shfl3(V3<double> v, int src)
               __shfl_sync(0xffffffffu, v.z, src));
 }
 
+// What the microstate of one manifold needs from the law (pt_microstate).
+struct PtMicroIn {
+    double mn[3], mc[3], th[3], twh[3], md, tot;
+    int on;
+};
+// The block's two warps meet here once per (item, body) in paired mode
+// (each warp reconverged first; named barrier 1, 64 threads).
+__device__ __forceinline__ void pt_pair_barrier()
+{
+    __syncwarp();
+    asm volatile("barrier.sync 1, 64;" ::: "memory");
+}
+
 template <typename TC, typename T>
 __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Recs r, const SceneC* __restrict__ sc, Tris tris,
-                                                 Bodies bodies, Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff)
+                                                 Bodies bodies, Hist<T> hb, Contacts<TC> ct, Counters k, double dt_eff,
+                                                 int pair_items)
 {
     constexpr unsigned FULL = 0xffffffffu;
-    __shared__ double2 s_ad[kPtWarpBlock / 32][kPtTriCache];
-    __shared__ int s_tri[kPtWarpBlock / 32][kPtTriCache];
+    constexpr int W = kPtWarpBlock / 32;
+    __shared__ double2 s_ad[W][kPtTriCache];
+    __shared__ int s_tri[W][kPtTriCache];
+    __shared__ PtMicroIn s_mi[2];
     const int step = *k.step;
     const int total = *ct.pt_ctotal_ptr;
     if (total > k.pt_warp_items) return;
     const StepTape tape = tape_at(ct.tape);
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
+    // paired: one item per block, warp 1 the observer (uniform over the grid)
+    const bool paired = total <= pair_items;
+    const int first = paired ? (int)blockIdx.x : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int stride = paired ? (int)gridDim.x : (int)((gridDim.x * blockDim.x) >> 5);
     int bover = 0, bhigh = 0;
-    for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < total; item += warps) {
+    int par = 0;  // the hand-over buffer of the next (item, body)
+    for (int item = first; item < total; item += stride) {
         const int t = ct.pt_clist[item];
         const int4 meta = r.meta[t];
         const int ci = meta.x;
         const SceneC& S = sc[meta.w];
+        if (paired && wib == 1) {
+            // the observer: one hand-over per body, in the law warp's order
+            const double rad = r.pos[t].w;
+            const double mass = o.mass[meta.y];
+            for (int j = 0; j < S.body_count; ++j) {
+                pt_pair_barrier();
+                const PtMicroIn& mi = s_mi[par];
+                par ^= 1;
+                if (!mi.on || lane != 0) continue;
+                PtItem it;
+                it.rad = rad;
+                it.mass = mass;
+                it.ev = mk(c.vx[ci], c.vy[ci], c.vz[ci]);
+                const PtBody bd = pt_body(bodies, S.body_begin + j);
+                double* rec = ct.pt_body + ((size_t)item * ct.nbs + j) * kPtRecord;
+                pt_microstate(S.pt, it, bd, mk(mi.mn[0], mi.mn[1], mi.mn[2]), mk(mi.mc[0], mi.mc[1], mi.mc[2]), mi.md,
+                              mi.tot, mk(mi.th[0], mi.th[1], mi.th[2]), mk(mi.twh[0], mi.twh[1], mi.twh[2]), rec + 10);
+            }
+            continue;
+        }
         const PtItem it = pt_item(c, o, r, t, ci, meta.y, dt_eff);
         const int lin = r.cell[t].w;
         const int tb = tris.tcell_start[lin];
@@ -1354,8 +1402,8 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
                         if (tn < kPbTris) ttri[tn] = t_;
                         ++tn;
                     }
-                    const double* W = tris.world + 16 * (size_t)t_;
-                    const V3<double> out = mk(W[12], W[13], W[14]);
+                    const double* Wt = tris.world + 16 * (size_t)t_;
+                    const V3<double> out = mk(Wt[12], Wt[13], Wt[14]);
                     const V3<double> ce = it.p - out * d_;
                     tot += a_;
                     wn = wn + out * (-a_);
@@ -1363,7 +1411,30 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
                     wd += d_ * a_;
                 }
             }
-            if (tot <= 0.0) continue;
+            // in paired mode every (item, body) hands a record to the observer
+            // warp, an empty one where there is no manifold
+            auto hand_over = [&](bool on, V3<double> mn, V3<double> mc, double md, const T* h) {
+                if (!paired) return;
+                if (lane == 0) {
+                    PtMicroIn& mi = s_mi[par];
+                    mi.on = on ? 1 : 0;
+                    if (on) {
+                        const V3<double> th = cvt<double>(hload(h, 1)), twh = cvt<double>(hload(h, 2));
+                        mi.mn[0] = mn.x; mi.mn[1] = mn.y; mi.mn[2] = mn.z;
+                        mi.mc[0] = mc.x; mi.mc[1] = mc.y; mi.mc[2] = mc.z;
+                        mi.th[0] = th.x; mi.th[1] = th.y; mi.th[2] = th.z;
+                        mi.twh[0] = twh.x; mi.twh[1] = twh.y; mi.twh[2] = twh.z;
+                        mi.md = md;
+                        mi.tot = tot;
+                    }
+                }
+                pt_pair_barrier();
+                par ^= 1;
+            };
+            if (tot <= 0.0) {
+                hand_over(false, wn, wc, wd, nullptr);
+                continue;
+            }
             const V3<double> mn = normalized(wn);
             const V3<double> mc = wc * (1.0 / tot);
             const double md = wd / tot;
@@ -1374,6 +1445,7 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
             bhw = __shfl_sync(FULL, bhw, 0);
             if (slot < 0) {
                 if (lane == 0) ++bover;
+                hand_over(false, mn, mc, md, nullptr);
                 continue;
             }
             T* hv = hb.val + ((size_t)ci * kBSlots + slot) * kHV;
@@ -1385,6 +1457,7 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
             bool slide = false, twist = false;
             pt_manifold_history<T>(m, it, bd, mn, mc, md, dt_eff, h, slide, twist);
             if (lane == 0) hv_store(hv, h);
+            hand_over(true, mn, mc, md, h);
             // pass 2: per-triangle loads, the terms summed in triangle order
             double maxdepth = 0.0;
             int tcount = 0;
@@ -1447,7 +1520,9 @@ __global__ void __launch_bounds__(kPtWarpBlock) k_pt_warp(Comps c, Owners o, Rec
                 rec[7] = maxdepth;
                 rec[8] = rFz;
                 rec[9] = (double)(1 | (slide ? 2 : 0) | (twist ? 4 : 0));
-                pt_microstate(m, it, bd, mn, mc, md, tot, cvt<double>(hload(h, 1)), cvt<double>(hload(h, 2)), rec + 10);
+                if (!paired)
+                    pt_microstate(m, it, bd, mn, mc, md, tot, cvt<double>(hload(h, 1)), cvt<double>(hload(h, 2)),
+                                  rec + 10);
             }
             __syncwarp();
         }
@@ -1794,7 +1869,8 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
         k_pt_items<TB><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 8)), kPtTile, 0, s>>>(
             g, r, t, hb, k, ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr, ct.pt_scan, g.err);
-        k_pt_warp<T, TB><<<sm_count * 32, kPtWarpBlock, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
+        k_pt_warp<T, TB><<<sm_count * 32, kPtWarpBlock, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff,
+                                                             sm_count * kPtPairBlocksPerSm);
         k_pt_thread<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);
     }
 }
