@@ -1119,7 +1119,67 @@ __device__ void tape_pb(const StepTape& tp, int ci, int b, int slot, bool fresh,
     for (int a = 0; a < 9; ++a) tp.pb_h[(size_t)k * kHV + a] = (double)h[a];
 }
 
+// One triangle's share added to a manifold's sums (:1154-1183), as the
+// warp-per-item kernel adds it.
+__device__ __noinline__ void manifold_add(double& tot, V3<double>& wn, V3<double>& wc, double& wd, V3<double> p,
+                                          V3<double> out, double as, double dist)
+{
+    const V3<double> ce = p - out * dist;
+    tot += as;
+    wn = wn + out * (-as);
+    wc = wc + ce * as;
+    wd += dist * as;
+}
+
 // ---------------------------------------------------- PT, thread per item
+// The thread-per-item kernel calls the law's pieces through these wrappers,
+// compiled once each (not inlined): its own code around them then cannot
+// change how they round, and they give the bits that the warp-per-item
+// kernel gets from the same pieces inlined (tests/test_gpu_pt_paths.py).
+template <typename T>
+__device__ __noinline__ double tri_area_scale_n(const double* W, V3<double> p, double r, double& dist)
+{
+    return tri_area_scale<T>(W, p, r, dist);
+}
+__device__ __noinline__ bool tri_disk_n(const double* W, V3<double> p, double r)
+{
+    TriDisk d;
+    return tri_disk(W, p, r, d);
+}
+__device__ __noinline__ PtItem pt_item_n(const Comps& c, const Owners& o, const Recs& r, int t, int ci, int w,
+                                         double dt_eff)
+{
+    return pt_item(c, o, r, t, ci, w, dt_eff);
+}
+__device__ __noinline__ PtBody pt_body_n(const Bodies& bodies, int b) { return pt_body(bodies, b); }
+__device__ __noinline__ void pt_manifold_frame_n(double tot, V3<double> wn, V3<double> wc, double wd, V3<double>& mn,
+                                                 V3<double>& mc, double& md)
+{
+    mn = normalized(wn);
+    mc = wc * (1.0 / tot);
+    md = wd / tot;
+}
+template <typename T>
+__device__ __noinline__ void pt_manifold_history_n(const MatC& m, const PtItem& it, const PtBody& bd, V3<double> mn,
+                                                   V3<double> mc, double md, double dt_eff, T* h, bool& slide,
+                                                   bool& twist)
+{
+    pt_manifold_history<T>(m, it, bd, mn, mc, md, dt_eff, h, slide, twist);
+}
+template <typename T>
+__device__ __noinline__ void pt_triangle_load_n(const MatC& m, const PtItem& it, const PtBody& bd, const double* W,
+                                                double as, double dist, V3<T> hroll, V3<T> htan, V3<T> htw, PtTri& o)
+{
+    const LawC<T> lc = law_constants<T>(m, T(it.mass), T(it.rad));
+    pt_triangle_load<T>(m, lc, it, bd, W, as, dist, hroll, htan, htw, o);
+}
+__device__ __noinline__ void pt_microstate_n(const MatC& m, const PtItem& it, const PtBody& bd, V3<double> mn,
+                                             V3<double> mc, double md, double tot, V3<double> th, V3<double> twh,
+                                             double* mcr)
+{
+    pt_microstate(m, it, bd, mn, mc, md, tot, th, twh, mcr);
+}
+
 constexpr int kTriCache = 24;
 
 template <typename TC, typename T>
@@ -1137,7 +1197,7 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
         const int4 meta = r.meta[t];
         const int ci = meta.x;
         const SceneC& S = sc[meta.w];
-        const PtItem it = pt_item(c, o, r, t, ci, meta.y, dt_eff);
+        const PtItem it = pt_item_n(c, o, r, t, ci, meta.y, dt_eff);
         const int lin = r.cell[t].w;
         const int tb = tris.tcell_start[lin];
         const int te = min(tris.tcell_start[lin + 1], tris.capacity);
@@ -1150,33 +1210,57 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
             for (int f = 0; f < kPtRecord; ++f) rec[f] = 0.0;
             double* outd = ct.pt_out ? ct.pt_out + ((size_t)item * ct.nbs + j) * 25 : nullptr;
             if (outd) for (int f = 0; f < 25; ++f) outd[f] = 0.0;
-            // manifold sums over the component's own cell (:1154-1183)
+            // manifold sums over the component's own cell (:1154-1183); the
+            // triangles with a share keep their area scale and distance
             int ctri[kTriCache];
-            double cas[kTriCache];
+            double cas[kTriCache], cdist[kTriCache];
             int ncache = 0;
             bool spill = false;
             double tot = 0.0, wd = 0.0;
             V3<double> wn = mk(0.0, 0.0, 0.0), wc = mk(0.0, 0.0, 0.0);
+            auto add = [&](int tri, const double* W, double as, double dist) {
+                manifold_add(tot, wn, wc, wd, it.p, mk(W[12], W[13], W[14]), as, dist);
+                if (ncache < kTriCache) { ctri[ncache] = tri; cas[ncache] = as; cdist[ncache] = dist; ++ncache; }
+                else spill = true;
+            };
+            // Three passes, each in triangle order, so that the lanes of a
+            // warp meet in the FP64 work instead of reaching it at different
+            // entries of their cells: the FP32 test over the cell's entries,
+            // the FP64 tests that need no edge sum, then the areas of the
+            // triangles left (one or two per item).
+            int cand[kTriCache];
+            int ncand = 0;
+            bool many = false;
             for (int e = tb; e < te; ++e) {
                 const int tri = tris.ttri[e];
                 if (tris.body[tri] != b || !pt_may_touch(tris.tf, tri, pq)) continue;
-                const double* W = tris.world + 16 * (size_t)tri;
-                double dist;
-                const double as = tri_area_scale<T>(W, it.p, it.rad, dist);
-                if (as <= 0.0) continue;
-                const V3<double> out = mk(W[12], W[13], W[14]);
-                const V3<double> ce = it.p - out * dist;
-                tot += as;
-                wn = wn + out * (-as);
-                wc = wc + ce * as;
-                wd += dist * as;
-                if (ncache < kTriCache) { ctri[ncache] = tri; cas[ncache] = as; ++ncache; }
-                else spill = true;
+                if (ncand < kTriCache) cand[ncand++] = tri;
+                else many = true;
+            }
+            if (!many) {
+                int nkeep = 0;
+                for (int q = 0; q < ncand; ++q)
+                    if (tri_disk_n(tris.world + 16 * (size_t)cand[q], it.p, it.rad)) cand[nkeep++] = cand[q];
+                for (int q = 0; q < nkeep; ++q) {
+                    const double* W = tris.world + 16 * (size_t)cand[q];
+                    double dist;
+                    const double as = tri_area_scale_n<T>(W, it.p, it.rad, dist);
+                    if (as > 0.0) add(cand[q], W, as, dist);
+                }
+            } else {
+                for (int e = tb; e < te; ++e) {
+                    const int tri = tris.ttri[e];
+                    if (tris.body[tri] != b || !pt_may_touch(tris.tf, tri, pq)) continue;
+                    const double* W = tris.world + 16 * (size_t)tri;
+                    double dist;
+                    const double as = tri_area_scale_n<T>(W, it.p, it.rad, dist);
+                    if (as > 0.0) add(tri, W, as, dist);
+                }
             }
             if (tot <= 0.0) continue;
-            const V3<double> mn = normalized(wn);
-            const V3<double> mc = wc * (1.0 / tot);
-            const double md = wd / tot;
+            V3<double> mn, mc;
+            double md;
+            pt_manifold_frame_n(tot, wn, wc, wd, mn, mc, md);
             bool fresh = false;
             const int slot = acquire(hb, kBSlots, ci, (uint64_t)(j + 1), step, bhw, bhigh, &fresh);
             if (slot < 0) { ++bover; continue; }
@@ -1184,15 +1268,14 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
             T h[9];
             hv_load(hv, h);
             if (tape.pb) tape_pb(tape, ci, b, slot, fresh, h, ctri, ncache, spill);
-            const PtBody bd = pt_body(bodies, b);
+            const PtBody bd = pt_body_n(bodies, b);
             const MatC& m = S.pt;
             bool slide = false, twist = false;
-            pt_manifold_history<T>(m, it, bd, mn, mc, md, dt_eff, h, slide, twist);
+            pt_manifold_history_n<T>(m, it, bd, mn, mc, md, dt_eff, h, slide, twist);
             hv_store(hv, h);
             rec[9] = (double)(1 | (slide ? 2 : 0) | (twist ? 4 : 0));
             double maxdepth = 0.0;
             int tcount = 0;
-            const LawC<T> lc = law_constants<T>(m, T(it.mass), T(it.rad));
             const V3<T> hroll = hload(h, 0), htan = hload(h, 1), htw = hload(h, 2);
             const int nloop = spill ? (te - tb) : ncache;
             for (int qi = 0; qi < nloop; ++qi) {
@@ -1202,19 +1285,19 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
                 if (!spill) {
                     tri = ctri[qi];
                     as = cas[qi];
+                    dist = cdist[qi];
                     W = tris.world + 16 * (size_t)tri;
-                    dist = dot(mk(W[12], W[13], W[14]), it.p - mk(W[3], W[4], W[5]));
                 } else {
                     tri = tris.ttri[tb + qi];
                     if (tris.body[tri] != b || !pt_may_touch(tris.tf, tri, pq)) continue;
                     W = tris.world + 16 * (size_t)tri;
-                    as = tri_area_scale<T>(W, it.p, it.rad, dist);
+                    as = tri_area_scale_n<T>(W, it.p, it.rad, dist);
                     if (as <= 0.0) continue;
                 }
                 const double depthd = it.rad - dist;
                 if (dist <= 0.0 || depthd <= 0.0) continue;
                 PtTri pr;
-                pt_triangle_load<T>(m, lc, it, bd, W, as, dist, hroll, htan, htw, pr);
+                pt_triangle_load_n<T>(m, it, bd, W, as, dist, hroll, htan, htw, pr);
                 bF = bF + pr.pf;
                 bT = bT + pr.ptq;
                 rec[0] += pr.rf.x; rec[1] += pr.rf.y; rec[2] += pr.rf.z;
@@ -1233,7 +1316,7 @@ __global__ void __launch_bounds__(128) k_pt_thread(Comps c, Owners o, Recs r, co
             }
             rec[6] = (double)tcount;
             rec[7] = maxdepth;
-            pt_microstate(m, it, bd, mn, mc, md, tot, cvt<double>(hload(h, 1)), cvt<double>(hload(h, 2)), rec + 10);
+            pt_microstate_n(m, it, bd, mn, mc, md, tot, cvt<double>(hload(h, 1)), cvt<double>(hload(h, 2)), rec + 10);
         }
         hb.hw[ci] = bhw;
         double* pr = ct.pt_res + 6 * (size_t)ci;

@@ -400,6 +400,57 @@ DEM_DEV void tri_world(const double* L, double qw, double qx, double qy, double 
     W[15] = sqrt(r2) * (1.0 + 1e-12) + 1e-15;
 }
 
+// Whether the contact disk (centre at the common origin of the in-plane
+// vertex offsets ra, rb, rc; squared radius c2) lies beyond one of the
+// triangle's edge lines, on the side away from the triangle, by more than
+// its radius: then disk and triangle are disjoint.  With s the signed
+// doubled area of (centre, a, b) and S that of the triangle, the centre is
+// beyond edge ab when s and S differ in sign, at the distance |s| / |b - a|.
+// The margin, 1e-6 of the squared distances, is far above the rounding of
+// these products.
+DEM_DEV bool disk_beyond_an_edge(V3<double> n, V3<double> ra, V3<double> rb, V3<double> rc, double c2)
+{
+    const V3<double> e0 = rb - ra, e1 = rc - rb, e2 = ra - rc;
+    const double S = dot(cross(e0, rc - ra), n);
+    const double s0 = dot(cross(ra, rb), n), s1 = dot(cross(rb, rc), n), s2 = dot(cross(rc, ra), n);
+    const double m = c2 * (1.0 + 1.0e-6);
+    return (s0 * S < 0.0 && s0 * s0 > m * dot(e0, e0)) || (s1 * S < 0.0 && s1 * s1 > m * dot(e1, e1)) ||
+           (s2 * S < 0.0 && s2 * s2 > m * dot(e2, e2));
+}
+
+// The contact disk of a sphere (centre p, radius r) on the plane of the
+// world triangle W: the sphere's distance above the plane along the normal,
+// the disk's squared radius and the vertex offsets from its centre (the
+// same arithmetic as the start of tri_area_scale64 below).
+struct TriDisk {
+    V3<double> n, ra, rb, rc;
+    double dist, c2;
+};
+// The tests of bodyTriangleAreaScale (:380-407) that need no edge sum: false
+// when the scale is certainly 0 -- the sphere not strictly above the plane
+// within its radius, or disk and triangle disjoint (disk centre farther from
+// the triangle's centroid than the disk radius plus the triangle's
+// circumradius about it, W[15], or beyond an edge by more than the disk
+// radius).  For disjoint shapes the reference's edge sum cancels to rounding
+// noise, far below its 1e-12 threshold, so the scale is 0 either way.
+DEM_DEV bool tri_disk(const double* W, V3<double> p, double r, TriDisk& d)
+{
+    d.n = mk(W[12], W[13], W[14]);
+    const V3<double> a = mk(W[3], W[4], W[5]);
+    d.dist = dot(d.n, p - a);
+    if (d.dist <= 0.0) return false;
+    d.c2 = r * r - d.dist * d.dist;
+    if (d.c2 <= 1.0e-30) return false;
+    const V3<double> ce = p - d.n * d.dist;
+    d.ra = a - ce;
+    d.rb = mk(W[6], W[7], W[8]) - ce;
+    d.rc = mk(W[9], W[10], W[11]) - ce;
+    const V3<double> cen = (d.ra + d.rb + d.rc) * (1.0 / 3.0);
+    const double reach = (sqrt(d.c2) + W[15]) * (1.0 + 1e-9);
+    if (dot(cen, cen) > reach * reach) return false;
+    return !disk_beyond_an_edge(d.n, d.ra, d.rb, d.rc, d.c2);
+}
+
 // bodyTriangleAreaScale (:380-407) in FP64: the share of the contact disk of
 // a sphere (centre p, radius r) that lies on the world triangle W, and the
 // sphere's distance above the triangle's plane (dist, along the normal).

@@ -126,6 +126,10 @@ __device__ __forceinline__ bool cell_coord_f32(double x, float inv_mesh_f, int& 
 
 // computeComponentKeysKernel (src/cuda/cuda_grid_backend.cu:51-71) plus the
 // per-scene cell box.
+// Grids of k_cell_keys above this many blocks read the cell box before
+// updating it.
+constexpr unsigned kBoxCheckBlocks = 2048;
+
 __global__ void k_cell_keys(Comps c, Owners o, Grid g)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,9 +184,24 @@ __global__ void k_cell_keys(Comps c, Owners o, Grid g)
                 for (int k = 0; k < 3; ++k) { a[k] = min(a[k], sh_box[v][1 + k]); b[k] = max(b[k], sh_box[v][4 + k]); }
                 sh_box[v][0] = INT_MAX;
             }
+            // The box only moves towards the block's values.  On large grids
+            // an atomic that the current value already satisfies is skipped
+            // (most blocks of a scene change none of the six, and thousands
+            // of atomics on six words serialise); the six loads go out
+            // together, past L1, and a stale value only costs an atomic.
+            // Small grids issue the atomics at once (the loads would only
+            // add their latency to the block's end).
             int* box = g.scene_box + 6 * sc;
-            atomicMin(box + 0, a[0]); atomicMin(box + 1, a[1]); atomicMin(box + 2, a[2]);
-            atomicMax(box + 3, b[0]); atomicMax(box + 4, b[1]); atomicMax(box + 5, b[2]);
+            int cur[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+            if (gridDim.x > kBoxCheckBlocks) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) cur[k] = __ldcg(box + k);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (a[k] < cur[k]) atomicMin(box + k, a[k]);
+                if (b[k] > cur[3 + k]) atomicMax(box + 3 + k, b[k]);
+            }
         }
     }
 }
