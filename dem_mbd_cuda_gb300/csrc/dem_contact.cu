@@ -131,20 +131,27 @@ __device__ __forceinline__ D4 ldg_d4(const D4* p)
     return v;
 }
 
-// expireHistory (:217-229) over the occupied prefix [0, hw).
-template <typename T> __device__ void expire(Hist<T> h, int slots, int c, int step)
+// expireHistory (:217-229) over the occupied prefix [0, hw).  Ahead: the
+// first two keys and last-seen steps load beside the high-water mark, not
+// after it (for the particle slots, which nearly every component uses;
+// every kind has at least two slots).
+template <bool Ahead, typename T> __device__ void expire(Hist<T> h, int slots, int c, int step)
 {
     const size_t base = (size_t)c * slots;
-    // the first two keys and last-seen steps load beside the high-water mark,
-    // not after it (every kind has at least two slots)
-    const uint64_t k0 = h.key[hslot(h, c, 0)], k1 = h.key[hslot(h, c, 1)];
-    const int l0 = h.last[hslot(h, c, 0)], l1 = h.last[hslot(h, c, 1)];
+    uint64_t k0 = 0, k1 = 0;
+    int l0 = 0, l1 = 0;
+    if (Ahead) {
+        k0 = h.key[hslot(h, c, 0)];
+        k1 = h.key[hslot(h, c, 1)];
+        l0 = h.last[hslot(h, c, 0)];
+        l1 = h.last[hslot(h, c, 1)];
+    }
     const int hw = h.hw[c];
     int nhw = 0;
     for (int s = 0; s < hw; ++s) {
-        const uint64_t key = s == 0 ? k0 : s == 1 ? k1 : h.key[hslot(h, c, s)];
+        const uint64_t key = Ahead && s == 0 ? k0 : Ahead && s == 1 ? k1 : h.key[hslot(h, c, s)];
         if (key != 0) {
-            const int last = s == 0 ? l0 : s == 1 ? l1 : h.last[hslot(h, c, s)];
+            const int last = Ahead && s == 0 ? l0 : Ahead && s == 1 ? l1 : h.last[hslot(h, c, s)];
             if (last < step - 1) {
                 h.key[hslot(h, c, s)] = 0;
                 h.last[hslot(h, c, s)] = -1;
@@ -342,7 +349,7 @@ __global__ void __launch_bounds__(256) k_walls_probe(Comps c, Owners o, const Sc
     if (ci < c.n) {
         // expireHistory (:1109-1117) of the wall slots, before pass 2
         // acquires any for this step
-        expire(hw, kWSlots, ci, *k.step);
+        expire<false>(hw, kWSlots, ci, *k.step);
         wflag[ci] = 0;
         const SceneC& S = sc[o.scene[c.owner[ci]]];
         if (S.wall_count > 0) {
@@ -470,7 +477,7 @@ __device__ int sweep_list_one(const Grid& g, const Recs& r, const SceneC* __rest
     const int* L = k.nl_idx + ci;
     const int l0 = L[0], l1 = L[nc], l2 = L[2 * (size_t)nc], l3 = L[3 * (size_t)nc];
     const int nn = min(k.nl_cnt[ci], kNL);
-    expire(hp, kPSlots, ci, step);
+    expire<true>(hp, kPSlots, ci, step);
     int phw = hp.hw[ci];
     int fkey[kNL], fcid[kNL];
     int found = 0;
@@ -586,7 +593,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
         // expireHistory (:1109-1117) for the component's particle slots,
         // before any slot of this step is acquired (the wall and body slots
         // expire in their own probes)
-        expire(hp, kPSlots, ci, step);
+        expire<true>(hp, kPSlots, ci, step);
         int phw = hp.hw[ci];
         int pending = 0;  // candidates in stage_t[count .. count + pending)
         // Phase 2 over the staged candidates, in order.  A candidate staged
@@ -875,9 +882,7 @@ __device__ __forceinline__ bool pt_cell_may_touch(const Tris& tris, int tb, int 
 // acquire any) and the probe; then its rank among the kept positions (block
 // scan plus the tiles before it, by single-pass look-back, ScanState) gives
 // the item list in sorted order and each component's item index (-1: none).
-constexpr int kPtTile = kPtItemTile;
-
-template <typename TB>
+template <typename TB, int kPtTile>
 __global__ void __launch_bounds__(kPtTile) k_pt_items(Grid g, Recs r, Tris tris, Hist<TB> hb, Counters k, int* clist,
                                                       int* pt_index, int* ctotal, ScanState st, unsigned* err)
 {
@@ -896,7 +901,7 @@ __global__ void __launch_bounds__(kPtTile) k_pt_items(Grid g, Recs r, Tris tris,
         int hit = 0, ci = -1;
         if (t < nvalid) {
             ci = g.sorted_id[t];
-            expire(hb, kBSlots, ci, step);
+            expire<false>(hb, kBSlots, ci, step);
             const int lin = r.cell[t].w;
             const int tb = tris.tcell_start[lin];
             const int te = min(tris.tcell_start[lin + 1], tris.capacity);
@@ -1950,8 +1955,14 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
     }
     if (stage & 4) k_pp_law<T><<<sm_count * (k.pp_bps > 0 ? k.pp_bps : 16), 256, 0, s>>>(r, sc, hp, ct, k, dt_eff, g.nscenes);
     if ((stage & 8) && t.nt > 0 && b.nb > 0) {
-        k_pt_items<TB><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 8)), kPtTile, 0, s>>>(
-            g, r, t, hb, k, ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr, ct.pt_scan, g.err);
+        if (c.n <= kPtWideTileComps)
+            k_pt_items<TB, kPtItemTileWide><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 2)),
+                                              kPtItemTileWide, 0, s>>>(g, r, t, hb, k, ct.pt_clist, ct.pt_index,
+                                                                       ct.pt_ctotal_ptr, ct.pt_scan, g.err);
+        else
+            k_pt_items<TB, kPtItemTile><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 8)), kPtItemTile, 0,
+                                          s>>>(g, r, t, hb, k, ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr,
+                                               ct.pt_scan, g.err);
         k_pt_warp<T, TB><<<sm_count * 32, kPtWarpBlock, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff,
                                                              sm_count * kPtPairBlocksPerSm);
         k_pt_thread<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);

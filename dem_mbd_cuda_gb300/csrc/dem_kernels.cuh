@@ -42,8 +42,13 @@ struct ScanState {
     int max_tiles;
 };
 
-// Sorted positions per tile of the particle-triangle item scan.
+// Sorted positions per tile of the particle-triangle item scan: 1,024 up to
+// kPtWideTileComps components (fewer tiles to chain on the short scenes,
+// where the scan sits on the triangle branch's critical path), 256 above
+// (more resident blocks); the scan state is sized for the smaller tile.
 constexpr int kPtItemTile = 256;
+constexpr int kPtItemTileWide = 1024;
+constexpr int kPtWideTileComps = 1000000;
 
 #ifdef __CUDACC__
 constexpr int kScanSpinLimit = 1 << 20;
