@@ -81,10 +81,11 @@ constexpr int kDefaultPtWarpItems = 3072;
 // rotational branches are short chains that must not wait for slots);
 // larger scenes are throughput bound and give the sweep and the gathers
 // more of each SM.  Measured on GB300 (200k- and 2M-sphere scenes); the
-// autotuner refines them per scene.  On the 2M drum 8 sweep blocks per SM
-// measured 1.5% faster than 16 and 5 (one process, alternating settings).
+// autotuner refines them per scene.  Six sweep blocks per SM is the sweep's
+// register-limited residency: that grid leaves nothing beside it and was
+// the slowest setting on the 2M drum.
 constexpr int kSmallScene = 500000;
-constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 8;
+constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 16;
 // The gathers and the particle law, likewise (blocks of 256 per SM).
 constexpr int kGatherBlocksSmall = 2, kGatherBlocksLarge = 8;
 constexpr int kDefaultPpBlocksPerSm = 16;
