@@ -45,9 +45,23 @@ def test_pt_path_single_evaluation(maker, path):
     assert np.abs(le - lo).max() <= 1e-9 * np.abs(lo).max() + 1e-12
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_pt_paths_bit_identical(precision):
-    sc = G.small_mbd(caps=False)
+@pytest.mark.parametrize("precision,scene", [("fp64", "small"), ("mixed", "small"), ("fp64", "drum")])
+def test_pt_paths_bit_identical(precision, scene):
+    """small_mbd: about 100 items, the warp kernel's paired mode (a block per
+    item, the second warp computing the microstate); the drum generator at
+    40,000 spheres: several thousand items, more than the paired blocks
+    resident at once, so the forced warp kernel runs one item per warp."""
+    if scene == "small":
+        sc = G.small_mbd(caps=False)
+    else:
+        import torch
+        sc = G.drum(n=40000)[0]
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        e = engine_for(sc)
+        e.run(1)
+        items = e.stepStats()["body_candidate_items"]
+        assert items > 4 * sms, (items, sms)
+        del e
     out = []
     for path in (WARP, THREAD):
         e = engine_for(sc, precision=precision).set_pt_warp_items(path)
