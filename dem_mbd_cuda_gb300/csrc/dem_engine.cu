@@ -619,10 +619,13 @@ public:
     // of a split finish + advance) at the head, beside the particle grid;
     // kTailFinishPos ends with the first part.
     // kHeadAdvance opens the first step of a run with the advance itself,
-    // split the same way (positions first, the rest on the branch).
+    // split the same way (positions first, the rest on the branch); with
+    // kHeadRest as well, the rest is k_advance_rest, for a run whose previous
+    // call ended with kTailFinishVel (the half-step velocities alone, the
+    // quaternion rate left to the next advance).
     enum : unsigned {
         kTailTransform = 1, kTailD2H = 2, kTailFinish = 4, kHeadRest = 8, kTailFinishPos = 16, kHeadAdvance = 32,
-        kTailDiag = 64
+        kTailDiag = 64, kTailFinishVel = 128
     };
 
     template <typename T, typename TB>
@@ -640,6 +643,7 @@ public:
         auto integrate = [&](cudaStream_t on) {
             if (tail & kTailFinishPos) launch_finish_advance_pos(O_, dt_, on);
             else if (tail & kTailFinish) launch_finish(O_, dt_, on);
+            else if (tail & kTailFinishVel) launch_finish_vel(O_, dt_, on);
         };
         // the rotational advance on a branch only for spheres: with clumps the
         // component update reads the quaternions at once
@@ -1061,8 +1065,12 @@ public:
         }
     }
 
-    // IntegrateDem / IntegrateDemMultiBody without output frames.
-    void run_steps(int steps)
+    // IntegrateDem / IntegrateDemMultiBody without output frames.  With
+    // `defer` the last step stores the half-step velocities and leaves the
+    // half-step quaternion rate pending (hq_pending_): the next run's first
+    // advance computes it beside its particle grid, as every step inside a
+    // run does, and any other use of the state first completes it (settle).
+    void run_steps(int steps, bool defer = false)
     {
         need_init();
         const double dt = dt_;
@@ -1076,7 +1084,7 @@ public:
             started_ = true;
         }
         if (steps <= 0) return;
-        step_loop(steps);
+        step_loop(steps, defer);
         collect_diagnostics(nullptr, true);
     }
 
@@ -1084,15 +1092,18 @@ public:
     // the captured force evaluation.  All but the last step end with the
     // finish and the first part of the next advance (positions); the next
     // step's graph starts with the second part beside its particle grid.
-    // The last step ends with finish alone.  With bodies the host MBD step
-    // runs between graph launches.
-    void step_loop(int steps)
+    // The last step ends with finish alone (its velocity part alone with
+    // `defer`).  With bodies the host MBD step runs between graph launches.
+    void step_loop(int steps, bool defer = false)
     {
         const bool mbd = nb_ > 0;
         ensure_graphs(mbd);
         for (int s = 0; s < steps; ++s) {
             const bool last = s == steps - 1;
-            cudaGraphExec_t g = graphs_[graph_index(mbd, s > 0 ? 1 : 2, last)];
+            const int head = s > 0 ? 1 : hq_pending_ ? 3 : 2;
+            const int tk = !last ? 0 : defer ? 2 : 1;
+            capture(graphs_[graph_index(mbd, head, tk)], mbd, head, tk);
+            cudaGraphExec_t g = graphs_[graph_index(mbd, head, tk)];
             std::vector<double> pose;
             if (mbd) {
                 body_position_update(dt_);
@@ -1105,6 +1116,8 @@ public:
             }
             check(cudaGraphLaunch(g, stream_), "cudaGraphLaunch");
             ++step_index_;
+            if (head == 3) hq_pending_ = false;
+            if (tk == 2) hq_pending_ = true;
             if (mbd) {
                 // the loads are on the host once the download's event fires;
                 // the particle integrator may still be running
@@ -1117,14 +1130,32 @@ public:
         // the callers synchronize (after their own downloads)
     }
 
-    // head: 1 the previous step's rotational advance, 2 this step's advance
-    static int graph_index(bool mbd, int head, bool last) { return (mbd ? 6 : 0) + head * 2 + (last ? 1 : 0); }
+    // head: 1 the previous step's rotational advance, 2 this step's advance,
+    // 3 this step's advance with the previous step's quaternion rate;
+    // tk: 0 not the last step, 1 the last, 2 the last with the rate deferred
+    static int graph_index(bool mbd, int head, int tk) { return (mbd ? 12 : 0) + head * 3 + tk; }
+
+    // Complete a deferred finish: the half-step quaternion rate of the last
+    // step run (before anything reads or replaces the particle state).
+    void settle()
+    {
+        if (!hq_pending_) return;
+        launch_finish_rot(O_, dt_, stream_);
+        check(cudaGetLastError(), "finish");
+        hq_pending_ = false;
+    }
+    Engine& settled()
+    {
+        settle();
+        return *this;
+    }
 
     // Captured force evaluation with dt, optionally with the body upload /
     // load download around it and an advance at its head (head 1: the rest
-    // of the previous step's, 2: this step's own), followed by finish (last)
-    // or finish + the position advance.
-    void capture(cudaGraphExec_t& ex, bool mbd, int head, bool last)
+    // of the previous step's, 2: this step's own, 3: this step's own with the
+    // previous step's quaternion rate), followed by finish + the position
+    // advance (tk 0), finish (tk 1) or its velocity part (tk 2).
+    void capture(cudaGraphExec_t& ex, bool mbd, int head, int tk)
     {
         if (ex) return;
         cudaGraph_t g = nullptr;
@@ -1132,8 +1163,9 @@ public:
         try {
             if (mbd) enqueue_body_h2d();
             forces(dt_, false, (mbd ? kTailTransform | kTailD2H : 0u) |
-                                   (head == 1 ? kHeadRest : head == 2 ? kHeadAdvance : 0u) |
-                                   (last ? kTailFinish | kTailDiag : kTailFinishPos));
+                                   (head == 1 ? kHeadRest : head == 2 ? kHeadAdvance : kHeadAdvance | kHeadRest) |
+                                   (tk == 0 ? kTailFinishPos : tk == 1 ? kTailFinish | kTailDiag
+                                                                       : kTailFinishVel | kTailDiag));
         } catch (...) {
             cudaStreamEndCapture(stream_, &g);
             if (g) cudaGraphDestroy(g);
@@ -1180,8 +1212,8 @@ public:
     void ensure_graphs(bool mbd)
     {
         for (int head = 1; head <= 2; ++head)
-            for (int last = 0; last < 2; ++last)
-                capture(graphs_[graph_index(mbd, head, last)], mbd, head, last);
+            for (int tk = 0; tk < 2; ++tk)
+                capture(graphs_[graph_index(mbd, head, tk)], mbd, head, tk);
     }
 
     // Time `steps` graph-launched steps (pure DEM) on the device; the state is
@@ -2004,6 +2036,7 @@ public:
 
     int n_ = 0, nc_ = 0, nw_ = 0, nb_ = 0, nt_ = 0, S_ = 0, nbs_ = 0;
     bool sphere_ = true, initialized_ = false, started_ = false, restored_ = false;
+    bool hq_pending_ = false;  // the last run deferred its quaternion rate (run_steps)
     bool keep_bp_ = false, keep_bd_ = false;
     int precision_ = 0, block_ = 128, sm_count_ = 0;
     bool pt_fp32_ = false;
@@ -2059,7 +2092,7 @@ public:
     char* diag_pin_ = nullptr;
     size_t diag_bytes_ = 0;
     size_t pinned_bytes_ = 0;
-    std::array<cudaGraphExec_t, 12> graphs_{};  // by graph_index(bodies, head, last step)
+    std::array<cudaGraphExec_t, 24> graphs_{};  // by graph_index(bodies, head, tail kind)
 
     Owners O_{};
     Comps C_{};
@@ -2176,14 +2209,14 @@ int dem_compute_forces(dem_engine* e, double, const dem_body_states* bodies, dou
     return guarded([&] {
         NEED(e);
         if (bodies) { NEED(bodies->center); NEED(bodies->quat); NEED(bodies->vel); NEED(bodies->omega); }
-        e->e.compute_forces(bodies, body_forces, diag);
+        e->e.settled().compute_forces(bodies, body_forces, diag);
     });
 }
 
-int dem_leapfrog_init(dem_engine* e, double h) { return guarded([&] { NEED(e); e->e.leapfrog_init(h); }); }
-int dem_leapfrog_advance(dem_engine* e, double dt) { return guarded([&] { NEED(e); e->e.advance(dt); }); }
-int dem_leapfrog_finish(dem_engine* e, double dt, double) { return guarded([&] { NEED(e); e->e.finish(dt); }); }
-int dem_run_steps(dem_engine* e, int steps) { return guarded([&] { NEED(e); e->e.run_steps(steps); }); }
+int dem_leapfrog_init(dem_engine* e, double h) { return guarded([&] { NEED(e); e->e.settled().leapfrog_init(h); }); }
+int dem_leapfrog_advance(dem_engine* e, double dt) { return guarded([&] { NEED(e); e->e.settled().advance(dt); }); }
+int dem_leapfrog_finish(dem_engine* e, double dt, double) { return guarded([&] { NEED(e); e->e.settled().finish(dt); }); }
+int dem_run_steps(dem_engine* e, int steps) { return guarded([&] { NEED(e); e->e.run_steps(steps, true); }); }
 
 int dem_get_bodies(dem_engine* e, double* c, double* q, double* v, double* w, double* loads)
 {
@@ -2199,8 +2232,8 @@ int dem_get_bodies(dem_engine* e, double* c, double* q, double* v, double* w, do
     });
 }
 
-int dem_save_history(dem_engine* e, const char* path) { return guarded([&] { NEED(e); e->e.save_history(path); }); }
-int dem_load_history(dem_engine* e, const char* path) { return guarded([&] { NEED(e); e->e.load_history(path); }); }
+int dem_save_history(dem_engine* e, const char* path) { return guarded([&] { NEED(e); e->e.settled().save_history(path); }); }
+int dem_load_history(dem_engine* e, const char* path) { return guarded([&] { NEED(e); e->e.settled().load_history(path); }); }
 int dem_has_restored_leapfrog_state(dem_engine* e, int* r)
 {
     return guarded([&] { NEED(e); NEED(r); *r = e->e.restored_ ? 1 : 0; });
@@ -2208,12 +2241,12 @@ int dem_has_restored_leapfrog_state(dem_engine* e, int* r)
 
 int dem_download_state(dem_engine* e, double* pos, double* vel, double* omg, double* quat)
 {
-    return guarded([&] { NEED(e); e->e.download_state(pos, vel, omg, quat); });
+    return guarded([&] { NEED(e); e->e.settled().download_state(pos, vel, omg, quat); });
 }
 
 int dem_download_forces(dem_engine* e, double* c, double* f, double* w, double* t, double* bp, double* bd)
 {
-    return guarded([&] { NEED(e); e->e.download_forces(c, f, w, t, bp, bd); });
+    return guarded([&] { NEED(e); e->e.settled().download_forces(c, f, w, t, bp, bd); });
 }
 
 int dem_stats(dem_engine* e, dem_step_stats* s) { return guarded([&] { NEED(e); NEED(s); *s = e->e.stats_; }); }
@@ -2301,17 +2334,17 @@ extern "C" {
 
 int dem_x_compute_forces_timed(dem_engine* e, int diag)
 {
-    return guarded([&] { NEED(e); e->e.compute_forces(nullptr, nullptr, diag, true); });
+    return guarded([&] { NEED(e); e->e.settled().compute_forces(nullptr, nullptr, diag, true); });
 }
 
 int dem_x_time_steps(dem_engine* e, int steps, float* ms)
 {
-    return guarded([&] { NEED(e); NEED(ms); *ms = e->e.time_steps(steps); });
+    return guarded([&] { NEED(e); NEED(ms); *ms = e->e.settled().time_steps(steps); });
 }
 
 int dem_x_download_half(dem_engine* e, double* vh, double* wh, double* hdq, double* acc, double* aacc)
 {
-    return guarded([&] { NEED(e); e->e.download_half(vh, wh, hdq, acc, aacc); });
+    return guarded([&] { NEED(e); e->e.settled().download_half(vh, wh, hdq, acc, aacc); });
 }
 
 int dem_x_set_pt_warp_items(dem_engine* e, int n)
@@ -2326,7 +2359,7 @@ int dem_x_set_launch(dem_engine* e, int what, int blocks_per_sm)
 
 int dem_adjoint_forward(dem_engine* e, int steps, int checkpoint_every)
 {
-    return guarded([&] { NEED(e); e->e.adjoint_forward(steps, checkpoint_every); });
+    return guarded([&] { NEED(e); e->e.settled().adjoint_forward(steps, checkpoint_every); });
 }
 
 int dem_adjoint_backward(dem_engine* e, const double* dl_dpos, const double* dl_dvel, double* dl_dpos0,
@@ -2334,7 +2367,7 @@ int dem_adjoint_backward(dem_engine* e, const double* dl_dpos, const double* dl_
 {
     return guarded([&] {
         NEED(e);
-        e->e.adjoint_backward(dl_dpos, dl_dvel, nullptr, nullptr, dl_dpos0, dl_dvel0, dl_domega0, dl_dparams);
+        e->e.settled().adjoint_backward(dl_dpos, dl_dvel, nullptr, nullptr, dl_dpos0, dl_dvel0, dl_domega0, dl_dparams);
     });
 }
 
@@ -2344,7 +2377,7 @@ int dem_adjoint_backward_mbd(dem_engine* e, const double* dl_dpos, const double*
 {
     return guarded([&] {
         NEED(e);
-        e->e.adjoint_backward(dl_dpos, dl_dvel, dl_dbody_center, dl_dbody_vel, dl_dpos0, dl_dvel0, dl_domega0,
+        e->e.settled().adjoint_backward(dl_dpos, dl_dvel, dl_dbody_center, dl_dbody_vel, dl_dpos0, dl_dvel0, dl_domega0,
                               dl_dparams);
     });
 }
@@ -2359,13 +2392,13 @@ int dem_adjoint_body_gradients(dem_engine* e, double* dl_dbody_center0, double* 
 {
     return guarded([&] {
         NEED(e);
-        e->e.adjoint_body_gradients(dl_dbody_center0, dl_dbody_quat0, dl_dbody_vel0, dl_dbody_omega0);
+        e->e.settled().adjoint_body_gradients(dl_dbody_center0, dl_dbody_quat0, dl_dbody_vel0, dl_dbody_omega0);
     });
 }
 
 int dem_x_set_adjoint_fp32(dem_engine* e, int on)
 {
-    return guarded([&] { NEED(e); e->e.set_adjoint_fp32(on != 0); });
+    return guarded([&] { NEED(e); e->e.settled().set_adjoint_fp32(on != 0); });
 }
 
 int dem_x_adjoint_bytes(dem_engine* e, size_t* checkpoints, size_t* tapes)
@@ -2379,7 +2412,7 @@ int dem_x_adjoint_bytes(dem_engine* e, size_t* checkpoints, size_t* tapes)
 
 int dem_x_scan_wait_probe(dem_engine* e, unsigned* err)
 {
-    return guarded([&] { NEED(e); NEED(err); *err = e->e.scan_wait_probe(); });
+    return guarded([&] { NEED(e); NEED(err); *err = e->e.settled().scan_wait_probe(); });
 }
 
 int dem_x_synchronize(dem_engine* e)

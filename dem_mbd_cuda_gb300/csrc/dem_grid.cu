@@ -648,22 +648,46 @@ __global__ void __launch_bounds__(256) k_advance_rot(Owners d, double dt)
     }
 }
 
-// advanceHalfVelocityKernel (:239-265)
-__global__ void k_finish(Owners d, double dt)
+// advanceHalfVelocityKernel (:239-265) in its two parts: the half-step
+// velocities, then the half-step quaternion rate from the quaternion, the
+// full-step spin and the updated half-step spin.
+__device__ __forceinline__ void finish_vel_one(Owners d, int i, double dt)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.n) return;
     d.vhx[i] += d.ax[i] * dt;
     d.vhy[i] += d.ay[i] * dt;
     d.vhz[i] += d.az[i] * dt;
     d.whx[i] += d.awx[i] * dt;
     d.why[i] += d.awy[i] * dt;
     d.whz[i] += d.awz[i] * dt;
+}
+__device__ __forceinline__ void finish_rot_one(Owners d, int i, double dt)
+{
     const double h = 0.5 * dt;
     double qw = d.qw[i], qx = d.qx[i], qy = d.qy[i], qz = d.qz[i];
     quat_half_step(qw, qx, qy, qz, d.wx[i], d.wy[i], d.wz[i], h);
     normalize_quat(qw, qx, qy, qz);
     quat_derivative(qw, qx, qy, qz, d.whx[i], d.why[i], d.whz[i], d.hqw[i], d.hqx[i], d.hqy[i], d.hqz[i]);
+}
+__global__ void k_finish(Owners d, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    finish_vel_one(d, i, dt);
+    finish_rot_one(d, i, dt);
+}
+// The parts alone: a run that ends between calls stores the half-step
+// velocities and leaves the quaternion rate to the next step's advance
+// (k_advance_rest computes it from the same values) or to k_finish_rot,
+// whichever comes first.
+__global__ void k_finish_vel(Owners d, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.n) finish_vel_one(d, i, dt);
+}
+__global__ void k_finish_rot(Owners d, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.n) finish_rot_one(d, i, dt);
 }
 
 // advanceHalfVelocityKernel of step s followed by advancePositionKernel of
@@ -859,6 +883,14 @@ void launch_advance_rot(const Owners& o, double dt, int sm_count, cudaStream_t s
 void launch_finish(const Owners& o, double dt, cudaStream_t s)
 {
     if (o.n > 0) k_finish<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_finish_vel(const Owners& o, double dt, cudaStream_t s)
+{
+    if (o.n > 0) k_finish_vel<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
+}
+void launch_finish_rot(const Owners& o, double dt, cudaStream_t s)
+{
+    if (o.n > 0) k_finish_rot<<<blocks(o.n, 256), 256, 0, s>>>(o, dt);
 }
 void launch_finish_advance_pos(const Owners& o, double dt, cudaStream_t s)
 {

@@ -367,6 +367,11 @@ void launch_universal_gravity(const Owners& o, cudaStream_t s);
 void launch_leapfrog_init(const Owners& o, double half_dt, cudaStream_t s);
 void launch_advance(const Owners& o, double dt, cudaStream_t s);
 void launch_finish(const Owners& o, double dt, cudaStream_t s);
+// launch_finish in two parts: the half-step velocities, then the half-step
+// quaternion rate (which launch_advance_rest also computes, from the same
+// values, before it advances the quaternion).
+void launch_finish_vel(const Owners& o, double dt, cudaStream_t s);
+void launch_finish_rot(const Owners& o, double dt, cudaStream_t s);
 // finishParticleStep of one step fused with advanceParticles of the next.
 // launch_finish followed by launch_advance, in two parts: positions (what
 // the next particle grid needs), then the rest of the advance.

@@ -195,7 +195,11 @@ int dem_leapfrog_finish(dem_engine* engine, double dt, double half_dt);
 /* Whole integration loop of the reference's IntegrateDem /
  * IntegrateDemMultiBody (src/cuda_simulation_integrator.cpp:245-446) for
  * `steps` steps, host MBD step included, with no output frames.  The first
- * call performs the step-0 force evaluation and the half-step start. */
+ * call performs the step-0 force evaluation and the half-step start.  The
+ * last step's half-step quaternion rate is computed by the next call: a
+ * following dem_run_steps takes it into its first advance, and every other
+ * call that reads, replaces or steps the particle state completes it first,
+ * so every call sees the reference's state after the last step. */
 int dem_run_steps(dem_engine* engine, int steps);
 
 /* Body state kept by dem_run_steps (host MBD): [nb][3] / [nb][4] arrays,

@@ -141,23 +141,37 @@ def test_candidate_counts_bound_the_contacts():
     assert st["wall_candidates"] >= with_wall
 
 
-@pytest.mark.parametrize("maker", ["plate_on_monolayer", "small_mbd"])
+@pytest.mark.parametrize("maker", ["plate_on_monolayer", "small_mbd", "clumps"])
 def test_run_split_into_calls_gives_the_same_bits(maker):
-    """A run of 24 steps as one call, as 8 + 8 + 8 and as 24 single steps:
-    the first step of each call advances in other kernels than the steps
-    inside a call, and they round alike."""
+    """A run of 24 steps as one call, as 8 + 8 + 8, as 24 single steps and
+    as 12 + 12 with the state read between the calls, and as 1 + 23 timed
+    steps (whose last step runs the whole finish).  The first step of
+    each call advances in other kernels than the steps inside a call; a call
+    leaves its last quaternion rate to the next call's first advance, or to
+    the read in between.  All round alike: the state and the half-step
+    state (velocities, spins, quaternion rates, accelerations) are the same
+    bits."""
     sc = getattr(G, maker)()
     runs = []
-    for parts in ([24], [8, 8, 8], [1] * 24):
+    for parts in ([24], [8, 8, 8], [1] * 24, [12, "read", 12], [1, "timed 23"]):
         e = engine_for(sc, precision="fp64")
         for p in parts:
-            e.run(p)
+            if p == "read":
+                e.downloadParticleState()
+            elif p == "timed 23":
+                e.time_steps(23)  # ends with the whole finish
+            else:
+                e.run(p)
         runs.append(e)
     ref = runs[0].downloadParticleState()
+    ref_half = runs[0].downloadHalfState()
     for e in runs[1:]:
         st = e.downloadParticleState()
         for k in ("pos", "vel", "omega", "quat"):
             np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+        half = e.downloadHalfState()
+        for k in ("vh", "wh", "hdq", "acc", "aacc"):
+            np.testing.assert_array_equal(half[k], ref_half[k], err_msg=k)
         np.testing.assert_array_equal(e.bodies()["center"], runs[0].bodies()["center"])
         np.testing.assert_array_equal(e.bodies()["quat"], runs[0].bodies()["quat"])
 
