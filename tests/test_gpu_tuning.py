@@ -141,8 +141,9 @@ def test_candidate_counts_bound_the_contacts():
     assert st["wall_candidates"] >= with_wall
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("maker", ["plate_on_monolayer", "small_mbd", "clumps"])
-def test_run_split_into_calls_gives_the_same_bits(maker):
+def test_run_split_into_calls_gives_the_same_bits(maker, precision):
     """A run of 24 steps as one call, as 8 + 8 + 8, as 24 single steps and
     as 12 + 12 with the state read between the calls, and as 1 + 23 timed
     steps (whose last step runs the whole finish).  The first step of
@@ -154,7 +155,7 @@ def test_run_split_into_calls_gives_the_same_bits(maker):
     sc = getattr(G, maker)()
     runs = []
     for parts in ([24], [8, 8, 8], [1] * 24, [12, "read", 12], [1, "timed 23"]):
-        e = engine_for(sc, precision="fp64")
+        e = engine_for(sc, precision=precision)
         for p in parts:
             if p == "read":
                 e.downloadParticleState()
