@@ -432,6 +432,16 @@ __global__ void k_tape_pp(Recs r, Hist<T> hp, Contacts<T> ct, Counters k)
 // ------------------------------------------------------------- particle sweep
 constexpr int kMaxContacts = kPSlots;
 constexpr int kCandidates = 96;  // FP32-prefilter survivors held before the exact pass
+
+// Residency asked of the latency-bound per-component and per-contact kernels
+// (blocks per SM at their launch width; the register budget follows): the
+// sweep 8 blocks of 128 (64 registers), the mixed particle law 4 of 256 (64)
+// and the mixed owner sum 6 of 256 (40).  Left to itself the compiler gave
+// them 96, 78 and 72 registers, and so 5, 3 and 3 blocks.  The FP64 forms
+// keep the residency they had (the particle law is FP64-pipe bound).
+constexpr int kSweepMinBlocks = 8;
+template <typename T> constexpr int kPpLawMinBlocks = sizeof(T) == sizeof(float) ? 4 : 2;
+template <typename T> constexpr int kOwnerSumMinBlocks = sizeof(T) == sizeof(float) ? 6 : 3;
 constexpr int kCertain = 1 << 30;  // staged candidate flag: contact decided by the FP32 test
 
 // Exact part of the reference's overlap test for one candidate (:587-597):
@@ -551,7 +561,7 @@ __device__ __forceinline__ bool mover_near(const Recs& r, const Counters& k, int
 // on them in order.  Contacts go to a flat list; results are stored per
 // (slot rank, component) so the owner sum reads them coalesced.
 template <typename T>
-__global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __restrict__ sc, Hist<T> hp,
+__global__ void __launch_bounds__(128, kSweepMinBlocks) k_sweep(Grid g, Recs r, const SceneC* __restrict__ sc, Hist<T> hp,
                                                Contacts<T> ct, Counters k, int nc)
 {
     const int step = *k.step;
@@ -712,7 +722,7 @@ __global__ void __launch_bounds__(128) k_sweep(Grid g, Recs r, const SceneC* __r
 // read-only path, the history slot as vectors), so the loads of a contact
 // are in flight together.
 template <typename T>
-__global__ void __launch_bounds__(256) k_pp_law(Recs r, const SceneC* __restrict__ sc, Hist<T> hp, Contacts<T> ct,
+__global__ void __launch_bounds__(256, kPpLawMinBlocks<T>) k_pp_law(Recs r, const SceneC* __restrict__ sc, Hist<T> hp, Contacts<T> ct,
                                                 Counters k, double dt_eff, int nscenes)
 {
     const int total = *k.ct_total;
@@ -1725,7 +1735,7 @@ __device__ __forceinline__ void owner_sum_sphere_f32(Owners o, Contacts<T> ct, i
 }
 
 template <typename T>
-__global__ void k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Contacts<T> ct, int outputs, double* fc,
+__global__ void __launch_bounds__(256, kOwnerSumMinBlocks<T>) k_owner_sum(Comps c, Owners o, const SceneC* __restrict__ sc, Contacts<T> ct, int outputs, double* fc,
                             double* ff, double* fw, double* ft)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
