@@ -35,7 +35,7 @@ import numpy as np  # noqa: E402
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # pipeline phases timed with CUDA events in one force evaluation
-PHASES = ["grid", "triangles+gather", "sweep", "walls", "pp_law", "pt", "owner_sum", "body_reduce"]
+PHASES = ["grid", "triangles+gather", "sweep", "walls", "pp_law", "pt_items", "pt_law", "owner_sum", "body_reduce"]
 
 
 def make_scene(config, particles=None):
@@ -148,8 +148,8 @@ KERNEL_BYTES = {
 
 
 def pt_bytes(items, manifolds, hv_body):
-    """Algorithmic bytes of the particle-triangle law phase (probe, items and
-    law kernels): per contact item its cell, record and owner state 208 B;
+    """Algorithmic bytes of the particle-triangle law kernel (k_pt_warp or
+    k_pt_thread): per contact item its cell, record and owner state 208 B;
     per manifold the body history slot read and written and its load record
     (32 doubles).  Triangle rows are shared by the items of a cell and not
     counted."""
@@ -160,9 +160,9 @@ def dominant_kernel(phases, n, sides, hv, list_length=None, items=0, manifolds=0
     """The single-kernel phase that takes longest (sweep, particle law,
     particle-triangle law or owner sum) and its roofline inputs."""
     times = dict(zip(PHASES, phases))
-    cands = list(KERNEL_BYTES) + (["pt"] if items else [])
+    cands = list(KERNEL_BYTES) + (["pt_law"] if items else [])
     name = max(cands, key=lambda k: times.get(k, 0.0))
-    if name == "pt":
+    if name == "pt_law":
         kernel = "k_pt_thread" if items > 3072 else "k_pt_warp"
         return name, kernel, times[name], pt_bytes(items, manifolds, 108)
     kernel, fn = KERNEL_BYTES[name]
@@ -328,7 +328,8 @@ def fp64_roofline(phases, config, precision):
     capture (sm__pipe_fp64_cycles_active, % of peak)."""
     times = dict(zip(PHASES, phases))
     out = {}
-    for phase, kernel in (("pp_law", "k_pp_law<double>" if precision == "fp64" else None), ("pt", "k_pt_thread")):
+    for phase, kernel in (("pp_law", "k_pp_law<double>" if precision == "fp64" else None), ("pt_law", "k_pt_thread"),
+                          ("pt_law", "k_pt_warp")):
         rec = traffic_record(kernel, config) if kernel else None
         if rec and rec.get("fp64_pipe_pct") is not None:
             out[kernel] = {"phase_ms": times.get(phase), "fp64_pipe_active_frac": rec["fp64_pipe_pct"] / 100.0,

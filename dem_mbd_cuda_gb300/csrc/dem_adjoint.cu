@@ -458,9 +458,11 @@ __device__ void adj_pw(Comps c, Owners o, const SceneC* __restrict__ sc, Walls w
 // the particle entries, the rest the wall entries.  Each entry's reverse law
 // is a long serial FP64 chain, and a warp issues one FP64 instruction per
 // about 68 cycles whatever its neighbours do, so with few contacts the two
-// sets cost their longer chain instead of the sum of both.
+// sets cost their longer chain instead of the sum of both.  The FP32 form is
+// compiled for 4 resident blocks (128 registers; the compiler's own choice
+// was 168, 3 blocks): the 64-scene batch's backward run 0.299 -> 0.293 s.
 template <typename R>
-__global__ void __launch_bounds__(128) k_adj_contacts(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
+__global__ void __launch_bounds__(128, sizeof(R) == sizeof(float) ? 4 : 1) k_adj_contacts(Comps c, Owners o, const SceneC* __restrict__ sc, Walls walls,
                                                       StepTape tp, int npp, int npw, int bpp, const double* P, double* T,
                                                       double* lh_pp, double* lh_pw, double dt_eff, double* grads,
                                                       int nscenes)

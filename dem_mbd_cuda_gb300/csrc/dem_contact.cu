@@ -1973,6 +1973,8 @@ void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs&
             k_pt_items<TB, kPtItemTile><<<std::max(1, std::min(ct.pt_scan.max_tiles, sm_count * 8)), kPtItemTile, 0,
                                           s>>>(g, r, t, hb, k, ct.pt_clist, ct.pt_index, ct.pt_ctotal_ptr,
                                                ct.pt_scan, g.err);
+    }
+    if ((stage & 16) && t.nt > 0 && b.nb > 0) {
         k_pt_warp<T, TB><<<sm_count * 32, kPtWarpBlock, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff,
                                                              sm_count * kPtPairBlocksPerSm);
         k_pt_thread<T, TB><<<sm_count * 4, 128, 0, s>>>(c, o, r, sc, t, b, hb, ct, k, dt_eff);

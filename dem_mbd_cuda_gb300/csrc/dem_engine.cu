@@ -680,7 +680,7 @@ public:
             launch_gather_geom(C_, O_, G_, R_, sm_count_, K_.gather_bps, K_, s);
             launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, K_.gather_bps, s);
             mark();
-            for (int stage : {2, 1, 4, 8}) {
+            for (int stage : {2, 1, 4, 8, 16}) {
                 contacts(stage, s);
                 mark();
             }
@@ -739,7 +739,7 @@ public:
         }
         link(s, br, 9);  // the velocity gather follows the sorted order
         launch_gather_vel<T>(C_, O_, G_, R_, dt_eff, sm_count_, K_.gather_bps, br);
-        if (pt) contacts(8, bt);
+        if (pt) contacts(8 | 16, bt);
         contacts(2, s);
         link(br, s, 11);  // the particle law reads the velocity records
         contacts(4, s);

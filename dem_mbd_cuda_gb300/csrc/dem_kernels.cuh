@@ -438,12 +438,13 @@ void launch_gather_vel(const Comps& c, const Owners& o, const Grid& g, const Rec
                        int bps, cudaStream_t s);
 // T: particle-particle and wall law / history type; TB: particle-triangle
 // law, area and body history type.  `stage` selects kernels (1 expiry and
-// walls, 2 sweep, 4 particle law, 8 particle-triangle) so callers can time
-// them separately; 15 runs all in order.
+// walls, 2 sweep, 4 particle law, 8 particle-triangle items, 16
+// particle-triangle law) so callers can time them separately; 31 runs all
+// in order.
 template <typename T, typename TB>
 void launch_contacts(const Comps& c, const Owners& o, const Grid& g, const Recs& r, const SceneC* sc, const Walls& w,
                      const Tris& t, const Bodies& b, Hist<T> hp, Hist<T> hw, Hist<TB> hb, Contacts<T> ct,
-                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s, int stage = 15);
+                     const Counters& k, double dt_eff, int block, int sm_count, cudaStream_t s, int stage = 31);
 template <typename T>
 void launch_owner_sum(const Comps& c, const Owners& o, const SceneC* sc, Contacts<T> ct, bool outputs, double* fc,
                       double* ff, double* fw, double* ft, cudaStream_t s);
