@@ -80,12 +80,13 @@ constexpr int kDefaultPtWarpItems = 3072;
 // Scenes of up to kSmallScene components leave more room (their PT and
 // rotational branches are short chains that must not wait for slots);
 // larger scenes are throughput bound and give the sweep and the gathers
-// more of each SM.  Measured on GB300 (200k- and 2M-sphere scenes); the
-// autotuner refines them per scene.  Six sweep blocks per SM is the sweep's
-// register-limited residency: that grid leaves nothing beside it and was
-// the slowest setting on the 2M drum.
+// more of each SM, grid-stride over three times the sweep's residency of 8
+// blocks (scenes without triangles too: one thread per component took the
+// 256-scene batch's step to 2.93 ms against 2.56 with 16 and 24 per SM).
+// Measured on GB300 (200k- and 2M-sphere scenes, the 5.46M-sphere batch);
+// the autotuner refines them per scene.
 constexpr int kSmallScene = 500000;
-constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 16;
+constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 24;
 // The gathers and the particle law, likewise (blocks of 256 per SM).
 constexpr int kGatherBlocksSmall = 2, kGatherBlocksLarge = 8;
 constexpr int kDefaultPpBlocksPerSm = 16;
@@ -499,7 +500,7 @@ public:
         K_.wl_total = cnt + 10;
         K_.pt_warp_items = kDefaultPtWarpItems;
         // without triangles no PT branch needs room beside the sweep
-        K_.sweep_bps = nt_ == 0 ? 0 : (nc_ <= kSmallScene ? kSweepBlocksSmall : kSweepBlocksLarge);
+        K_.sweep_bps = nt_ > 0 && nc_ <= kSmallScene ? kSweepBlocksSmall : kSweepBlocksLarge;
         K_.gather_bps = nc_ <= kSmallScene ? kGatherBlocksSmall : kGatherBlocksLarge;
         K_.pp_bps = kDefaultPpBlocksPerSm;
         // neighbour lists (set_launch 3 turns them off)
