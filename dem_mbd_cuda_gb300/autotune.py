@@ -31,7 +31,7 @@ from .engine import CudaDemSolver
 
 FACTORS = (2.0, 2.25, 2.5, 3.0, 3.5)
 SWEEP_BLOCKS = (2, 3, 4, 6, 8, 16, 24)
-GATHER_BLOCKS = (1, 2, 4, 8)
+GATHER_BLOCKS = (2, 3, 4, 6, 8)
 WARP_ITEMS = (512, 3072, 16384)
 SKINS = (0, 250, 500, 900)  # per mille of the room the cell edge leaves beyond the largest pair
 _cache: dict = {}

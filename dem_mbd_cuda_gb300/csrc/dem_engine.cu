@@ -87,8 +87,11 @@ constexpr int kDefaultPtWarpItems = 3072;
 // the autotuner refines them per scene.
 constexpr int kSmallScene = 500000;
 constexpr int kSweepBlocksSmall = 3, kSweepBlocksLarge = 24;
-// The gathers and the particle law, likewise (blocks of 256 per SM).
-constexpr int kGatherBlocksSmall = 2, kGatherBlocksLarge = 8;
+// The gathers and the particle law, likewise (blocks of 256 per SM).  With
+// the sweep at 8 resident blocks the gathers want fewer blocks than before
+// (8 -> 4 on the drum 1.035 -> 1.031 ms and on the 256-scene batch 2.55 ->
+// 2.53; 2 -> 3 on C1 0.1933 -> 0.1925).
+constexpr int kGatherBlocksSmall = 3, kGatherBlocksLarge = 4;
 constexpr int kDefaultPpBlocksPerSm = 16;
 
 static MatF to_float(const MatC& c)
